@@ -1,0 +1,121 @@
+/*
+ * mdet_tnf.h -- C ABI of the GB300 (sm_103a) MetaBAT2 TNF path.
+ *
+ * Plain C types only: host or device pointers plus sizes, int status codes,
+ * an opaque context that owns its device memory and CUDA stream.  One host
+ * thread at a time per context.  Every call that takes HOST buffers copies
+ * them in and out itself (pinned staging inside the context); the *_dev
+ * variants take device pointers that stay resident.
+ *
+ * Each entry point names the reference interface it replaces (paths
+ * relative to the MdeT project root).  The reference itself has no library
+ * boundary: its stages are free functions over globals that exit(1) on any
+ * CUDA error (getError, cuda/Cuda2.cu:341-354); here every failure is a
+ * status code and mdet_last_error() says why.
+ */
+#ifndef MDET_TNF_H
+#define MDET_TNF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MDET_OK 0
+#define MDET_ERR_INVALID 1     /* bad argument (null pointer, size out of range) */
+#define MDET_ERR_CUDA 2        /* CUDA runtime / driver error */
+#define MDET_ERR_NOMEM 3       /* device or pinned allocation failed */
+#define MDET_ERR_CAPACITY 4    /* caller's output buffer too small; *n_out holds the size needed */
+#define MDET_ERR_TIMEOUT 5     /* a bounded device-side wait ran out; the context stays usable */
+#define MDET_ERR_UNSUPPORTED 6 /* mode not available (e.g. tensor-core path on a non-sm_103 device) */
+
+/* distance-filter forms of the pairwise stage */
+#define MDET_MODE_PLAIN 0   /* FP32 SIMT all-pairs distance in the reference's element order */
+#define MDET_MODE_BF16 1    /* tcgen05 BF16 tile GEMM, FP32 accumulation in TMEM */
+#define MDET_MODE_TF32 2    /* tcgen05 TF32 tile GEMM, FP32 accumulation in TMEM */
+#define MDET_MODE_LEARNED 3 /* learned embedding proposal + BF16 tiles (see mdet_tnf_learned_*) */
+
+typedef struct mdet_ctx mdet_ctx;
+
+typedef struct {
+    uint64_t n_candidates;   /* pairs that passed the conservative distance filter */
+    uint64_t n_above_cutoff; /* unordered pairs whose exact probability beats the cutoff */
+    uint64_t n_edges;        /* emitted (from < to) edges */
+    uint64_t tiles_total;    /* tile pairs in the pairwise schedule */
+    uint64_t tiles_computed; /* tile pairs actually evaluated (< total with the learned proposal) */
+    uint32_t gpu_launches;   /* kernels this call launched */
+    uint32_t reserved;
+    double ms_prep, ms_filter, ms_exact, ms_select, ms_total; /* device time per phase */
+} mdet_graph_stats;
+
+/* ---- context ---------------------------------------------------------- */
+int mdet_ctx_create(int device, mdet_ctx** out);
+int mdet_ctx_destroy(mdet_ctx* ctx);
+/* Last error message of this context ("" if none). */
+const char* mdet_last_error(const mdet_ctx* ctx);
+/* Use `stream` (a cudaStream_t) for all later work instead of the context's own. */
+int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream);
+/* Build identification: "sm_103a ..." */
+const char* mdet_version(void);
+
+/* ---- TNF counting ------------------------------------------------------
+ * Replaces the TNF loop of main (cuda/Cuda2.cu:1825-1863) and the copy of
+ * TNF/logSizes to the devices (cuda/Cuda2.cu:1866-1874).  bytes[off[i] ..
+ * off[i]+len[i]) is contig i's sequence view exactly as the reference's
+ * reader builds it (newlines included, cuda/Cuda2.cu:1521-1530).  Outputs
+ * counts (n*136 uint32, canonical tetranucleotide columns in TNF.bin order)
+ * and tnf (n*136 float, c / sqrt(sum float(c*c))).  A contig with no valid
+ * tetranucleotide gets zero counts and NaN TNF (0/0), as in the reference. */
+int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint64_t* off,
+                   const uint64_t* len, uint64_t n, uint32_t* counts, float* tnf);
+int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const uint64_t* d_off,
+                       const uint64_t* d_len, uint64_t n, uint32_t* d_counts, float* d_tnf);
+
+/* ---- max-probability sample --------------------------------------------
+ * Replaces launch_tnf_max_prob_sample_kernel_multi (cuda/Cuda2.cu:356-379)
+ * with get_tnf_max_prob_sample (cuda/Cuda2.cu:281-314): for each sampled
+ * position b < m of the permutation `contigs` (length n), the similarity
+ * sigmoid(max pre-probability) against every other contig.
+ * floor_prob: values at or above it are exact; a sampled contig whose true
+ * maximum is below floor_prob reports some value below floor_prob (the
+ * reference's pTNF search never looks below 0.701).  floor_prob <= 0 makes
+ * every value exact (all pairs scored). */
+int mdet_tnf_max_prob(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n,
+                      const uint64_t* contigs, uint64_t m, int mode, double floor_prob, double* out);
+int mdet_tnf_max_prob_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                          const uint64_t* d_contigs, uint64_t m, int mode, double floor_prob,
+                          double* d_out);
+
+/* ---- pTNF search -------------------------------------------------------
+ * Replaces gen_tnf_graph_sample and its driver (cuda/Cuda2.cu:972-1025,
+ * 1883-1904): samples with glibc rand() in the reference's order (the caller
+ * seeds it with srand, as the reference's main does) and returns pTNF in
+ * permille in *ptnf_out. coverage = maxP/100. */
+int mdet_tnf_ptnf_search(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n,
+                         double coverage, int mode, double* ptnf_out);
+int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                             double coverage, int mode, double* ptnf_out);
+
+/* ---- TNF graph ---------------------------------------------------------
+ * Replaces gen_tnf_graph (cuda/Cuda2.cu:861-970) with kernel get_tnf_graph2
+ * (cuda/Cuda2.cu:243-262): every pair with pre-probability above
+ * logit(cutoff) is scored sigmoid(pre); each contig keeps its max_edges best
+ * (ties by lower column), and edge (i, j, sTNF) is emitted when i < j and j
+ * is among i's kept.  Output rows ascending, inside a row by similarity
+ * descending then j ascending (the reference's order across tiles is
+ * unspecified).  Host arrays of `capacity` entries; *n_edges receives the
+ * count (on MDET_ERR_CAPACITY, the count needed). */
+int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                   uint32_t max_edges, int mode, uint64_t* from, uint64_t* to, double* stnf,
+                   uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
+/* Device-resident form: d_tnf/d_log_size and the three outputs on the device. */
+int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                       double cutoff, uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to,
+                       double* d_stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

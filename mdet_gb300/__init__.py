@@ -1,0 +1,4 @@
+"""mdet_gb300 -- GB300 (sm_103a) MetaBAT2 TNF path: tetranucleotide counting,
+all-pairs TNF probability, cutoff and per-contig top-k edge selection,
+behind the C ABI of include/mdet_tnf.h."""
+from .tnf import Context, Graph, MdetError, MODES, load_library, version  # noqa: F401

@@ -1,0 +1,160 @@
+// common.cuh -- shared internals of libmdet_tnf: the context, its scratch
+// arena, status handling, PTX wrappers (mbarrier, bulk copies, tcgen05) and
+// the MetaBAT2 logistic-model coefficients.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <unordered_map>
+
+#include "../../include/mdet_tnf.h"
+
+#define MDET_NTNF 136
+
+// ---------------------------------------------------------------- context --
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct mdet_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    int cc_major = 0, cc_minor = 0;
+    std::string err;
+    std::unordered_map<std::string, DevBuf> bufs;  // named grow-only device scratch
+    void* pinned = nullptr;                        // pinned host staging
+    size_t pinned_cap = 0;
+    int* d_flag = nullptr;     // device error flag (bounded waits that ran out)
+    uint32_t launches = 0;     // kernels launched by the current call
+    void* encode_tiled = nullptr;  // cuTensorMapEncodeTiled entry point
+    bool count_scratch_dirty = false;
+};
+
+// Returns a device buffer of at least `bytes` named `name`, growing it if
+// needed.  zero_on_grow: freshly grown buffers are memset to 0.
+void* ctx_scratch(mdet_ctx* ctx, const char* name, size_t bytes, bool zero_on_grow = false);
+void* ctx_pinned(mdet_ctx* ctx, size_t bytes);
+int ctx_fail(mdet_ctx* ctx, int code, const char* fmt, ...);
+int ctx_cuda(mdet_ctx* ctx, cudaError_t e, const char* what);
+int ctx_check_launch(mdet_ctx* ctx, const char* what);
+
+#define MDET_TRY(call)                     \
+    do {                                   \
+        int _rc = (call);                  \
+        if (_rc != MDET_OK) return _rc;    \
+    } while (0)
+#define MDET_CUDA(ctx, call) MDET_TRY(ctx_cuda((ctx), (call), #call))
+#define MDET_LAUNCHED(ctx, what)                   \
+    do {                                           \
+        (ctx)->launches++;                         \
+        MDET_TRY(ctx_check_launch((ctx), (what))); \
+    } while (0)
+
+// Device-wide bounded-wait budget: ~2 s at 2 GHz.
+#define MDET_SPIN_CYCLES (4000000000ull)
+#define MDET_FLAG_TIMEOUT 1
+
+// ------------------------------------------------------ canonical tables --
+
+// 8-bit raw 4-mer code (base codes A=0,C=1,T=2,G=3, oldest base in the high
+// bits) -> canonical TNF column; and per column its forward and
+// reverse-complement raw codes.  Built on the host from the column order.
+struct TnTables {
+    uint8_t raw_to_col[256];
+    uint8_t col_fw[MDET_NTNF];
+    uint8_t col_rc[MDET_NTNF];
+};
+const TnTables& tn_tables();
+
+// Uploads the canonical tables to __constant__ memory once per device.
+int ensure_constants(mdet_ctx* ctx);
+
+// ------------------------------------------------------- model pieces ----
+// b(x,y) and c(x,y) of both logistic models split as F(x) + G(y) + H(x*y)
+// with x = min log size, y = max log size (cuda/Cuda2.cu:199-236).
+struct ModelSplit {
+    // F coefficients: powers x^0..x^7; G: y^1..y^6; H: t^1..t^5 (t = x*y)
+    double F[4][8];
+    double G[4][7];
+    double H[4][6];
+};
+const ModelSplit& model_split();
+
+// Host FP64 evaluation of the largest distance d* with pre-probability above
+// logit_cut for log sizes (x <= y); returns +inf where the model is not
+// decreasing in d.
+double host_dstar(double x, double y, double logit_cut);
+
+// ------------------------------------------------------------ PTX helpers --
+
+static __device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+static __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+static __device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+static __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+static __device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (and raises the device flag) when the budget
+// runs out, so no wait in this library can spin forever.
+static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* flag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    long long t0 = clock64();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((unsigned long long)(clock64() - t0) > MDET_SPIN_CYCLES) {
+            if (flag) atomicOr(flag, MDET_FLAG_TIMEOUT);
+            return false;
+        }
+        if (flag && *(volatile int*)flag) return false;
+    }
+}
+
+// 1-D bulk copy global -> shared (TMA engine), completion on an mbarrier.
+static __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+static __device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+static __device__ __forceinline__ uint32_t lane_id() {
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}

@@ -1,0 +1,502 @@
+// graph.cu -- C ABI of the pairwise stage: TNF graph, max-probability
+// sample and the pTNF search, orchestrating prep -> filter -> exact ->
+// per-contig top-k on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <numeric>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "graph.cuh"
+
+namespace {
+
+struct PhaseTimer {
+    cudaEvent_t ev[6];
+    int n = 0;
+    cudaStream_t s;
+    explicit PhaseTimer(cudaStream_t st) : s(st) {
+        for (auto& e : ev) cudaEventCreate(&e);
+    }
+    ~PhaseTimer() {
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    void mark() {
+        if (n < 6) cudaEventRecord(ev[n++], s);
+    }
+    double ms(int a, int b) {
+        if (b >= n) return 0;
+        float t = 0;
+        cudaEventSynchronize(ev[b]);
+        cudaEventElapsedTime(&t, ev[a], ev[b]);
+        return t;
+    }
+};
+
+__global__ void k_sample_sort_keys(const uint64_t* __restrict__ contigs, const uint32_t* __restrict__ inv, uint64_t m,
+                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= m) return;
+    keys[b] = inv[contigs[b]];
+    vals[b] = (uint32_t)b;
+}
+
+__global__ void k_sample_gather(const uint32_t* __restrict__ row_map, const uint32_t* __restrict__ order, uint64_t m,
+                                const float* __restrict__ x32, const double* __restrict__ ls,
+                                float* __restrict__ a32, double* __restrict__ als, uint32_t* __restrict__ slot_of) {
+    uint64_t r = blockIdx.x;
+    if (r >= m) return;
+    uint32_t sp = row_map[r];
+    for (int k = threadIdx.x; k < MDET_NTNF; k += blockDim.x) a32[r * MDET_NTNF + k] = x32[(uint64_t)sp * MDET_NTNF + k];
+    if (threadIdx.x == 0) {
+        als[r] = ls[sp];
+        slot_of[order[r]] = (uint32_t)r;
+    }
+}
+
+__global__ void k_sample_gather_bf16(const uint32_t* __restrict__ row_map, uint64_t m, uint64_t mpad,
+                                     const uint16_t* __restrict__ xb, const float* __restrict__ nsq,
+                                     uint16_t* __restrict__ ab, float* __restrict__ ansq) {
+    uint64_t r = blockIdx.x;
+    if (r >= mpad) return;
+    if (r < m) {
+        uint32_t sp = row_map[r];
+        for (int k = threadIdx.x; k < MDET_KPAD; k += blockDim.x) ab[r * MDET_KPAD + k] = xb[(uint64_t)sp * MDET_KPAD + k];
+        if (threadIdx.x == 0) ansq[r] = nsq[sp];
+    } else {
+        for (int k = threadIdx.x; k < MDET_KPAD; k += blockDim.x) ab[r * MDET_KPAD + k] = 0;
+        if (threadIdx.x == 0) ansq[r] = __int_as_float(0x7f800000);
+    }
+}
+
+// per-128 block metadata of the gathered sample (log-size range, and for
+// BF16 rows the max rounding error / norm of the gathered rows)
+__global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, const double* __restrict__ ls,
+                              const BlockMeta* __restrict__ src_meta, uint64_t nblk, BlockMeta* __restrict__ out) {
+    uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    uint64_t r0 = b * MDET_BLK, r1 = min(m, r0 + MDET_BLK);
+    BlockMeta o;
+    o.lo = o.hi = 0.f;
+    o.emax = o.nmax = 0.f;
+    if (r0 < m) {
+        o.lo = __double2float_rd(ls[row_map[r0]]);
+        o.hi = __double2float_ru(ls[row_map[r1 - 1]]);
+        for (uint64_t r = r0; r < r1; ++r) {
+            const BlockMeta& sm = src_meta[row_map[r] / MDET_BLK];
+            o.emax = fmaxf(o.emax, sm.emax);
+            o.nmax = fmaxf(o.nmax, sm.nmax);
+        }
+    } else {
+        o.lo = o.hi = __double2float_rd(ls[row_map[m - 1]]);
+    }
+    out[b] = o;
+}
+
+double logit(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
+
+int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
+               const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
+               const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out) {
+    cudaStream_t s = ctx->stream;
+    std::string cap_key = std::string(tag) + ".cap";
+    unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
+    if (!cnt) return MDET_ERR_NOMEM;
+    // remembered capacity (bytes of the candidate buffer) from earlier calls
+    size_t guess = ((size_t)256 * (rect ? na : g.n) + (1u << 20)) * sizeof(uint2);
+    DevBuf& cb = ctx->bufs[std::string(tag) + ".cand"];
+    if (cb.cap > guess) guess = cb.cap;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        uint2* cand = (uint2*)ctx_scratch(ctx, (std::string(tag) + ".cand").c_str(), guess);
+        if (!cand) return MDET_ERR_NOMEM;
+        unsigned long long cap = ctx->bufs[std::string(tag) + ".cand"].cap / sizeof(uint2);
+        MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
+        CandBuf out{cand, cnt, cap};
+        if (mode == MDET_MODE_PLAIN) {
+            const float* A = rect ? a32 : g.x32;
+            MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect, tbl,
+                                 out));
+        } else {
+            const uint16_t* A = rect ? ab : g.xb;
+            const float* An = rect ? ansq : g.nsq;
+            MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.nsq, g.n, g.meta, !rect,
+                               tbl, out));
+        }
+        unsigned long long found = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        if (found <= cap) {
+            *cand_out = cand;
+            *ncand_out = found;
+            return MDET_OK;
+        }
+        guess = (size_t)(found + found / 8 + 1024) * sizeof(uint2);
+    }
+    return ctx_fail(ctx, MDET_ERR_NOMEM, "candidate buffer kept overflowing");
+}
+
+int check_mode(mdet_ctx* ctx, int mode) {
+    if (mode == MDET_MODE_PLAIN) return MDET_OK;
+    if (mode == MDET_MODE_BF16) {
+        if (ctx->cc_major != 10 || ctx->cc_minor != 3)
+            return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "tensor-core forms need an sm_103 device (have sm_%d%d)",
+                            ctx->cc_major, ctx->cc_minor);
+        return MDET_OK;
+    }
+    return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "mode %d not available", mode);
+}
+
+int check_flag(mdet_ctx* ctx) {
+    int h = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MDET_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream);
+        return ctx_fail(ctx, MDET_ERR_TIMEOUT, "a bounded device wait ran out (flag %d)", h);
+    }
+    return MDET_OK;
+}
+
+int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
+               int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total) {
+    PhaseTimer tm(ctx->stream);
+    tm.mark();
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, mode != MDET_MODE_PLAIN, &g));
+    const double L = logit(cutoff);
+    DstarTable tbl;
+    MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl));
+    tm.mark();
+    uint2* cand = nullptr;
+    unsigned long long ncand = 0;
+    MDET_TRY(run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "g", &cand, &ncand));
+    tm.mark();
+    Edge* edges = nullptr;
+    unsigned long long ne = 0;
+    uint32_t* deg = nullptr;
+    MDET_TRY(exact_graph(ctx, g, cand, ncand, L, &edges, &ne, &deg));
+    tm.mark();
+    MDET_TRY(select_topk(ctx, g, edges, ne, deg, max_edges, total));
+    tm.mark();
+    if (st) {
+        st->n_candidates = ncand;
+        st->n_above_cutoff = ne;
+        uint64_t t = (n + 127) / 128;
+        st->tiles_total = t * (t + 1) / 2;
+        st->tiles_computed = st->tiles_total;
+        st->ms_prep = tm.ms(0, 1);
+        st->ms_filter = tm.ms(1, 2);
+        st->ms_exact = tm.ms(2, 3);
+        st->ms_select = tm.ms(3, 4);
+    }
+    return MDET_OK;
+}
+
+int validate_graph_args(mdet_ctx* ctx, uint64_t n, double cutoff, uint32_t max_edges, int mode) {
+    if (!(cutoff > 0.0 && cutoff < 1.0)) return ctx_fail(ctx, MDET_ERR_INVALID, "cutoff must lie in (0, 1)");
+    if (max_edges == 0 || max_edges > 4096) return ctx_fail(ctx, MDET_ERR_INVALID, "max_edges must be in [1, 4096]");
+    if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
+    return check_mode(ctx, mode);
+}
+
+// --- max-probability sample on a prepared contig set ---
+int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, uint64_t m, int mode,
+                 double floor_prob, double* d_out) {
+    cudaStream_t s = ctx->stream;
+    if (m == 0) return MDET_OK;
+    uint32_t* keys = (uint32_t*)ctx_scratch(ctx, "mp.keys", m * 4);
+    uint32_t* keys2 = (uint32_t*)ctx_scratch(ctx, "mp.keys2", m * 4);
+    uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "mp.vals", m * 4);
+    uint32_t* order = (uint32_t*)ctx_scratch(ctx, "mp.order", m * 4);
+    uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "mp.slot", m * 4);
+    uint64_t mpad = (m + 255) / 256 * 256;
+    float* a32 = (float*)ctx_scratch(ctx, "mp.a32", m * MDET_NTNF * 4);
+    double* als = (double*)ctx_scratch(ctx, "mp.als", m * 8);
+    uint64_t nblk = mpad / MDET_BLK;
+    BlockMeta* ameta32 = (BlockMeta*)ctx_scratch(ctx, "mp.meta32", nblk * sizeof(BlockMeta));
+    BlockMeta* ameta = (BlockMeta*)ctx_scratch(ctx, "mp.meta", nblk * sizeof(BlockMeta));
+    if (!keys || !keys2 || !vals || !order || !slot_of || !a32 || !als || !ameta32 || !ameta) return MDET_ERR_NOMEM;
+    k_sample_sort_keys<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(d_contigs, g.inv, m, keys, vals);
+    MDET_LAUNCHED(ctx, "k_sample_sort_keys");
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, order, (int)m, 0, 32, s);
+    void* tmp = ctx_scratch(ctx, "mp.cubtmp", tb);
+    if (!tmp) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, order, (int)m, 0, 32, s));
+    const uint32_t* row_map = keys2;  // sorted positions of the sample, ascending
+    k_sample_gather<<<(unsigned)m, 64, 0, s>>>(row_map, order, m, g.x32, g.ls, a32, als, slot_of);
+    MDET_LAUNCHED(ctx, "k_sample_gather");
+    k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta32, nblk, ameta32);
+    MDET_LAUNCHED(ctx, "k_sample_meta");
+    uint16_t* ab = nullptr;
+    float* ansq = nullptr;
+    if (mode != MDET_MODE_PLAIN) {
+        ab = (uint16_t*)ctx_scratch(ctx, "mp.ab", mpad * MDET_KPAD * 2);
+        ansq = (float*)ctx_scratch(ctx, "mp.ansq", mpad * 4);
+        if (!ab || !ansq) return MDET_ERR_NOMEM;
+        k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xb, g.nsq, ab, ansq);
+        MDET_LAUNCHED(ctx, "k_sample_gather_bf16");
+        k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
+        MDET_LAUNCHED(ctx, "k_sample_meta");
+    }
+    const double L = floor_prob > 0 ? logit(floor_prob) : -INFINITY;
+    DstarTable tbl;
+    MDET_TRY(build_dstar_table(ctx, g.ls, g.n, L, &tbl));
+    uint2* cand = nullptr;
+    unsigned long long ncand = 0;
+    MDET_TRY(run_filter(ctx, mode, g, true, a32, ab, ansq, (uint32_t)m, ameta, ameta32, tbl, "mp", &cand, &ncand));
+    MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out));
+    return MDET_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
+                       uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to, double* d_stnf,
+                       uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats) {
+    if (!ctx || !n_edges) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    *n_edges = 0;
+    MDET_TRY(validate_graph_args(ctx, n, cutoff, max_edges, mode));
+    if (n < 2) return MDET_OK;
+    if (!d_tnf || !d_log_size) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    GraphPrep g;
+    uint64_t total = 0;
+    int rc = graph_core(ctx, d_tnf, d_log_size, n, cutoff, max_edges, mode, stats, g, &total);
+    if (rc == MDET_OK) {
+        *n_edges = total;
+        if (total > capacity)
+            rc = ctx_fail(ctx, MDET_ERR_CAPACITY, "edge output needs %llu entries, capacity %llu",
+                          (unsigned long long)total, (unsigned long long)capacity);
+        else if (total && (!d_from || !d_to || !d_stnf))
+            rc = ctx_fail(ctx, MDET_ERR_INVALID, "null output pointer");
+        else
+            rc = emit_topk(ctx, g, max_edges, d_from, d_to, d_stnf, total);
+    }
+    cudaEventRecord(e1, ctx->stream);
+    if (rc == MDET_OK) rc = check_flag(ctx);
+    if (stats) {
+        float ms = 0;
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats->ms_total = ms;
+        stats->n_edges = total;
+        stats->gpu_launches = ctx->launches;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                   uint32_t max_edges, int mode, uint64_t* from, uint64_t* to, double* stnf, uint64_t capacity,
+                   uint64_t* n_edges, mdet_graph_stats* stats) {
+    if (!ctx || !n_edges) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    *n_edges = 0;
+    MDET_TRY(validate_graph_args(ctx, n, cutoff, max_edges, mode));
+    if (n < 2) return MDET_OK;
+    if (!tnf || !log_size) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    cudaStream_t s = ctx->stream;
+    float* d_tnf = (float*)ctx_scratch(ctx, "io.gtnf", n * MDET_NTNF * 4);
+    double* d_ls = (double*)ctx_scratch(ctx, "io.gls", n * 8);
+    if (!d_tnf || !d_ls) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_tnf, tnf, n * MDET_NTNF * 4, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_ls, log_size, n * 8, cudaMemcpyHostToDevice, s));
+    GraphPrep g;
+    uint64_t total = 0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    int rc = graph_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, mode, stats, g, &total);
+    if (rc == MDET_OK) {
+        *n_edges = total;
+        if (total > capacity) {
+            rc = ctx_fail(ctx, MDET_ERR_CAPACITY, "edge output needs %llu entries, capacity %llu",
+                          (unsigned long long)total, (unsigned long long)capacity);
+        } else if (total) {
+            uint64_t* df = (uint64_t*)ctx_scratch(ctx, "io.from", total * 8);
+            uint64_t* dt = (uint64_t*)ctx_scratch(ctx, "io.to", total * 8);
+            double* ds = (double*)ctx_scratch(ctx, "io.stnf", total * 8);
+            if (!df || !dt || !ds) {
+                rc = MDET_ERR_NOMEM;
+            } else if (!from || !to || !stnf) {
+                rc = ctx_fail(ctx, MDET_ERR_INVALID, "null output pointer");
+            } else {
+                rc = emit_topk(ctx, g, max_edges, df, dt, ds, total);
+                if (rc == MDET_OK) {
+                    cudaMemcpyAsync(from, df, total * 8, cudaMemcpyDeviceToHost, s);
+                    cudaMemcpyAsync(to, dt, total * 8, cudaMemcpyDeviceToHost, s);
+                    rc = ctx_cuda(ctx, cudaMemcpyAsync(stnf, ds, total * 8, cudaMemcpyDeviceToHost, s), "copy out");
+                }
+            }
+        }
+    }
+    cudaEventRecord(e1, s);
+    if (rc == MDET_OK) rc = check_flag(ctx);
+    if (stats) {
+        float ms = 0;
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        stats->ms_total = ms;
+        stats->n_edges = total;
+        stats->gpu_launches = ctx->launches;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int mdet_tnf_max_prob_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                          const uint64_t* d_contigs, uint64_t m, int mode, double floor_prob, double* d_out) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    MDET_TRY(check_mode(ctx, mode));
+    if (m > n) return ctx_fail(ctx, MDET_ERR_INVALID, "sample larger than the contig set");
+    if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
+    if (m == 0) return MDET_OK;
+    if (!d_tnf || !d_log_size || !d_contigs || !d_out) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    GraphPrep g;
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, mode != MDET_MODE_PLAIN, &g));
+    MDET_TRY(maxprob_core(ctx, g, d_contigs, m, mode, floor_prob, d_out));
+    return check_flag(ctx);
+}
+
+int mdet_tnf_max_prob(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, const uint64_t* contigs,
+                      uint64_t m, int mode, double floor_prob, double* out) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (m > n) return ctx_fail(ctx, MDET_ERR_INVALID, "sample larger than the contig set");
+    if (m == 0) return MDET_OK;
+    if (!tnf || !log_size || !contigs || !out) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    for (uint64_t b = 0; b < m; ++b)
+        if (contigs[b] >= n) return ctx_fail(ctx, MDET_ERR_INVALID, "contig index out of range");
+    cudaStream_t s = ctx->stream;
+    float* d_tnf = (float*)ctx_scratch(ctx, "io.gtnf", n * MDET_NTNF * 4);
+    double* d_ls = (double*)ctx_scratch(ctx, "io.gls", n * 8);
+    uint64_t* d_c = (uint64_t*)ctx_scratch(ctx, "io.contigs", m * 8);
+    double* d_o = (double*)ctx_scratch(ctx, "io.mpout", m * 8);
+    if (!d_tnf || !d_ls || !d_c || !d_o) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_tnf, tnf, n * MDET_NTNF * 4, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_ls, log_size, n * 8, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_c, contigs, m * 8, cudaMemcpyHostToDevice, s));
+    MDET_TRY(mdet_tnf_max_prob_dev(ctx, d_tnf, d_ls, n, d_c, m, mode, floor_prob, d_o));
+    MDET_CUDA(ctx, cudaMemcpyAsync(out, d_o, m * 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDET_OK;
+}
+
+// gen_tnf_graph_sample + driver (cuda/Cuda2.cu:972-1025, 1883-1904).
+int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                             double coverage, int mode, double* ptnf_out) {
+    if (!ctx || !ptnf_out) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    MDET_TRY(check_mode(ctx, mode));
+    if (n < 2) return ctx_fail(ctx, MDET_ERR_INVALID, "need at least two contigs");
+    if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
+    cudaStream_t s = ctx->stream;
+    GraphPrep g;
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, mode != MDET_MODE_PLAIN, &g));
+    std::vector<uint64_t> idx(n);
+    std::vector<double> mx;
+    uint64_t* d_idx = (uint64_t*)ctx_scratch(ctx, "pt.idx", n * 8);
+    double* d_mx = (double*)ctx_scratch(ctx, "pt.mx", n * 8);
+    if (!d_idx || !d_mx) return MDET_ERR_NOMEM;
+    // the search only compares maxima against cutoffs above 0.700
+    const double floor_prob = 0.7;
+    auto sample = [&](bool full, double* p_out) -> int {
+        uint64_t m = full ? n : std::min<uint64_t>(n, 2500);
+        std::iota(idx.begin(), idx.end(), (uint64_t)0);
+        {  // random_unique (cuda/Cuda2.cu:500-511)
+            uint64_t left = n, k = m;
+            uint64_t* begin = idx.data();
+            while (k--) {
+                uint64_t* r = begin + (uint64_t)rand() % left;
+                std::swap(*begin, *r);
+                ++begin;
+                --left;
+            }
+        }
+        MDET_CUDA(ctx, cudaMemcpyAsync(d_idx, idx.data(), m * 8, cudaMemcpyHostToDevice, s));
+        MDET_TRY(maxprob_core(ctx, g, d_idx, m, mode, floor_prob, d_mx));
+        mx.resize(m);
+        MDET_CUDA(ctx, cudaMemcpyAsync(mx.data(), d_mx, m * 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        std::sort(mx.begin(), mx.end(), std::greater<double>());
+        uint64_t p = 999, pp = 1000, counton = 0;
+        double cov = 0, pcov = 0;
+        for (; p > 700;) {
+            double cut = (double)p / 1000.;
+            while (counton < m && mx[counton] >= cut) counton++;
+            cov = (double)counton / m;
+            if (cov >= coverage) {
+                if (cov - coverage > coverage - pcov) {
+                    p = pp;
+                    cov = pcov;
+                }
+                break;
+            }
+            pp = p;
+            pcov = cov;
+            if (p > 990)
+                p -= rand() % 3 + 1;
+            else if (p > 900)
+                p -= rand() % 3 + 3;
+            else
+                p -= rand() % 3 + 9;
+        }
+        *p_out = (double)p;
+        return MDET_OK;
+    };
+    double ptnf = 0;
+    if (n <= 25000) {
+        MDET_TRY(sample(true, &ptnf));
+    } else {
+        for (int i = 0; i < 10; ++i) {
+            double minp = 0;
+            MDET_TRY(sample(false, &minp));
+            if (minp < 701) minp = 700.;
+            ptnf += minp;
+            if (i == 1 && ptnf / 2 < 701) {
+                ptnf = 700.;
+                break;
+            }
+            if (i == 9) ptnf /= 10.;
+        }
+    }
+    *ptnf_out = ptnf;
+    return check_flag(ctx);
+}
+
+int mdet_tnf_ptnf_search(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double coverage,
+                         int mode, double* ptnf_out) {
+    if (!ctx || !ptnf_out) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!tnf || !log_size) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
+    cudaStream_t s = ctx->stream;
+    float* d_tnf = (float*)ctx_scratch(ctx, "io.gtnf", n * MDET_NTNF * 4);
+    double* d_ls = (double*)ctx_scratch(ctx, "io.gls", (n ? n : 1) * 8);
+    if (!d_tnf || !d_ls) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_tnf, tnf, n * MDET_NTNF * 4, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_ls, log_size, n * 8, cudaMemcpyHostToDevice, s));
+    return mdet_tnf_ptnf_search_dev(ctx, d_tnf, d_ls, n, coverage, mode, ptnf_out);
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// graph.cuh -- internals shared by the pairwise-stage kernels.
+#pragma once
+
+#include "common.cuh"
+
+#define MDET_KPAD 144     // BF16 row length: 136 features + 8 zeros (9 x 16)
+#define MDET_TBL 256      // threshold table cells per axis
+#define MDET_TBL_LEVELS 9 // sparse-table levels (2^8 = 256)
+#define MDET_BLK 128      // rows per metadata block
+
+// Per 128-row block of the length-sorted order.
+struct BlockMeta {
+    float lo, hi;  // log10 size range
+    float emax;    // max rounding error ||x~ - x|| of the block's reduced-precision rows
+    float nmax;    // max norm of the block's centred reduced-precision rows
+};
+
+// Conservative upper bound of d*(x, y) over boxes of log sizes: a
+// 256 x 256 cell table over [lmin, lmax] with a sparse table along y.
+struct DstarTable {
+    const float* st;  // [levels][TBL][TBL]
+    float lmin, inv_h;
+};
+
+// Pairs handed from the distance filter to the exact stage.
+struct CandBuf {
+    uint2* cand;                 // (row, col) in the filter's index spaces
+    unsigned long long* count;   // total found (may exceed cap: then rerun bigger)
+    unsigned long long cap;
+};
+
+// Model parts of one contig: F_m(x) and G_m(y) for m in {b1, c1, b2, c2}.
+struct ModelParts {
+    double f[4];
+    double g[4];
+};
+
+struct ModelH {
+    double h[4][6];  // H_m(t) coefficients t^1..t^5 (index 0 unused)
+};
+
+__device__ __forceinline__ int tbl_cell_lo(float v, const DstarTable& t) {
+    int c = (int)floorf((v - t.lmin) * t.inv_h - 1e-3f);
+    return c < 0 ? 0 : (c >= MDET_TBL ? MDET_TBL - 1 : c);
+}
+__device__ __forceinline__ int tbl_cell_hi(float v, const DstarTable& t) {
+    int c = (int)floorf((v - t.lmin) * t.inv_h + 1e-3f);
+    return c < 0 ? 0 : (c >= MDET_TBL ? MDET_TBL - 1 : c);
+}
+
+// Largest d* over all pairs whose sizes come from blocks with log-size
+// ranges [alo, ahi] and [blo, bhi].
+__device__ __forceinline__ float tile_dstar(const DstarTable& t, float alo, float ahi, float blo, float bhi) {
+    float xlo = fminf(alo, blo), xhi = fminf(ahi, bhi);
+    float ylo = fmaxf(alo, blo), yhi = fmaxf(ahi, bhi);
+    int cx0 = tbl_cell_lo(xlo, t), cx1 = tbl_cell_hi(xhi, t);
+    int cy0 = tbl_cell_lo(ylo, t), cy1 = tbl_cell_hi(yhi, t);
+    int span = cy1 - cy0 + 1;
+    int k = 31 - __clz(span);
+    const float* lvl = t.st + (size_t)k * MDET_TBL * MDET_TBL;
+    float m = 0.f;
+    for (int a = cx0; a <= cx1; ++a) {
+        float v0 = __ldg(lvl + a * MDET_TBL + cy0);
+        float v1 = __ldg(lvl + a * MDET_TBL + (cy1 - (1 << k) + 1));
+        m = fmaxf(m, fmaxf(v0, v1));
+    }
+    return m;
+}
+
+// Host-side entry points of the stages (graph_*.cu).
+struct GraphPrep {
+    uint32_t n, npad;                // contigs, rows padded to 256
+    uint32_t* perm;                  // sorted position -> original index
+    uint32_t* inv;                   // original index -> sorted position
+    float* x32;                      // sorted FP32 TNF rows [n][136]
+    double* ls;                      // sorted log sizes
+    ModelParts* parts;               // sorted model parts
+    uint16_t* xb;                    // sorted centred BF16 rows [npad][144]
+    float* nsq;                      // ||x~||^2 per sorted row (inf for padding rows)
+    BlockMeta* meta;                 // per 128-row block (bf16 rounding)
+    BlockMeta* meta32;               // per 128-row block (no rounding term)
+    float* mu;                       // column means [136]
+};
+
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out);
+int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out);
+ModelH model_h();
+
+// Above-cutoff pair found by the exact stage (sorted positions).
+struct Edge {
+    uint32_t i, j;
+    double sim;
+};
+
+// One entry of a contig's edge list.
+struct Ent {
+    double sim;
+    uint32_t ocol;  // original column index
+    uint32_t pad;
+};
+
+int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ameta, const float* b, uint32_t nb,
+                const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out);
+// Tensor-core filter over centred BF16 rows (a: na rows, b: nb rows, both
+// padded to 256 with zero rows and nsq = +inf).
+int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+              const uint16_t* b, const float* b_nsq, uint32_t nb, const BlockMeta* bmeta, bool triangular,
+              const DstarTable& tbl, CandBuf out);
+int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
+                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out);
+int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
+                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out);
+int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
+                uint32_t max_edges, uint64_t* n_out);
+int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
+              double* d_stnf, uint64_t total);

@@ -1,0 +1,480 @@
+// graph_exact.cu -- exact scoring of filtered pairs and per-contig top-k.
+//
+// Every pair that passed a distance filter is scored again from the FP32
+// TNF rows: the reference's terms float((a_k - b_k)^2) (cuda/Cuda2.cu:194-196)
+// summed in four FP32 partial sums combined in FP64, sqrt in FP64, then the
+// MetaBAT2 logistic model in FP64 (cuda/Cuda2.cu:199-240) from per-contig
+// parts F(x), G(y) and the pair term H(x*y).  A pair is an edge when its
+// pre-probability beats logit(cutoff) (cuda/Cuda2.cu:257-260); its score is
+// sigmoid(pre).  Edges are then grouped per contig (both directions), each
+// contig keeps its best max_edges by (score desc, original column asc), and
+// (i, j) is emitted for i < j in original indices (cuda/Cuda2.cu:921-946).
+#include <cub/cub.cuh>
+
+#include "graph.cuh"
+
+namespace {
+
+constexpr double kLn9 = 2.1972245773362196;
+
+__device__ __forceinline__ double horner_h(const double* h, double t) {
+    return t * fma(t, fma(t, fma(t, fma(t, h[5], h[4]), h[3]), h[2]), h[1]);
+}
+
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dkey_inv(unsigned long long k) {
+    unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// d in the reference's terms: float((a-b)^2), FP32 partial sums, FP64 total.
+__device__ __forceinline__ double exact_dist(const float* __restrict__ a, const float* __restrict__ b) {
+    const float4* ra = reinterpret_cast<const float4*>(a);
+    const float4* rb = reinterpret_cast<const float4*>(b);
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 2
+    for (int q = 0; q < MDET_NTNF / 4; ++q) {
+        float4 x = __ldg(ra + q), y = __ldg(rb + q);
+        float d0 = __fsub_rn(x.x, y.x), d1 = __fsub_rn(x.y, y.y), d2 = __fsub_rn(x.z, y.z), d3 = __fsub_rn(x.w, y.w);
+        s0 = __fadd_rn(s0, __fmul_rn(d0, d0));
+        s1 = __fadd_rn(s1, __fmul_rn(d1, d1));
+        s2 = __fadd_rn(s2, __fmul_rn(d2, d2));
+        s3 = __fadd_rn(s3, __fmul_rn(d3, d3));
+    }
+    return sqrt(((double)s0 + (double)s1) + ((double)s2 + (double)s3));
+}
+
+// pre-probability of sorted contigs i, j at distance d.  need_model2: also
+// evaluate the second model when the first is at or below log(9).
+__device__ __forceinline__ double pre_prob(const ModelParts& pi, const ModelParts& pj, double li, double lj, double d,
+                                           const ModelH& H, bool need_model2) {
+    const bool imin = li <= lj;
+    const ModelParts& pmin = imin ? pi : pj;
+    const ModelParts& pmax = imin ? pj : pi;
+    const double t = li * lj;
+    double b = pmin.f[0] + pmax.g[0] + horner_h(H.h[0], t);
+    double c = pmin.f[1] + pmax.g[1] + horner_h(H.h[1], t);
+    double pre = -(b + c * d);
+    if (pre <= kLn9) {
+        if (!need_model2) return pre;
+        b = pmin.f[2] + pmax.g[2] + horner_h(H.h[2], t);
+        c = pmin.f[3] + pmax.g[3] + horner_h(H.h[3], t);
+        pre = -(b + c * d);
+        if (pre > kLn9) pre = kLn9;
+    }
+    return pre;
+}
+
+struct ExactArgs {
+    const uint2* cand;
+    unsigned long long ncand;
+    const uint32_t* row_map;  // maxprob: sample slot -> sorted position; graph: null
+    const float* x32;
+    const double* ls;
+    const ModelParts* parts;
+    ModelH H;
+    double L;
+    // graph outputs
+    Edge* edges;
+    unsigned long long* nedges;
+    uint32_t* deg;
+    // maxprob output
+    unsigned long long* maxkey;
+};
+
+__global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
+    const bool model2 = p.L < kLn9;
+    const uint32_t lane = threadIdx.x & 31;
+    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < p.ncand;
+         base += (unsigned long long)gridDim.x * blockDim.x) {
+        unsigned long long idx = base + threadIdx.x;
+        bool edge = false;
+        uint32_t si = 0, sj = 0;
+        double sim = 0;
+        if (idx < p.ncand) {
+            uint2 c = p.cand[idx];
+            si = c.x;
+            sj = c.y;
+            double d = exact_dist(p.x32 + (uint64_t)si * MDET_NTNF, p.x32 + (uint64_t)sj * MDET_NTNF);
+            ModelParts pi = p.parts[si], pj = p.parts[sj];
+            double pre = pre_prob(pi, pj, p.ls[si], p.ls[sj], d, p.H, model2);
+            if (pre > p.L) {
+                edge = true;
+                sim = 1. - 1. / (1. + exp(pre));
+            }
+        }
+        uint32_t bal = __ballot_sync(0xffffffffu, edge);
+        if (bal) {
+            unsigned long long wb = 0;
+            int leader = __ffs(bal) - 1;
+            if (lane == (uint32_t)leader) wb = atomicAdd(p.nedges, (unsigned long long)__popc(bal));
+            wb = __shfl_sync(0xffffffffu, wb, leader);
+            if (edge) {
+                Edge e;
+                e.i = si;
+                e.j = sj;
+                e.sim = sim;
+                p.edges[wb + __popc(bal & ((1u << lane) - 1u))] = e;
+                atomicAdd(&p.deg[si], 1u);
+                atomicAdd(&p.deg[sj], 1u);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_exact_maxprob(ExactArgs p) {
+    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < p.ncand;
+         idx += (unsigned long long)gridDim.x * blockDim.x) {
+        uint2 c = p.cand[idx];
+        uint32_t si = p.row_map[c.x], sj = c.y;
+        if (si == sj) continue;  // the sampled contig itself
+        double d = exact_dist(p.x32 + (uint64_t)si * MDET_NTNF, p.x32 + (uint64_t)sj * MDET_NTNF);
+        ModelParts pi = p.parts[si], pj = p.parts[sj];
+        double pre = pre_prob(pi, pj, p.ls[si], p.ls[sj], d, p.H, true);
+        atomicMax(&p.maxkey[c.x], dkey(pre));
+    }
+}
+
+__global__ void k_scatter(const Edge* __restrict__ edges, unsigned long long ne, const uint32_t* __restrict__ perm,
+                          const unsigned long long* __restrict__ rowptr, uint32_t* __restrict__ cursor,
+                          Ent* __restrict__ list) {
+    for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        Edge ed = edges[e];
+        uint32_t a = atomicAdd(&cursor[ed.i], 1u);
+        uint32_t b = atomicAdd(&cursor[ed.j], 1u);
+        Ent x;
+        x.sim = ed.sim;
+        x.pad = 0;
+        x.ocol = perm[ed.j];
+        list[rowptr[ed.i] + a] = x;
+        x.ocol = perm[ed.i];
+        list[rowptr[ed.j] + b] = x;
+    }
+}
+
+__device__ __forceinline__ bool before(const Ent& a, const Ent& b) {
+    return a.sim > b.sim || (a.sim == b.sim && a.ocol < b.ocol);
+}
+
+constexpr int kWarpCap = 1024;
+constexpr int kTopkWarps = 4;
+
+// Warp per contig (sorted position s) with at most 1024 edges: bitonic sort
+// in shared memory, keep the best max_edges in place.
+__global__ void __launch_bounds__(kTopkWarps * 32) k_topk_warp(
+    const unsigned long long* __restrict__ rowptr, const uint32_t* __restrict__ deg, const uint32_t* __restrict__ perm,
+    uint32_t n, uint32_t max_edges, Ent* __restrict__ list, uint32_t* __restrict__ out_cnt,
+    uint32_t* __restrict__ big, unsigned int* __restrict__ nbig) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Ent* e = reinterpret_cast<Ent*>(sm) + (size_t)w * kWarpCap;
+    for (uint32_t s = blockIdx.x * kTopkWarps + w; s < n; s += gridDim.x * kTopkWarps) {
+        const uint32_t cnt = deg[s];
+        const uint32_t orow = perm[s];
+        if (cnt > kWarpCap) {
+            if (lane == 0) big[atomicAdd(nbig, 1u)] = s;
+            continue;
+        }
+        Ent* row = list + rowptr[s];
+        uint32_t P = 1;
+        while (P < cnt) P <<= 1;
+        if (cnt > max_edges || cnt > 1) {
+            for (uint32_t i = lane; i < P; i += 32) {
+                if (i < cnt)
+                    e[i] = row[i];
+                else {
+                    e[i].sim = -1.0;
+                    e[i].ocol = 0xFFFFFFFFu;
+                }
+            }
+            __syncwarp();
+            for (uint32_t k = 2; k <= P; k <<= 1)
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t i = lane; i < P; i += 32) {
+                        uint32_t ixj = i ^ j;
+                        if (ixj > i) {
+                            Ent a = e[i], b = e[ixj];
+                            bool up = (i & k) == 0;
+                            if (up ? before(b, a) : before(a, b)) {
+                                e[i] = b;
+                                e[ixj] = a;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+        } else {
+            for (uint32_t i = lane; i < cnt; i += 32) e[i] = row[i];
+            __syncwarp();
+        }
+        const uint32_t keep = cnt < max_edges ? cnt : max_edges;
+        uint32_t c = 0;
+        for (uint32_t i = lane; i < keep; i += 32) {
+            row[i] = e[i];
+            c += e[i].ocol > orow;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if (lane == 0) out_cnt[orow] = c;
+        __syncwarp();
+    }
+}
+
+constexpr int kBigCap = 8192;
+
+// Block per contig with more than 1024 edges: repeated sort of the running
+// best plus the next chunk in a 8192-entry shared buffer.
+__global__ void __launch_bounds__(1024) k_topk_big(const uint32_t* __restrict__ big, const unsigned int* __restrict__ nbig,
+                                                   const unsigned long long* __restrict__ rowptr,
+                                                   const uint32_t* __restrict__ deg, const uint32_t* __restrict__ perm,
+                                                   uint32_t max_edges, Ent* __restrict__ list,
+                                                   uint32_t* __restrict__ out_cnt) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    Ent* e = reinterpret_cast<Ent*>(sm);
+    __shared__ uint32_t red;
+    const uint32_t nb = *nbig;
+    for (uint32_t bi = blockIdx.x; bi < nb; bi += gridDim.x) {
+        const uint32_t s = big[bi];
+        const uint32_t cnt = deg[s], orow = perm[s];
+        Ent* row = list + rowptr[s];
+        uint32_t kept = 0, base = 0;
+        while (base < cnt) {
+            uint32_t take = min((uint32_t)kBigCap - kept, cnt - base);
+            for (uint32_t i = threadIdx.x; i < (uint32_t)kBigCap - kept; i += blockDim.x) {
+                if (i < take)
+                    e[kept + i] = row[base + i];
+                else {
+                    e[kept + i].sim = -1.0;
+                    e[kept + i].ocol = 0xFFFFFFFFu;
+                }
+            }
+            __syncthreads();
+            for (uint32_t k = 2; k <= (uint32_t)kBigCap; k <<= 1)
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t i = threadIdx.x; i < (uint32_t)kBigCap; i += blockDim.x) {
+                        uint32_t ixj = i ^ j;
+                        if (ixj > i) {
+                            Ent a = e[i], b = e[ixj];
+                            bool up = (i & k) == 0;
+                            if (up ? before(b, a) : before(a, b)) {
+                                e[i] = b;
+                                e[ixj] = a;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            base += take;
+            kept = min(max_edges, kept + take);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) red = 0;
+        __syncthreads();
+        uint32_t c = 0;
+        for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+            row[i] = e[i];
+            c += e[i].ocol > orow;
+        }
+        atomicAdd(&red, c);
+        __syncthreads();
+        if (threadIdx.x == 0) out_cnt[orow] = red;
+        __syncthreads();
+    }
+}
+
+// Warp per original row: write its kept edges with ocol > row, in order.
+__global__ void k_emit(const uint32_t* __restrict__ inv, const unsigned long long* __restrict__ rowptr,
+                       const uint32_t* __restrict__ deg, const Ent* __restrict__ list,
+                       const unsigned long long* __restrict__ outptr, uint32_t n, uint32_t max_edges,
+                       uint64_t* __restrict__ from, uint64_t* __restrict__ to, double* __restrict__ stnf) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t o = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); o < n; o += gridDim.x * (blockDim.x / 32)) {
+        const uint32_t s = inv[o];
+        const uint32_t keep = min(deg[s], max_edges);
+        const Ent* row = list + rowptr[s];
+        unsigned long long pos = outptr[o];
+        for (uint32_t b = 0; b < keep; b += 32) {
+            uint32_t i = b + lane;
+            Ent x;
+            bool ok = false;
+            if (i < keep) {
+                x = row[i];
+                ok = x.ocol > o;
+            }
+            uint32_t bal = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                unsigned long long q = pos + __popc(bal & ((1u << lane) - 1u));
+                from[q] = o;
+                to[q] = x.ocol;
+                stnf[q] = x.sim;
+            }
+            pos += __popc(bal);
+        }
+    }
+}
+
+__global__ void k_maxprob_finish(const unsigned long long* __restrict__ maxkey, const uint32_t* __restrict__ slot_of,
+                                 uint64_t m, double* __restrict__ out) {
+    uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= m) return;
+    double pre = dkey_inv(maxkey[slot_of[b]]);
+    // the reference seeds its running max with DBL_MIN (cuda/Cuda2.cu:287)
+    const double dbl_min = 2.2250738585072014e-308;
+    if (!(pre > dbl_min)) pre = dbl_min;
+    out[b] = 1. - (1. / (1. + exp(pre)));
+}
+
+__global__ void k_widen(const uint32_t* __restrict__ src, uint64_t n, unsigned long long* __restrict__ dst) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+    if (i == n) dst[i] = 0;
+}
+
+__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ host side --
+
+int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
+                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out) {
+    cudaStream_t s = ctx->stream;
+    Edge* edges = (Edge*)ctx_scratch(ctx, "ex.edges", (ncand ? ncand : 1) * sizeof(Edge));
+    unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "ex.cnt", 8);
+    uint32_t* deg = (uint32_t*)ctx_scratch(ctx, "ex.deg", (uint64_t)g.n * 4);
+    if (!edges || !cnt || !deg) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (uint64_t)g.n * 4, s));
+    if (ncand) {
+        ExactArgs p;
+        memset(&p, 0, sizeof(p));
+        p.cand = cand;
+        p.ncand = ncand;
+        p.x32 = g.x32;
+        p.ls = g.ls;
+        p.parts = g.parts;
+        p.H = model_h();
+        p.L = L;
+        p.edges = edges;
+        p.nedges = cnt;
+        p.deg = deg;
+        unsigned long long blocks = (ncand + 255) / 256;
+        unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
+        k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
+        MDET_LAUNCHED(ctx, "k_exact_graph");
+    }
+    MDET_CUDA(ctx, cudaMemcpyAsync(nedges_out, cnt, 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    *edges_out = edges;
+    *deg_out = deg;
+    return MDET_OK;
+}
+
+int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
+                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out) {
+    cudaStream_t s = ctx->stream;
+    unsigned long long* maxkey = (unsigned long long*)ctx_scratch(ctx, "mp.maxkey", (m ? m : 1) * 8);
+    if (!maxkey) return MDET_ERR_NOMEM;
+    k_fill_u64<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(maxkey, m, 0ull);
+    MDET_LAUNCHED(ctx, "k_fill_u64");
+    if (ncand) {
+        ExactArgs p;
+        memset(&p, 0, sizeof(p));
+        p.cand = cand;
+        p.ncand = ncand;
+        p.row_map = row_map;
+        p.x32 = g.x32;
+        p.ls = g.ls;
+        p.parts = g.parts;
+        p.H = model_h();
+        p.maxkey = maxkey;
+        unsigned long long blocks = (ncand + 255) / 256;
+        unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
+        k_exact_maxprob<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
+        MDET_LAUNCHED(ctx, "k_exact_maxprob");
+    }
+    k_maxprob_finish<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(maxkey, slot_of, m, d_out);
+    MDET_LAUNCHED(ctx, "k_maxprob_finish");
+    return MDET_OK;
+}
+
+int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
+                uint32_t max_edges, uint64_t* n_out) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = g.n;
+    unsigned long long* rowptr = (unsigned long long*)ctx_scratch(ctx, "tk.rowptr", ((uint64_t)n + 1) * 8);
+    uint32_t* cursor = (uint32_t*)ctx_scratch(ctx, "tk.cursor", (uint64_t)n * 4);
+    Ent* list = (Ent*)ctx_scratch(ctx, "tk.list", (ne ? 2 * ne : 1) * sizeof(Ent));
+    uint32_t* out_cnt = (uint32_t*)ctx_scratch(ctx, "tk.outcnt", (uint64_t)n * 4);
+    unsigned long long* outptr = (unsigned long long*)ctx_scratch(ctx, "tk.outptr", ((uint64_t)n + 1) * 8);
+    uint32_t* big = (uint32_t*)ctx_scratch(ctx, "tk.big", (uint64_t)n * 4);
+    unsigned int* nbig = (unsigned int*)ctx_scratch(ctx, "tk.nbig", 8);
+    if (!rowptr || !cursor || !list || !out_cnt || !outptr || !big || !nbig) return MDET_ERR_NOMEM;
+    // 64-bit scans: widen the per-row counts (plus a trailing zero) first
+    unsigned long long* w64 = (unsigned long long*)ctx_scratch(ctx, "tk.w64", ((uint64_t)n + 1) * 8);
+    if (!w64) return MDET_ERR_NOMEM;
+    size_t tb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, tb, w64, rowptr, (int)n + 1, s);
+    void* tmp = ctx_scratch(ctx, "tk.cubtmp", tb);
+    if (!tmp) return MDET_ERR_NOMEM;
+    const unsigned wblocks = (unsigned)(((uint64_t)n + 1 + 255) / 256);
+    k_widen<<<wblocks, 256, 0, s>>>(deg, n, w64);
+    MDET_LAUNCHED(ctx, "k_widen");
+    MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, w64, rowptr, (int)n + 1, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(cursor, 0, (uint64_t)n * 4, s));
+    if (ne) {
+        unsigned long long blocks = (ne + 255) / 256, cap = (unsigned long long)ctx->num_sms * 16;
+        k_scatter<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(edges, ne, g.perm, rowptr, cursor, list);
+        MDET_LAUNCHED(ctx, "k_scatter");
+    }
+    MDET_CUDA(ctx, cudaMemsetAsync(nbig, 0, 4, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(out_cnt, 0, (uint64_t)n * 4, s));
+    {
+        size_t dyn = (size_t)kTopkWarps * kWarpCap * sizeof(Ent);
+        static bool set[64] = {false};
+        if (!set[ctx->device & 63]) {
+            MDET_CUDA(ctx, cudaFuncSetAttribute(k_topk_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+            MDET_CUDA(ctx, cudaFuncSetAttribute(k_topk_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)(kBigCap * sizeof(Ent))));
+            set[ctx->device & 63] = true;
+        }
+        unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + kTopkWarps - 1) / kTopkWarps,
+                                                       (uint64_t)ctx->num_sms * 32);
+        k_topk_warp<<<blocks, kTopkWarps * 32, dyn, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt, big, nbig);
+        MDET_LAUNCHED(ctx, "k_topk_warp");
+        k_topk_big<<<ctx->num_sms, 1024, kBigCap * sizeof(Ent), s>>>(big, nbig, rowptr, deg, g.perm, max_edges, list,
+                                                                    out_cnt);
+        MDET_LAUNCHED(ctx, "k_topk_big");
+    }
+    k_widen<<<wblocks, 256, 0, s>>>(out_cnt, n, w64);
+    MDET_LAUNCHED(ctx, "k_widen");
+    MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, w64, outptr, (int)n + 1, s));
+    unsigned long long total = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&total, outptr + n, 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    *n_out = total;
+    return MDET_OK;
+}
+
+int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
+              double* d_stnf, uint64_t total) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = g.n;
+    const unsigned long long* rowptr = (const unsigned long long*)ctx->bufs["tk.rowptr"].p;
+    const unsigned long long* outptr = (const unsigned long long*)ctx->bufs["tk.outptr"].p;
+    const Ent* list = (const Ent*)ctx->bufs["tk.list"].p;
+    const uint32_t* deg = (const uint32_t*)ctx->bufs["ex.deg"].p;
+    if (total) {
+        unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + 7) / 8, (uint64_t)ctx->num_sms * 32);
+        k_emit<<<blocks, 256, 0, s>>>(g.inv, rowptr, deg, list, outptr, n, max_edges, d_from, d_to, d_stnf);
+        MDET_LAUNCHED(ctx, "k_emit");
+    }
+    return MDET_OK;
+}

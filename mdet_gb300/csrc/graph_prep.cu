@@ -1,0 +1,303 @@
+// graph_prep.cu -- per-call preparation of the pairwise stage.
+//
+// Contigs are put in ascending log-size order (stable, by original index on
+// ties) so that every tile of the pairwise schedule covers a narrow range of
+// sizes; the size-dependent distance threshold d*(x, y) of the MetaBAT2
+// model (cuda/Cuda2.cu:199-240 solved for d) is then nearly constant over a
+// tile and one conservative bound per tile filters its pairs.  This file
+// builds: the permutation, sorted FP32 rows and log sizes, the per-contig
+// FP64 model parts used by the exact stage, the centred BF16 rows with their
+// norms and rounding errors for the tensor-core filter, per-block metadata,
+// and the d* table.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <cstring>
+
+#include "graph.cuh"
+
+namespace {
+
+__device__ __forceinline__ unsigned long long dkey(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_keys(const double* __restrict__ ls, uint64_t n, unsigned long long* __restrict__ keys,
+                       uint32_t* __restrict__ vals) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = dkey(ls[i]);
+    vals[i] = (uint32_t)i;
+}
+
+__device__ __forceinline__ double poly(const double* c, int deg, double v) {
+    double r = c[deg];
+    for (int k = deg - 1; k >= 0; --k) r = fma(r, v, c[k]);
+    return r;
+}
+
+__global__ void k_gather(const float* __restrict__ tnf, const double* __restrict__ ls, const uint32_t* __restrict__ perm,
+                         uint64_t n, uint32_t* __restrict__ inv, float* __restrict__ x32, double* __restrict__ ls_s,
+                         ModelParts* __restrict__ parts, ModelSplit ms) {
+    uint64_t s = blockIdx.x;
+    if (s >= n) return;
+    uint32_t o = perm[s];
+    const float* src = tnf + (uint64_t)o * MDET_NTNF;
+    float* dst = x32 + s * MDET_NTNF;
+    for (int k = threadIdx.x; k < MDET_NTNF; k += blockDim.x) dst[k] = src[k];
+    if (threadIdx.x == 0) {
+        inv[o] = (uint32_t)s;
+        double v = ls[o];
+        ls_s[s] = v;
+        ModelParts p;
+        for (int m = 0; m < 4; ++m) {
+            p.f[m] = poly(ms.F[m], 7, v);
+            double g[7] = {0, ms.G[m][1], ms.G[m][2], ms.G[m][3], ms.G[m][4], ms.G[m][5], ms.G[m][6]};
+            p.g[m] = poly(g, 6, v);
+        }
+        parts[s] = p;
+    }
+}
+
+__global__ void k_colsum(const float* __restrict__ x32, uint64_t n, double* __restrict__ sums) {
+    // block: 136 threads (one per column), rows strided over the grid
+    int k = threadIdx.x;
+    if (k >= MDET_NTNF) return;
+    double acc = 0;
+    for (uint64_t s = blockIdx.x; s < n; s += gridDim.x) acc += x32[s * MDET_NTNF + k];
+    atomicAdd(&sums[k], acc);
+}
+
+__global__ void k_mean(const double* __restrict__ sums, uint64_t n, float* __restrict__ mu) {
+    int k = threadIdx.x;
+    if (k < MDET_NTNF) mu[k] = (float)(sums[k] / (double)n);
+}
+
+// Warp per sorted row: centred BF16 copy, its squared norm and its exact
+// distance to the unrounded centred row.
+__global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ mu, uint64_t n, uint64_t npad,
+                       uint16_t* __restrict__ xb, float* __restrict__ nsq, float* __restrict__ err,
+                       float* __restrict__ nrm) {
+    uint64_t s = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    uint32_t lane = threadIdx.x & 31;
+    if (s >= npad) return;
+    uint16_t* row = xb + s * MDET_KPAD;
+    if (s >= n) {
+        for (int k = lane; k < MDET_KPAD; k += 32) row[k] = 0;
+        if (lane == 0) {
+            nsq[s] = __int_as_float(0x7f800000);
+            err[s] = 0.f;
+            nrm[s] = 0.f;
+        }
+        return;
+    }
+    double e2 = 0, q = 0;
+    for (int k = lane; k < MDET_KPAD; k += 32) {
+        uint16_t b = 0;
+        if (k < MDET_NTNF) {
+            float a = x32[s * MDET_NTNF + k];
+            float v = a - mu[k];
+            __nv_bfloat16 h = __float2bfloat16_rn(v);
+            b = *reinterpret_cast<uint16_t*>(&h);
+            double hv = (double)__bfloat162float(h);
+            double ex = (double)a - (double)mu[k];
+            e2 += (hv - ex) * (hv - ex);
+            q += hv * hv;
+        }
+        row[k] = b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        q += __shfl_xor_sync(0xffffffffu, q, o);
+    }
+    if (lane == 0) {
+        nsq[s] = (float)q;
+        err[s] = __double2float_ru(sqrt(e2));
+        nrm[s] = __double2float_ru(sqrt(q));
+    }
+}
+
+__global__ void k_meta(const double* __restrict__ ls_s, const float* __restrict__ err, const float* __restrict__ nrm,
+                       uint64_t n, uint64_t nblk, BlockMeta* __restrict__ meta, BlockMeta* __restrict__ meta32) {
+    uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= nblk) return;
+    uint64_t s0 = b * MDET_BLK, s1 = min(n, s0 + MDET_BLK);
+    BlockMeta m;
+    if (s0 >= n) {
+        m.lo = m.hi = (float)ls_s[n - 1];
+        m.emax = m.nmax = 0.f;
+    } else {
+        m.lo = __double2float_rd(ls_s[s0]);
+        m.hi = __double2float_ru(ls_s[s1 - 1]);
+        float e = 0.f, nm = 0.f;
+        if (err)
+            for (uint64_t s = s0; s < s1; ++s) {
+                e = fmaxf(e, err[s]);
+                nm = fmaxf(nm, nrm[s]);
+            }
+        m.emax = e;
+        m.nmax = nm;
+    }
+    if (meta) meta[b] = m;
+    BlockMeta m32 = m;
+    m32.emax = 0.f;
+    m32.nmax = 0.f;
+    meta32[b] = m32;
+}
+
+// ---- d* table ----
+
+__device__ double dev_dstar(double x, double y, double L, const ModelSplit& ms) {
+    const double ln9 = 2.1972245773362196;
+    double t = x * y, c[4];
+    for (int m = 0; m < 4; ++m) {
+        double g[7] = {0, ms.G[m][1], ms.G[m][2], ms.G[m][3], ms.G[m][4], ms.G[m][5], ms.G[m][6]};
+        double h[6] = {0, ms.H[m][1], ms.H[m][2], ms.H[m][3], ms.H[m][4], ms.H[m][5]};
+        c[m] = poly(ms.F[m], 7, x) + poly(g, 6, y) + poly(h, 5, t);
+    }
+    const double inf = __longlong_as_double(0x7ff0000000000000ll);
+    if (!(c[1] > 0)) return inf;
+    if (L >= ln9) return (-L - c[0]) / c[1];
+    if (!(c[3] > 0)) return inf;
+    double d1 = (-ln9 - c[0]) / c[1];
+    double d2 = (-L - c[2]) / c[3];
+    return d1 > d2 ? d1 : d2;
+}
+
+constexpr int kPts = 4 * MDET_TBL + 1;
+
+__global__ void k_dstar_points(double lmin, double h, double L, ModelSplit ms, float* __restrict__ pts) {
+    int a = blockIdx.y, b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= kPts) return;
+    int lo = min(a, b), hi = max(a, b);
+    double x = lmin + lo * (h / 4), y = lmin + hi * (h / 4);
+    double d = dev_dstar(x, y, L, ms);
+    pts[a * kPts + b] = __double2float_ru(d);
+}
+
+__global__ void k_dstar_cells(const float* __restrict__ pts, float* __restrict__ st0) {
+    int a = blockIdx.x, b = threadIdx.x;
+    float mx = -__int_as_float(0x7f800000), mn = __int_as_float(0x7f800000);
+    for (int i = 0; i <= 4; ++i)
+        for (int j = 0; j <= 4; ++j) {
+            float v = pts[(4 * a + i) * kPts + (4 * b + j)];
+            mx = fmaxf(mx, v);
+            mn = fminf(mn, v);
+        }
+    float T = mx + 0.5f * (mx - mn) + 1e-6f + 1e-5f * fabsf(mx);
+    if (isinf(mx) || isnan(mx)) T = __int_as_float(0x7f800000);
+    st0[a * MDET_TBL + b] = T;
+}
+
+__global__ void k_sparse(float* __restrict__ st, int k) {
+    int a = blockIdx.x, b = threadIdx.x;
+    const float* prev = st + (size_t)(k - 1) * MDET_TBL * MDET_TBL;
+    float* cur = st + (size_t)k * MDET_TBL * MDET_TBL;
+    int b2 = min(b + (1 << (k - 1)), MDET_TBL - 1);
+    cur[a * MDET_TBL + b] = fmaxf(prev[a * MDET_TBL + b], prev[a * MDET_TBL + b2]);
+}
+
+__global__ void k_minmax(const double* __restrict__ ls_s, uint64_t n, double* __restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        out[0] = ls_s[0];
+        out[1] = ls_s[n - 1];
+    }
+}
+
+}  // namespace
+
+ModelH model_h() {
+    ModelH h;
+    const ModelSplit& s = model_split();
+    for (int m = 0; m < 4; ++m)
+        for (int k = 0; k < 6; ++k) h.h[m][k] = s.H[m][k];
+    return h;
+}
+
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g) {
+    cudaStream_t s = ctx->stream;
+    g->n = (uint32_t)n;
+    g->npad = (uint32_t)((n + 255) / 256 * 256);
+    const uint64_t npad = g->npad;
+    unsigned long long* keys = (unsigned long long*)ctx_scratch(ctx, "pre.keys", n * 8);
+    unsigned long long* keys2 = (unsigned long long*)ctx_scratch(ctx, "pre.keys2", n * 8);
+    uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "pre.vals", n * 4);
+    g->perm = (uint32_t*)ctx_scratch(ctx, "pre.perm", n * 4);
+    g->inv = (uint32_t*)ctx_scratch(ctx, "pre.inv", n * 4);
+    g->x32 = (float*)ctx_scratch(ctx, "pre.x32", n * MDET_NTNF * 4);
+    g->ls = (double*)ctx_scratch(ctx, "pre.ls", n * 8);
+    g->parts = (ModelParts*)ctx_scratch(ctx, "pre.parts", n * sizeof(ModelParts));
+    uint64_t nblk = npad / MDET_BLK;
+    g->meta32 = (BlockMeta*)ctx_scratch(ctx, "pre.meta32", nblk * sizeof(BlockMeta));
+    g->mu = (float*)ctx_scratch(ctx, "pre.mu", MDET_NTNF * 4);
+    double* sums = (double*)ctx_scratch(ctx, "pre.sums", MDET_NTNF * 8);
+    if (!keys || !keys2 || !vals || !g->perm || !g->inv || !g->x32 || !g->ls || !g->parts || !g->meta32 || !g->mu ||
+        !sums)
+        return MDET_ERR_NOMEM;
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    k_keys<<<blocks, 256, 0, s>>>(d_ls, n, keys, vals);
+    MDET_LAUNCHED(ctx, "k_keys");
+    size_t tmpb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s);
+    void* tmp = ctx_scratch(ctx, "pre.cubtmp", tmpb);
+    if (!tmp) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s));
+    k_gather<<<(unsigned)n, 64, 0, s>>>(d_tnf, d_ls, g->perm, n, g->inv, g->x32, g->ls, g->parts, model_split());
+    MDET_LAUNCHED(ctx, "k_gather");
+    g->xb = nullptr;
+    g->nsq = nullptr;
+    g->meta = nullptr;
+    float* err = nullptr;
+    float* nrm = nullptr;
+    if (need_bf16) {
+        MDET_CUDA(ctx, cudaMemsetAsync(sums, 0, MDET_NTNF * 8, s));
+        k_colsum<<<std::min<uint64_t>(1024, n), MDET_NTNF, 0, s>>>(g->x32, n, sums);
+        MDET_LAUNCHED(ctx, "k_colsum");
+        k_mean<<<1, MDET_NTNF, 0, s>>>(sums, n, g->mu);
+        MDET_LAUNCHED(ctx, "k_mean");
+        g->xb = (uint16_t*)ctx_scratch(ctx, "pre.xb", npad * MDET_KPAD * 2);
+        g->nsq = (float*)ctx_scratch(ctx, "pre.nsq", npad * 4);
+        err = (float*)ctx_scratch(ctx, "pre.err", npad * 4);
+        nrm = (float*)ctx_scratch(ctx, "pre.nrm", npad * 4);
+        g->meta = (BlockMeta*)ctx_scratch(ctx, "pre.meta", nblk * sizeof(BlockMeta));
+        if (!g->xb || !g->nsq || !err || !nrm || !g->meta) return MDET_ERR_NOMEM;
+        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(g->x32, g->mu, n, npad, g->xb, g->nsq, err, nrm);
+        MDET_LAUNCHED(ctx, "k_bf16");
+    }
+    k_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(g->ls, err, nrm, n, nblk, g->meta, g->meta32);
+    MDET_LAUNCHED(ctx, "k_meta");
+    return MDET_OK;
+}
+
+int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out) {
+    cudaStream_t s = ctx->stream;
+    double* mm = (double*)ctx_scratch(ctx, "tbl.mm", 16);
+    float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
+    float* st = (float*)ctx_scratch(ctx, "tbl.st", (size_t)MDET_TBL_LEVELS * MDET_TBL * MDET_TBL * 4);
+    if (!mm || !pts || !st) return MDET_ERR_NOMEM;
+    // the range is needed on the host to place the grid
+    double range[2];
+    k_minmax<<<1, 32, 0, s>>>(d_ls_sorted, n, mm);
+    MDET_LAUNCHED(ctx, "k_minmax");
+    MDET_CUDA(ctx, cudaMemcpyAsync(range, mm, 16, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    double lmin = range[0], lmax = range[1];
+    double h = (lmax - lmin) / MDET_TBL;
+    if (!(h > 1e-7)) h = 1e-7;
+    lmin -= 1e-9;
+    dim3 grid((kPts + 127) / 128, kPts);
+    k_dstar_points<<<grid, 128, 0, s>>>(lmin, h, logit_cut, model_split(), pts);
+    MDET_LAUNCHED(ctx, "k_dstar_points");
+    k_dstar_cells<<<MDET_TBL, MDET_TBL, 0, s>>>(pts, st);
+    MDET_LAUNCHED(ctx, "k_dstar_cells");
+    for (int k = 1; k < MDET_TBL_LEVELS; ++k) {
+        k_sparse<<<MDET_TBL, MDET_TBL, 0, s>>>(st, k);
+        MDET_LAUNCHED(ctx, "k_sparse");
+    }
+    out->st = st;
+    out->lmin = (float)lmin;
+    out->inv_h = (float)(1.0 / h);
+    return MDET_OK;
+}

@@ -1,0 +1,233 @@
+"""Python host mirror of the reference's TNF-path interface over the C ABI.
+
+The reference (cuda/Cuda2.cu) exposes its TNF path as free functions over
+globals; this module gives the same operations as methods of a Context that
+owns device memory, with the reference's names kept as aliases:
+
+  calc_tnf            TNF loop of main            (cuda/Cuda2.cu:1825-1863)
+  max_prob_sample     launch_tnf_max_prob_sample_kernel_multi (356-379)
+  gen_tnf_graph_sample  pTNF search + driver    (972-1025, 1883-1904)
+  gen_tnf_graph       gen_tnf_graph             (861-970)
+
+Every call goes through libmdet_tnf.so (include/mdet_tnf.h).  There is no
+CPU fallback: if the library is missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libmdet_tnf.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_CAPACITY, ERR_TIMEOUT, ERR_UNSUPPORTED = range(7)
+MODES = {"plain": 0, "bf16": 1, "tf32": 2, "learned": 3}
+
+u64 = ctypes.c_uint64
+u32 = ctypes.c_uint32
+P = ctypes.c_void_p
+D = ctypes.c_double
+
+
+class GraphStats(ctypes.Structure):
+    _fields_ = [
+        ("n_candidates", u64),
+        ("n_above_cutoff", u64),
+        ("n_edges", u64),
+        ("tiles_total", u64),
+        ("tiles_computed", u64),
+        ("gpu_launches", u32),
+        ("reserved", u32),
+        ("ms_prep", D),
+        ("ms_filter", D),
+        ("ms_exact", D),
+        ("ms_select", D),
+        ("ms_total", D),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+# (name, restype, argtypes) of every entry point in include/mdet_tnf.h
+SIGNATURES = [
+    ("mdet_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
+    ("mdet_ctx_destroy", ctypes.c_int, [P]),
+    ("mdet_last_error", ctypes.c_char_p, [P]),
+    ("mdet_ctx_set_stream", ctypes.c_int, [P, P]),
+    ("mdet_version", ctypes.c_char_p, []),
+    ("mdet_tnf_count", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
+    ("mdet_tnf_count_dev", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
+    ("mdet_tnf_max_prob", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
+    ("mdet_tnf_max_prob_dev", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
+    ("mdet_tnf_ptnf_search", ctypes.c_int, [P, P, P, u64, D, ctypes.c_int, ctypes.POINTER(D)]),
+    ("mdet_tnf_ptnf_search_dev", ctypes.c_int, [P, P, P, u64, D, ctypes.c_int, ctypes.POINTER(D)]),
+    ("mdet_tnf_graph", ctypes.c_int,
+     [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
+    ("mdet_tnf_graph_dev", ctypes.c_int,
+     [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
+]
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libmdet_tnf.so (raises OSError if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or _LIB_PATH
+    if not os.path.exists(p):
+        raise OSError(f"{p} not found: build the CUDA extension first (python -m mdet_gb300.build)")
+    lib = ctypes.CDLL(p)
+    for name, res, args in SIGNATURES:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class MdetError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[mdet status {code}] {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+@dataclass
+class Graph:
+    """Edge list of the TNF graph (the reference's Graph from/to/sTNF)."""
+    n: int
+    from_: np.ndarray
+    to: np.ndarray
+    sTNF: np.ndarray
+    stats: dict
+
+    def getEdgeCount(self) -> int:
+        return int(self.from_.size)
+
+
+class Context:
+    """Owns a device, a CUDA stream and scratch memory (mdet_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = P()
+        rc = self.lib.mdet_ctx_create(device, ctypes.byref(h))
+        if rc != OK:
+            raise MdetError(rc, f"mdet_ctx_create(device={device}) failed")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mdet_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != OK:
+            raise MdetError(rc, self.lib.mdet_last_error(self.h).decode())
+
+    def set_stream(self, stream_handle: int):
+        self._check(self.lib.mdet_ctx_set_stream(self.h, P(stream_handle)))
+
+    # ---- TNF counting -------------------------------------------------
+    def tnf_count(self, data: np.ndarray, seq_off: np.ndarray, seq_len: np.ndarray):
+        data = np.ascontiguousarray(data, dtype=np.uint8)
+        off = np.ascontiguousarray(seq_off, dtype=np.uint64)
+        ln = np.ascontiguousarray(seq_len, dtype=np.uint64)
+        n = off.size
+        counts = np.zeros((n, 136), np.uint32)
+        tnf = np.zeros((n, 136), np.float32)
+        self._check(self.lib.mdet_tnf_count(self.h, _ptr(data), data.size, _ptr(off), _ptr(ln), n, _ptr(counts),
+                                            _ptr(tnf)))
+        return counts, tnf
+
+    def tnf_count_dev(self, d_bytes: int, nbytes: int, d_off: int, d_len: int, n: int, d_counts: int, d_tnf: int):
+        self._check(self.lib.mdet_tnf_count_dev(self.h, P(d_bytes), nbytes, P(d_off), P(d_len), n, P(d_counts),
+                                                P(d_tnf)))
+
+    # ---- max-probability sample --------------------------------------
+    def max_prob(self, tnf, log_size, contigs, m=None, mode="bf16", floor_prob=0.7):
+        tnf = np.ascontiguousarray(tnf, dtype=np.float32)
+        ls = np.ascontiguousarray(log_size, dtype=np.float64)
+        c = np.ascontiguousarray(contigs, dtype=np.uint64)
+        n = tnf.shape[0]
+        m = c.size if m is None else m
+        out = np.zeros(m, np.float64)
+        self._check(self.lib.mdet_tnf_max_prob(self.h, _ptr(tnf), _ptr(ls), n, _ptr(c), m, MODES[mode],
+                                               float(floor_prob), _ptr(out)))
+        return out
+
+    def max_prob_dev(self, d_tnf, d_ls, n, d_contigs, m, mode, floor_prob, d_out):
+        self._check(self.lib.mdet_tnf_max_prob_dev(self.h, P(d_tnf), P(d_ls), n, P(d_contigs), m, MODES[mode],
+                                                   float(floor_prob), P(d_out)))
+
+    def ptnf_search(self, tnf, log_size, coverage: float = 0.95, mode: str = "bf16") -> float:
+        """pTNF in permille; consumes glibc rand() like the reference (seed it with srand)."""
+        tnf = np.ascontiguousarray(tnf, dtype=np.float32)
+        ls = np.ascontiguousarray(log_size, dtype=np.float64)
+        out = D()
+        self._check(self.lib.mdet_tnf_ptnf_search(self.h, _ptr(tnf), _ptr(ls), tnf.shape[0], coverage, MODES[mode],
+                                                  ctypes.byref(out)))
+        return out.value
+
+    def ptnf_search_dev(self, d_tnf: int, d_ls: int, n: int, coverage: float = 0.95, mode: str = "bf16") -> float:
+        out = D()
+        self._check(self.lib.mdet_tnf_ptnf_search_dev(self.h, P(d_tnf), P(d_ls), n, coverage, MODES[mode],
+                                                      ctypes.byref(out)))
+        return out.value
+
+    gen_tnf_graph_sample = ptnf_search
+
+    # ---- graph ----------------------------------------------------------
+    def tnf_graph(self, tnf, log_size, cutoff, max_edges=200, mode="bf16") -> Graph:
+        tnf = np.ascontiguousarray(tnf, dtype=np.float32)
+        ls = np.ascontiguousarray(log_size, dtype=np.float64)
+        n = tnf.shape[0]
+        cap = max(1, n * max_edges)
+        fr = np.empty(cap, np.uint64)
+        to = np.empty(cap, np.uint64)
+        st = np.empty(cap, np.float64)
+        ne = u64(0)
+        stats = GraphStats()
+        self._check(self.lib.mdet_tnf_graph(self.h, _ptr(tnf), _ptr(ls), n, float(cutoff), max_edges, MODES[mode],
+                                            _ptr(fr), _ptr(to), _ptr(st), cap, ctypes.byref(ne),
+                                            ctypes.byref(stats)))
+        k = ne.value
+        return Graph(n, fr[:k].copy(), to[:k].copy(), st[:k].copy(), stats.as_dict())
+
+    def tnf_graph_dev(self, d_tnf, d_ls, n, cutoff, max_edges, mode, d_from, d_to, d_stnf, capacity):
+        ne = u64(0)
+        stats = GraphStats()
+        self._check(self.lib.mdet_tnf_graph_dev(self.h, P(d_tnf), P(d_ls), n, float(cutoff), max_edges,
+                                                MODES[mode], P(d_from), P(d_to), P(d_stnf), capacity,
+                                                ctypes.byref(ne), ctypes.byref(stats)))
+        return ne.value, stats.as_dict()
+
+    # ---- reference-named aliases ----------------------------------------
+    calc_tnf = tnf_count
+    gen_tnf_graph = tnf_graph
+    max_prob_sample = max_prob
+
+
+def version() -> str:
+    return load_library().mdet_version().decode()

@@ -1,0 +1,145 @@
+"""ctypes view of the CPU oracle (oracle/tnf_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg -- never by the product.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_PROB = os.path.join(HERE, "_ref", "libref_prob.so")
+REF_TNF = os.path.join(HERE, "_ref", "omp_ex")
+
+P = ctypes.c_void_p
+u64 = ctypes.c_uint64
+D = ctypes.c_double
+_lib = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        L.orc_tn_order.restype = ctypes.c_char_p
+        L.orc_tnmap.argtypes = [P]
+        L.orc_base_code.argtypes = [P]
+        L.orc_tnf_count.argtypes = [P, P, P, u64, P, P, ctypes.c_int]
+        L.orc_tnf_normalize_f64.argtypes = [P, u64, P]
+        for f in ("orc_pre_prob", "orc_tnf_dist_cpu"):
+            getattr(L, f).restype = D
+            getattr(L, f).argtypes = [D, D, P, P]
+        L.orc_tnf_distance.restype = D
+        L.orc_tnf_distance.argtypes = [P, P]
+        L.orc_pre_prob_from_d.restype = D
+        L.orc_pre_prob_from_d.argtypes = [D, D, D]
+        L.orc_logit_cutoff.restype = D
+        L.orc_logit_cutoff.argtypes = [D]
+        L.orc_tnf_graph.restype = u64
+        L.orc_tnf_graph.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int]
+        L.orc_tnf_topk_rows.restype = u64
+        L.orc_tnf_topk_rows.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int]
+        L.orc_max_prob.argtypes = [P, P, u64, P, u64, P, ctypes.c_int]
+        L.orc_srand.argtypes = [ctypes.c_uint32]
+        L.orc_rand.restype = ctypes.c_int
+        L.orc_ptnf_search.restype = D
+        L.orc_ptnf_search.argtypes = [P, P, u64, D, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def tnmap():
+    m = np.zeros(256, np.uint8)
+    lib().orc_tnmap(_p(m))
+    return m
+
+
+def tn_order():
+    s = lib().orc_tn_order().decode()
+    return [s[4 * i:4 * i + 4] for i in range(136)]
+
+
+def tnf_count(data, off, ln, threads=0):
+    data = np.ascontiguousarray(data, np.uint8)
+    off = np.ascontiguousarray(off, np.uint64)
+    ln = np.ascontiguousarray(ln, np.uint64)
+    n = off.size
+    c = np.zeros((n, 136), np.uint32)
+    t = np.zeros((n, 136), np.float32)
+    lib().orc_tnf_count(_p(data), _p(off), _p(ln), n, _p(c), _p(t), threads)
+    return c, t
+
+
+def normalize_f64(counts):
+    counts = np.ascontiguousarray(counts, np.uint32)
+    out = np.zeros(counts.shape, np.float64)
+    lib().orc_tnf_normalize_f64(_p(counts), counts.shape[0], _p(out))
+    return out
+
+
+def pre_prob(r1, r2, a, b):
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    return lib().orc_pre_prob(r1, r2, _p(a), _p(b))
+
+
+def graph(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    n = tnf.shape[0]
+    row1 = n if row1 is None else row1
+    cap = max(1, (row1 - row0) * max_edges)
+    fr = np.zeros(cap, np.uint64)
+    to = np.zeros(cap, np.uint64)
+    st = np.zeros(cap, np.float64)
+    k = lib().orc_tnf_graph(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(fr), _p(to), _p(st), cap, threads)
+    return fr[:k], to[:k], st[:k]
+
+
+def topk_rows(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    n = tnf.shape[0]
+    row1 = n if row1 is None else row1
+    cap = max(1, (row1 - row0) * max_edges)
+    rp = np.zeros(row1 - row0 + 1, np.uint64)
+    cols = np.zeros(cap, np.uint64)
+    sims = np.zeros(cap, np.float64)
+    lib().orc_tnf_topk_rows(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(rp), _p(cols), _p(sims), cap,
+                            threads)
+    return rp, cols, sims
+
+
+def max_prob(tnf, ls, contigs, m, threads=0):
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    c = np.ascontiguousarray(contigs, np.uint64)
+    out = np.zeros(m, np.float64)
+    lib().orc_max_prob(_p(tnf), _p(ls), tnf.shape[0], _p(c), m, _p(out), threads)
+    return out
+
+
+def ptnf_search(tnf, ls, coverage=0.95, seed=1, threads=0):
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    lib().orc_srand(seed)
+    return lib().orc_ptnf_search(_p(tnf), _p(ls), tnf.shape[0], coverage, threads)
+
+
+def srand(seed):
+    lib().orc_srand(seed)

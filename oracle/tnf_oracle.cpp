@@ -1,0 +1,478 @@
+/*
+ * tnf_oracle.cpp -- CPU oracle for MdeT's MetaBAT2 TNF path.
+ *
+ * TEST INFRASTRUCTURE ONLY: loaded by tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py, never by the product.  It restates the
+ * reference's arithmetic so the CUDA kernels can be checked; each function
+ * names the reference lines it follows.  Built with -ffp-contract=off so the
+ * FP64 expressions are evaluated term by term as written in the reference.
+ *
+ * Pinning: the counting half is pinned against TNF.bin files written by the
+ * unmodified openmp/TNF.cpp (tests/golden/), the canonical-index table against
+ * the reference's TNmap_d/BN tables (tests/golden/ref_tables.json).  The
+ * probability half has no reference golden vectors (the reference ships no
+ * tests); it is a line-by-line restatement of cuda/Cuda2.cu:192-241 and
+ * 721-779, cross-checked against each other in tests/test_oracle.py.
+ */
+#include "tnf_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+/* Column order of the 136 canonical tetranucleotides: the TNF.bin format
+ * (openmp/TNF.cpp:14-24).  The order is the file format, so it is kept. */
+const char kTnOrder[] =
+    "GGTAAGCCAAAAACATAGTCACGACATACGAAAAGTCAAACCAGGGACATTAGATCCCTCCTAAACTAAGGCGCAACCGCCGCCAAAC"
+    "ACTCATCCGACCGAGAATAGATCACAGAAGTAATGAAAATTTAATATAAGTGAGCTCCACGGCCACCCGGGAGCGCATACCTGATAGA"
+    "ATATGTCACTCCACAAACCTTAAAAACGCGAGAGGGATCGACGCTCAACTACCTCAGACAGGAACTTCGCCCCTGCTGCAGGCACACG"
+    "GAGCAACTCATGAATTACAGAGATATAACATCGCCATCGACACACAACAAGGAGCAATGGATTCGTGAACCGGATAGCTACGTCCCCG"
+    "AAGCCGTAGTACAGGAAATGCACCCAGCCGGCACACCCGGCCGACCCCTGAAAACAAGAGCCCACGGATACAACCAACGTGAACGTAA"
+    "ATGCGTTATCCACAGGACTGAAAGAAGACAAGGCGAAACCACGGCCAACTTAAGACAGCGGAAAAATCATTGGCACCCTACGACCTAG"
+    "AGAACGCACGCGAATA";
+
+/* ASCII -> 2-bit code used by the reference's get_tn (cuda/Cuda2.cu:162-168):
+ * A/a=0, C/c=1, T/t=2, G/g=3, anything else 4. */
+inline uint8_t base_code(unsigned char c) {
+    switch (c) {
+        case 'A': case 'a': return 0;
+        case 'C': case 'c': return 1;
+        case 'T': case 't': return 2;
+        case 'G': case 'g': return 3;
+        default: return 4;
+    }
+}
+
+const char kCodeBase[4] = {'A', 'C', 'T', 'G'};
+
+char complement(char b) {
+    switch (b) {
+        case 'A': return 'T';
+        case 'T': return 'A';
+        case 'C': return 'G';
+        default: return 'C';
+    }
+}
+
+struct TnTables {
+    uint8_t map[256];
+    TnTables() {
+        for (int code = 0; code < 256; ++code) {
+            char s[4], rc[4];
+            for (int p = 0; p < 4; ++p) s[p] = kCodeBase[(code >> (2 * (3 - p))) & 3];
+            for (int p = 0; p < 4; ++p) rc[p] = complement(s[3 - p]);
+            int idx = -1;
+            for (int t = 0; t < 136 && idx < 0; ++t) {
+                if (memcmp(kTnOrder + 4 * t, s, 4) == 0 || memcmp(kTnOrder + 4 * t, rc, 4) == 0) idx = t;
+            }
+            map[code] = (uint8_t)(idx < 0 ? 255 : idx);
+        }
+    }
+};
+
+const TnTables& tables() {
+    static TnTables t;
+    return t;
+}
+
+/* Logistic-model coefficients of MetaBAT2 (cuda/Cuda2.cu:170-188); these are
+ * the model's parameters and must be identical. */
+const double B1[18] = {46349.1624324381,  -76092.3748553155, -639.918334183,  53873.3933743949, -156.6547554844,
+                       -21263.6010657275, 64.7719132839,     5003.2646455284, -8.5014386744,    -700.5825500292,
+                       0.3968284526,      54.037542743,      -1.7713972342,   474.0850141891,   -23.966597785,
+                       0.7800219061,      -0.0138723693,     0.0001027543};
+const double C1[18] = {-443565.465710869, 718862.10804858, 5114.1630934534,   -501588.206183097, 784.4442123743,
+                       194712.394138513,  -377.9645994741, -45088.7863182741, 50.5960513287,     6220.3310639927,
+                       -2.3670776453,     -473.269785487,  15.3213264134,     -3282.8510348085,  164.0438603974,
+                       -5.2778800755,     0.0929379305,    -0.0006826817};
+const double B2[17] = {6770.9351457442, -5933.7589419767, -2976.2879986855, 3279.7524685865, 1602.7544794819,
+                       -967.2906583423, -462.0149190219,  159.8317289682,   74.4884405822,   -14.0267151808,
+                       -6.3644917671,   0.5108811613,     0.2252455343,     0.965040193,     -0.0546309127,
+                       0.0012917084,    -1.14383e-05};
+const double C2[19] = {39406.5712626297,  -77863.1741143294, 9586.8761567725, 55360.1701572325, -5825.2491611377,
+                       -21887.8400068324, 1751.6803621934,   5158.3764225203, -290.1765894829,  -724.0348081819,
+                       25.364646181,      56.0522105105,     -0.9172073892,   -1.8470088417,    449.4660736502,
+                       -24.4141920625,    0.8465834103,      -0.0158943762,   0.0001235384};
+const double kFloorPreProb = 2.1972245773362196; /* log(9), cuda/Cuda2.cu:190 */
+
+int resolve_threads(int threads) {
+#ifdef _OPENMP
+    return threads > 0 ? threads : omp_get_max_threads();
+#else
+    (void)threads;
+    return 1;
+#endif
+}
+
+/* One row of gen_tnf_graph: visit columns in ascending order and keep the
+ * reference's per-row min-heap (cuda/Cuda2.cu:921-934, CompareEdge 660-664). */
+struct CompareEdge {
+    bool operator()(const std::pair<uint64_t, double>& a, const std::pair<uint64_t, double>& b) const {
+        return a.second > b.second;
+    }
+};
+typedef std::priority_queue<std::pair<uint64_t, double>, std::vector<std::pair<uint64_t, double>>, CompareEdge> EdgeHeap;
+
+void row_heap(const float* tnf, const double* logsize, uint64_t n, double floor_cut, uint32_t max_edges, uint64_t i,
+              EdgeHeap& heap) {
+    const float* ti = tnf + i * 136;
+    for (uint64_t j = 0; j < n; ++j) {
+        if (i == j) continue;
+        double pre = orc_pre_prob(logsize[i], logsize[j], ti, tnf + j * 136);
+        double s = pre > floor_cut ? 1. - 1. / (1. + exp(pre)) : 0.;
+        if (s != 0. && (heap.size() < max_edges || (heap.size() == max_edges && s > heap.top().second))) {
+            if (heap.size() == max_edges) heap.pop();
+            heap.push(std::make_pair(j, s));
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* orc_tn_order(void) { return kTnOrder; }
+
+void orc_tnmap(uint8_t map[256]) { memcpy(map, tables().map, 256); }
+
+void orc_base_code(uint8_t bn[256]) {
+    for (int c = 0; c < 256; ++c) bn[c] = base_code((unsigned char)c);
+}
+
+/* cuda/Cuda2.cu:1830-1853 with next_contig (330-339) and get_tn (317-327):
+ * a rolling 4-char window; '\n' overwrites the window's oldest char with a
+ * non-base marker instead of shifting, so the k-mer that spans a line break
+ * is still counted; any non-ACGT char skips the windows containing it. */
+void orc_tnf_count(const char* bytes, const uint64_t* off, const uint64_t* len, uint64_t n, uint32_t* counts,
+                   float* tnf, int threads) {
+    const uint8_t* map = tables().map;
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nt)
+    for (int64_t r = 0; r < (int64_t)n; ++r) {
+        const unsigned char* seq = (const unsigned char*)bytes + off[r];
+        uint64_t L = len[r];
+        unsigned char win[4] = {0, 0, 0, 0};
+        float cnt[136];
+        for (int c = 0; c < 136; ++c) cnt[c] = 0.f;
+        if (L >= 4) {
+            for (uint64_t j = 0; j < L; ++j) {
+                unsigned char ch = seq[j];
+                if (ch == '\n') {
+                    win[0] = 'X';
+                } else {
+                    win[0] = win[1];
+                    win[1] = win[2];
+                    win[2] = win[3];
+                    win[3] = ch;
+                }
+                if (j < 3) continue;
+                int tn = 0, bad = 0;
+                for (int p = 0; p < 4; ++p) {
+                    uint8_t b = base_code(win[p]);
+                    if (b & 4) { bad = 1; break; }
+                    tn = (tn << 2) | b;
+                }
+                if (bad) continue;
+                cnt[map[tn]] += 1.f;
+            }
+        }
+        double rsum = 0;
+        for (int c = 0; c < 136; ++c) {
+            float sq = cnt[c] * cnt[c];
+            rsum += sq;
+        }
+        rsum = sqrt(rsum);
+        for (int c = 0; c < 136; ++c) {
+            counts[r * 136 + c] = (uint32_t)cnt[c];
+            tnf[r * 136 + c] = (float)(cnt[c] / rsum);
+        }
+    }
+}
+
+void orc_tnf_normalize_f64(const uint32_t* counts, uint64_t n, double* out) {
+    for (uint64_t r = 0; r < n; ++r) {
+        double rsum = 0;
+        for (int c = 0; c < 136; ++c) rsum += (double)counts[r * 136 + c] * (double)counts[r * 136 + c];
+        rsum = sqrt(rsum);
+        for (int c = 0; c < 136; ++c) out[r * 136 + c] = (double)counts[r * 136 + c] / rsum;
+    }
+}
+
+double orc_tnf_distance(const float* a, const float* b) {
+    double d = 0;
+    for (int k = 0; k < 136; ++k) {
+        float df = a[k] - b[k];
+        float sq = df * df;
+        d += sq;
+    }
+    return sqrt(d);
+}
+
+/* cuda/Cuda2.cu:199-240: powers of x = min(log sizes), y = max(log sizes),
+ * model 1; if its pre-probability is at or below log(9) model 2, capped at
+ * log(9). */
+double orc_pre_prob_from_d(double r1, double r2, double d) {
+    double lw[19];
+    lw[0] = std::min(r1, r2);
+    lw[1] = std::max(r1, r2);
+    lw[2] = lw[0] * lw[0];
+    lw[4] = lw[2] * lw[0];
+    lw[6] = lw[4] * lw[0];
+    lw[8] = lw[6] * lw[0];
+    lw[10] = lw[8] * lw[0];
+    lw[11] = lw[10] * lw[0];
+    lw[3] = lw[1] * lw[1];
+    lw[5] = lw[3] * lw[1];
+    lw[7] = lw[5] * lw[1];
+    lw[9] = lw[7] * lw[1];
+    lw[12] = lw[0] * lw[1];
+    lw[14] = lw[4] * lw[5];
+    lw[15] = lw[6] * lw[7];
+    lw[16] = lw[8] * lw[9];
+    lw[13] = lw[2] * lw[3];
+    lw[18] = lw[9] * lw[1];
+    double b = B1[0] + B1[1] * lw[0] + B1[2] * lw[1] + B1[3] * lw[2] + B1[4] * lw[3] + B1[5] * lw[4] + B1[6] * lw[5] +
+               B1[7] * lw[6] + B1[8] * lw[7] + B1[9] * lw[8] + B1[10] * lw[9] + B1[11] * lw[10] + B1[12] * lw[11] +
+               B1[13] * lw[12] + B1[14] * lw[13] + B1[15] * lw[14] + B1[16] * lw[15] + B1[17] * lw[16];
+    double c = C1[0] + C1[1] * lw[0] + C1[2] * lw[1] + C1[3] * lw[2] + C1[4] * lw[3] + C1[5] * lw[4] + C1[6] * lw[5] +
+               C1[7] * lw[6] + C1[8] * lw[7] + C1[9] * lw[8] + C1[10] * lw[9] + C1[11] * lw[10] + C1[12] * lw[11] +
+               C1[13] * lw[12] + C1[14] * lw[13] + C1[15] * lw[14] + C1[16] * lw[15] + C1[17] * lw[16];
+    double pre = -(b + c * d);
+    if (pre <= kFloorPreProb) {
+        b = B2[0] + B2[1] * lw[0] + B2[2] * lw[1] + B2[3] * lw[2] + B2[4] * lw[3] + B2[5] * lw[4] + B2[6] * lw[5] +
+            B2[7] * lw[6] + B2[8] * lw[7] + B2[9] * lw[8] + B2[10] * lw[9] + B2[11] * lw[10] + B2[12] * lw[18] +
+            B2[13] * lw[13] + B2[14] * lw[14] + B2[15] * lw[15] + B2[16] * lw[16];
+        c = C2[0] + C2[1] * lw[0] + C2[2] * lw[1] + C2[3] * lw[2] + C2[4] * lw[3] + C2[5] * lw[4] + C2[6] * lw[5] +
+            C2[7] * lw[6] + C2[8] * lw[7] + C2[9] * lw[8] + C2[10] * lw[9] + C2[11] * lw[10] + C2[12] * lw[18] +
+            C2[13] * lw[11] + C2[14] * lw[12] + C2[15] * lw[13] + C2[16] * lw[14] + C2[17] * lw[15] + C2[18] * lw[16];
+        pre = -(b + c * d);
+        if (pre > kFloorPreProb) pre = kFloorPreProb;
+    }
+    return pre;
+}
+
+double orc_pre_prob(double r1, double r2, const float* a, const float* b) {
+    return orc_pre_prob_from_d(r1, r2, orc_tnf_distance(a, b));
+}
+
+/* cuda/Cuda2.cu:721-779, the host form with its own grouping. */
+double orc_tnf_dist_cpu(double r1, double r2, const float* a, const float* bb) {
+    const double floor_prob = 0.1;
+    const double floor_pre = log((1.0 / floor_prob) - 1.0);
+    double d = 0;
+    for (int i = 0; i < 136; ++i) {
+        float df = a[i] - bb[i];
+        float sq = df * df;
+        d += sq;
+    }
+    d = sqrt(d);
+    double lw11 = std::min(r1, r2), lw21 = std::max(r1, r2);
+    double lw12 = lw11 * lw11, lw13 = lw12 * lw11, lw14 = lw13 * lw11, lw15 = lw14 * lw11, lw16 = lw15 * lw11,
+           lw17 = lw16 * lw11;
+    double lw22 = lw21 * lw21, lw23 = lw22 * lw21, lw24 = lw23 * lw21, lw25 = lw24 * lw21, lw26 = lw25 * lw21;
+    double b = 46349.1624324381 + -76092.3748553155 * lw11 + -639.918334183 * lw21 + 53873.3933743949 * lw12 +
+               -156.6547554844 * lw22 + -21263.6010657275 * lw13 + 64.7719132839 * lw23 + 5003.2646455284 * lw14 +
+               -8.5014386744 * lw24 + -700.5825500292 * lw15 + 0.3968284526 * lw25 + 54.037542743 * lw16 +
+               -1.7713972342 * lw17 + 474.0850141891 * lw11 * lw21 + -23.966597785 * lw12 * lw22 +
+               0.7800219061 * lw13 * lw23 + -0.0138723693 * lw14 * lw24 + 0.0001027543 * lw15 * lw25;
+    double c = -443565.465710869 + 718862.10804858 * lw11 + 5114.1630934534 * lw21 + -501588.206183097 * lw12 +
+               784.4442123743 * lw22 + 194712.394138513 * lw13 + -377.9645994741 * lw23 + -45088.7863182741 * lw14 +
+               50.5960513287 * lw24 + 6220.3310639927 * lw15 + -2.3670776453 * lw25 + -473.269785487 * lw16 +
+               15.3213264134 * lw17 + -3282.8510348085 * lw11 * lw21 + 164.0438603974 * lw12 * lw22 +
+               -5.2778800755 * lw13 * lw23 + 0.0929379305 * lw14 * lw24 + -0.0006826817 * lw15 * lw25;
+    double pre = -(b + c * d);
+    double prob = pre <= floor_pre ? floor_prob : 1.0 / (1 + exp(pre));
+    if (prob >= floor_prob) {
+        b = 6770.9351457442 + -5933.7589419767 * lw11 + -2976.2879986855 * lw21 + 3279.7524685865 * lw12 +
+            1602.7544794819 * lw22 + -967.2906583423 * lw13 + -462.0149190219 * lw23 + 159.8317289682 * lw14 +
+            74.4884405822 * lw24 + -14.0267151808 * lw15 + -6.3644917671 * lw25 + 0.5108811613 * lw16 +
+            0.2252455343 * lw26 + 0.965040193 * lw12 * lw22 + -0.0546309127 * lw13 * lw23 +
+            0.0012917084 * lw14 * lw24 + -1.14383e-05 * lw15 * lw25;
+        c = 39406.5712626297 + -77863.1741143294 * lw11 + 9586.8761567725 * lw21 + 55360.1701572325 * lw12 +
+            -5825.2491611377 * lw22 + -21887.8400068324 * lw13 + 1751.6803621934 * lw23 + 5158.3764225203 * lw14 +
+            -290.1765894829 * lw24 + -724.0348081819 * lw15 + 25.364646181 * lw25 + 56.0522105105 * lw16 +
+            -0.9172073892 * lw26 + -1.8470088417 * lw17 + 449.4660736502 * lw11 * lw21 +
+            -24.4141920625 * lw12 * lw22 + 0.8465834103 * lw13 * lw23 + -0.0158943762 * lw14 * lw24 +
+            0.0001235384 * lw15 * lw25;
+        pre = -(b + c * d);
+        prob = pre <= floor_pre ? 1.0 / (1 + exp(pre)) : floor_prob;
+    }
+    return prob;
+}
+
+double orc_logit_cutoff(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
+
+uint64_t orc_tnf_graph(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
+                       uint64_t row0, uint64_t row1, uint64_t* from, uint64_t* to, double* stnf, uint64_t cap,
+                       int threads) {
+    if (row1 > n) row1 = n;
+    if (row0 >= row1) return 0;
+    const double floor_cut = orc_logit_cutoff(cutoff);
+    uint64_t nr = row1 - row0;
+    std::vector<std::vector<std::pair<uint64_t, double>>> per_row(nr);
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t r = 0; r < (int64_t)nr; ++r) {
+        uint64_t i = row0 + (uint64_t)r;
+        EdgeHeap heap;
+        row_heap(tnf, logsize, n, floor_cut, max_edges, i, heap);
+        /* emission rule of cuda/Cuda2.cu:936-946: only i < j */
+        while (!heap.empty()) {
+            std::pair<uint64_t, double> e = heap.top();
+            if (i < e.first) per_row[r].push_back(e);
+            heap.pop();
+        }
+    }
+    uint64_t total = 0;
+    for (uint64_t r = 0; r < nr; ++r) {
+        for (auto& e : per_row[r]) {
+            if (total < cap) {
+                from[total] = row0 + r;
+                to[total] = e.first;
+                stnf[total] = e.second;
+            }
+            ++total;
+        }
+    }
+    return total;
+}
+
+uint64_t orc_tnf_topk_rows(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
+                           uint64_t row0, uint64_t row1, uint64_t* row_ptr, uint64_t* cols, double* sims, uint64_t cap,
+                           int threads) {
+    if (row1 > n) row1 = n;
+    if (row0 >= row1) {
+        row_ptr[0] = 0;
+        return 0;
+    }
+    const double floor_cut = orc_logit_cutoff(cutoff);
+    uint64_t nr = row1 - row0;
+    std::vector<std::vector<std::pair<uint64_t, double>>> per_row(nr);
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t r = 0; r < (int64_t)nr; ++r) {
+        EdgeHeap heap;
+        row_heap(tnf, logsize, n, floor_cut, max_edges, row0 + (uint64_t)r, heap);
+        while (!heap.empty()) {
+            per_row[r].push_back(heap.top());
+            heap.pop();
+        }
+    }
+    uint64_t total = 0;
+    for (uint64_t r = 0; r < nr; ++r) {
+        row_ptr[r] = total;
+        for (auto& e : per_row[r]) {
+            if (total < cap) {
+                cols[total] = e.first;
+                sims[total] = e.second;
+            }
+            ++total;
+        }
+    }
+    row_ptr[nr] = total;
+    return total;
+}
+
+/* cuda/Cuda2.cu:281-314: position b of the permutation against every other
+ * position; the running max starts at DBL_MIN (a tiny positive number), so a
+ * contig whose pre-probabilities are all <= 0 reports sigmoid(DBL_MIN)=0.5. */
+void orc_max_prob(const float* tnf, const double* logsize, uint64_t n, const uint64_t* contigs, uint64_t m,
+                  double* out, int threads) {
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t b = 0; b < (int64_t)m; ++b) {
+        uint64_t ci = contigs[b];
+        double local_max = DBL_MIN;
+        for (uint64_t i = 0; i < n; ++i) {
+            if (i == (uint64_t)b) continue;
+            double pre = orc_pre_prob(logsize[ci], logsize[contigs[i]], tnf + ci * 136, tnf + contigs[i] * 136);
+            if (pre > local_max) local_max = pre;
+        }
+        out[b] = 1. - (1. / (1. + exp(local_max)));
+    }
+}
+
+void orc_srand(uint32_t seed) { srand(seed); }
+int orc_rand(void) { return rand(); }
+
+/* gen_tnf_graph_sample (cuda/Cuda2.cu:972-1025). */
+static double ptnf_sample(const float* tnf, const double* logsize, uint64_t n, double coverage, bool full,
+                          int threads) {
+    uint64_t m = full ? n : std::min(n, (uint64_t)2500);
+    std::vector<uint64_t> idx(n);
+    std::iota(idx.begin(), idx.end(), (uint64_t)0);
+    /* random_unique, cuda/Cuda2.cu:500-511 */
+    {
+        uint64_t left = n;
+        uint64_t* begin = idx.data();
+        uint64_t k = m;
+        while (k--) {
+            uint64_t* r = begin + (uint64_t)rand() % left;
+            std::swap(*begin, *r);
+            ++begin;
+            --left;
+        }
+    }
+    std::vector<double> mx(m);
+    orc_max_prob(tnf, logsize, n, idx.data(), m, mx.data(), threads);
+    std::sort(mx.begin(), mx.end(), std::greater<double>());
+    uint64_t p = 999, pp = 1000;
+    double cov = 0, pcov = 0;
+    uint64_t counton = 0;
+    for (; p > 700;) {
+        double cutoff = (double)p / 1000.;
+        while (counton < m && mx[counton] >= cutoff) counton++;
+        cov = (double)counton / m;
+        if (cov >= coverage) {
+            if (cov - coverage > coverage - pcov) {
+                p = pp;
+                cov = pcov;
+            }
+            break;
+        }
+        pp = p;
+        pcov = cov;
+        if (p > 990)
+            p -= rand() % 3 + 1;
+        else if (p > 900)
+            p -= rand() % 3 + 3;
+        else
+            p -= rand() % 3 + 9;
+    }
+    return (double)p;
+}
+
+/* driver, cuda/Cuda2.cu:1885-1901 */
+double orc_ptnf_search(const float* tnf, const double* logsize, uint64_t n, double coverage, int threads) {
+    double ptnf = 0;
+    if (n <= 25000) return ptnf_sample(tnf, logsize, n, coverage, true, threads);
+    for (int i = 0; i < 10; ++i) {
+        double minp = ptnf_sample(tnf, logsize, n, coverage, false, threads);
+        if (minp < 701) minp = 700.;
+        ptnf += minp;
+        if (i == 1 && ptnf / 2 < 701) {
+            ptnf = 700.;
+            break;
+        }
+        if (i == 9) ptnf /= 10.;
+    }
+    return ptnf;
+}
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+"""K1 on the GPU: bit-exact counts against the oracle (itself pinned to
+TNF.bin of the reference's TNF.cpp) and normalised TNF within 1e-6."""
+import os
+
+import numpy as np
+import pytest
+
+from mdet_gb300.fasta import parse_fasta_bytes, read_fasta
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _check(ctx, data, off, ln, ref64=None):
+    counts, tnf = ctx.tnf_count(data, off, ln)
+    oc, ot = oracle.tnf_count(data, off, ln)
+    assert np.array_equal(counts, oc)
+    # float(c / rsum): the GPU multiplies by 1/rsum, identical except at
+    # double-rounding ties (allow a one-ulp difference on at most 1e-6 of entries)
+    same = (tnf.view(np.uint32) == ot.view(np.uint32)) | (np.isnan(tnf) & np.isnan(ot))
+    if not same.all():
+        d = np.abs(tnf.view(np.int32).astype(np.int64) - ot.view(np.int32).astype(np.int64))[~same]
+        assert d.max() <= 1 and (~same).mean() < 1e-6
+    if ref64 is not None:
+        ok = ~np.isnan(ref64)
+        rel = np.abs(tnf[ok].astype(np.float64) - ref64[ok]) / np.where(ref64[ok] == 0, 1, ref64[ok])
+        assert rel.max() < 1e-6
+    return counts
+
+
+@pytest.mark.parametrize("name", ["count_synth.fa.gz", "count_edge.fa"])
+def test_golden_files(gpu_ctx, name):
+    a = read_fasta(os.path.join(G, name))
+    ref = np.load(os.path.join(G, name.split(".")[0] + "_tnf.npy"))
+    _check(gpu_ctx, a.data, a.seq_off, a.seq_len, ref)
+
+
+def test_config0_size(gpu_ctx):
+    from mdet_gb300 import synth
+
+    a = synth.generate(seed=1000000, n=20000, genomes=50, threads=8)
+    _check(gpu_ctx, a.data, a.seq_off, a.seq_len)
+
+
+def test_random_layouts(gpu_ctx):
+    rng = np.random.default_rng(7)
+    recs = []
+    for k in range(300):
+        L = int(rng.integers(0, 40000))
+        s = rng.choice(np.frombuffer(b"ACGTacgtNNRY\r", np.uint8), L, p=[.2, .2, .2, .2, .04, .04, .04, .04, .01, .01,
+                                                                        .005, .004, .001])
+        w = int(rng.integers(1, 130))
+        body = b"\n".join(s[i:i + w].tobytes() for i in range(0, L, w))
+        if rng.random() < 0.1:
+            body = body.replace(b"\n", b"\n\n", 3)
+        recs.append(b">r%d\n" % k + body + (b"\n" if rng.random() < 0.9 else b""))
+    data = np.frombuffer(b"".join(recs), np.uint8)
+    p = parse_fasta_bytes(data, min_contig=0)
+    _check(gpu_ctx, data, p.seq_off, p.seq_len)
+
+
+def test_short_and_empty_contigs(gpu_ctx):
+    txt = b">e\n>a\nA\n>b\nACG\n>c\nACGT\n>d\nAC\nGT\n>f\nNNNNNNNN\n"
+    data = np.frombuffer(txt, np.uint8)
+    p = parse_fasta_bytes(data, min_contig=0)
+    counts, tnf = gpu_ctx.tnf_count(data, p.seq_off, p.seq_len)
+    assert counts.sum(1).tolist() == [0, 0, 0, 1, 1, 0]
+    assert np.isnan(tnf[0]).all() and np.isnan(tnf[5]).all()
+    assert np.nansum(tnf[3]) == 1.0
+
+
+def test_device_api_alignment_check(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    from mdet_gb300 import MdetError
+
+    a = read_fasta(os.path.join(G, "count_edge.fa"))
+    n = a.seq_off.size
+    buf = torch.zeros(a.data.size + 64, dtype=torch.uint8, device="cuda")
+    buf[:a.data.size] = torch.from_numpy(a.data.copy()).cuda()
+    off = torch.from_numpy(a.seq_off.astype(np.int64)).cuda()
+    ln = torch.from_numpy(a.seq_len.astype(np.int64)).cuda()
+    cnt = torch.zeros((n, 136), dtype=torch.int32, device="cuda")
+    tnf = torch.zeros((n, 136), dtype=torch.float32, device="cuda")
+    gpu_ctx.tnf_count_dev(buf.data_ptr(), a.data.size, off.data_ptr(), ln.data_ptr(), n, cnt.data_ptr(),
+                          tnf.data_ptr())
+    oc, _ = oracle.tnf_count(a.data, a.seq_off, a.seq_len)
+    assert np.array_equal(cnt.cpu().numpy().view(np.uint32), oc)
+    with pytest.raises(MdetError):
+        gpu_ctx.tnf_count_dev(buf.data_ptr() + 3, a.data.size, off.data_ptr(), ln.data_ptr(), n, cnt.data_ptr(),
+                              tnf.data_ptr())

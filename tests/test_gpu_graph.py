@@ -1,0 +1,99 @@
+"""Pairwise stage on the GPU against the oracle: edge sets identical outside
+the 1e-5 tolerance band, sTNF within 1e-9; the tensor-core form equal to
+the plain form; max-probability sample and pTNF search equal to the oracle."""
+import numpy as np
+import sys, os
+sys.path.insert(0, os.path.dirname(__file__))
+import pytest
+
+from gpu_util import compare_graph, synth_set
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def set_a():
+    return synth_set(seed=21, n=1800, genomes=30)
+
+
+@pytest.mark.parametrize("cutoff,k", [(0.95, 200), (0.95, 5), (0.8, 40), (0.999, 200)])
+def test_plain_vs_oracle(gpu_ctx, set_a, cutoff, k):
+    a, _, tnf = set_a
+    g = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="plain")
+    common, exempt = compare_graph(g.from_, g.to, g.sTNF, tnf, a.log_sizes, cutoff, k)
+    assert common > 0 or cutoff > 0.99
+    assert exempt <= max(2, common // 1000)
+    # output order: rows ascending, similarity descending inside a row
+    assert np.all(np.diff(g.from_.astype(np.int64)) >= 0)
+
+
+@pytest.mark.parametrize("cutoff,k", [(0.95, 200), (0.9, 10)])
+def test_bf16_equals_plain(gpu_ctx, set_a, cutoff, k):
+    a, _, tnf = set_a
+    p = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="plain")
+    t = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="bf16")
+    assert np.array_equal(p.from_, t.from_)
+    assert np.array_equal(p.to, t.to)
+    assert np.array_equal(p.sTNF, t.sTNF)
+    assert t.stats["n_candidates"] >= t.stats["n_above_cutoff"]
+
+
+def test_identical_contigs_big_rows(gpu_ctx):
+    # 1500 copies of a handful of profiles: rows with > 1024 tied edges
+    a, _, tnf = synth_set(seed=22, n=40, genomes=2, max_len=30000)
+    rep = np.repeat(np.arange(4), 375)
+    t2 = tnf[rep]
+    ls = a.log_sizes[rep]
+    for mode in ("plain", "bf16"):
+        g = gpu_ctx.tnf_graph(t2, ls, 0.9, 300, mode=mode)
+        compare_graph(g.from_, g.to, g.sTNF, t2, ls, 0.9, 300)
+
+
+def test_tiny_inputs(gpu_ctx):
+    a, _, tnf = synth_set(seed=23, n=3, genomes=1, max_len=200000)
+    for n in (0, 1, 2, 3):
+        g = gpu_ctx.tnf_graph(tnf[:n], a.log_sizes[:n], 0.7, 200, mode="plain")
+        fr, to, st = oracle.graph(tnf[:n], a.log_sizes[:n], 0.7, 200) if n else ([], [], [])
+        assert sorted(zip(g.from_.tolist(), g.to.tolist())) == sorted(zip(list(map(int, fr)), list(map(int, to))))
+
+
+def test_capacity_error(gpu_ctx, set_a):
+    import ctypes
+
+    from mdet_gb300 import tnf as T
+
+    a, _, tnf = set_a
+    lib = T.load_library()
+    n = tnf.shape[0]
+    fr = np.zeros(4, np.uint64)
+    ne = ctypes.c_uint64(0)
+    t32 = np.ascontiguousarray(tnf)
+    rc = lib.mdet_tnf_graph(gpu_ctx.h, t32.ctypes.data, a.log_sizes.ctypes.data, n, 0.9, 200, 0, fr.ctypes.data,
+                            fr.ctypes.data, fr.ctypes.data, 4, ctypes.byref(ne), None)
+    assert rc == T.ERR_CAPACITY and ne.value > 4
+
+
+@pytest.mark.parametrize("mode", ["plain", "bf16"])
+def test_max_prob_vs_oracle(gpu_ctx, set_a, mode):
+    a, _, tnf = set_a
+    n = tnf.shape[0]
+    rng = np.random.default_rng(3)
+    perm = rng.permutation(n).astype(np.uint64)
+    m = 250
+    ref = oracle.max_prob(tnf, a.log_sizes, perm, m)
+    got = gpu_ctx.max_prob(tnf, a.log_sizes, perm, m, mode=mode, floor_prob=0.7)
+    hi = ref >= 0.7
+    assert np.abs(got[hi] - ref[hi]).max() <= 1e-9
+    assert np.all(got[~hi] < 0.7)
+    exact = gpu_ctx.max_prob(tnf, a.log_sizes, perm, 60, mode="plain", floor_prob=0.0)
+    assert np.abs(exact - ref[:60]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("mode", ["plain", "bf16"])
+def test_ptnf_search_vs_oracle(gpu_ctx, set_a, mode):
+    a, _, tnf = set_a
+    want = oracle.ptnf_search(tnf, a.log_sizes, 0.95, seed=77)
+    oracle.srand(77)
+    got = gpu_ctx.ptnf_search(tnf, a.log_sizes, 0.95, mode=mode)
+    assert got == want

@@ -1,0 +1,400 @@
+#!/usr/bin/env python3
+"""Benchmark of the MetaBAT2 TNF path on GB300.
+
+Workload (one "step"): a synthetic 1,000,000-contig assembly (2,000 order-3
+Markov genomes, log-normal(5 kb, 1) lengths clamped to 2.5-500 kb, 0.5% N,
+60-column FASTA, ~8.5 GB) taken through the whole TNF path of the reference
+program: tetranucleotide counting of every contig, the pTNF search
+(maxP 95: 10 samples of 2,500 contigs against all contigs) and the TNF graph
+(maxEdges 200) at the cutoff it finds.
+
+  value  device-resident: inputs already in HBM, the *_dev entry points
+  e2e    the host-buffer entry points a drop-in caller uses (mdet_tnf_count,
+         mdet_tnf_ptnf_search, mdet_tnf_graph) from pinned host memory,
+         every copy inside the timed region
+
+Lower is better (seconds per step).  `--impl reference` times the
+reference's CPU arithmetic (the oracle restatement; the reference's own
+openmp/TNF.cpp cannot be built on the GPU machine) on bounded samples.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1M-contig TNF graph time: TC/learned vs plain FP32 GPU at ≥99.9% edge recall"
+MAX_EDGES = 200
+MAXP = 95.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_config(n, genomes, mode, ws):
+    return {
+        "workload": f"synthetic assembly, {n} contigs from {genomes} Markov genomes; TNF count + pTNF search "
+                    f"(maxP {MAXP:g}) + TNF graph (maxEdges {MAX_EDGES})",
+        "n_contigs": n,
+        "genomes": genomes,
+        "length": "lognormal(ln 5000, 1) clamped to [2500, 500000], 0.5% N, 60-col FASTA",
+        "max_edges": MAX_EDGES,
+        "maxP": MAXP,
+        "filter": mode,
+        "exact_stage": "fp32 compensated distance + fp64 logistic model",
+        "cache": "inputs larger than L2 (FASTA bytes ~8.5 GB per assembly)",
+        "parallelism": f"{ws} independent assemblies, one per GPU" if ws > 1 else "1 GPU",
+    }
+
+
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms",
+                                       "200", "-i", str(gpu_index)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ------------------------------------------------------------ CPU baseline --
+
+def cpu_baseline(a, tnf_host, n, target_s=8.0):
+    """The oracle (the reference's arithmetic restated in C++/OpenMP) on a
+    bounded sample, extrapolated to the full step."""
+    from oracle import oracle
+
+    cores = os.cpu_count() or 1
+    # counting sample: the first contigs up to ~200 MB of sequence
+    k = int(np.searchsorted(np.cumsum(a.seq_len.astype(np.float64)), 2e8)) + 1
+    k = min(k, n)
+    t = time.perf_counter()
+    oracle.tnf_count(a.data, a.seq_off[:k], a.seq_len[:k], threads=cores)
+    t_cnt = time.perf_counter() - t
+    count_est = t_cnt * float(a.seq_len.sum()) / float(a.seq_len[:k].sum())
+    # pairwise sample: rows [0, R) against all n columns, R sized to ~target_s
+    r0 = max(cores, 16)
+    t = time.perf_counter()
+    oracle.graph(tnf_host, a.log_sizes, 0.95, MAX_EDGES, 0, r0, threads=cores)
+    per_row = (time.perf_counter() - t) / r0
+    R = int(max(r0, min(n, target_s / max(per_row, 1e-9))))
+    t = time.perf_counter()
+    oracle.graph(tnf_host, a.log_sizes, 0.95, MAX_EDGES, 0, R, threads=cores)
+    per_row = (time.perf_counter() - t) / R
+    graph_est = per_row * n
+    sample_est = per_row * (10 * min(n, 2500) if n > 25000 else n)
+    total = count_est + sample_est + graph_est
+    return {
+        "value": total,
+        "unit": "s",
+        "cores": cores,
+        "kind": "port",
+        "sample": (f"oracle counting of {k} contigs ({a.seq_len[:k].sum() / 1e6:.0f} MB) scaled by bytes; oracle "
+                   f"pairwise probability + top-{MAX_EDGES} for {R} rows x {n} columns scaled to the graph's {n} "
+                   f"rows and the search's {10 * 2500 if n > 25000 else n} rows"),
+        "parts_s": {"count": count_est, "ptnf_search": sample_est, "graph": graph_est},
+    }
+
+
+# --------------------------------------------------------------- our arm --
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import mdet_gb300 as m
+    from mdet_gb300 import synth
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    n, G = args.n, args.genomes
+    seed = 2 + 1000 * rank  # the assembly of rank r; rank 0 is the 1M-contig set of the workload
+    L, g, ro, total = synth.plan(seed, n, G)
+    pinned = torch.empty(total + 64, dtype=torch.uint8, pin_memory=True)
+    a = synth.generate(seed, n, G, out=pinned.numpy())
+    nbytes = int(total)
+    dev = torch.device(f"cuda:{local}")
+    d_bytes = torch.empty(nbytes + 64, dtype=torch.uint8, device=dev)
+    d_bytes[:nbytes].copy_(pinned[:nbytes])
+    d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+    d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+    d_ls = torch.from_numpy(a.log_sizes).to(dev)
+    d_cnt = torch.empty((n, 136), dtype=torch.int32, device=dev)
+    d_tnf = torch.empty((n, 136), dtype=torch.float32, device=dev)
+    cap = n * MAX_EDGES
+    d_from = torch.empty(cap, dtype=torch.int64, device=dev)
+    d_to = torch.empty(cap, dtype=torch.int64, device=dev)
+    d_st = torch.empty(cap, dtype=torch.float64, device=dev)
+    ctx = m.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    libc = __import__("ctypes").CDLL(None)
+
+    info = {}
+
+    def step():
+        ctx.tnf_count_dev(d_bytes.data_ptr(), nbytes, d_off.data_ptr(), d_len.data_ptr(), n, d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+        libc.srand(12345)
+        p = ctx.ptnf_search_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, MAXP / 100.0, args.mode)
+        ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, p / 1000.0, MAX_EDGES, args.mode,
+                                   d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), cap)
+        info["ptnf"] = p
+        info["edges"] = ne
+        info["stats"] = st
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    ctx.set_timing(True)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if ws > 1:
+        dist.barrier()
+    launches = ctx.launch_count() - launches0
+    ms = e0.elapsed_time(e1) / args.steps
+    kern = {k: ctx.kernel_ms(k) for k in ("k_filter_tc", "k_filter_simt", "k_count", "k_exact_graph",
+                                          "k_exact_maxprob")}
+    ctx.set_timing(False)
+    t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    ms = float(t_max.item())
+
+    # ---- e2e through the host-buffer C ABI (pinned buffers, copies timed) ----
+    cnt_h = torch.empty((n, 136), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    tnf_h = torch.empty((n, 136), dtype=torch.float32, pin_memory=True).numpy()
+    from_h = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    to_h = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+    st_h = torch.empty(cap, dtype=torch.float64, pin_memory=True).numpy()
+    off_h = torch.from_numpy(a.seq_off.astype(np.int64)).pin_memory().numpy().view(np.uint64)
+    len_h = torch.from_numpy(a.seq_len.astype(np.int64)).pin_memory().numpy().view(np.uint64)
+    ls_h = torch.from_numpy(a.log_sizes.copy()).pin_memory().numpy()
+    data_h = pinned.numpy()[:nbytes]
+    e2e_info = {}
+
+    def step_e2e():
+        ctx.tnf_count(data_h, off_h, len_h, out=(cnt_h, tnf_h))
+        libc.srand(12345)
+        p = ctx.ptnf_search(tnf_h, ls_h, MAXP / 100.0, args.mode)
+        g = ctx.tnf_graph(tnf_h, ls_h, p / 1000.0, MAX_EDGES, args.mode, out=(from_h, to_h, st_h))
+        e2e_info["edges"] = g.getEdgeCount()
+
+    e2e_steps = max(1, min(args.steps, 3))
+    step_e2e()
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t) / e2e_steps
+    t_e = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if ws > 1:
+        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
+    e2e_s = float(t_e.item())
+    ne = e2e_info["edges"]
+    h2d = nbytes + 2 * n * 8 + 2 * (n * 136 * 4 + n * 8)
+    d2h = n * 136 * 8 + ne * 24
+
+    result = None
+    if rank == 0:
+        pk, pk_kind = peaks()
+        st = info["stats"]
+        # dominant kernel and its roofline
+        totals = {k: v[0] for k, v in kern.items() if v[1] > 0}
+        dom = max(totals, key=totals.get)
+        dom_ms, dom_launches = kern[dom]
+        nsample = 10 * min(n, 2500) if n > 25000 else n
+        pairs_graph = n * (n - 1) / 2
+        pairs_sample = (10 if n > 25000 else 1) * min(n, 2500 if n > 25000 else n) * n
+        if dom in ("k_filter_tc", "k_filter_simt"):
+            flops_step = 2 * 136 * (pairs_graph + pairs_sample)
+            achieved = flops_step * args.steps / (dom_ms / 1e3) / 1e12
+            peak_v = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+            roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak_v, "unit": "TFLOP/s",
+                    "frac": achieved / peak_v, "traffic": None,
+                    "algorithmic_per_launch": flops_step * args.steps / dom_launches,
+                    "avg_launch_ms": dom_ms / dom_launches, "peak_source": f"bf16 sustained ({pk_kind})"}
+        else:
+            bytes_step = nbytes + n * 136 * 8
+            achieved = bytes_step * args.steps / (dom_ms / 1e3) / 1e9
+            peak_v = pk["hbm_gbs"]
+            roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak_v, "unit": "GB/s",
+                    "frac": achieved / peak_v, "traffic": None, "avg_launch_ms": dom_ms / dom_launches,
+                    "peak_source": f"hbm copy ({pk_kind})"}
+        cnt_ms, cnt_l = kern["k_count"]
+        count_roof = None
+        if cnt_l:
+            gbs = (nbytes + n * 136 * 8) * args.steps / (cnt_ms / 1e3) / 1e9
+            count_roof = {"kernel": "k_count", "bound": "hbm", "achieved": gbs, "peak": pk["hbm_gbs"],
+                          "unit": "GB/s", "frac": gbs / pk["hbm_gbs"], "avg_launch_ms": cnt_ms / cnt_l}
+        result = {
+            "metric": METRIC,
+            "value": ms / 1e3,
+            "unit": "s",
+            "n_gpus": ws,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms,
+            "higher_is_better": False,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "bf16",
+            "data": "synthetic (seeded Markov-genome assembly; no public dataset is shipped)",
+            "config": workload_config(n, G, args.mode, ws),
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "count_roofline": count_roof,
+            "clocks": clk,
+            "phases_ms": {"graph_total": st["ms_total"], "graph_filter": st["ms_filter"],
+                          "graph_exact": st["ms_exact"], "graph_select": st["ms_select"],
+                          "graph_prep": st["ms_prep"],
+                          "kernels_per_step": {k: v[0] / args.steps for k, v in kern.items() if v[1]}},
+            "ptnf_permille": info["ptnf"],
+            "edges": int(info["edges"]),
+            "candidates": int(st["n_candidates"]),
+            "above_cutoff": int(st["n_above_cutoff"]),
+        }
+        if not args.no_plain:
+            torch.cuda.synchronize()
+            ne_p, stp = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, info["ptnf"] / 1000.0, MAX_EDGES,
+                                          "plain", d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), cap)
+            result["plain_fp32_graph_s"] = stp["ms_total"] / 1e3
+            result["graph_speedup_vs_plain"] = stp["ms_total"] / st["ms_total"]
+            result["plain_edges_equal_count"] = int(ne_p) == int(info["edges"])
+        if not args.no_cpu and ws == 1:
+            tnf_host = d_tnf.cpu().numpy()
+            result["cpu_baseline"] = cpu_baseline(a, tnf_host, n)
+    ctx.close()
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if result is not None:
+        print(json.dumps(result), flush=True)
+
+
+# --------------------------------------------------------- reference arm --
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from mdet_gb300 import synth
+    from oracle import oracle
+
+    n, G = args.n, args.genomes
+    a = synth.generate(2, n, G)
+    cores = os.cpu_count() or 1
+    _, tnf = oracle.tnf_count(a.data, a.seq_off, a.seq_len, threads=cores)  # all columns, outside the timing
+    times = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        b = cpu_baseline(a, tnf, n, target_s=5.0)
+        if i >= args.warmup:
+            times.append(b["value"])
+            base = b
+        _ = time.perf_counter() - t
+    v = float(np.median(times))
+    base = dict(base)
+    base["value"] = v
+    print(json.dumps({
+        "metric": METRIC, "impl": "reference", "value": v, "unit": "s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Markov-genome assembly)",
+        "config": workload_config(n, G, "reference CPU arithmetic", ws),
+        "cpu_baseline": base,
+        "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "oracle port of the reference's CPU path timed on the host cores on a bounded sample per step, "
+                "extrapolated to the full step; openmp/TNF.cpp itself is only built where the reference is mounted",
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--genomes", type=int, default=2000)
+    ap.add_argument("--mode", default="bf16", choices=["bf16", "plain"])
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,15 @@ const char* mdet_last_error(const mdet_ctx* ctx);
 int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream);
 /* Build identification: "sm_103a ..." */
 const char* mdet_version(void);
+/* Kernel timing: when enabled, the main kernels (k_count, k_filter_tc,
+ * k_filter_simt, k_exact_graph, k_exact_maxprob) are bracketed by CUDA events
+ * on the context's stream; mdet_ctx_kernel_ms returns the summed device time
+ * of the named kernel's launches since timing was last enabled, and *launches
+ * their number. */
+int mdet_ctx_set_timing(mdet_ctx* ctx, int enable);
+int mdet_ctx_kernel_ms(mdet_ctx* ctx, const char* kernel, double* ms, uint32_t* launches);
+/* Kernels this context has launched since it was created. */
+uint64_t mdet_ctx_launch_count(const mdet_ctx* ctx);
 
 /* ---- TNF counting ------------------------------------------------------
  * Replaces the TNF loop of main (cuda/Cuda2.cu:1825-1863) and the copy of

@@ -9,6 +9,8 @@
 
 #include <string>
 #include <unordered_map>
+#include <utility>
+#include <vector>
 
 #include "../../include/mdet_tnf.h"
 
@@ -19,6 +21,12 @@
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+};
+
+struct KernelTimer {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;  // pending and finished launches
+    double ms = 0;
+    uint32_t launches = 0;
 };
 
 struct mdet_ctx {
@@ -35,7 +43,14 @@ struct mdet_ctx {
     uint32_t launches = 0;     // kernels launched by the current call
     void* encode_tiled = nullptr;  // cuTensorMapEncodeTiled entry point
     bool count_scratch_dirty = false;
+    uint64_t total_launches = 0;
+    bool timing = false;
+    std::unordered_map<std::string, KernelTimer> timers;
 };
+
+// Event pair around one launch of a named kernel when timing is enabled.
+void ctx_timer_begin(mdet_ctx* ctx, const char* kernel);
+void ctx_timer_end(mdet_ctx* ctx, const char* kernel);
 
 // Returns a device buffer of at least `bytes` named `name`, growing it if
 // needed.  zero_on_grow: freshly grown buffers are memset to 0.
@@ -54,6 +69,7 @@ int ctx_check_launch(mdet_ctx* ctx, const char* what);
 #define MDET_LAUNCHED(ctx, what)                   \
     do {                                           \
         (ctx)->launches++;                         \
+        (ctx)->total_launches++;                   \
         MDET_TRY(ctx_check_launch((ctx), (what))); \
     } while (0)
 

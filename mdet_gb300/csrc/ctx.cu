@@ -29,6 +29,31 @@ int ctx_cuda(mdet_ctx* ctx, cudaError_t e, const char* what) {
 
 int ctx_check_launch(mdet_ctx* ctx, const char* what) { return ctx_cuda(ctx, cudaGetLastError(), what); }
 
+void ctx_timer_begin(mdet_ctx* ctx, const char* kernel) {
+    if (!ctx->timing) return;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, ctx->stream);
+    ctx->timers[kernel].ev.push_back({a, b});
+}
+
+void ctx_timer_end(mdet_ctx* ctx, const char* kernel) {
+    if (!ctx->timing) return;
+    auto it = ctx->timers.find(kernel);
+    if (it == ctx->timers.end() || it->second.ev.empty()) return;
+    cudaEventRecord(it->second.ev.back().second, ctx->stream);
+}
+
+static void timers_clear(mdet_ctx* ctx) {
+    for (auto& kv : ctx->timers)
+        for (auto& e : kv.second.ev) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
+    ctx->timers.clear();
+}
+
 void* ctx_scratch(mdet_ctx* ctx, const char* name, size_t bytes, bool zero_on_grow) {
     if (bytes == 0) bytes = 16;
     DevBuf& b = ctx->bufs[name];
@@ -259,6 +284,7 @@ int mdet_ctx_destroy(mdet_ctx* ctx) {
     if (!ctx) return MDET_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    timers_clear(ctx);
     for (auto& kv : ctx->bufs)
         if (kv.second.p) cudaFree(kv.second.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
@@ -280,5 +306,38 @@ int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream) {
     ctx->stream = (cudaStream_t)stream;
     return MDET_OK;
 }
+
+int mdet_ctx_set_timing(mdet_ctx* ctx, int enable) {
+    if (!ctx) return MDET_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    timers_clear(ctx);
+    ctx->timing = enable != 0;
+    return MDET_OK;
+}
+
+int mdet_ctx_kernel_ms(mdet_ctx* ctx, const char* kernel, double* ms, uint32_t* launches) {
+    if (!ctx || !kernel || !ms) return MDET_ERR_INVALID;
+    *ms = 0;
+    if (launches) *launches = 0;
+    auto it = ctx->timers.find(kernel);
+    if (it == ctx->timers.end()) return MDET_OK;
+    KernelTimer& t = it->second;
+    for (auto& e : t.ev) {
+        float f = 0;
+        if (cudaEventSynchronize(e.second) != cudaSuccess) return ctx_cuda(ctx, cudaGetLastError(), "event");
+        cudaEventElapsedTime(&f, e.first, e.second);
+        t.ms += f;
+        t.launches++;
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    t.ev.clear();
+    *ms = t.ms;
+    if (launches) *launches = t.launches;
+    return MDET_OK;
+}
+
+uint64_t mdet_ctx_launch_count(const mdet_ctx* ctx) { return ctx ? ctx->total_launches : 0; }
 
 }  // extern "C"

@@ -2,7 +2,7 @@
 //
 // Every pair that passed a distance filter is scored again from the FP32
 // TNF rows: the reference's terms float((a_k - b_k)^2) (cuda/Cuda2.cu:194-196)
-// summed in four FP32 partial sums combined in FP64, sqrt in FP64, then the
+// summed with compensated FP32 arithmetic, sqrt in FP64, then the
 // MetaBAT2 logistic model in FP64 (cuda/Cuda2.cu:199-240) from per-contig
 // parts F(x), G(y) and the pair term H(x*y).  A pair is an edge when its
 // pre-probability beats logit(cutoff) (cuda/Cuda2.cu:257-260); its score is
@@ -30,21 +30,33 @@ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
-// d in the reference's terms: float((a-b)^2), FP32 partial sums, FP64 total.
+// d in the reference's terms float((a_k-b_k)^2) (cuda/Cuda2.cu:194-196).
+// The reference adds them in FP64; FP64 throughput is scarce on this part, so
+// two FP32 chains with error-free TwoSum compensation carry the sum instead
+// (relative error ~1e-14, the same order as the FP64 accumulation), and only
+// the final combine and sqrt run in FP64.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float t) {
+    const float sum = __fadd_rn(s, t);
+    const float bp = __fsub_rn(sum, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(sum, bp)), __fsub_rn(t, bp));
+    s = sum;
+    c = __fadd_rn(c, err);
+}
+
 __device__ __forceinline__ double exact_dist(const float* __restrict__ a, const float* __restrict__ b) {
     const float4* ra = reinterpret_cast<const float4*>(a);
     const float4* rb = reinterpret_cast<const float4*>(b);
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
 #pragma unroll 2
     for (int q = 0; q < MDET_NTNF / 4; ++q) {
         float4 x = __ldg(ra + q), y = __ldg(rb + q);
         float d0 = __fsub_rn(x.x, y.x), d1 = __fsub_rn(x.y, y.y), d2 = __fsub_rn(x.z, y.z), d3 = __fsub_rn(x.w, y.w);
-        s0 = __fadd_rn(s0, __fmul_rn(d0, d0));
-        s1 = __fadd_rn(s1, __fmul_rn(d1, d1));
-        s2 = __fadd_rn(s2, __fmul_rn(d2, d2));
-        s3 = __fadd_rn(s3, __fmul_rn(d3, d3));
+        two_sum_acc(s0, c0, __fmul_rn(d0, d0));
+        two_sum_acc(s1, c1, __fmul_rn(d1, d1));
+        two_sum_acc(s0, c0, __fmul_rn(d2, d2));
+        two_sum_acc(s1, c1, __fmul_rn(d3, d3));
     }
-    return sqrt(((double)s0 + (double)s1) + ((double)s2 + (double)s3));
+    return sqrt(((double)s0 + (double)s1) + ((double)c0 + (double)c1));
 }
 
 // pre-probability of sorted contigs i, j at distance d.  need_model2: also
@@ -367,8 +379,10 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.deg = deg;
         unsigned long long blocks = (ncand + 255) / 256;
         unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
-        k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
-        MDET_LAUNCHED(ctx, "k_exact_graph");
+        ctx_timer_begin(ctx, "k_exact_graph");
+    k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
+        ctx_timer_end(ctx, "k_exact_graph");
+    MDET_LAUNCHED(ctx, "k_exact_graph");
     }
     MDET_CUDA(ctx, cudaMemcpyAsync(nedges_out, cnt, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
@@ -397,8 +411,10 @@ int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned
         p.maxkey = maxkey;
         unsigned long long blocks = (ncand + 255) / 256;
         unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
-        k_exact_maxprob<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
-        MDET_LAUNCHED(ctx, "k_exact_maxprob");
+        ctx_timer_begin(ctx, "k_exact_maxprob");
+    k_exact_maxprob<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
+        ctx_timer_end(ctx, "k_exact_maxprob");
+    MDET_LAUNCHED(ctx, "k_exact_maxprob");
     }
     k_maxprob_finish<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(maxkey, slot_of, m, d_out);
     MDET_LAUNCHED(ctx, "k_maxprob_finish");

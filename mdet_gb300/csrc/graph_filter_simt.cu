@@ -161,7 +161,9 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
     if (per_sm < 1) per_sm = 1;
     unsigned long long grid = (unsigned long long)ctx->num_sms * per_sm * 8;
     if (grid > p.ntiles) grid = p.ntiles;
+    ctx_timer_begin(ctx, "k_filter_simt");
     k_filter_simt<<<(unsigned)grid, TH, 0, ctx->stream>>>(p);
+    ctx_timer_end(ctx, "k_filter_simt");
     MDET_LAUNCHED(ctx, "k_filter_simt");
     return MDET_OK;
 }

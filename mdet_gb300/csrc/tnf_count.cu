@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                     bulk_g2s(buf0 + (bi ^ 1) * kStage, bytes + nabs, nb, &bars[w][bi ^ 1]);
                 }
             }
-            if (!mbar_wait(&bars[w][bi], phase[bi], flag)) {  // bounded
+            if (!__all_sync(0xffffffffu, mbar_wait(&bars[w][bi], phase[bi], flag))) {  // bounded, warp-uniform
                 ok = false;
                 break;
             }
@@ -360,9 +360,11 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_count, kWarps * 32, dyn);
     if (per_sm < 1) per_sm = 1;
+    ctx_timer_begin(ctx, "k_count");
     k_count<<<ctx->num_sms * per_sm, kWarps * 32, dyn, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
                                                             npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
                                                             ctx->d_flag);
+    ctx_timer_end(ctx, "k_count");
     MDET_LAUNCHED(ctx, "k_count");
     return MDET_OK;
 }

@@ -58,6 +58,9 @@ SIGNATURES = [
     ("mdet_last_error", ctypes.c_char_p, [P]),
     ("mdet_ctx_set_stream", ctypes.c_int, [P, P]),
     ("mdet_version", ctypes.c_char_p, []),
+    ("mdet_ctx_set_timing", ctypes.c_int, [P, ctypes.c_int]),
+    ("mdet_ctx_kernel_ms", ctypes.c_int, [P, ctypes.c_char_p, ctypes.POINTER(D), ctypes.POINTER(u32)]),
+    ("mdet_ctx_launch_count", u64, [P]),
     ("mdet_tnf_count", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_dev", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_max_prob", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
@@ -149,14 +152,33 @@ class Context:
     def set_stream(self, stream_handle: int):
         self._check(self.lib.mdet_ctx_set_stream(self.h, P(stream_handle)))
 
+    def set_timing(self, enable: bool):
+        self._check(self.lib.mdet_ctx_set_timing(self.h, 1 if enable else 0))
+
+    def kernel_ms(self, kernel: str):
+        ms = D()
+        n = u32()
+        self._check(self.lib.mdet_ctx_kernel_ms(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def launch_count(self) -> int:
+        return int(self.lib.mdet_ctx_launch_count(self.h))
+
     # ---- TNF counting -------------------------------------------------
-    def tnf_count(self, data: np.ndarray, seq_off: np.ndarray, seq_len: np.ndarray):
+    def tnf_count(self, data: np.ndarray, seq_off: np.ndarray, seq_len: np.ndarray, out=None):
+        """Counts (n x 136 uint32) and TNF (n x 136 float32); `out` may give
+        preallocated (e.g. pinned) output arrays."""
         data = np.ascontiguousarray(data, dtype=np.uint8)
         off = np.ascontiguousarray(seq_off, dtype=np.uint64)
         ln = np.ascontiguousarray(seq_len, dtype=np.uint64)
         n = off.size
-        counts = np.zeros((n, 136), np.uint32)
-        tnf = np.zeros((n, 136), np.float32)
+        if out is None:
+            counts = np.zeros((n, 136), np.uint32)
+            tnf = np.zeros((n, 136), np.float32)
+        else:
+            counts, tnf = out
+            assert counts.dtype == np.uint32 and tnf.dtype == np.float32 and counts.size >= n * 136
+            assert tnf.size >= n * 136 and counts.flags.c_contiguous and tnf.flags.c_contiguous
         self._check(self.lib.mdet_tnf_count(self.h, _ptr(data), data.size, _ptr(off), _ptr(ln), n, _ptr(counts),
                                             _ptr(tnf)))
         return counts, tnf
@@ -199,20 +221,28 @@ class Context:
     gen_tnf_graph_sample = ptnf_search
 
     # ---- graph ----------------------------------------------------------
-    def tnf_graph(self, tnf, log_size, cutoff, max_edges=200, mode="bf16") -> Graph:
+    def tnf_graph(self, tnf, log_size, cutoff, max_edges=200, mode="bf16", out=None) -> Graph:
+        """Edges (from < to) with sTNF; `out` may give preallocated (e.g.
+        pinned) from/to/sTNF arrays, whose size is the capacity."""
         tnf = np.ascontiguousarray(tnf, dtype=np.float32)
         ls = np.ascontiguousarray(log_size, dtype=np.float64)
         n = tnf.shape[0]
-        cap = max(1, n * max_edges)
-        fr = np.empty(cap, np.uint64)
-        to = np.empty(cap, np.uint64)
-        st = np.empty(cap, np.float64)
+        if out is None:
+            cap = max(1, n * max_edges)
+            fr = np.empty(cap, np.uint64)
+            to = np.empty(cap, np.uint64)
+            st = np.empty(cap, np.float64)
+        else:
+            fr, to, st = out
+            cap = min(fr.size, to.size, st.size)
         ne = u64(0)
         stats = GraphStats()
         self._check(self.lib.mdet_tnf_graph(self.h, _ptr(tnf), _ptr(ls), n, float(cutoff), max_edges, MODES[mode],
                                             _ptr(fr), _ptr(to), _ptr(st), cap, ctypes.byref(ne),
                                             ctypes.byref(stats)))
         k = ne.value
+        if out is not None:
+            return Graph(n, fr[:k], to[:k], st[:k], stats.as_dict())
         return Graph(n, fr[:k].copy(), to[:k].copy(), st[:k].copy(), stats.as_dict())
 
     def tnf_graph_dev(self, d_tnf, d_ls, n, cutoff, max_edges, mode, d_from, d_to, d_stnf, capacity):

@@ -82,6 +82,24 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
 int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const uint64_t* d_off,
                        const uint64_t* d_len, uint64_t n, uint32_t* d_counts, float* d_tnf);
 
+/* Allocation-free TNF counting.  No counterpart in the reference: it exists
+ * for callers that cannot allocate device memory -- a host application that
+ * owns a fixed device arena and passes this library only its own buffers, or
+ * a pipeline where a cudaMalloc (which synchronises the device and can fail
+ * under memory pressure) is not allowed between stages.  Same inputs, outputs
+ * and results as mdet_tnf_count_dev, but no context: the work runs on
+ * `stream` (a cudaStream_t, 0 for the default stream) with its scratch in a
+ * static device array of about 4.9 MB that every GPU loading the library
+ * holds until exit.  Limits: n <= 8192 contigs and at most 65536 16-KB pieces
+ * of sequence (about 1 GB); larger inputs return MDET_ERR_CAPACITY.  The
+ * first call on a device resolves the array's device address there (make it
+ * before any stream capture).  All calls share the one array, so calls whose
+ * work overlaps on the GPU race; serialise them.  The call returns after its
+ * work has finished.  Errors are status codes only (there is no context for
+ * mdet_last_error). */
+int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, const uint64_t* d_off, const uint64_t* d_len,
+                           uint64_t n, uint32_t* d_counts, float* d_tnf, void* stream);
+
 /* ---- max-probability sample --------------------------------------------
  * Replaces launch_tnf_max_prob_sample_kernel_multi (cuda/Cuda2.cu:356-379)
  * with get_tnf_max_prob_sample (cuda/Cuda2.cu:281-314): for each sampled

@@ -18,6 +18,8 @@
 // and the last piece to finish normalises it (and clears the scratch row).
 #include <cub/cub.cuh>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace {
@@ -430,3 +432,125 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- allocation-free variant --
+// Some callers cannot allocate device memory at all: a host application that
+// hands this library fixed device buffers from its own arena, or a pipeline
+// in which a cudaMalloc (which synchronises the device and can fail under
+// memory pressure) is not allowed between its stages.  For them,
+// mdet_tnf_count_noalloc runs the same counting kernels with their scratch in
+// the file-scope array below instead of context-owned buffers.  The array is
+// loaded with the library and held by every GPU that loads it until exit.
+
+#define MDET_NOALLOC_MAX_CONTIGS 8192u
+#define MDET_NOALLOC_MAX_PIECES 65536u
+#define MDET_NOALLOC_CUB_BYTES (64u * 1024u)
+
+namespace {
+// word offsets inside the static scratch
+constexpr uint32_t kNaNp = 0;                                           // npieces[MAX_CONTIGS]
+constexpr uint32_t kNaStart = kNaNp + MDET_NOALLOC_MAX_CONTIGS;         // piece starts
+constexpr uint32_t kNaDone = kNaStart + MDET_NOALLOC_MAX_CONTIGS;       // finished pieces per contig
+constexpr uint32_t kNaMap = kNaDone + MDET_NOALLOC_MAX_CONTIGS;         // piece -> contig
+constexpr uint32_t kNaAcc = kNaMap + MDET_NOALLOC_MAX_PIECES;           // multi-piece accumulators
+constexpr uint32_t kNaWork = kNaAcc + MDET_NOALLOC_MAX_CONTIGS * MDET_NTNF;  // work counter + flag (64 words)
+constexpr uint32_t kNaCub = kNaWork + 64;                               // CUB scan temp storage
+constexpr uint32_t kNaWords = kNaCub + MDET_NOALLOC_CUB_BYTES / 4;      // ~4.9 MB in total
+}  // namespace
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
+
+namespace {
+struct NoallocDevice {
+    uint32_t* scratch = nullptr;  // device address of g_noalloc_scratch
+    int num_sms = 0;
+    int per_sm = 0;
+};
+NoallocDevice g_na_dev[64];
+std::mutex g_na_mutex;
+}  // namespace
+
+extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, const uint64_t* d_off,
+                                      const uint64_t* d_len, uint64_t n, uint32_t* d_counts, float* d_tnf,
+                                      void* stream) {
+    if (n == 0) return MDET_OK;
+    if (!d_bytes || !d_off || !d_len || !d_counts || !d_tnf) return MDET_ERR_INVALID;
+    if (n > MDET_NOALLOC_MAX_CONTIGS) return MDET_ERR_CAPACITY;
+    if (((uintptr_t)d_bytes & 15) != 0) return MDET_ERR_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MDET_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t dyn = (size_t)kWarps * 2 * kStage;
+    {
+        // once per device, with that device current: resolve the array's
+        // device address (host code cannot use the symbol itself)
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        NoallocDevice& d = g_na_dev[dev];
+        if (!d.scratch) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return MDET_ERR_CUDA;
+            }
+            if (cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess ||
+                cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.per_sm, k_count, kWarps * 32, dyn) != cudaSuccess) {
+                cudaGetLastError();
+                return MDET_ERR_CUDA;
+            }
+            if (d.per_sm < 1) d.per_sm = 1;
+            d.scratch = (uint32_t*)p;
+        }
+    }
+    const NoallocDevice& d = g_na_dev[dev];
+    uint32_t* sc = d.scratch;
+    uint32_t* npieces = sc + kNaNp;
+    uint32_t* start = sc + kNaStart;
+    uint32_t* done = sc + kNaDone;
+    uint32_t* pmap = sc + kNaMap;
+    uint32_t* acc = sc + kNaAcc;
+    uint32_t* work = sc + kNaWork;
+    int* flag = (int*)(sc + kNaWork + 1);
+    void* cub_tmp = sc + kNaCub;
+    // the array keeps the previous call's contents: clear what must start at zero
+    if (cudaMemsetAsync(done, 0, (size_t)n * 4, s) != cudaSuccess ||
+        cudaMemsetAsync(acc, 0, (size_t)n * MDET_NTNF * 4, s) != cudaSuccess ||
+        cudaMemsetAsync(work, 0, 64 * 4, s) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_piece_counts<<<blocks, 256, 0, s>>>(d_len, n, npieces);
+    size_t tmp_bytes = 0;
+    if (cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess ||
+        tmp_bytes > MDET_NOALLOC_CUB_BYTES)
+        return MDET_ERR_CUDA;
+    if (cub::DeviceScan::ExclusiveSum(cub_tmp, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    uint32_t tail[2] = {0, 0};
+    if (cudaMemcpyAsync(&tail[0], start + n - 1, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&tail[1], npieces + n - 1, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    if ((uint64_t)tail[0] + tail[1] > MDET_NOALLOC_MAX_PIECES) return MDET_ERR_CAPACITY;
+    k_piece_map<<<blocks, 256, 0, s>>>(npieces, start, n, pmap);
+    FoldTables tabs;
+    const TnTables& t = tn_tables();
+    memcpy(tabs.fw, t.col_fw, MDET_NTNF);
+    memcpy(tabs.rc, t.col_rc, MDET_NTNF);
+    k_count<<<d.num_sms * d.per_sm, kWarps * 32, dyn, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
+                                                           npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
+                                                           flag);
+    if (cudaGetLastError() != cudaSuccess) return MDET_ERR_CUDA;
+    int h_flag = 0;
+    if (cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    return h_flag ? MDET_ERR_TIMEOUT : MDET_OK;
+}

@@ -43,6 +43,24 @@ def dist_env():
     return ws, rank, local
 
 
+def assembly_seed(rank: int) -> int:
+    """Seed of the assembly a rank processes: rank 0 runs the workload's own
+    1M-contig set (seed 2, genomes seeded 2e6+g); every other rank gets an
+    independent assembly of the same shape (weak scaling, no shared data)."""
+    return 2 + 1000 * rank
+
+
+def reduce_max(value: float, device) -> float:
+    """Max over ranks (a no-op without an initialised process group)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_config(n, genomes, mode, ws):
     return {
         "workload": f"synthetic assembly, {n} contigs from {genomes} Markov genomes; TNF count + pTNF search "
@@ -163,7 +181,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
     torch.cuda.set_device(local)
     n, G = args.n, args.genomes
-    seed = 2 + 1000 * rank  # the assembly of rank r; rank 0 is the 1M-contig set of the workload
+    seed = assembly_seed(rank)
     L, g, ro, total = synth.plan(seed, n, G)
     pinned = torch.empty(total + 64, dtype=torch.uint8, pin_memory=True)
     a = synth.generate(seed, n, G, out=pinned.numpy())
@@ -221,10 +239,7 @@ def run_ours(args):
     kern = {k: ctx.kernel_ms(k) for k in ("k_filter_tc", "k_filter_simt", "k_count", "k_exact_graph",
                                           "k_exact_maxprob")}
     ctx.set_timing(False)
-    t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    ms = float(t_max.item())
+    ms = reduce_max(ms, dev)
 
     # ---- e2e through the host-buffer C ABI (pinned buffers, copies timed) ----
     cnt_h = torch.empty((n, 136), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
@@ -255,10 +270,7 @@ def run_ours(args):
         step_e2e()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t) / e2e_steps
-    t_e = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t_e, op=dist.ReduceOp.MAX)
-    e2e_s = float(t_e.item())
+    e2e_s = reduce_max(e2e_s, dev)
     ne = e2e_info["edges"]
     h2d = nbytes + 2 * n * 8 + 2 * (n * 136 * 4 + n * 8)
     d2h = n * 136 * 8 + ne * 24

@@ -44,6 +44,9 @@ struct mdet_ctx {
     void* encode_tiled = nullptr;  // cuTensorMapEncodeTiled entry point
     bool count_scratch_dirty = false;
     uint64_t total_launches = 0;
+    // key of the d* table currently held in scratch "tbl.st"
+    bool tbl_valid = false;
+    double tbl_L = 0, tbl_lmin = 0, tbl_lmax = 0;
     bool timing = false;
     std::unordered_map<std::string, KernelTimer> timers;
 };

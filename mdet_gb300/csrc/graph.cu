@@ -68,7 +68,9 @@ __global__ void k_sample_gather_bf16(const uint32_t* __restrict__ row_map, uint6
         for (int k = threadIdx.x; k < MDET_KPAD; k += blockDim.x) ab[r * MDET_KPAD + k] = xb[(uint64_t)sp * MDET_KPAD + k];
         if (threadIdx.x == 0) ansq[r] = nsq[sp];
     } else {
-        for (int k = threadIdx.x; k < MDET_KPAD; k += blockDim.x) ab[r * MDET_KPAD + k] = 0;
+        // padding row of the A role: zeros with the two unit columns
+        for (int k = threadIdx.x; k < MDET_KPAD; k += blockDim.x)
+            ab[r * MDET_KPAD + k] = (k == MDET_NTNF || k == MDET_NTNF + 1) ? 0x3F80 : 0;
         if (threadIdx.x == 0) ansq[r] = __int_as_float(0x7f800000);
     }
 }
@@ -121,10 +123,10 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
             MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect, tbl,
                                  out));
         } else {
-            const uint16_t* A = rect ? ab : g.xb;
+            const uint16_t* A = rect ? ab : g.xa;
             const float* An = rect ? ansq : g.nsq;
-            MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.nsq, g.n, g.meta, !rect,
-                               tbl, out));
+            MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
+                               out));
         }
         unsigned long long found = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
@@ -237,7 +239,7 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
         ab = (uint16_t*)ctx_scratch(ctx, "mp.ab", mpad * MDET_KPAD * 2);
         ansq = (float*)ctx_scratch(ctx, "mp.ansq", mpad * 4);
         if (!ab || !ansq) return MDET_ERR_NOMEM;
-        k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xb, g.nsq, ab, ansq);
+        k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xa, g.nsq, ab, ansq);
         MDET_LAUNCHED(ctx, "k_sample_gather_bf16");
         k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
         MDET_LAUNCHED(ctx, "k_sample_meta");

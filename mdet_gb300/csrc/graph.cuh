@@ -75,7 +75,8 @@ struct GraphPrep {
     float* x32;                      // sorted FP32 TNF rows [n][136]
     double* ls;                      // sorted log sizes
     ModelParts* parts;               // sorted model parts
-    uint16_t* xb;                    // sorted centred BF16 rows [npad][144]
+    uint16_t* xa;                    // A role: sorted centred BF16 rows [x~, 1, 1, 0..] [npad][144]
+    uint16_t* xb;                    // B role: [x~, -hi(||x~||^2/2), -lo(||x~||^2/2), 0..]; padding -inf
     float* nsq;                      // ||x~||^2 per sorted row (inf for padding rows)
     BlockMeta* meta;                 // per 128-row block (bf16 rounding)
     BlockMeta* meta32;               // per 128-row block (no rounding term)
@@ -101,11 +102,12 @@ struct Ent {
 
 int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ameta, const float* b, uint32_t nb,
                 const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out);
-// Tensor-core filter over centred BF16 rows (a: na rows, b: nb rows, both
-// padded to 256 with zero rows and nsq = +inf).
+// Tensor-core filter over centred BF16 rows: a (A role, na rows) against b
+// (B role, nb rows), both padded to 256 rows; a_nsq = ||a~||^2 (+inf on
+// padding rows).
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
-              const uint16_t* b, const float* b_nsq, uint32_t nb, const BlockMeta* bmeta, bool triangular,
-              const DstarTable& tbl, CandBuf out);
+              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+              CandBuf out);
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
                 Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out);
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,

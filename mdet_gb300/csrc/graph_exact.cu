@@ -298,6 +298,144 @@ __global__ void __launch_bounds__(1024) k_topk_big(const uint32_t* __restrict__ 
     }
 }
 
+// ---- register top-k: warp per contig, entries held in registers ----------
+// Entry i of a chunk of C = 32*E lives in lane i % 32, slot i / 32.  A
+// bitonic network sorts a chunk best-first (exchanges across lanes by
+// shuffles, within a lane by register swaps); a longer row is consumed chunk
+// by chunk, each sorted chunk merged into the running best C (elementwise
+// better of best[i] and chunk[C-1-i] is bitonic, then a bitonic merge), so a
+// row of any length needs C >= max_edges registers' worth of entries only.
+
+__device__ __forceinline__ bool kv_less(double s1, uint32_t c1, double s2, uint32_t c2) {
+    return s1 > s2 || (s1 == s2 && c1 < c2);
+}
+
+template <int E>
+__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, int k, int j,
+                                              bool all_up) {
+    if (j >= 32) {
+        const int je = j >> 5;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            if ((e & je) == 0) {
+                const int e2 = e | je;
+                const bool up = all_up || ((((uint32_t)e * 32u + lane) & (uint32_t)k) == 0);
+                const bool sw = up ? kv_less(s[e2], c[e2], s[e], c[e]) : kv_less(s[e], c[e], s[e2], c[e2]);
+                if (sw) {
+                    const double ts = s[e];
+                    const uint32_t tc = c[e];
+                    s[e] = s[e2];
+                    c[e] = c[e2];
+                    s[e2] = ts;
+                    c[e2] = tc;
+                }
+            }
+        }
+    } else {
+        const bool lower = (lane & (uint32_t)j) == 0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const bool up = all_up || ((((uint32_t)e * 32u + lane) & (uint32_t)k) == 0);
+            const double os = __shfl_xor_sync(0xffffffffu, s[e], j);
+            const uint32_t oc = __shfl_xor_sync(0xffffffffu, c[e], j);
+            const bool take = (lower == up) ? kv_less(os, oc, s[e], c[e]) : kv_less(s[e], c[e], os, oc);
+            if (take) {
+                s[e] = os;
+                c[e] = oc;
+            }
+        }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void bitonic_sort(double (&s)[E], uint32_t (&c)[E], uint32_t lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * E; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) bitonic_stage<E>(s, c, lane, k, j, false);
+}
+
+template <int E>
+__device__ __forceinline__ void load_chunk(const Ent* __restrict__ row, uint32_t base, uint32_t cnt, uint32_t lane,
+                                           double (&s)[E], uint32_t (&c)[E]) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t i = base + (uint32_t)e * 32u + lane;
+        if (i < cnt) {
+            const Ent x = row[i];
+            s[e] = x.sim;
+            c[e] = x.ocol;
+        } else {
+            s[e] = -1.0;
+            c[e] = 0xFFFFFFFFu;
+        }
+    }
+}
+
+// Sorts the row's best min(cnt, keep) entries into row[0..) and returns how
+// many of them have a column above orow (lane 0 holds the total).
+template <int E>
+__device__ __forceinline__ uint32_t topk_row(Ent* __restrict__ row, uint32_t cnt, uint32_t keep, uint32_t orow,
+                                             uint32_t lane) {
+    double bs[E], cs[E];
+    uint32_t bc[E], cc[E];
+    load_chunk<E>(row, 0, cnt, lane, bs, bc);
+    bitonic_sort<E>(bs, bc, lane);
+    for (uint32_t base = 32u * E; base < cnt; base += 32u * E) {
+        load_chunk<E>(row, base, cnt, lane, cs, cc);
+        bitonic_sort<E>(cs, cc, lane);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const double os = __shfl_sync(0xffffffffu, cs[E - 1 - e], 31 - lane);
+            const uint32_t oc = __shfl_sync(0xffffffffu, cc[E - 1 - e], 31 - lane);
+            if (kv_less(os, oc, bs[e], bc[e])) {
+                bs[e] = os;
+                bc[e] = oc;
+            }
+        }
+#pragma unroll
+        for (int j = 16 * E; j > 0; j >>= 1) bitonic_stage<E>(bs, bc, lane, 0, j, true);
+    }
+    __syncwarp();
+    uint32_t n_up = 0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t i = (uint32_t)e * 32u + lane;
+        if (i < keep) {
+            Ent x;
+            x.sim = bs[e];
+            x.ocol = bc[e];
+            x.pad = 0;
+            row[i] = x;
+            n_up += bc[e] > orow;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n_up += __shfl_xor_sync(0xffffffffu, n_up, o);
+    return n_up;
+}
+
+template <int EMAX>
+__global__ void __launch_bounds__(256) k_topk_reg(const unsigned long long* __restrict__ rowptr,
+                                                  const uint32_t* __restrict__ deg, const uint32_t* __restrict__ perm,
+                                                  uint32_t n, uint32_t max_edges, Ent* __restrict__ list,
+                                                  uint32_t* __restrict__ out_cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); s < n; s += gridDim.x * (blockDim.x / 32)) {
+        const uint32_t cnt = deg[s], orow = perm[s];
+        const uint32_t keep = cnt < max_edges ? cnt : max_edges;
+        Ent* row = list + rowptr[s];
+        uint32_t c;
+        if (cnt <= 64)
+            c = topk_row<2>(row, cnt, keep, orow, lane);
+        else if (cnt <= 128 && EMAX >= 4)
+            c = topk_row<(EMAX >= 4 ? 4 : EMAX)>(row, cnt, keep, orow, lane);
+        else
+            c = topk_row<EMAX>(row, cnt, keep, orow, lane);
+        if (lane == 0) out_cnt[orow] = c;
+    }
+}
+
 // Warp per original row: write its kept edges with ocol > row, in order.
 __global__ void k_emit(const uint32_t* __restrict__ inv, const unsigned long long* __restrict__ rowptr,
                        const uint32_t* __restrict__ deg, const Ent* __restrict__ list,
@@ -452,7 +590,17 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
     }
     MDET_CUDA(ctx, cudaMemsetAsync(nbig, 0, 4, s));
     MDET_CUDA(ctx, cudaMemsetAsync(out_cnt, 0, (uint64_t)n * 4, s));
-    {
+    if (max_edges <= 512) {
+        // register top-k (chunk of 256 or 512 entries per warp)
+        const unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + 7) / 8, (uint64_t)ctx->num_sms * 16);
+        ctx_timer_begin(ctx, "k_topk_reg");
+        if (max_edges <= 256)
+            k_topk_reg<8><<<blocks, 256, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+        else
+            k_topk_reg<16><<<blocks, 256, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+        ctx_timer_end(ctx, "k_topk_reg");
+        MDET_LAUNCHED(ctx, "k_topk_reg");
+    } else {
         size_t dyn = (size_t)kTopkWarps * kWarpCap * sizeof(Ent);
         static bool set[64] = {false};
         if (!set[ctx->device & 63]) {

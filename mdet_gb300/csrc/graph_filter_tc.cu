@@ -1,13 +1,14 @@
 // graph_filter_tc.cu -- tensor-core distance filter (tcgen05, sm_103a).
 //
 // The pairwise stage restructured as ||a||^2 + ||b||^2 - 2 a.b over centred
-// BF16 rows: a.b is a 128 x 256 x 144 tile GEMM per (row tile, column tile)
+// BF16 rows: a.b - ||b||^2/2 is a 128 x 256 x 144 tile GEMM per (row tile,
+// column tile) -- the column term rides in two spare K columns --
 // issued by one thread with tcgen05.mma (kind::f16, BF16 x BF16 -> FP32),
 // operands staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
 // swizzle for K 0..127, 32-byte swizzle for K 128..143), accumulators in TMEM
 // (two 256-column buffers, so the epilogue of one tile overlaps the MMA of
 // the next).  The epilogue reads TMEM with tcgen05.ld and keeps pairs with
-//     dot > (||a~||^2 - R^2)/2 + ||b~||^2/2,
+//     a~.b~ - ||b~||^2/2 > (||a~||^2 - R^2)/2,
 // R = d*_tile + e_a + e_b + slack, where d*_tile bounds the model's distance
 // threshold over the tile's sizes and e_a, e_b bound the BF16 rounding of the
 // rows (||a~ - a||).  By the triangle inequality no pair whose exact
@@ -16,8 +17,8 @@
 //
 // Warp roles (10 warps): 0 = TMA producer, 1 = MMA issuer + TMEM owner,
 // 2..9 = epilogue (TMEM lane quarter = warp % 4, column half = (warp-2)/4).
-// Every CTA walks a contiguous range of the row-major tile list, so the A
-// tile (128 rows) is loaded once per row tile and B tiles stream through a
+// CTAs take whole row tiles in waves (see the schedule below), so the A tile
+// (128 rows) is loaded once per row tile and B tiles stream through a
 // two-stage ring.  All waits are bounded.
 #include <cudaTypedefs.h>
 
@@ -39,10 +40,9 @@ constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kSmemBytes = kABytes + 2 * kBBytes + 1024;  // + alignment slack
 
 struct TcArgs {
-    uint32_t na, nb, ta, tb;
+    uint32_t na, nb, ta, tb, segs;
     int triangular;
     const float* a_nsq;
-    const float* b_nsq;
     const BlockMeta* ameta;
     const BlockMeta* bmeta;
     DstarTable tbl;
@@ -105,63 +105,79 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// 64 consecutive FP32 columns of this thread's TMEM lane; the wait sits in
+// the same asm statement, so no use of the registers can be scheduled early.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
+    uint32_t r[64];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+        "%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,"
+        "%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+          "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+          "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+          "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+          "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
-    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+    for (int k = 0; k < 64; ++k) v[k] = __uint_as_float(r[k]);
 }
 
 // ------------------------------------------------------------ schedule --
-
-// Tiles before row tile I in the row-major list (column tiles J >= I/2 in
-// the triangular schedule, all J otherwise).
-__device__ __forceinline__ unsigned long long row_start(const TcArgs& p, unsigned long long I) {
-    if (!p.triangular) return I * p.tb;
-    unsigned long long m = I >> 1;
-    unsigned long long f = (I & 1) ? m * m : m * (m - (m ? 1 : 0));
-    if (!(I & 1) && m == 0) f = 0;
-    return I * p.tb - f;
-}
+// Waves of G row tiles (G = grid size): in wave w, CTA c takes row tile
+// w*G + c (w even) or w*G + G-1-c (w odd), and walks its column tiles J from
+// j_start(I) upward.  All CTAs of a wave sweep the same B tiles at about the
+// same time, so each B tile comes from DRAM about once per wave and from L2
+// for the other CTAs; the snake order evens out the triangular row lengths.
 
 __device__ __forceinline__ uint32_t j_start(const TcArgs& p, uint32_t I) { return p.triangular ? (I >> 1) : 0u; }
 
+// A work unit is one segment of one row tile's column range: p.segs segments
+// per row tile (1 when row tiles outnumber the CTAs).
 struct Cursor {
-    uint32_t I, J;
-    unsigned long long t, t1;
+    uint32_t I, J, Jend, w;
+    bool valid;
 };
 
-__device__ __forceinline__ Cursor cursor_at(const TcArgs& p, unsigned long long t0, unsigned long long t1) {
-    // largest I with row_start(I) <= t0
-    uint32_t lo = 0, hi = p.ta;  // row_start(ta) = ntiles > t0
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (row_start(p, mid) <= t0)
-            lo = mid;
-        else
-            hi = mid;
-    }
-    Cursor c;
-    c.I = lo;
-    c.J = j_start(p, lo) + (uint32_t)(t0 - row_start(p, lo));
-    c.t = t0;
-    c.t1 = t1;
-    return c;
+__device__ __forceinline__ uint32_t unit_of_wave(uint32_t w, uint32_t c, uint32_t G) {
+    return w * G + ((w & 1) ? (G - 1 - c) : c);
 }
 
-__device__ __forceinline__ void advance(const TcArgs& p, Cursor& c) {
-    ++c.t;
-    if (++c.J >= p.tb) {
-        ++c.I;
-        c.J = j_start(p, c.I);
+__device__ __forceinline__ bool set_unit(const TcArgs& p, Cursor& k, uint32_t u) {
+    const uint32_t I = u / p.segs, seg = u % p.segs;
+    if (I >= p.ta) return false;
+    const uint32_t j0 = j_start(p, I), len = p.tb - j0;
+    k.I = I;
+    k.J = j0 + (uint32_t)((uint64_t)len * seg / p.segs);
+    k.Jend = j0 + (uint32_t)((uint64_t)len * (seg + 1) / p.segs);
+    return true;
+}
+
+__device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G);
+
+__device__ __forceinline__ Cursor cursor_first(const TcArgs& p, uint32_t c, uint32_t G) {
+    Cursor k;
+    k.w = 0;
+    k.valid = set_unit(p, k, unit_of_wave(0, c, G));
+    if (k.valid && k.J >= k.Jend) advance(p, k, c, G);  // empty segment
+    return k;
+}
+
+__device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G) {
+    if (++k.J < k.Jend) return;
+    while (true) {
+        ++k.w;
+        if (!set_unit(p, k, unit_of_wave(k.w, c, G))) {
+            k.valid = false;
+            return;
+        }
+        if (k.J < k.Jend) return;
     }
 }
 
@@ -178,8 +194,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     unsigned char* sB = smem + kABytes;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    const unsigned long long G = gridDim.x;
-    const unsigned long long t0 = p.ntiles * blockIdx.x / G, t1 = p.ntiles * (blockIdx.x + 1) / G;
+    const uint32_t G = gridDim.x, cta = blockIdx.x;
 
     if (threadIdx.x == 0) {
         mbar_init(&ctl.a_full, 1);
@@ -210,14 +225,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (t0 < t1) {
+    if (cta < p.ta * p.segs) {
         if (warp == 0) {
             // ------------------------------------------------ TMA producer
             if (lane == 0) {
-                Cursor c = cursor_at(p, t0, t1);
+                Cursor c = cursor_first(p, cta, G);
                 uint32_t a_e_ph = 0, b_e_ph[2] = {0, 0};
                 uint32_t curI = 0xFFFFFFFFu;
-                for (uint32_t lt = 0; c.t < c.t1; ++lt, advance(p, c)) {
+                for (uint32_t lt = 0; c.valid; ++lt, advance(p, c, cta, G)) {
                     if (c.I != curI) {
                         if (!mbar_wait(&ctl.a_empty, a_e_ph ^ 1, p.flag)) break;
                         a_e_ph ^= 1;
@@ -242,11 +257,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         } else if (warp == 1) {
             // -------------------------------------------------- MMA issuer
             if (lane == 0) {
-                Cursor c = cursor_at(p, t0, t1);
+                Cursor c = cursor_first(p, cta, G);
                 uint32_t a_ph = 0, b_ph[2] = {0, 0}, e_ph[2] = {0, 0};
                 uint32_t curI = 0xFFFFFFFFu;
                 const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
-                for (uint32_t lt = 0; c.t < c.t1; ++lt) {
+                for (uint32_t lt = 0; c.valid; ++lt) {
                     if (c.I != curI) {
                         if (!mbar_wait(&ctl.a_full, a_ph, p.flag)) break;
                         a_ph ^= 1;
@@ -276,8 +291,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                     mma_commit(&ctl.b_empty[s]);
                     mma_commit(&ctl.acc_full[s]);
                     Cursor nx = c;
-                    advance(p, nx);
-                    if (nx.t >= nx.t1 || nx.I != c.I) mma_commit(&ctl.a_empty);
+                    advance(p, nx, cta, G);
+                    if (!nx.valid || nx.I != c.I) mma_commit(&ctl.a_empty);
                     c = nx;
                 }
             }
@@ -288,9 +303,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t half = ew >> 2;          // column half of the 256-wide tile
             uint32_t* qc = &ctl.qcount[ew];
             uint2* q = queue[ew];
-            Cursor c = cursor_at(p, t0, t1);
+            Cursor c = cursor_first(p, cta, G);
             uint32_t f_ph[2] = {0, 0};
-            for (uint32_t lt = 0; c.t < c.t1; ++lt, advance(p, c)) {
+            for (uint32_t lt = 0; c.valid; ++lt, advance(p, c, cta, G)) {
                 const uint32_t s = lt & 1;
                 const uint32_t row = c.I * kBM + quarter * 32 + lane;
                 // tile threshold
@@ -300,8 +315,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const float T = tile_dstar(p.tbl, ma.lo, ma.hi, blo, bhi);
                 const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
                 const float N2 = ma.nmax * fmaxf(mb0.nmax, mb1.nmax);
+                // TMEM holds a~.b~ - ||b~||^2/2 (the column term rides in K
+                // columns 136/137); the pair passes when it exceeds
+                // hr = (||a~||^2 - R^2)/2.  Slack: BF16 rounding of rows (E),
+                // FP32 accumulation and the two-term split of ||b~||^2/2.
                 const float R = T * (1.f + 2e-5f) + 1e-6f + E;
-                float R2 = R * R + 4e-5f * N2 + 1e-7f;
+                const float NB2 = fmaxf(mb0.nmax, mb1.nmax) * fmaxf(mb0.nmax, mb1.nmax);
+                float R2 = R * R + 4e-5f * (N2 + NB2) + 1e-7f;
                 if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
                 const float hr = 0.5f * (__ldg(p.a_nsq + row) - R2);
                 const bool diag = p.triangular && (c.J * kBN < c.I * kBM + kBM);
@@ -310,32 +330,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                 f_ph[s] ^= 1;
                 tc_fence_after();
 #pragma unroll 1
-                for (uint32_t ch = 0; ch < 4; ++ch) {
-                    const uint32_t col0 = half * 128 + ch * 32;
-                    float v[32];
-                    tmem_ld32(tmem + ((quarter * 32) << 16) + s * kBN + col0, v);
+                for (uint32_t ch = 0; ch < 2; ++ch) {
+                    const uint32_t col0 = half * 128 + ch * 64;
+                    float v[64];
+                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * kBN + col0, v);
                     const uint32_t gc0 = c.J * kBN + col0;
-                    const float4* hcp = reinterpret_cast<const float4*>(p.b_nsq + gc0);
-                    float m0 = -__int_as_float(0x7f800000), m1 = m0, m2 = m0, m3 = m0;
+                    float mx[8];
 #pragma unroll
-                    for (int k4 = 0; k4 < 8; ++k4) {
-                        const float4 h = __ldg(hcp + k4);
-                        v[4 * k4 + 0] = fmaf(-0.5f, h.x, v[4 * k4 + 0]);
-                        v[4 * k4 + 1] = fmaf(-0.5f, h.y, v[4 * k4 + 1]);
-                        v[4 * k4 + 2] = fmaf(-0.5f, h.z, v[4 * k4 + 2]);
-                        v[4 * k4 + 3] = fmaf(-0.5f, h.w, v[4 * k4 + 3]);
-                        m0 = fmaxf(m0, v[4 * k4 + 0]);
-                        m1 = fmaxf(m1, v[4 * k4 + 1]);
-                        m2 = fmaxf(m2, v[4 * k4 + 2]);
-                        m3 = fmaxf(m3, v[4 * k4 + 3]);
-                    }
-                    const float m = fmaxf(fmaxf(m0, m1), fmaxf(m2, m3));
+                    for (int k = 0; k < 8; ++k) mx[k] = fmaxf(v[k], v[k + 8]);
+#pragma unroll
+                    for (int k = 16; k < 64; k += 8)
+#pragma unroll
+                        for (int t = 0; t < 8; ++t) mx[t] = fmaxf(mx[t], v[k + t]);
+                    const float m = fmaxf(fmaxf(fmaxf(mx[0], mx[1]), fmaxf(mx[2], mx[3])),
+                                          fmaxf(fmaxf(mx[4], mx[5]), fmaxf(mx[6], mx[7])));
                     if (m > hr) {
-                        uint32_t mask = 0;
+                        unsigned long long mask = 0;
 #pragma unroll
-                        for (int k = 0; k < 32; ++k) mask |= (v[k] > hr ? 1u : 0u) << k;
+                        for (int k = 0; k < 64; ++k) mask |= (unsigned long long)(v[k] > hr ? 1u : 0u) << k;
                         while (mask) {
-                            const int k = __ffs(mask) - 1;
+                            const int k = __ffsll((long long)mask) - 1;
                             mask &= mask - 1;
                             const uint32_t col = gc0 + k;
                             if (col < p.nb && row < p.na && (!diag || col > row)) {
@@ -421,8 +435,8 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
 }  // namespace
 
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
-              const uint16_t* b, const float* b_nsq, uint32_t nb, const BlockMeta* bmeta, bool triangular,
-              const DstarTable& tbl, CandBuf out) {
+              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+              CandBuf out) {
     if (na == 0 || nb == 0) return MDET_OK;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
@@ -437,7 +451,6 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     p.tb = (nb + kBN - 1) / kBN;
     p.triangular = triangular ? 1 : 0;
     p.a_nsq = a_nsq;
-    p.b_nsq = b_nsq;
     p.ameta = ameta;
     p.bmeta = bmeta;
     p.tbl = tbl;
@@ -455,7 +468,11 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
         MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
         attr[ctx->device & 63] = true;
     }
-    unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)ctx->num_sms, total);
+    // enough work units for every SM: split row tiles into column segments when they are few
+    p.segs = 1;
+    while ((uint64_t)p.ta * p.segs < 2ull * ctx->num_sms && p.segs < p.tb) ++p.segs;
+    unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)ctx->num_sms,
+                                                           (unsigned long long)p.ta * p.segs);
     ctx_timer_begin(ctx, "k_filter_tc");
     k_filter_tc<<<grid, kThreads, kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");

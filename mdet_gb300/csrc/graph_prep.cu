@@ -74,17 +74,26 @@ __global__ void k_mean(const double* __restrict__ sums, uint64_t n, float* __res
     if (k < MDET_NTNF) mu[k] = (float)(sums[k] / (double)n);
 }
 
-// Warp per sorted row: centred BF16 copy, its squared norm and its exact
-// distance to the unrounded centred row.
+// Warp per sorted row: centred BF16 copies in both GEMM roles, the squared
+// norm of the rounded row, and its exact distance to the unrounded centred
+// row.  Columns 136/137 fold the column term of ||a||^2+||b||^2-2a.b into the
+// GEMM: the A role carries 1, 1 and the B role -hi, -lo of ||b~||^2/2 (a
+// two-term BF16 split), so a.b' = a.b - ||b~||^2/2 comes out of TMEM.
 __global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ mu, uint64_t n, uint64_t npad,
-                       uint16_t* __restrict__ xb, float* __restrict__ nsq, float* __restrict__ err,
-                       float* __restrict__ nrm) {
+                       uint16_t* __restrict__ xa, uint16_t* __restrict__ xb, float* __restrict__ nsq,
+                       float* __restrict__ err, float* __restrict__ nrm) {
     uint64_t s = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
     uint32_t lane = threadIdx.x & 31;
     if (s >= npad) return;
-    uint16_t* row = xb + s * MDET_KPAD;
+    uint16_t* rowa = xa + s * MDET_KPAD;
+    uint16_t* rowb = xb + s * MDET_KPAD;
+    const uint16_t one = 0x3F80;      // bf16 1.0
+    const uint16_t neg_inf = 0xFF80;  // bf16 -inf
     if (s >= n) {
-        for (int k = lane; k < MDET_KPAD; k += 32) row[k] = 0;
+        for (int k = lane; k < MDET_KPAD; k += 32) {
+            rowa[k] = (k == MDET_NTNF || k == MDET_NTNF + 1) ? one : 0;
+            rowb[k] = (k == MDET_NTNF) ? neg_inf : 0;
+        }
         if (lane == 0) {
             nsq[s] = __int_as_float(0x7f800000);
             err[s] = 0.f;
@@ -93,24 +102,31 @@ __global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ 
         return;
     }
     double e2 = 0, q = 0;
-    for (int k = lane; k < MDET_KPAD; k += 32) {
-        uint16_t b = 0;
-        if (k < MDET_NTNF) {
-            float a = x32[s * MDET_NTNF + k];
-            float v = a - mu[k];
-            __nv_bfloat16 h = __float2bfloat16_rn(v);
-            b = *reinterpret_cast<uint16_t*>(&h);
-            double hv = (double)__bfloat162float(h);
-            double ex = (double)a - (double)mu[k];
-            e2 += (hv - ex) * (hv - ex);
-            q += hv * hv;
-        }
-        row[k] = b;
+    for (int k = lane; k < MDET_NTNF; k += 32) {
+        float a = x32[s * MDET_NTNF + k];
+        float v = a - mu[k];
+        __nv_bfloat16 h = __float2bfloat16_rn(v);
+        uint16_t b = *reinterpret_cast<uint16_t*>(&h);
+        double hv = (double)__bfloat162float(h);
+        double ex = (double)a - (double)mu[k];
+        e2 += (hv - ex) * (hv - ex);
+        q += hv * hv;
+        rowa[k] = b;
+        rowb[k] = b;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         e2 += __shfl_xor_sync(0xffffffffu, e2, o);
         q += __shfl_xor_sync(0xffffffffu, q, o);
+    }
+    const float half = (float)(0.5 * q);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(half);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(half - __bfloat162float(hi));
+    const uint16_t nhi = *reinterpret_cast<const uint16_t*>(&hi) ^ 0x8000u;
+    const uint16_t nlo = *reinterpret_cast<const uint16_t*>(&lo) ^ 0x8000u;
+    for (int k = MDET_NTNF + lane; k < MDET_KPAD; k += 32) {
+        rowa[k] = (k < MDET_NTNF + 2) ? one : 0;
+        rowb[k] = k == MDET_NTNF ? nhi : (k == MDET_NTNF + 1 ? nlo : 0);
     }
     if (lane == 0) {
         nsq[s] = (float)q;
@@ -246,6 +262,7 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
     MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s));
     k_gather<<<(unsigned)n, 64, 0, s>>>(d_tnf, d_ls, g->perm, n, g->inv, g->x32, g->ls, g->parts, model_split());
     MDET_LAUNCHED(ctx, "k_gather");
+    g->xa = nullptr;
     g->xb = nullptr;
     g->nsq = nullptr;
     g->meta = nullptr;
@@ -257,13 +274,14 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
         MDET_LAUNCHED(ctx, "k_colsum");
         k_mean<<<1, MDET_NTNF, 0, s>>>(sums, n, g->mu);
         MDET_LAUNCHED(ctx, "k_mean");
+        g->xa = (uint16_t*)ctx_scratch(ctx, "pre.xa", npad * MDET_KPAD * 2);
         g->xb = (uint16_t*)ctx_scratch(ctx, "pre.xb", npad * MDET_KPAD * 2);
         g->nsq = (float*)ctx_scratch(ctx, "pre.nsq", npad * 4);
         err = (float*)ctx_scratch(ctx, "pre.err", npad * 4);
         nrm = (float*)ctx_scratch(ctx, "pre.nrm", npad * 4);
         g->meta = (BlockMeta*)ctx_scratch(ctx, "pre.meta", nblk * sizeof(BlockMeta));
-        if (!g->xb || !g->nsq || !err || !nrm || !g->meta) return MDET_ERR_NOMEM;
-        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(g->x32, g->mu, n, npad, g->xb, g->nsq, err, nrm);
+        if (!g->xa || !g->xb || !g->nsq || !err || !nrm || !g->meta) return MDET_ERR_NOMEM;
+        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(g->x32, g->mu, n, npad, g->xa, g->xb, g->nsq, err, nrm);
         MDET_LAUNCHED(ctx, "k_bf16");
     }
     k_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(g->ls, err, nrm, n, nblk, g->meta, g->meta32);
@@ -284,8 +302,19 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
     MDET_CUDA(ctx, cudaMemcpyAsync(range, mm, 16, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
     double lmin = range[0], lmax = range[1];
+    const bool same = ctx->tbl_valid && ctx->tbl_L == logit_cut && ctx->tbl_lmin == lmin && ctx->tbl_lmax == lmax;
     double h = (lmax - lmin) / MDET_TBL;
     if (!(h > 1e-7)) h = 1e-7;
+    if (same) {  // the table in scratch was built for this cutoff and size range
+        out->st = st;
+        out->lmin = (float)(lmin - 1e-9);
+        out->inv_h = (float)(1.0 / h);
+        return MDET_OK;
+    }
+    ctx->tbl_valid = false;
+    ctx->tbl_L = logit_cut;
+    ctx->tbl_lmin = lmin;
+    ctx->tbl_lmax = lmax;
     lmin -= 1e-9;
     dim3 grid((kPts + 127) / 128, kPts);
     k_dstar_points<<<grid, 128, 0, s>>>(lmin, h, logit_cut, model_split(), pts);
@@ -299,5 +328,6 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
     out->st = st;
     out->lmin = (float)lmin;
     out->inv_h = (float)(1.0 / h);
+    ctx->tbl_valid = true;
     return MDET_OK;
 }

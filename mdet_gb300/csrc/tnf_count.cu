@@ -115,15 +115,22 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint32_t hist_all[kWarps][256];
     __shared__ uint64_t bars[kWarps][2];
+    // byte -> update word: 2-bit base code | 0x300 when not a base | 0x8000 for '\n'
+    __shared__ uint16_t lut[256];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned char* buf0 = smem + (size_t)w * 2 * kStage;
     uint32_t* hist = hist_all[w];
+    for (uint32_t c = threadIdx.x; c < 256; c += blockDim.x) {
+        const uint32_t u = (c | 0x20u) - 0x61u;
+        const uint32_t valid = (u < 20u) ? ((0x80045u >> u) & 1u) : 0u;
+        lut[c] = (uint16_t)(c == '\n' ? 0x8000u : (((c >> 1) & 3u) | (valid ? 0u : 0x300u)));
+    }
     if (lane == 0) {
         mbar_init(&bars[w][0], 1);
         mbar_init(&bars[w][1], 1);
         mbar_fence_init();
     }
-    __syncwarp();
+    __syncthreads();
     uint32_t phase[2] = {0, 0};
     const uint32_t total = piece_start[n - 1] + npieces[n - 1];
 
@@ -207,15 +214,33 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                 if (cofs >= sbytes) act = 0;
                 uint32_t words[4] = {v.x, v.y, v.z, v.w};
                 // pass over the chunk from a fully poisoned state
-                uint32_t x = kPoison, nact = 0;
+                uint32_t x = kPoison, nact = 0, x3 = 0, nlm = 0;
+                const bool full = act == 0xFFFFu;
+                if (full) {
+                    // every byte of the chunk is in the piece: table-driven
+                    // update, newline bytes leave the state unchanged
 #pragma unroll
-                for (int b = 0; b < 16; ++b) {
-                    uint32_t ch = (words[b >> 2] >> (8 * (b & 3))) & 0xFFu;
-                    bool on = ((act >> b) & 1u) && ch != '\n';
-                    if (on) {
-                        x = shift_in(x, ch);
-                        ++nact;
-                        if (x < 256u) atomicAdd(&hist[x], 1u);
+                    for (int b = 0; b < 16; ++b) {
+                        const uint32_t ch = __byte_perm(words[b >> 2], 0u, 0x4440u | (uint32_t)(b & 3));
+                        const uint32_t m = lut[ch];
+                        const uint32_t nl = m >> 15;
+                        const uint32_t xn = ((x << 2) & 0xFCFCu) | (m & 0x3FFu);
+                        x = nl ? x : xn;
+                        nlm |= nl << b;
+                        if (!nl && x < 256u) atomicAdd(&hist[x], 1u);
+                        if (b == 2) x3 = x;
+                    }
+                    nact = 16u - __popc(nlm);
+                } else {
+#pragma unroll
+                    for (int b = 0; b < 16; ++b) {
+                        uint32_t ch = (words[b >> 2] >> (8 * (b & 3))) & 0xFFu;
+                        bool on = ((act >> b) & 1u) && ch != '\n';
+                        if (on) {
+                            x = shift_in(x, ch);
+                            ++nact;
+                            if (x < 256u) atomicAdd(&hist[x], 1u);
+                        }
                     }
                 }
                 uint32_t cnt = nact < 4 ? nact : 4;
@@ -248,7 +273,15 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                     carry = (last >> 16) >= 3 ? (last & 0xFFFFu) : compose(carry, last & 0xFFFFu, last >> 16);
                 }
                 // the first (up to) three windows of the chunk depend on the carry-in
-                if (nact > 0) {
+                if (full && (nlm & 7u) == 0) {
+                    // bytes 0..2 are bases: x3 holds them in slots 2, 1, 0
+                    const uint32_t w1 = compose(cin, x3 >> 4, 1);
+                    const uint32_t w2 = compose(cin, x3 >> 2, 2);
+                    const uint32_t w3 = compose(cin, x3, 3);
+                    if (w1 < 256u) atomicAdd(&hist[w1], 1u);
+                    if (w2 < 256u) atomicAdd(&hist[w2], 1u);
+                    if (w3 < 256u) atomicAdd(&hist[w3], 1u);
+                } else if (nact > 0) {
                     uint32_t y = cin, seen = 0;
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {

@@ -237,7 +237,7 @@ def run_ours(args):
     launches = ctx.launch_count() - launches0
     ms = e0.elapsed_time(e1) / args.steps
     kern = {k: ctx.kernel_ms(k) for k in ("k_filter_tc", "k_filter_simt", "k_count", "k_exact_graph",
-                                          "k_exact_maxprob")}
+                                          "k_exact_maxprob", "k_topk_reg", "k_scatter")}
     ctx.set_timing(False)
     ms = reduce_max(ms, dev)
 
@@ -280,7 +280,7 @@ def run_ours(args):
         pk, pk_kind = peaks()
         st = info["stats"]
         # dominant kernel and its roofline
-        totals = {k: v[0] for k, v in kern.items() if v[1] > 0}
+        totals = {k: v[0] for k, v in kern.items() if v[1] > 0 and k in ("k_filter_tc", "k_filter_simt", "k_count")}
         dom = max(totals, key=totals.get)
         dom_ms, dom_launches = kern[dom]
         nsample = 10 * min(n, 2500) if n > 25000 else n

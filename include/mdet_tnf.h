@@ -142,6 +142,58 @@ int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_si
                        double cutoff, uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to,
                        double* d_stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
 
+/* ---- learned proposal (no counterpart in the reference) ----------------
+ * A 136 -> 256 -> 128 -> 64 GELU network (BF16 weights, FP32 accumulation)
+ * embeds each TNF row.  In MDET_MODE_LEARNED the graph orders contigs by
+ * their embedding, skips tile pairs whose embedded distance bound exceeds
+ * the trained margin tau, scores the remaining tiles exactly (tensor-core
+ * filter + exact stage), then measures edge recall on a row sample against
+ * the all-pairs result and falls back to the all-pairs form below target. */
+typedef struct mdet_mlp mdet_mlp;
+
+typedef struct {
+    uint64_t pairs;            /* training pair pool (0: 50,000,000) */
+    double candidate_fraction; /* share of the pool drawn from the distance filter's candidates */
+    double label_cutoff;       /* edge labels: exact probability above this cutoff (0.7) */
+    uint64_t steps;            /* optimiser steps (0: one pass over the pool) */
+    uint32_t batch_pairs;      /* pairs per step (0: 8192) */
+    float lr, m_pos, m_neg;    /* Adam learning rate; contrastive margins of edges / non-edges */
+    double tau_quantile;       /* quantile of held-out edge distances that sets tau (0: 0.9995) */
+    uint64_t seed;
+} mdet_train_params;
+
+typedef struct {
+    uint64_t steps, pairs, candidate_pairs, held_pos, held_neg;
+    double final_loss, tau, pos_median, neg_median, neg_below_tau;
+} mdet_train_report;
+
+typedef struct {
+    double recall_target;      /* fall back to all pairs below this estimated recall (0.999) */
+    uint32_t recall_rows;      /* rows sampled for the recall estimate (1024) */
+    uint32_t reserved;
+    double recall;             /* out: estimated edge recall of the learned graph */
+    uint32_t fell_back;        /* out: 1 when the all-pairs graph was returned */
+    uint32_t reserved2;
+    uint64_t tiles_skipped;    /* out */
+} mdet_learned_report;
+
+int mdet_mlp_create(mdet_ctx* ctx, uint64_t seed, mdet_mlp** out);
+int mdet_mlp_destroy(mdet_mlp* mlp);
+uint64_t mdet_mlp_param_count(void);
+int mdet_mlp_get_params(mdet_ctx* ctx, const mdet_mlp* mlp, float* host, uint64_t count);
+int mdet_mlp_set_params(mdet_ctx* ctx, mdet_mlp* mlp, const float* host, uint64_t count);
+int mdet_mlp_embed_dev(mdet_ctx* ctx, const mdet_mlp* mlp, const float* d_tnf, uint64_t n, float* d_out);
+/* Mean contrastive loss and its gradient over host rows x (rows x 136 TNF),
+ * pairs[2p], pairs[2p+1] indexing x -- for checking the backward kernels. */
+int mdet_mlp_grad(mdet_ctx* ctx, const mdet_mlp* mlp, const float* x, uint64_t rows, const uint32_t* pairs,
+                  const float* labels, uint64_t n_pairs, float m_pos, float m_neg, float* grad_out,
+                  double* loss_out);
+int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* mlp, const float* d_tnf, const double* d_log_size, uint64_t n,
+                   const mdet_train_params* params, mdet_train_report* report);
+/* Network (and options) used by MDET_MODE_LEARNED calls of this context;
+ * report may be null; the context keeps both pointers. */
+int mdet_ctx_set_learned(mdet_ctx* ctx, const mdet_mlp* mlp, mdet_learned_report* report);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,7 +83,10 @@ struct GraphPrep {
     float* mu;                       // column means [136]
 };
 
-int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out);
+// Prepares the contigs in ascending log-size order, or in `order` (original
+// index per position, device) when given.
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out,
+                const uint32_t* order = nullptr);
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out);
 ModelH model_h();
 
@@ -105,9 +108,11 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
 // Tensor-core filter over centred BF16 rows: a (A role, na rows) against b
 // (B role, nb rows), both padded to 256 rows; a_nsq = ||a~||^2 (+inf on
 // padding rows).
+// tiles/nlist: optional row-major list (I * tiles_b + J) of the tile pairs
+// to evaluate (column tiles of 256); null evaluates the whole schedule.
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
-              CandBuf out);
+              CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0);
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
                 Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out);
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,

@@ -11,74 +11,11 @@
 // (i, j) is emitted for i < j in original indices (cuda/Cuda2.cu:921-946).
 #include <cub/cub.cuh>
 
-#include "graph.cuh"
+#include "exact.cuh"
+
+using namespace mdet_exact;
 
 namespace {
-
-constexpr double kLn9 = 2.1972245773362196;
-
-__device__ __forceinline__ double horner_h(const double* h, double t) {
-    return t * fma(t, fma(t, fma(t, fma(t, h[5], h[4]), h[3]), h[2]), h[1]);
-}
-
-__device__ __forceinline__ unsigned long long dkey(double v) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
-}
-__device__ __forceinline__ double dkey_inv(unsigned long long k) {
-    unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
-    return __longlong_as_double((long long)b);
-}
-
-// d in the reference's terms float((a_k-b_k)^2) (cuda/Cuda2.cu:194-196).
-// The reference adds them in FP64; FP64 throughput is scarce on this part, so
-// two FP32 chains with error-free TwoSum compensation carry the sum instead
-// (relative error ~1e-14, the same order as the FP64 accumulation), and only
-// the final combine and sqrt run in FP64.
-__device__ __forceinline__ void two_sum_acc(float& s, float& c, float t) {
-    const float sum = __fadd_rn(s, t);
-    const float bp = __fsub_rn(sum, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(sum, bp)), __fsub_rn(t, bp));
-    s = sum;
-    c = __fadd_rn(c, err);
-}
-
-__device__ __forceinline__ double exact_dist(const float* __restrict__ a, const float* __restrict__ b) {
-    const float4* ra = reinterpret_cast<const float4*>(a);
-    const float4* rb = reinterpret_cast<const float4*>(b);
-    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
-#pragma unroll 2
-    for (int q = 0; q < MDET_NTNF / 4; ++q) {
-        float4 x = __ldg(ra + q), y = __ldg(rb + q);
-        float d0 = __fsub_rn(x.x, y.x), d1 = __fsub_rn(x.y, y.y), d2 = __fsub_rn(x.z, y.z), d3 = __fsub_rn(x.w, y.w);
-        two_sum_acc(s0, c0, __fmul_rn(d0, d0));
-        two_sum_acc(s1, c1, __fmul_rn(d1, d1));
-        two_sum_acc(s0, c0, __fmul_rn(d2, d2));
-        two_sum_acc(s1, c1, __fmul_rn(d3, d3));
-    }
-    return sqrt(((double)s0 + (double)s1) + ((double)c0 + (double)c1));
-}
-
-// pre-probability of sorted contigs i, j at distance d.  need_model2: also
-// evaluate the second model when the first is at or below log(9).
-__device__ __forceinline__ double pre_prob(const ModelParts& pi, const ModelParts& pj, double li, double lj, double d,
-                                           const ModelH& H, bool need_model2) {
-    const bool imin = li <= lj;
-    const ModelParts& pmin = imin ? pi : pj;
-    const ModelParts& pmax = imin ? pj : pi;
-    const double t = li * lj;
-    double b = pmin.f[0] + pmax.g[0] + horner_h(H.h[0], t);
-    double c = pmin.f[1] + pmax.g[1] + horner_h(H.h[1], t);
-    double pre = -(b + c * d);
-    if (pre <= kLn9) {
-        if (!need_model2) return pre;
-        b = pmin.f[2] + pmax.g[2] + horner_h(H.h[2], t);
-        c = pmin.f[3] + pmax.g[3] + horner_h(H.h[3], t);
-        pre = -(b + c * d);
-        if (pre > kLn9) pre = kLn9;
-    }
-    return pre;
-}
 
 struct ExactArgs {
     const uint2* cand;
@@ -310,49 +247,55 @@ __device__ __forceinline__ bool kv_less(double s1, uint32_t c1, double s2, uint3
     return s1 > s2 || (s1 == s2 && c1 < c2);
 }
 
-template <int E>
-__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, int k, int j,
+// In-lane compare-exchange of slots e and e | JE (stride >= 32 entries).
+template <int E, int JE>
+__device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k,
                                               bool all_up) {
-    if (j >= 32) {
-        const int je = j >> 5;
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            if ((e & je) == 0) {
-                const int e2 = e | je;
-                const bool up = all_up || ((((uint32_t)e * 32u + lane) & (uint32_t)k) == 0);
-                const bool sw = up ? kv_less(s[e2], c[e2], s[e], c[e]) : kv_less(s[e], c[e], s[e2], c[e2]);
-                if (sw) {
-                    const double ts = s[e];
-                    const uint32_t tc = c[e];
-                    s[e] = s[e2];
-                    c[e] = c[e2];
-                    s[e2] = ts;
-                    c[e2] = tc;
-                }
-            }
+    for (int e = 0; e < E; ++e) {
+        if ((e & JE) == 0) {
+            const int e2 = e | JE;
+            const bool up = all_up || ((((uint32_t)e * 32u + lane) & k) == 0);
+            const bool sw = up ? kv_less(s[e2], c[e2], s[e], c[e]) : kv_less(s[e], c[e], s[e2], c[e2]);
+            const double s1 = sw ? s[e2] : s[e], s2 = sw ? s[e] : s[e2];
+            const uint32_t c1 = sw ? c[e2] : c[e], c2 = sw ? c[e] : c[e2];
+            s[e] = s1;
+            s[e2] = s2;
+            c[e] = c1;
+            c[e2] = c2;
         }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k, uint32_t j,
+                                           bool all_up) {
+    if (j >= 32) {
+        const uint32_t je = j >> 5;
+        if (je == 1) stage_in_lane<E, 1>(s, c, lane, k, all_up);
+        if (E >= 4 && je == 2) stage_in_lane<E, (E >= 4 ? 2 : 1)>(s, c, lane, k, all_up);
+        if (E >= 8 && je == 4) stage_in_lane<E, (E >= 8 ? 4 : 1)>(s, c, lane, k, all_up);
+        if (E >= 16 && je == 8) stage_in_lane<E, (E >= 16 ? 8 : 1)>(s, c, lane, k, all_up);
     } else {
-        const bool lower = (lane & (uint32_t)j) == 0;
+        const bool lower = (lane & j) == 0;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            const bool up = all_up || ((((uint32_t)e * 32u + lane) & (uint32_t)k) == 0);
-            const double os = __shfl_xor_sync(0xffffffffu, s[e], j);
-            const uint32_t oc = __shfl_xor_sync(0xffffffffu, c[e], j);
+            const bool up = all_up || ((((uint32_t)e * 32u + lane) & k) == 0);
+            const double os = __shfl_xor_sync(0xffffffffu, s[e], (int)j);
+            const uint32_t oc = __shfl_xor_sync(0xffffffffu, c[e], (int)j);
             const bool take = (lower == up) ? kv_less(os, oc, s[e], c[e]) : kv_less(s[e], c[e], os, oc);
-            if (take) {
-                s[e] = os;
-                c[e] = oc;
-            }
+            s[e] = take ? os : s[e];
+            c[e] = take ? oc : c[e];
         }
     }
 }
 
 template <int E>
 __device__ __forceinline__ void bitonic_sort(double (&s)[E], uint32_t (&c)[E], uint32_t lane) {
-#pragma unroll
-    for (int k = 2; k <= 32 * E; k <<= 1)
-#pragma unroll
-        for (int j = k >> 1; j > 0; j >>= 1) bitonic_stage<E>(s, c, lane, k, j, false);
+#pragma unroll 1
+    for (uint32_t k = 2; k <= 32u * E; k <<= 1)
+#pragma unroll 1
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_stage<E>(s, c, lane, k, j, false);
 }
 
 template <int E>
@@ -393,8 +336,8 @@ __device__ __forceinline__ uint32_t topk_row(Ent* __restrict__ row, uint32_t cnt
                 bc[e] = oc;
             }
         }
-#pragma unroll
-        for (int j = 16 * E; j > 0; j >>= 1) bitonic_stage<E>(bs, bc, lane, 0, j, true);
+#pragma unroll 1
+        for (uint32_t j = 16u * E; j > 0; j >>= 1) bitonic_stage<E>(bs, bc, lane, 0, j, true);
     }
     __syncwarp();
     uint32_t n_up = 0;
@@ -426,10 +369,8 @@ __global__ void __launch_bounds__(256) k_topk_reg(const unsigned long long* __re
         const uint32_t keep = cnt < max_edges ? cnt : max_edges;
         Ent* row = list + rowptr[s];
         uint32_t c;
-        if (cnt <= 64)
-            c = topk_row<2>(row, cnt, keep, orow, lane);
-        else if (cnt <= 128 && EMAX >= 4)
-            c = topk_row<(EMAX >= 4 ? 4 : EMAX)>(row, cnt, keep, orow, lane);
+        if (cnt <= 128)
+            c = topk_row<4>(row, cnt, keep, orow, lane);
         else
             c = topk_row<EMAX>(row, cnt, keep, orow, lane);
         if (lane == 0) out_cnt[orow] = c;
@@ -585,7 +526,9 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
     MDET_CUDA(ctx, cudaMemsetAsync(cursor, 0, (uint64_t)n * 4, s));
     if (ne) {
         unsigned long long blocks = (ne + 255) / 256, cap = (unsigned long long)ctx->num_sms * 16;
+        ctx_timer_begin(ctx, "k_scatter");
         k_scatter<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(edges, ne, g.perm, rowptr, cursor, list);
+        ctx_timer_end(ctx, "k_scatter");
         MDET_LAUNCHED(ctx, "k_scatter");
     }
     MDET_CUDA(ctx, cudaMemsetAsync(nbig, 0, 4, s));

@@ -41,6 +41,8 @@ constexpr uint32_t kSmemBytes = kABytes + 2 * kBBytes + 1024;  // + alignment sl
 
 struct TcArgs {
     uint32_t na, nb, ta, tb, segs;
+    const uint32_t* tiles;  // optional list of tiles (I * tb + J, row-major); null: full schedule
+    uint64_t nlist;
     int triangular;
     const float* a_nsq;
     const BlockMeta* ameta;
@@ -142,6 +144,7 @@ __device__ __forceinline__ uint32_t j_start(const TcArgs& p, uint32_t I) { retur
 // per row tile (1 when row tiles outnumber the CTAs).
 struct Cursor {
     uint32_t I, J, Jend, w;
+    uint64_t li, lend;  // list mode: current and end index
     bool valid;
 };
 
@@ -161,8 +164,24 @@ __device__ __forceinline__ bool set_unit(const TcArgs& p, Cursor& k, uint32_t u)
 
 __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G);
 
+__device__ __forceinline__ void list_decode(const TcArgs& p, Cursor& k) {
+    k.valid = k.li < k.lend;
+    if (k.valid) {
+        const uint32_t t = p.tiles[k.li];
+        k.I = t / p.tb;
+        k.J = t % p.tb;
+    }
+}
+
 __device__ __forceinline__ Cursor cursor_first(const TcArgs& p, uint32_t c, uint32_t G) {
     Cursor k;
+    if (p.tiles) {
+        // list mode: CTA c takes a contiguous range of the row-major list
+        k.li = p.nlist * c / G;
+        k.lend = p.nlist * (c + 1) / G;
+        list_decode(p, k);
+        return k;
+    }
     k.w = 0;
     k.valid = set_unit(p, k, unit_of_wave(0, c, G));
     if (k.valid && k.J >= k.Jend) advance(p, k, c, G);  // empty segment
@@ -170,6 +189,11 @@ __device__ __forceinline__ Cursor cursor_first(const TcArgs& p, uint32_t c, uint
 }
 
 __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G) {
+    if (p.tiles) {
+        ++k.li;
+        list_decode(p, k);
+        return;
+    }
     if (++k.J < k.Jend) return;
     while (true) {
         ++k.w;
@@ -225,7 +249,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     tc_fence_after();
     const uint32_t tmem = ctl.tmem_base;
 
-    if (cta < p.ta * p.segs) {
+    {
         if (warp == 0) {
             // ------------------------------------------------ TMA producer
             if (lane == 0) {
@@ -436,7 +460,7 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
 
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
-              CandBuf out) {
+              CandBuf out, const uint32_t* tiles, uint64_t nlist) {
     if (na == 0 || nb == 0) return MDET_OK;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
@@ -471,8 +495,11 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     // enough work units for every SM: split row tiles into column segments when they are few
     p.segs = 1;
     while ((uint64_t)p.ta * p.segs < 2ull * ctx->num_sms && p.segs < p.tb) ++p.segs;
+    p.tiles = tiles;
+    p.nlist = nlist;
     unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)ctx->num_sms,
-                                                           (unsigned long long)p.ta * p.segs);
+                                                           tiles ? nlist : (unsigned long long)p.ta * p.segs);
+    if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
     k_filter_tc<<<grid, kThreads, kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");

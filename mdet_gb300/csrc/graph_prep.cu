@@ -145,8 +145,14 @@ __global__ void k_meta(const double* __restrict__ ls_s, const float* __restrict_
         m.lo = m.hi = (float)ls_s[n - 1];
         m.emax = m.nmax = 0.f;
     } else {
-        m.lo = __double2float_rd(ls_s[s0]);
-        m.hi = __double2float_ru(ls_s[s1 - 1]);
+        // true range (the rows need not be in size order)
+        double lo = ls_s[s0], hi = ls_s[s0];
+        for (uint64_t s = s0 + 1; s < s1; ++s) {
+            lo = fmin(lo, ls_s[s]);
+            hi = fmax(hi, ls_s[s]);
+        }
+        m.lo = __double2float_rd(lo);
+        m.hi = __double2float_ru(hi);
         float e = 0.f, nm = 0.f;
         if (err)
             for (uint64_t s = s0; s < s1; ++s) {
@@ -232,7 +238,8 @@ ModelH model_h() {
     return h;
 }
 
-int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g) {
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g,
+                const uint32_t* order) {
     cudaStream_t s = ctx->stream;
     g->n = (uint32_t)n;
     g->npad = (uint32_t)((n + 255) / 256 * 256);
@@ -253,13 +260,18 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
         !sums)
         return MDET_ERR_NOMEM;
     unsigned blocks = (unsigned)((n + 255) / 256);
-    k_keys<<<blocks, 256, 0, s>>>(d_ls, n, keys, vals);
-    MDET_LAUNCHED(ctx, "k_keys");
-    size_t tmpb = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s);
-    void* tmp = ctx_scratch(ctx, "pre.cubtmp", tmpb);
-    if (!tmp) return MDET_ERR_NOMEM;
-    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s));
+    if (order) {
+        // caller's order (original index per position)
+        MDET_CUDA(ctx, cudaMemcpyAsync(g->perm, order, n * 4, cudaMemcpyDeviceToDevice, s));
+    } else {
+        k_keys<<<blocks, 256, 0, s>>>(d_ls, n, keys, vals);
+        MDET_LAUNCHED(ctx, "k_keys");
+        size_t tmpb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s);
+        void* tmp = ctx_scratch(ctx, "pre.cubtmp", tmpb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s));
+    }
     k_gather<<<(unsigned)n, 64, 0, s>>>(d_tnf, d_ls, g->perm, n, g->inv, g->x32, g->ls, g->parts, model_split());
     MDET_LAUNCHED(ctx, "k_gather");
     g->xa = nullptr;

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                                                       uint32_t* __restrict__ done, uint32_t* __restrict__ counts,
                                                       float* __restrict__ tnf, FoldTables tabs, int* flag) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t hist_all[kWarps][256];
+    __shared__ uint32_t hist_all[kWarps][257];  // 256 raw 4-mer codes + a bin for discarded windows
     __shared__ uint64_t bars[kWarps][2];
     // byte -> update word: 2-bit base code | 0x300 when not a base | 0x8000 for '\n'
     __shared__ uint16_t lut[256];
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                 if (t < 3 - need) carry = shift_in(carry, got[t]);
         }
 
-        for (int i = lane; i < 256; i += 32) hist[i] = 0;
+        for (int i = lane; i < 257; i += 32) hist[i] = 0;
         __syncwarp();
 
         const uint64_t a0 = p0 & ~(uint64_t)15;
@@ -218,17 +218,26 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                 const bool full = act == 0xFFFFu;
                 if (full) {
                     // every byte of the chunk is in the piece: table-driven
-                    // update, newline bytes leave the state unchanged
+                    // update, newline bytes leave the state unchanged, and
+                    // every window lands in a bin (bin 256 takes the invalid
+                    // ones) so the loop has no branches
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
                         const uint32_t ch = __byte_perm(words[b >> 2], 0u, 0x4440u | (uint32_t)(b & 3));
                         const uint32_t m = lut[ch];
-                        const uint32_t nl = m >> 15;
-                        const uint32_t xn = ((x << 2) & 0xFCFCu) | (m & 0x3FFu);
+                        const bool nl = m >= 0x8000u;
+                        const uint32_t xn = ((x << 2) & 0xFCFCu) | m;
                         x = nl ? x : xn;
-                        nlm |= nl << b;
-                        if (!nl && x < 256u) atomicAdd(&hist[x], 1u);
+                        const uint32_t bin = (nl || x >= 256u) ? 256u : x;
+                        atomicAdd(&hist[bin], 1u);
                         if (b == 2) x3 = x;
+                    }
+                    // newline bytes of the chunk (SWAR zero-byte test on w ^ '\n')
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint32_t z = words[q] ^ 0x0A0A0A0Au;
+                        const uint32_t hit = ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
+                        nlm |= hit ? (((hit >> 7) * 0x01020408u) >> 24 & 0xFu) << (4 * q) : 0u;
                     }
                     nact = 16u - __popc(nlm);
                 } else {
@@ -278,9 +287,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                     const uint32_t w1 = compose(cin, x3 >> 4, 1);
                     const uint32_t w2 = compose(cin, x3 >> 2, 2);
                     const uint32_t w3 = compose(cin, x3, 3);
-                    if (w1 < 256u) atomicAdd(&hist[w1], 1u);
-                    if (w2 < 256u) atomicAdd(&hist[w2], 1u);
-                    if (w3 < 256u) atomicAdd(&hist[w3], 1u);
+                    atomicAdd(&hist[w1 < 256u ? w1 : 256u], 1u);
+                    atomicAdd(&hist[w2 < 256u ? w2 : 256u], 1u);
+                    atomicAdd(&hist[w3 < 256u ? w3 : 256u], 1u);
                 } else if (nact > 0) {
                     uint32_t y = cin, seen = 0;
 #pragma unroll

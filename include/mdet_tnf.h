@@ -155,7 +155,7 @@ typedef struct {
     uint64_t pairs;            /* training pair pool (0: 50,000,000) */
     double candidate_fraction; /* share of the pool drawn from the distance filter's candidates */
     double label_cutoff;       /* edge labels: exact probability above this cutoff (0.7) */
-    uint64_t steps;            /* optimiser steps (0: one pass over the pool) */
+    uint64_t steps;            /* optimiser steps (0: none -- only the input scaling and tau are set) */
     uint32_t batch_pairs;      /* pairs per step (0: 8192) */
     float lr, m_pos, m_neg;    /* Adam learning rate; contrastive margins of edges / non-edges */
     double tau_quantile;       /* quantile of held-out edge distances that sets tau (0: 0.9995) */

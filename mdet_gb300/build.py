@@ -30,6 +30,8 @@ CU_UNITS = [
     "graph_filter_tc",
     "graph_exact",
     "graph",
+    "learned",
+    "graph_learned",
 ]
 
 

@@ -49,6 +49,8 @@ struct mdet_ctx {
     double tbl_L = 0, tbl_lmin = 0, tbl_lmax = 0;
     bool timing = false;
     std::unordered_map<std::string, KernelTimer> timers;
+    const struct mdet_mlp* mlp = nullptr;          // network of MDET_MODE_LEARNED
+    mdet_learned_report* learned_report = nullptr;  // optional caller-owned report
 };
 
 // Event pair around one launch of a named kernel when timing is enabled.

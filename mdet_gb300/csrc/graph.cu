@@ -86,8 +86,13 @@ __global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, 
     o.lo = o.hi = 0.f;
     o.emax = o.nmax = 0.f;
     if (r0 < m) {
-        o.lo = __double2float_rd(ls[row_map[r0]]);
-        o.hi = __double2float_ru(ls[row_map[r1 - 1]]);
+        double lo = ls[row_map[r0]], hi = lo;
+        for (uint64_t r = r0 + 1; r < r1; ++r) {
+            lo = fmin(lo, ls[row_map[r]]);
+            hi = fmax(hi, ls[row_map[r]]);
+        }
+        o.lo = __double2float_rd(lo);
+        o.hi = __double2float_ru(hi);
         for (uint64_t r = r0; r < r1; ++r) {
             const BlockMeta& sm = src_meta[row_map[r] / MDET_BLK];
             o.emax = fmaxf(o.emax, sm.emax);
@@ -99,11 +104,14 @@ __global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, 
     out[b] = o;
 }
 
+}  // namespace
+
 double logit(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
 
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
-               const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out) {
+               const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
+               const uint32_t* tiles, uint64_t nlist) {
     cudaStream_t s = ctx->stream;
     std::string cap_key = std::string(tag) + ".cap";
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
@@ -126,7 +134,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
             const uint16_t* A = rect ? ab : g.xa;
             const float* An = rect ? ansq : g.nsq;
             MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
-                               out));
+                               out, tiles, nlist));
         }
         unsigned long long found = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
@@ -149,6 +157,12 @@ int check_mode(mdet_ctx* ctx, int mode) {
                             ctx->cc_major, ctx->cc_minor);
         return MDET_OK;
     }
+    if (mode == MDET_MODE_LEARNED) {
+        if (ctx->cc_major != 10 || ctx->cc_minor != 3)
+            return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "the learned form needs an sm_103 device");
+        if (!ctx->mlp) return ctx_fail(ctx, MDET_ERR_INVALID, "no network set (mdet_ctx_set_learned)");
+        return MDET_OK;
+    }
     return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "mode %d not available", mode);
 }
 
@@ -163,8 +177,35 @@ int check_flag(mdet_ctx* ctx) {
     return MDET_OK;
 }
 
+int gather_rows_bf16(mdet_ctx* ctx, const GraphPrep& g, const uint32_t* row_map, uint64_t m, const char* tag,
+                     RowSet* out) {
+    cudaStream_t s = ctx->stream;
+    const std::string t(tag);
+    const uint64_t mpad = (m + 255) / 256 * 256, nblk = mpad / MDET_BLK;
+    out->ab = (uint16_t*)ctx_scratch(ctx, (t + ".ab").c_str(), mpad * MDET_KPAD * 2);
+    out->ansq = (float*)ctx_scratch(ctx, (t + ".ansq").c_str(), mpad * 4);
+    out->meta = (BlockMeta*)ctx_scratch(ctx, (t + ".meta").c_str(), nblk * sizeof(BlockMeta));
+    if (!out->ab || !out->ansq || !out->meta) return MDET_ERR_NOMEM;
+    if (m == 0) return MDET_OK;
+    k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xa, g.nsq, out->ab, out->ansq);
+    MDET_LAUNCHED(ctx, "k_sample_gather_bf16");
+    k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, out->meta);
+    MDET_LAUNCHED(ctx, "k_sample_meta");
+    return MDET_OK;
+}
+
+int graph_candidates(mdet_ctx* ctx, const GraphPrep& g, double cutoff, int mode, uint2** cand, uint64_t* ncand) {
+    DstarTable tbl;
+    MDET_TRY(build_dstar_table(ctx, g.ls, g.n, logit(cutoff), &tbl));
+    unsigned long long nc = 0;
+    MDET_TRY(run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "g", cand, &nc));
+    *ncand = nc;
+    return MDET_OK;
+}
+
 int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
                int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total) {
+    if (mode == MDET_MODE_LEARNED) return graph_learned(ctx, d_tnf, d_ls, n, cutoff, max_edges, st, g, total);
     PhaseTimer tm(ctx->stream);
     tm.mark();
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, mode != MDET_MODE_PLAIN, &g));
@@ -253,8 +294,6 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
     MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out));
     return MDET_OK;
 }
-
-}  // namespace
 
 extern "C" {
 

@@ -87,7 +87,9 @@ struct GraphPrep {
 // index per position, device) when given.
 int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out,
                 const uint32_t* order = nullptr);
-int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out);
+// sorted: d_ls_sorted is ascending (else its range is found by a scan).
+int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
+                      bool sorted = true);
 ModelH model_h();
 
 // Above-cutoff pair found by the exact stage (sorted positions).
@@ -121,3 +123,27 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
                 uint32_t max_edges, uint64_t* n_out);
 int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
               double* d_stnf, uint64_t total);
+
+// Orchestration shared by the graph entry points (graph.cu, graph_learned.cu).
+double logit(double cutoff);
+int check_flag(mdet_ctx* ctx);
+int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
+               const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
+               const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
+               const uint32_t* tiles = nullptr, uint64_t nlist = 0);
+int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
+               int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total);
+int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
+                  mdet_graph_stats* st, GraphPrep& g, uint64_t* total);
+// Candidate pairs (prepared positions) of the triangular pass at `cutoff`.
+int graph_candidates(mdet_ctx* ctx, const GraphPrep& g, double cutoff, int mode, uint2** cand, uint64_t* ncand);
+// A-role BF16 rows of a prepared set gathered for a rectangular pass
+// (row_map: ascending prepared positions on the device, m entries), padded
+// to 256 rows, with their norms and block metadata.
+struct RowSet {
+    uint16_t* ab;
+    float* ansq;
+    BlockMeta* meta;
+};
+int gather_rows_bf16(mdet_ctx* ctx, const GraphPrep& g, const uint32_t* row_map, uint64_t m, const char* tag,
+                     RowSet* out);

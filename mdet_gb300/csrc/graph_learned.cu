@@ -1,0 +1,425 @@
+// graph_learned.cu -- MDET_MODE_LEARNED: the TNF graph with the learned
+// proposal.  The network embeds every contig (64 dims); contigs are ordered
+// along a Morton curve over the leading principal axes of the embedding and
+// their log size, so that 128-row blocks gather similar contigs; each tile
+// pair (128-row block I, 256-row block J) is kept when the triangle bound
+// ||c_I - c_J|| - r_I - r_J on embedded distances is within the trained
+// margin tau.  The kept tiles go through the same tensor-core filter and
+// exact stage as the all-pairs form, so every emitted edge is exact; the only
+// loss is recall, which is measured on a row sample against an all-columns
+// pass before the graph is built, with the all-pairs form as the fallback.
+// The reference has no learned component.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "exact.cuh"
+#include "mlp.cuh"
+
+using namespace mdet_exact;
+
+namespace {
+
+constexpr int kPcs = 7;           // principal axes in the Morton key (+ log size)
+constexpr int kFlagGroup = 8;     // row tiles per thread in the tile-flag kernel
+
+// Morton key of one contig: 8 bits each of kPcs principal coordinates and of
+// the log size, interleaved most significant bit first; the log size takes
+// the lowest position of each bit level.
+__global__ void k_morton(const float* __restrict__ proj, const double* __restrict__ ls, uint64_t n,
+                         const float* __restrict__ off, const float* __restrict__ inv_span, float ls0, float ls_inv,
+                         unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t q[kPcs + 1];
+#pragma unroll
+    for (int d = 0; d < kPcs; ++d) {
+        const float u = (proj[i * kPcs + d] - off[d]) * inv_span[d];
+        q[d] = (uint32_t)fminf(fmaxf(u * 256.f, 0.f), 255.f);
+    }
+    q[kPcs] = (uint32_t)fminf(fmaxf(((float)ls[i] - ls0) * ls_inv * 256.f, 0.f), 255.f);
+    unsigned long long key = 0;
+#pragma unroll
+    for (int b = 7; b >= 0; --b)
+#pragma unroll
+        for (int d = 0; d <= kPcs; ++d) key = (key << 1) | ((q[d] >> b) & 1u);
+    keys[i] = key;
+    vals[i] = (uint32_t)i;
+}
+
+// Centroid and radius (in embedding space) of each block of `rows` prepared
+// positions.  Centroids are written row-major [blk][64] or, for dim_major,
+// [64][nblk] (the layout the tile-flag kernel reads coalesced).
+__global__ void __launch_bounds__(256) k_block_stats(const float* __restrict__ z, const uint32_t* __restrict__ perm,
+                                                     uint32_t n, uint32_t rows, uint32_t nblk, int dim_major,
+                                                     float* __restrict__ cent, float* __restrict__ rad) {
+    __shared__ float part[4][MLP_OUT];
+    __shared__ float c[MLP_OUT];
+    __shared__ float wmax[8];
+    const uint32_t b = blockIdx.x;
+    const uint32_t r0 = b * rows, r1 = min(n, r0 + rows);
+    const uint32_t cnt = r1 > r0 ? r1 - r0 : 0;
+    const uint32_t t = threadIdx.x, dim = t & 63, sub = t >> 6;
+    float s = 0.f;
+    for (uint32_t r = sub; r < cnt; r += 4) s += z[(uint64_t)perm[r0 + r] * MLP_OUT + dim];
+    part[sub][dim] = s;
+    __syncthreads();
+    if (t < MLP_OUT) {
+        const float v = cnt ? (part[0][t] + part[1][t] + part[2][t] + part[3][t]) / (float)cnt : 0.f;
+        c[t] = v;
+        if (dim_major)
+            cent[(uint64_t)t * nblk + b] = v;
+        else
+            cent[(uint64_t)b * MLP_OUT + t] = v;
+    }
+    __syncthreads();
+    float m = 0.f;
+    for (uint32_t r = t; r < cnt; r += blockDim.x) {
+        const float4* zr = reinterpret_cast<const float4*>(z + (uint64_t)perm[r0 + r] * MLP_OUT);
+        float d2 = 0.f;
+#pragma unroll
+        for (int q = 0; q < MLP_OUT / 4; ++q) {
+            const float4 v = zr[q];
+            const float a = v.x - c[4 * q], bb = v.y - c[4 * q + 1], cc = v.z - c[4 * q + 2], dd = v.w - c[4 * q + 3];
+            d2 += a * a + bb * bb + cc * cc + dd * dd;
+        }
+        m = fmaxf(m, d2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((t & 31) == 0) wmax[t >> 5] = m;
+    __syncthreads();
+    if (t == 0) {
+        float v = 0.f;
+        for (int w = 0; w < 8; ++w) v = fmaxf(v, wmax[w]);
+        // float rounding slack on the radius
+        rad[b] = cnt ? sqrtf(v) * 1.0001f + 1e-5f : -INFINITY;
+    }
+}
+
+// keep[I * tb + J] = tile pair (row tile I of 128, column tile J of 256) of
+// the upper triangle has an embedded lower bound within tau.
+__global__ void __launch_bounds__(256) k_tile_flags(const float* __restrict__ rc, const float* __restrict__ rr,
+                                                    const float* __restrict__ cc_t, const float* __restrict__ cr,
+                                                    uint32_t ta, uint32_t tb, float tau, uint8_t* __restrict__ keep) {
+    __shared__ float ci[kFlagGroup][MLP_OUT];
+    __shared__ float ri[kFlagGroup];
+    const uint32_t I0 = blockIdx.y * kFlagGroup;
+    for (uint32_t e = threadIdx.x; e < kFlagGroup * MLP_OUT; e += blockDim.x) {
+        const uint32_t I = I0 + e / MLP_OUT;
+        ci[e / MLP_OUT][e % MLP_OUT] = I < ta ? rc[(uint64_t)I * MLP_OUT + e % MLP_OUT] : 0.f;
+    }
+    if (threadIdx.x < kFlagGroup) ri[threadIdx.x] = I0 + threadIdx.x < ta ? rr[I0 + threadIdx.x] : -INFINITY;
+    __syncthreads();
+    const uint32_t J = blockIdx.x * blockDim.x + threadIdx.x;
+    if (J >= tb) return;
+    float cj[MLP_OUT];
+#pragma unroll
+    for (int d = 0; d < MLP_OUT; ++d) cj[d] = cc_t[(uint64_t)d * tb + J];
+    const float rj = cr[J];
+#pragma unroll 1
+    for (int g = 0; g < kFlagGroup; ++g) {
+        const uint32_t I = I0 + g;
+        if (I >= ta) break;
+        float d2 = 0.f;
+#pragma unroll
+        for (int d = 0; d < MLP_OUT; ++d) {
+            const float a = ci[g][d] - cj[d];
+            d2 = fmaf(a, a, d2);
+        }
+        const bool live = ri[g] > -INFINITY && rj > -INFINITY && J >= (I >> 1);
+        keep[(uint64_t)I * tb + J] = (live && sqrtf(d2) - ri[g] - rj <= tau) ? 1 : 0;
+    }
+}
+
+// Recall of the kept tiles over the true edges of the sampled rows: every
+// candidate of the all-columns pass is scored exactly; an edge counts as
+// recalled when its tile pair is kept.
+__global__ void __launch_bounds__(256) k_recall(const uint2* __restrict__ cand, unsigned long long ncand,
+                                                const uint32_t* __restrict__ row_map, const float* __restrict__ x32,
+                                                const double* __restrict__ ls, const ModelParts* __restrict__ parts,
+                                                ModelH H, double L, const uint8_t* __restrict__ keep, uint32_t tb,
+                                                unsigned long long* __restrict__ counts) {
+    const bool model2 = L < kLn9;
+    unsigned long long tot = 0, hit = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ncand;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 c = cand[i];
+        const uint32_t r = row_map[c.x], q = c.y;
+        if (r == q) continue;
+        const double d = exact_dist(x32 + (uint64_t)r * MDET_NTNF, x32 + (uint64_t)q * MDET_NTNF);
+        const double pre = pre_prob(parts[r], parts[q], ls[r], ls[q], d, H, model2);
+        if (pre > L) {
+            const uint32_t lo = min(r, q), hi = max(r, q);
+            ++tot;
+            hit += keep[(uint64_t)(lo / 128) * tb + hi / 256];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        hit += __shfl_xor_sync(0xffffffffu, hit, o);
+    }
+    if ((threadIdx.x & 31) == 0 && tot) {
+        atomicAdd(counts, tot);
+        atomicAdd(counts + 1, hit);
+    }
+}
+
+__global__ void k_sample_rows(uint32_t n, uint32_t m, uint32_t* __restrict__ rows) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < m) rows[k] = (uint32_t)(((uint64_t)k * 2 + 1) * n / (2ull * m));
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric k x k matrix (row-major,
+// destroyed); eigenvalues in w, eigenvectors as columns of V.
+void jacobi_eigen(std::vector<double>& A, int k, std::vector<double>& w, std::vector<double>& V) {
+    V.assign((size_t)k * k, 0.0);
+    for (int i = 0; i < k; ++i) V[(size_t)i * k + i] = 1.0;
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < k; ++p)
+            for (int q = p + 1; q < k; ++q) off += A[(size_t)p * k + q] * A[(size_t)p * k + q];
+        if (off < 1e-22) break;
+        for (int p = 0; p < k; ++p)
+            for (int q = p + 1; q < k; ++q) {
+                const double apq = A[(size_t)p * k + q];
+                if (std::fabs(apq) < 1e-300) continue;
+                const double theta = (A[(size_t)q * k + q] - A[(size_t)p * k + p]) / (2 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int r = 0; r < k; ++r) {  // A <- A J
+                    const double arp = A[(size_t)r * k + p], arq = A[(size_t)r * k + q];
+                    A[(size_t)r * k + p] = c * arp - s * arq;
+                    A[(size_t)r * k + q] = s * arp + c * arq;
+                }
+                for (int r = 0; r < k; ++r) {  // A <- J^T A
+                    const double apr = A[(size_t)p * k + r], aqr = A[(size_t)q * k + r];
+                    A[(size_t)p * k + r] = c * apr - s * aqr;
+                    A[(size_t)q * k + r] = s * apr + c * aqr;
+                }
+                for (int r = 0; r < k; ++r) {  // V <- V J
+                    const double vrp = V[(size_t)r * k + p], vrq = V[(size_t)r * k + q];
+                    V[(size_t)r * k + p] = c * vrp - s * vrq;
+                    V[(size_t)r * k + q] = s * vrp + c * vrq;
+                }
+            }
+    }
+    w.resize(k);
+    for (int i = 0; i < k; ++i) w[i] = A[(size_t)i * k + i];
+}
+
+struct PhaseClock {
+    cudaEvent_t ev[8];
+    int n = 0;
+    cudaStream_t s;
+    explicit PhaseClock(cudaStream_t st) : s(st) {
+        for (auto& e : ev) cudaEventCreate(&e);
+    }
+    ~PhaseClock() {
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    void mark() {
+        if (n < 8) cudaEventRecord(ev[n++], s);
+    }
+    double ms(int a, int b) {
+        if (b >= n) return 0;
+        float t = 0;
+        cudaEventSynchronize(ev[b]);
+        cudaEventElapsedTime(&t, ev[a], ev[b]);
+        return t;
+    }
+};
+
+// Embeds the contigs and returns the Morton order (original index per
+// position) in `order`.
+int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const double* d_ls, uint64_t n, float* z,
+                  uint32_t* order) {
+    cudaStream_t s = ctx->stream;
+    MDET_TRY(mlp_embed(ctx, net->params, d_tnf, n, z));
+    // principal axes of the embedding: C = Z^T Z / n - mu mu^T
+    float* G = (float*)ctx_scratch(ctx, "lrn.gram", MLP_OUT * MLP_OUT * 4);
+    float* colsum = (float*)ctx_scratch(ctx, "lrn.colsum", MLP_OUT * 4);
+    float* V = (float*)ctx_scratch(ctx, "lrn.v", MLP_OUT * kPcs * 4);
+    float* off = (float*)ctx_scratch(ctx, "lrn.off", 2 * kPcs * 4);
+    float* proj = (float*)ctx_scratch(ctx, "lrn.proj", n * kPcs * 4);
+    unsigned long long* keys = (unsigned long long*)ctx_scratch(ctx, "lrn.keys", n * 8);
+    unsigned long long* keys2 = (unsigned long long*)ctx_scratch(ctx, "lrn.keys2", n * 8);
+    uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "lrn.vals", n * 4);
+    if (!G || !colsum || !V || !off || !proj || !keys || !keys2 || !vals) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(G, 0, MLP_OUT * MLP_OUT * 4, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(colsum, 0, MLP_OUT * 4, s));
+    MDET_TRY(mlp_gram(ctx, z, n, G));
+    MDET_TRY(mlp_colsum(ctx, z, n, colsum));
+    std::vector<float> hg(MLP_OUT * MLP_OUT), hs(MLP_OUT);
+    MDET_CUDA(ctx, cudaMemcpyAsync(hg.data(), G, hg.size() * 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(hs.data(), colsum, hs.size() * 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    std::vector<double> C((size_t)MLP_OUT * MLP_OUT), w, E;
+    for (int i = 0; i < MLP_OUT; ++i)
+        for (int j = 0; j < MLP_OUT; ++j)
+            C[(size_t)i * MLP_OUT + j] = (double)hg[(size_t)i * MLP_OUT + j] / (double)n -
+                                         ((double)hs[i] / (double)n) * ((double)hs[j] / (double)n);
+    jacobi_eigen(C, MLP_OUT, w, E);
+    std::vector<int> idx(MLP_OUT);
+    for (int i = 0; i < MLP_OUT; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return w[a] > w[b]; });
+    std::vector<float> hv((size_t)MLP_OUT * kPcs), hoff(2 * kPcs);
+    for (int p = 0; p < kPcs; ++p) {
+        const int e = idx[p];
+        double mproj = 0;
+        for (int r = 0; r < MLP_OUT; ++r) {
+            hv[(size_t)r * kPcs + p] = (float)E[(size_t)r * MLP_OUT + e];
+            mproj += E[(size_t)r * MLP_OUT + e] * (double)hs[r] / (double)n;
+        }
+        const double sd = std::sqrt(std::max(w[e], 1e-20));
+        hoff[p] = (float)(mproj - 3.0 * sd);            // the key spans mean +- 3 sd
+        hoff[kPcs + p] = (float)(1.0 / (6.0 * sd));
+    }
+    MDET_CUDA(ctx, cudaMemcpyAsync(V, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(off, hoff.data(), hoff.size() * 4, cudaMemcpyHostToDevice, s));
+    MDET_TRY(mlp_project(ctx, z, n, V, kPcs, proj));
+    // log10 size over 3..7 (1 kb .. 10 Mb)
+    k_morton<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, d_ls, n, off, off + kPcs, 3.f, 0.25f, keys, vals);
+    MDET_LAUNCHED(ctx, "k_morton");
+    size_t tb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, order, (int)n, 0, 64, s);
+    void* tmp = ctx_scratch(ctx, "lrn.sorttmp", tb);
+    if (!tmp) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, order, (int)n, 0, 64, s));
+    return MDET_OK;
+}
+
+}  // namespace
+
+int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
+                  mdet_graph_stats* st, GraphPrep& g, uint64_t* total) {
+    cudaStream_t s = ctx->stream;
+    const mdet_mlp* net = ctx->mlp;
+    mdet_learned_report* rep = ctx->learned_report;
+    double target = rep && rep->recall_target > 0 ? rep->recall_target : 0.999;
+    const uint32_t want_rows = rep && rep->recall_rows ? rep->recall_rows : 1024;
+    if (rep) {
+        rep->recall = 0;
+        rep->fell_back = 0;
+        rep->tiles_skipped = 0;
+    }
+    float tau = INFINITY;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&tau, net->params + MLP_TAU, 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    const uint32_t ta = (uint32_t)((n + 127) / 128), tb = (uint32_t)((n + 255) / 256);
+    const uint64_t full = [&] {
+        uint64_t t = (uint64_t)ta * tb;
+        const uint64_t m = ta >> 1;
+        return t - ((ta & 1) ? m * m : (m ? m * (m - 1) : 0));
+    }();
+    auto fallback = [&](double recall) -> int {
+        if (rep) {
+            rep->recall = recall;
+            rep->fell_back = 1;
+            rep->tiles_skipped = 0;
+        }
+        return graph_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, MDET_MODE_BF16, st, g, total);
+    };
+    if (!(tau < INFINITY) || n < 512) return fallback(0.0);
+
+    PhaseClock tm(s);
+    tm.mark();
+    float* z = (float*)ctx_scratch(ctx, "lrn.z", n * MLP_OUT * 4);
+    uint32_t* order = (uint32_t*)ctx_scratch(ctx, "lrn.order", n * 4);
+    if (!z || !order) return MDET_ERR_NOMEM;
+    MDET_TRY(learned_order(ctx, net, d_tnf, d_ls, n, z, order));
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, true, &g, order));
+    const double L = logit(cutoff);
+    DstarTable tbl;
+    MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl, false));
+
+    // block statistics and the tile list
+    float* rcent = (float*)ctx_scratch(ctx, "lrn.rcent", (uint64_t)ta * MLP_OUT * 4);
+    float* rrad = (float*)ctx_scratch(ctx, "lrn.rrad", (uint64_t)ta * 4);
+    float* ccent = (float*)ctx_scratch(ctx, "lrn.ccent", (uint64_t)tb * MLP_OUT * 4);
+    float* crad = (float*)ctx_scratch(ctx, "lrn.crad", (uint64_t)tb * 4);
+    uint8_t* keep = (uint8_t*)ctx_scratch(ctx, "lrn.keep", (uint64_t)ta * tb);
+    uint32_t* list = (uint32_t*)ctx_scratch(ctx, "lrn.list", (uint64_t)ta * tb * 4);
+    int* nsel = (int*)ctx_scratch(ctx, "lrn.nsel", 8);
+    if (!rcent || !rrad || !ccent || !crad || !keep || !list || !nsel) return MDET_ERR_NOMEM;
+    if ((uint64_t)ta * tb >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many tiles for the learned form");
+    k_block_stats<<<ta, 256, 0, s>>>(z, g.perm, (uint32_t)n, 128, ta, 0, rcent, rrad);
+    MDET_LAUNCHED(ctx, "k_block_stats");
+    k_block_stats<<<tb, 256, 0, s>>>(z, g.perm, (uint32_t)n, 256, tb, 1, ccent, crad);
+    MDET_LAUNCHED(ctx, "k_block_stats");
+    k_tile_flags<<<dim3((tb + 255) / 256, (ta + kFlagGroup - 1) / kFlagGroup), 256, 0, s>>>(rcent, rrad, ccent, crad,
+                                                                                           ta, tb, tau, keep);
+    MDET_LAUNCHED(ctx, "k_tile_flags");
+    {
+        size_t tmpb = 0;
+        thrust::counting_iterator<uint32_t> it(0);
+        cub::DeviceSelect::Flagged(nullptr, tmpb, it, keep, list, nsel, (int)((uint64_t)ta * tb), s);
+        void* tmp = ctx_scratch(ctx, "lrn.seltmp", tmpb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceSelect::Flagged(tmp, tmpb, it, keep, list, nsel, (int)((uint64_t)ta * tb), s));
+    }
+    int hsel = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&hsel, nsel, 4, cudaMemcpyDeviceToHost, s));
+
+    // recall on a systematic row sample: all-columns pass, exact scoring
+    const uint32_t m = (uint32_t)std::min<uint64_t>(n, want_rows);
+    uint32_t* rows = (uint32_t*)ctx_scratch(ctx, "lrn.rows", (uint64_t)m * 4);
+    unsigned long long* counts = (unsigned long long*)ctx_scratch(ctx, "lrn.counts", 16);
+    if (!rows || !counts) return MDET_ERR_NOMEM;
+    k_sample_rows<<<(m + 255) / 256, 256, 0, s>>>((uint32_t)n, m, rows);
+    MDET_LAUNCHED(ctx, "k_sample_rows");
+    RowSet rs;
+    MDET_TRY(gather_rows_bf16(ctx, g, rows, m, "lrn.s", &rs));
+    uint2* rc = nullptr;
+    unsigned long long nrc = 0;
+    MDET_TRY(run_filter(ctx, MDET_MODE_BF16, g, true, nullptr, rs.ab, rs.ansq, m, rs.meta, nullptr, tbl, "lrn.rc", &rc,
+                        &nrc));
+    MDET_CUDA(ctx, cudaMemsetAsync(counts, 0, 16, s));
+    if (nrc) {
+        const uint64_t blocks = std::min<uint64_t>((nrc + 255) / 256, (uint64_t)ctx->num_sms * 8);
+        k_recall<<<(unsigned)blocks, 256, 0, s>>>(rc, nrc, rows, g.x32, g.ls, g.parts, model_h(), L, keep, tb, counts);
+        MDET_LAUNCHED(ctx, "k_recall");
+    }
+    unsigned long long hc[2] = {0, 0};
+    MDET_CUDA(ctx, cudaMemcpyAsync(hc, counts, 16, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    MDET_TRY(check_flag(ctx));
+    const double recall = hc[0] ? (double)hc[1] / (double)hc[0] : 1.0;
+    if (recall < target) return fallback(recall);
+    tm.mark();
+
+    uint2* cand = nullptr;
+    unsigned long long ncand = 0;
+    if (hsel > 0)
+        MDET_TRY(run_filter(ctx, MDET_MODE_BF16, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "g",
+                            &cand, &ncand, list, (uint64_t)hsel));
+    tm.mark();
+    Edge* edges = nullptr;
+    unsigned long long ne = 0;
+    uint32_t* deg = nullptr;
+    MDET_TRY(exact_graph(ctx, g, cand, ncand, L, &edges, &ne, &deg));
+    tm.mark();
+    MDET_TRY(select_topk(ctx, g, edges, ne, deg, max_edges, total));
+    tm.mark();
+    if (st) {
+        st->n_candidates = ncand;
+        st->n_above_cutoff = ne;
+        st->tiles_total = full;
+        st->tiles_computed = (uint64_t)hsel;
+        st->ms_prep = tm.ms(0, 1);
+        st->ms_filter = tm.ms(1, 2);
+        st->ms_exact = tm.ms(2, 3);
+        st->ms_select = tm.ms(3, 4);
+    }
+    if (rep) {
+        rep->recall = recall;
+        rep->fell_back = 0;
+        rep->tiles_skipped = full - (uint64_t)hsel;
+    }
+    return MDET_OK;
+}

@@ -221,10 +221,37 @@ __global__ void k_sparse(float* __restrict__ st, int k) {
     cur[a * MDET_TBL + b] = fmaxf(prev[a * MDET_TBL + b], prev[a * MDET_TBL + b2]);
 }
 
-__global__ void k_minmax(const double* __restrict__ ls_s, uint64_t n, double* __restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        out[0] = ls_s[0];
-        out[1] = ls_s[n - 1];
+// Range of the log sizes: the end points when sorted, else a one-block scan.
+__global__ void k_minmax(const double* __restrict__ ls_s, uint64_t n, int sorted, double* __restrict__ out) {
+    if (sorted) {
+        if (threadIdx.x == 0) {
+            out[0] = ls_s[0];
+            out[1] = ls_s[n - 1];
+        }
+        return;
+    }
+    __shared__ double smin[32], smax[32];
+    double lo = INFINITY, hi = -INFINITY;
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        lo = fmin(lo, ls_s[i]);
+        hi = fmax(hi, ls_s[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        smin[threadIdx.x >> 5] = lo;
+        smax[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            lo = fmin(lo, smin[w]);
+            hi = fmax(hi, smax[w]);
+        }
+        out[0] = lo;
+        out[1] = hi;
     }
 }
 
@@ -301,7 +328,8 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
     return MDET_OK;
 }
 
-int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out) {
+int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
+                      bool sorted) {
     cudaStream_t s = ctx->stream;
     double* mm = (double*)ctx_scratch(ctx, "tbl.mm", 16);
     float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
@@ -309,7 +337,7 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
     if (!mm || !pts || !st) return MDET_ERR_NOMEM;
     // the range is needed on the host to place the grid
     double range[2];
-    k_minmax<<<1, 32, 0, s>>>(d_ls_sorted, n, mm);
+    k_minmax<<<1, sorted ? 32 : 1024, 0, s>>>(d_ls_sorted, n, sorted ? 1 : 0, mm);
     MDET_LAUNCHED(ctx, "k_minmax");
     MDET_CUDA(ctx, cudaMemcpyAsync(range, mm, 16, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));

@@ -15,14 +15,6 @@
 
 using namespace mdet_exact;
 
-struct mdet_mlp {
-    float* params = nullptr;  // device, MLP_NPARAM floats
-    float* m = nullptr;       // Adam moments (MLP_NTRAIN each)
-    float* v = nullptr;
-    uint64_t step = 0;
-    int device = 0;
-};
-
 namespace {
 
 __device__ __forceinline__ float bf16r(float w) { return __bfloat162float(__float2bfloat16_rn(w)); }
@@ -212,10 +204,18 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// uniformly random distinct pairs (i != j)
-__global__ void k_random_pairs(uint64_t seed, uint64_t count, uint32_t n, uint2* __restrict__ out) {
+// Pair pool: each entry is, with probability frac, a candidate pair of the
+// distance filter drawn at random, else a uniformly random pair (i != j).
+__global__ void k_pair_pool(uint64_t seed, uint64_t count, uint32_t n, const uint2* __restrict__ cand, uint64_t ncand,
+                            double frac, uint2* __restrict__ out) {
+    const uint64_t thr = (uint64_t)(frac * 4294967296.0);
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t r = mix64(seed + 0x9E3779B97F4A7C15ull * (i + 1));
+        const uint64_t r2 = mix64(r ^ 0x632BE59BD9B4E019ull);
+        if (ncand && (r2 & 0xFFFFFFFFull) < thr) {
+            out[i] = cand[(uint64_t)(((r2 >> 32) * ncand) >> 32)];
+            continue;
+        }
         uint32_t a = (uint32_t)(((r & 0xFFFFFFFFull) * n) >> 32);
         uint32_t b = (uint32_t)(((r >> 32) * (uint64_t)(n - 1)) >> 32);
         if (b >= a) ++b;
@@ -341,8 +341,33 @@ int mlp_backward(mdet_ctx* ctx, const float* P, const MlpActs& a, uint64_t np, c
     return MDET_OK;
 }
 
-// declared in graph.cu: candidate pairs (sorted positions) of a prepared set
-int graph_candidates(mdet_ctx* ctx, const GraphPrep& g, double cutoff, int mode, uint2** cand, uint64_t* ncand);
+int mlp_embed(mdet_ctx* ctx, const float* P, const float* tnf, uint64_t n, float* z) {
+    const uint64_t chunk = 1u << 18;
+    for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
+        const uint64_t k = std::min(chunk, n - r0);
+        MlpActs a;
+        MDET_TRY(mlp_alloc_acts(ctx, "mlpe", k, &a));
+        a.z3 = z + r0 * MLP_OUT;
+        MDET_TRY(mlp_forward(ctx, P, tnf + r0 * MLP_IN, nullptr, k, a));
+    }
+    return MDET_OK;
+}
+
+int mlp_gram(mdet_ctx* ctx, const float* z, uint64_t n, float* G) {
+    return gemm<true, false, false, 2>(ctx, MLP_OUT, MLP_OUT, (int)n, z, MLP_OUT, z, MLP_OUT, G, MLP_OUT, nullptr,
+                                       nullptr);
+}
+
+int mlp_colsum(mdet_ctx* ctx, const float* z, uint64_t n, float* sum) {
+    if (n == 0) return MDET_OK;
+    k_colsum_add<<<dim3(1, (unsigned)((n + 255) / 256)), MLP_OUT, 0, ctx->stream>>>(z, n, MLP_OUT, sum);
+    MDET_LAUNCHED(ctx, "k_colsum_add");
+    return MDET_OK;
+}
+
+int mlp_project(mdet_ctx* ctx, const float* z, uint64_t n, const float* V, int k, float* P) {
+    return gemm<false, false, false, 0>(ctx, (int)n, k, MLP_OUT, z, MLP_OUT, V, k, P, k, nullptr, nullptr);
+}
 
 extern "C" {
 
@@ -397,21 +422,21 @@ int mdet_mlp_set_params(mdet_ctx* ctx, mdet_mlp* m, const float* host, uint64_t 
 int mdet_mlp_embed_dev(mdet_ctx* ctx, const mdet_mlp* m, const float* d_tnf, uint64_t n, float* d_out) {
     if (!ctx || !m || (n && (!d_tnf || !d_out))) return MDET_ERR_INVALID;
     MDET_CUDA(ctx, cudaSetDevice(ctx->device));
-    const uint64_t chunk = 1u << 18;
-    for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
-        const uint64_t k = std::min(chunk, n - r0);
-        MlpActs a;
-        MDET_TRY(mlp_alloc_acts(ctx, "mlpe", k, &a));
-        a.z3 = d_out + r0 * MLP_OUT;
-        MDET_TRY(mlp_forward(ctx, m->params, d_tnf + r0 * MLP_IN, nullptr, k, a));
-    }
+    MDET_TRY(mlp_embed(ctx, m->params, d_tnf, n, d_out));
     MDET_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MDET_OK;
 }
 
+int mdet_ctx_set_learned(mdet_ctx* ctx, const mdet_mlp* mlp, mdet_learned_report* report) {
+    if (!ctx) return MDET_ERR_INVALID;
+    ctx->mlp = mlp;
+    ctx->learned_report = report;
+    return MDET_OK;
+}
+
 // Loss and gradient (host buffers) of the mean contrastive loss of `np`
-// pairs over the rows of x (B x 136 TNF rows): pairs[2p], pairs[2p+1] index
-// rows of x.  For gradient checks against a CPU reference.
+// pairs over the rows of x (rows x 136 TNF rows): pairs[2p], pairs[2p+1]
+// index rows of x.  For gradient checks against a CPU reference.
 int mdet_mlp_grad(mdet_ctx* ctx, const mdet_mlp* m, const float* x, uint64_t rows, const uint32_t* pairs,
                   const float* labels, uint64_t np, float m_pos, float m_neg, float* grad_out, double* loss_out) {
     if (!ctx || !m || !x || !pairs || !labels || !grad_out || !loss_out || np == 0) return MDET_ERR_INVALID;
@@ -465,18 +490,16 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
     uint2* cand = nullptr;
     uint64_t ncand = 0;
     MDET_TRY(graph_candidates(ctx, g, tp->label_cutoff, mode, &cand, &ncand));
-    // pair pool: candidates (up to frac of the pool) + random pairs
+    // pair pool: candidate pairs and random pairs, mixed at random so that
+    // the held-out tail has both kinds
     const uint64_t pool = tp->pairs ? tp->pairs : 50000000ull;
-    uint64_t nc = std::min<uint64_t>(ncand, (uint64_t)(pool * tp->candidate_fraction));
-    const uint64_t nr = pool - nc;
+    const double frac = std::min(1.0, std::max(0.0, tp->candidate_fraction));
+    const uint64_t nc = ncand ? (uint64_t)(pool * frac) : 0;
     uint2* pairs = (uint2*)ctx_scratch(ctx, "mlpt.pairs", pool * sizeof(uint2));
     float* labels = (float*)ctx_scratch(ctx, "mlpt.labels", pool * 4);
     if (!pairs || !labels) return MDET_ERR_NOMEM;
-    if (nc) MDET_CUDA(ctx, cudaMemcpyAsync(pairs, cand, nc * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
-    if (nr) {
-        k_random_pairs<<<ctx->num_sms * 8, 256, 0, s>>>(tp->seed, nr, (uint32_t)n, pairs + nc);
-        MDET_LAUNCHED(ctx, "k_random_pairs");
-    }
+    k_pair_pool<<<ctx->num_sms * 8, 256, 0, s>>>(tp->seed, pool, (uint32_t)n, cand, ncand, frac, pairs);
+    MDET_LAUNCHED(ctx, "k_pair_pool");
     const double L = log((1.0 / (1. - tp->label_cutoff)) - 1.0);
     k_label_pairs<<<ctx->num_sms * 16, 256, 0, s>>>(pairs, pool, g.x32, g.ls, g.parts, model_h(), L, labels);
     MDET_LAUNCHED(ctx, "k_label_pairs");
@@ -500,7 +523,7 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
         MDET_CUDA(ctx, cudaMemcpy(m->params + MLP_MU, mu.data(), MLP_IN * 4, cudaMemcpyHostToDevice));
         MDET_CUDA(ctx, cudaMemcpy(m->params + MLP_SCALE, &scale, 4, cudaMemcpyHostToDevice));
     }
-    const uint64_t steps = tp->steps ? tp->steps : (pool + B - 1) / B;
+    const uint64_t steps = tp->steps;
     double loss_acc = 0;
     uint64_t loss_n = 0;
     for (uint64_t st = 0; st < steps; ++st) {
@@ -514,7 +537,9 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
         const float c1 = 1.f - powf(0.9f, (float)m->step), c2 = 1.f - powf(0.999f, (float)m->step);
         const float lr = tp->lr * (st < steps / 10 ? 1.f : 0.5f * (1.f + cosf(3.14159265f * (float)(st - steps / 10) /
                                                                               (float)(steps - steps / 10 + 1))));
-        k_adam<<<(MLP_NTRAIN + 255) / 256, 256, 0, s>>>(m->params, m->m, m->v, grad, MLP_NTRAIN, lr, 0.9f, 0.999f,
+        // warm-up keeps the first Adam steps small
+        const float lr_w = st < 100 ? lr * (float)(st + 1) / 100.f : lr;
+        k_adam<<<(MLP_NTRAIN + 255) / 256, 256, 0, s>>>(m->params, m->m, m->v, grad, MLP_NTRAIN, lr_w, 0.9f, 0.999f,
                                                          1e-8f, c1, c2);
         MDET_LAUNCHED(ctx, "k_adam");
         if (st + 50 >= steps) {

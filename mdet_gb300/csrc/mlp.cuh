@@ -25,6 +25,14 @@
 #define MLP_NPARAM (MLP_TAU + 1)    // 76362 floats
 #define MLP_NTRAIN MLP_MU           // parameters updated by the optimiser
 
+struct mdet_mlp {
+    float* params = nullptr;  // device, MLP_NPARAM floats
+    float* m = nullptr;       // Adam moments (MLP_NTRAIN each)
+    float* v = nullptr;
+    uint64_t step = 0;
+    int device = 0;
+};
+
 struct MlpActs {
     float* x;   // [rows][136] normalised input
     float* z1;  // [rows][256] pre-activation
@@ -42,3 +50,10 @@ int mlp_forward(mdet_ctx* ctx, const float* params, const float* tnf, const uint
 int mlp_backward(mdet_ctx* ctx, const float* params, const MlpActs& a, uint64_t npairs, const float* labels,
                  float m_pos, float m_neg, float* grad, double* loss_sum);
 int mlp_alloc_acts(mdet_ctx* ctx, const char* tag, uint64_t rows, MlpActs* a);
+// Embeddings of n rows (original order) into z (n x 64).
+int mlp_embed(mdet_ctx* ctx, const float* params, const float* tnf, uint64_t n, float* z);
+// G = Z^T Z (64 x 64, accumulated into a zeroed G) and P = Z V (n x k, V 64 x k).
+int mlp_gram(mdet_ctx* ctx, const float* z, uint64_t n, float* G);
+// column sums of Z added into a zeroed s (64)
+int mlp_colsum(mdet_ctx* ctx, const float* z, uint64_t n, float* s);
+int mlp_project(mdet_ctx* ctx, const float* z, uint64_t n, const float* V, int k, float* P);

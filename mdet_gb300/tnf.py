@@ -51,6 +51,54 @@ class GraphStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class TrainParams(ctypes.Structure):
+    _fields_ = [
+        ("pairs", u64),
+        ("candidate_fraction", D),
+        ("label_cutoff", D),
+        ("steps", u64),
+        ("batch_pairs", u32),
+        ("lr", ctypes.c_float),
+        ("m_pos", ctypes.c_float),
+        ("m_neg", ctypes.c_float),
+        ("tau_quantile", D),
+        ("seed", u64),
+    ]
+
+
+class TrainReport(ctypes.Structure):
+    _fields_ = [
+        ("steps", u64),
+        ("pairs", u64),
+        ("candidate_pairs", u64),
+        ("held_pos", u64),
+        ("held_neg", u64),
+        ("final_loss", D),
+        ("tau", D),
+        ("pos_median", D),
+        ("neg_median", D),
+        ("neg_below_tau", D),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LearnedReport(ctypes.Structure):
+    _fields_ = [
+        ("recall_target", D),
+        ("recall_rows", u32),
+        ("reserved", u32),
+        ("recall", D),
+        ("fell_back", u32),
+        ("reserved2", u32),
+        ("tiles_skipped", u64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
+
+
 # (name, restype, argtypes) of every entry point in include/mdet_tnf.h
 SIGNATURES = [
     ("mdet_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(P)]),
@@ -72,6 +120,17 @@ SIGNATURES = [
      [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
     ("mdet_tnf_graph_dev", ctypes.c_int,
      [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
+    ("mdet_mlp_create", ctypes.c_int, [P, u64, ctypes.POINTER(P)]),
+    ("mdet_mlp_destroy", ctypes.c_int, [P]),
+    ("mdet_mlp_param_count", u64, []),
+    ("mdet_mlp_get_params", ctypes.c_int, [P, P, P, u64]),
+    ("mdet_mlp_set_params", ctypes.c_int, [P, P, P, u64]),
+    ("mdet_mlp_embed_dev", ctypes.c_int, [P, P, P, u64, P]),
+    ("mdet_mlp_grad", ctypes.c_int,
+     [P, P, P, u64, P, P, u64, ctypes.c_float, ctypes.c_float, P, ctypes.POINTER(D)]),
+    ("mdet_mlp_train", ctypes.c_int,
+     [P, P, P, P, u64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)]),
+    ("mdet_ctx_set_learned", ctypes.c_int, [P, P, ctypes.POINTER(LearnedReport)]),
 ]
 
 _lib = None
@@ -254,10 +313,84 @@ class Context:
                                                 ctypes.byref(ne), ctypes.byref(stats)))
         return ne.value, stats.as_dict()
 
+    # ---- learned proposal -----------------------------------------------
+    def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 1024):
+        """Network used by mode="learned" graph calls; returns the report that
+        those calls fill (recall estimate, fallback, tiles skipped)."""
+        rep = LearnedReport()
+        rep.recall_target = recall_target
+        rep.recall_rows = recall_rows
+        self._learned = (net, rep)  # the context keeps both pointers
+        self._check(self.lib.mdet_ctx_set_learned(self.h, net.h if net else None, ctypes.byref(rep)))
+        return rep
+
     # ---- reference-named aliases ----------------------------------------
     calc_tnf = tnf_count
     gen_tnf_graph = tnf_graph
     max_prob_sample = max_prob
+
+
+class Network:
+    """The learned proposal's 136 -> 256 -> 128 -> 64 embedding network
+    (mdet_mlp): parameters live on the context's device."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = P()
+        ctx._check(self.lib.mdet_mlp_create(ctx.h, seed, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mdet_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def param_count() -> int:
+        return int(load_library().mdet_mlp_param_count())
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.param_count(), np.float32)
+        self.ctx._check(self.lib.mdet_mlp_get_params(self.ctx.h, self.h, _ptr(out), out.size))
+        return out
+
+    def set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self.ctx._check(self.lib.mdet_mlp_set_params(self.ctx.h, self.h, _ptr(p), p.size))
+
+    def embed_dev(self, d_tnf: int, n: int, d_out: int):
+        self.ctx._check(self.lib.mdet_mlp_embed_dev(self.ctx.h, self.h, P(d_tnf), n, P(d_out)))
+
+    def grad(self, x: np.ndarray, pairs: np.ndarray, labels: np.ndarray, m_pos: float, m_neg: float):
+        """(loss, gradient) of the mean contrastive loss; x rows x 136,
+        pairs (np x 2) indexing rows of x, labels (np,) in {0, 1}."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        pr = np.ascontiguousarray(pairs, dtype=np.uint32)
+        lab = np.ascontiguousarray(labels, dtype=np.float32)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = D()
+        self.ctx._check(self.lib.mdet_mlp_grad(self.ctx.h, self.h, _ptr(x), x.shape[0], _ptr(pr), _ptr(lab),
+                                               lab.size, m_pos, m_neg, _ptr(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_dev(self, d_tnf: int, d_ls: int, n: int, **kw) -> dict:
+        """Trains on a device-resident assembly; keyword arguments set
+        TrainParams fields.  Returns the training report."""
+        tp = TrainParams(pairs=4_000_000, candidate_fraction=0.5, label_cutoff=0.7, steps=3000, batch_pairs=8192,
+                         lr=1e-3, m_pos=0.5, m_neg=3.0, tau_quantile=0.9995, seed=7)
+        for k, v in kw.items():
+            setattr(tp, k, v)
+        rep = TrainReport()
+        self.ctx._check(self.lib.mdet_mlp_train(self.ctx.h, self.h, P(d_tnf), P(d_ls), n, ctypes.byref(tp),
+                                                ctypes.byref(rep)))
+        return rep.as_dict()
 
 
 def version() -> str:

@@ -1,0 +1,126 @@
+"""The learned proposal on the GPU: the network's forward pass and gradient
+against the float64 oracle (oracle/mlp_ref.py), training on one generated
+assembly and the learned graph on another, with recall against the
+all-pairs graph and the gain over the same method with an untrained network."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(__file__))
+
+from oracle import mlp_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+def _net_with_margins(gpu_ctx, seed, x, pairs):
+    import mdet_gb300 as m
+
+    net = m.Network(gpu_ctx, seed=seed)
+    p = net.get_params()
+    e = np.linalg.norm(R.embed(p, x[pairs[:, 0]]) - R.embed(p, x[pairs[:, 1]]), axis=1)
+    return net, p, 0.7 * float(np.median(e)), 1.3 * float(np.median(e))
+
+
+def test_gradient_matches_oracle(gpu_ctx):
+    rng = np.random.default_rng(11)
+    rows, npairs = 96, 80
+    x = rng.normal(0.0, 0.08, (rows, R.IN)).astype(np.float32) + 0.05
+    pairs = rng.integers(0, rows, (npairs, 2)).astype(np.uint32)
+    y = (rng.random(npairs) < 0.5).astype(np.float32)
+    net, p, mp, mn = _net_with_margins(gpu_ctx, 3, x, pairs.astype(np.int64))
+    loss, g = net.grad(x, pairs, y, mp, mn)
+    rl, rg = R.loss_and_grad(p, x, pairs, y, mp, mn)
+    assert abs(loss - rl) <= 1e-5 * abs(rl) + 1e-9
+    for lo, hi in [(R.W1, R.B1), (R.B1, R.W2), (R.W2, R.B2), (R.B2, R.W3), (R.W3, R.B3), (R.B3, R.MU)]:
+        err = np.linalg.norm(g[lo:hi] - rg[lo:hi]) / max(np.linalg.norm(rg[lo:hi]), 1e-30)
+        assert err < 1e-4, (lo, hi, err)   # FP32 accumulation against float64
+    net.close()
+
+
+def test_embedding_matches_oracle(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    import mdet_gb300 as m
+
+    rng = np.random.default_rng(12)
+    n = 3000
+    x = np.abs(rng.normal(0.07, 0.03, (n, R.IN))).astype(np.float32)
+    net = m.Network(gpu_ctx, seed=4)
+    p = net.get_params()
+    p[R.MU:R.SCALE] = x.mean(0)
+    p[R.SCALE] = 10.0
+    net.set_params(p)
+    dx = torch.from_numpy(x).cuda()
+    dz = torch.zeros((n, R.OUT), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    net.embed_dev(dx.data_ptr(), n, dz.data_ptr())
+    z = dz.cpu().numpy()
+    ref = R.embed(p, x)
+    err = np.abs(z - ref).max() / np.abs(ref).max()
+    assert err < 1e-5, err
+    net.close()
+
+
+def _device_set(gpu_ctx, seed, n, genomes):
+    import torch
+
+    from gpu_util import synth_set
+
+    a, _, tnf = synth_set(seed=seed, n=n, genomes=genomes, max_len=200000)
+    return a, tnf, torch.from_numpy(tnf).cuda(), torch.from_numpy(a.log_sizes.astype(np.float64)).cuda()
+
+
+@pytest.fixture(scope="module")
+def trained(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    import mdet_gb300 as m
+
+    _, _, dt, dl = _device_set(gpu_ctx, 401, 24000, 60)
+    torch.cuda.synchronize()
+    net = m.Network(gpu_ctx, seed=5)
+    rep = net.train_dev(dt.data_ptr(), dl.data_ptr(), dt.shape[0], pairs=2_000_000, steps=1500, seed=3)
+    base = m.Network(gpu_ctx, seed=5)
+    rep0 = base.train_dev(dt.data_ptr(), dl.data_ptr(), dt.shape[0], pairs=2_000_000, steps=0, seed=3)
+    yield net, rep, base, rep0
+    net.close()
+    base.close()
+
+
+def test_training_separates_edges(trained):
+    _, rep, _, rep0 = trained
+    assert rep["held_pos"] > 100 and rep["held_neg"] > 1000
+    assert np.isfinite(rep["tau"]) and rep["tau"] > 0
+    # trained: non-edges sit well beyond the edge margin
+    assert rep["neg_below_tau"] < rep0["neg_below_tau"]
+
+
+def test_learned_graph_recall_and_gain(gpu_ctx, trained):
+    import torch
+
+    net, _, base, _ = trained
+    a, tnf, _, _ = _device_set(gpu_ctx, 402, 24000, 60)   # unseen genomes
+    cutoff, k = 0.9, 200
+    full = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="bf16")
+    ref = {(int(f), int(t)): s for f, t, s in zip(full.from_, full.to, full.sTNF)}
+    out = {}
+    for name, nw in (("trained", net), ("untrained", base)):
+        rep = gpu_ctx.set_learned(nw, recall_target=0.999, recall_rows=1024)
+        g = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="learned")
+        got = {(int(f), int(t)): s for f, t, s in zip(g.from_, g.to, g.sTNF)}
+        common = set(ref) & set(got)
+        recall = len(common) / max(1, len(ref))
+        for key in common:
+            assert got[key] == ref[key]           # the same exact stage scores every edge
+        out[name] = dict(recall=recall, est=rep.recall, fell_back=rep.fell_back, skipped=rep.tiles_skipped,
+                         computed=g.stats["tiles_computed"], total=g.stats["tiles_total"])
+        assert recall >= 0.999 or rep.fell_back, out[name]
+        if rep.fell_back:
+            assert recall == 1.0
+    gpu_ctx.set_learned(None)
+    print(out)
+    tr, un = out["trained"], out["untrained"]
+    assert not tr["fell_back"], tr
+    # the gain: the trained network skips more of the all-pairs tiles
+    assert tr["skipped"] > max(un["skipped"], 0) and tr["skipped"] >= 0.3 * tr["total"], out

@@ -237,7 +237,7 @@ def run_ours(args):
     launches = ctx.launch_count() - launches0
     ms = e0.elapsed_time(e1) / args.steps
     kern = {k: ctx.kernel_ms(k) for k in ("k_filter_tc", "k_filter_simt", "k_count", "k_exact_graph",
-                                          "k_exact_maxprob", "k_topk_reg", "k_scatter")}
+                                          "k_exact_maxprob", "k_topk_sel", "k_scatter")}
     ctx.set_timing(False)
     ms = reduce_max(ms, dev)
 

@@ -145,10 +145,12 @@ int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_si
 /* ---- learned proposal (no counterpart in the reference) ----------------
  * A 136 -> 256 -> 128 -> 64 GELU network (BF16 weights, FP32 accumulation)
  * embeds each TNF row.  In MDET_MODE_LEARNED the graph orders contigs by
- * their embedding, skips tile pairs whose embedded distance bound exceeds
- * the trained margin tau, scores the remaining tiles exactly (tensor-core
- * filter + exact stage), then measures edge recall on a row sample against
- * the all-pairs result and falls back to the all-pairs form below target. */
+ * their embedding, scores a sample of rows against all columns exactly, sets
+ * the margin tau from half of the sample's edges (embedded distances), skips
+ * tile pairs whose embedded distance bound exceeds tau, measures the recall
+ * of the kept tiles on the other half and falls back to the all-pairs form
+ * below target; kept tiles are scored exactly (tensor-core filter + exact
+ * stage), so every emitted edge is exact. */
 typedef struct mdet_mlp mdet_mlp;
 
 typedef struct {
@@ -168,13 +170,14 @@ typedef struct {
 } mdet_train_report;
 
 typedef struct {
-    double recall_target;      /* fall back to all pairs below this estimated recall (0.999) */
-    uint32_t recall_rows;      /* rows sampled for the recall estimate (1024) */
-    uint32_t reserved;
+    double recall_target;      /* fall back to all pairs below this estimated recall (0: 0.999) */
+    uint32_t recall_rows;      /* rows sampled to calibrate tau and estimate recall (0: 2048) */
+    uint32_t segment;          /* contigs per size-sorted run of the embedding order (0: 1024; 1: none) */
     double recall;             /* out: estimated edge recall of the learned graph */
     uint32_t fell_back;        /* out: 1 when the all-pairs graph was returned */
-    uint32_t reserved2;
-    uint64_t tiles_skipped;    /* out */
+    uint32_t reserved;
+    uint64_t tiles_skipped;    /* out: 128 x 256 tiles skipped */
+    double tau;                /* out: embedded-distance margin used */
 } mdet_learned_report;
 
 int mdet_mlp_create(mdet_ctx* ctx, uint64_t seed, mdet_mlp** out);

@@ -4,15 +4,12 @@
 // and the labelling of training pairs for the learned proposal.
 #pragma once
 
+#include "ff.cuh"
 #include "graph.cuh"
 
 namespace mdet_exact {
 
 constexpr double kLn9 = 2.1972245773362196;
-
-__device__ __forceinline__ double horner_h(const double* h, double t) {
-    return t * fma(t, fma(t, fma(t, fma(t, h[5], h[4]), h[3]), h[2]), h[1]);
-}
 
 __device__ __forceinline__ unsigned long long dkey(double v) {
     unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -23,11 +20,8 @@ __device__ __forceinline__ double dkey_inv(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
-// d in the reference's terms float((a_k-b_k)^2) (cuda/Cuda2.cu:194-196).
-// The reference adds them in FP64; FP64 throughput is scarce on this part, so
-// two FP32 chains with error-free TwoSum compensation carry the sum instead
-// (relative error ~1e-14, the same order as the FP64 accumulation), and only
-// the final combine and sqrt run in FP64.
+// s + c accumulates t with the rounding error of each addition kept in c
+// (TwoSum, error-free)
 __device__ __forceinline__ void two_sum_acc(float& s, float& c, float t) {
     const float sum = __fadd_rn(s, t);
     const float bp = __fsub_rn(sum, s);
@@ -36,7 +30,12 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& c, float t) {
     c = __fadd_rn(c, err);
 }
 
-__device__ __forceinline__ double exact_dist(const float* __restrict__ a, const float* __restrict__ b) {
+// d in the reference's terms float((a_k-b_k)^2) (cuda/Cuda2.cu:194-196).
+// The reference adds them in FP64; FP64 throughput is scarce on this part, so
+// two FP32 chains with error-free TwoSum compensation carry the sum instead
+// (relative error ~1e-14, the same order as the FP64 accumulation); the sum
+// and its root are kept in float-float.
+__device__ __forceinline__ ff exact_dist(const float* __restrict__ a, const float* __restrict__ b) {
     const float4* ra = reinterpret_cast<const float4*>(a);
     const float4* rb = reinterpret_cast<const float4*>(b);
     float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
@@ -49,29 +48,49 @@ __device__ __forceinline__ double exact_dist(const float* __restrict__ a, const 
         two_sum_acc(s0, c0, __fmul_rn(d2, d2));
         two_sum_acc(s1, c1, __fmul_rn(d3, d3));
     }
-    return sqrt(((double)s0 + (double)s1) + ((double)c0 + (double)c1));
+    const ff s = two_sum(s0, s1);
+    const ff d2 = quick_two_sum(s.hi, __fadd_rn(__fadd_rn(c0, c1), s.lo));
+    return ff_sqrt(d2);
 }
 
-// pre-probability of sorted contigs i, j at distance d.  need_model2: also
-// evaluate the second model when the first is at or below log(9).
-__device__ __forceinline__ double pre_prob(const ModelParts& pi, const ModelParts& pj, double li, double lj, double d,
-                                           const ModelH& H, bool need_model2) {
-    const bool imin = li <= lj;
-    const ModelParts& pmin = imin ? pi : pj;
-    const ModelParts& pmax = imin ? pj : pi;
-    const double t = li * lj;
-    double b = pmin.f[0] + pmax.g[0] + horner_h(H.h[0], t);
-    double c = pmin.f[1] + pmax.g[1] + horner_h(H.h[1], t);
-    double pre = -(b + c * d);
-    if (pre <= kLn9) {
+__device__ __forceinline__ ff horner_h(const ff* h, ff t) {
+    ff acc = h[5];
+    acc = ff_add(ff_mul(acc, t), h[4]);
+    acc = ff_add(ff_mul(acc, t), h[3]);
+    acc = ff_add(ff_mul(acc, t), h[2]);
+    acc = ff_add(ff_mul(acc, t), h[1]);
+    return ff_mul(acc, t);
+}
+
+// pre-probability of contigs i, j at distance d (cuda/Cuda2.cu:199-241), in
+// float-float.  need_model2: also evaluate the second model when the first
+// is at or below log(9).
+__device__ __forceinline__ ff pre_prob(const PartsFF& pi, const PartsFF& pj, ff d, const ModelHFF& H,
+                                       bool need_model2) {
+    const ff kLn9ff = ff_make(0x1.193ea8p+1f, -0x1.54bf3ep-25f);
+    const bool imin = ff_le(pi.ls, pj.ls);
+    const PartsFF& pmin = imin ? pi : pj;
+    const PartsFF& pmax = imin ? pj : pi;
+    const ff t = ff_mul(pi.ls, pj.ls);
+    ff b = ff_add(ff_add(pmin.f[0], pmax.g[0]), horner_h(H.h[0], t));
+    ff c = ff_add(ff_add(pmin.f[1], pmax.g[1]), horner_h(H.h[1], t));
+    ff pre = ff_neg(ff_add(b, ff_mul(c, d)));
+    if (ff_le(pre, kLn9ff)) {
         if (!need_model2) return pre;
-        b = pmin.f[2] + pmax.g[2] + horner_h(H.h[2], t);
-        c = pmin.f[3] + pmax.g[3] + horner_h(H.h[3], t);
-        pre = -(b + c * d);
-        if (pre > kLn9) pre = kLn9;
+        b = ff_add(ff_add(pmin.f[2], pmax.g[2]), horner_h(H.h[2], t));
+        c = ff_add(ff_add(pmin.f[3], pmax.g[3]), horner_h(H.h[3], t));
+        pre = ff_neg(ff_add(b, ff_mul(c, d)));
+        if (ff_gt(pre, kLn9ff)) pre = kLn9ff;
     }
     return pre;
 }
 
+// sTNF = 1 - 1/(1 + e^pre) (cuda/Cuda2.cu:255), returned in double
+__device__ __forceinline__ double sim_of(ff pre) {
+    if (pre.hi > 80.f) return 1.0;
+    if (!(pre.hi > -80.f)) return 0.0;
+    const ff s = ff_recip(ff_add_f(ff_exp(pre), 1.f));
+    return 1.0 - ff_to_double(s);
+}
 
 }  // namespace mdet_exact

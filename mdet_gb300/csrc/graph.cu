@@ -227,8 +227,9 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
     if (st) {
         st->n_candidates = ncand;
         st->n_above_cutoff = ne;
-        uint64_t t = (n + 127) / 128;
-        st->tiles_total = t * (t + 1) / 2;
+        // 128 x 256 tiles of the triangular schedule
+        const uint64_t ta = (n + 127) / 128, tb = (n + 255) / 256, h = ta >> 1;
+        st->tiles_total = ta * tb - ((ta & 1) ? h * h : (h ? h * (h - 1) : 0));
         st->tiles_computed = st->tiles_total;
         st->ms_prep = tm.ms(0, 1);
         st->ms_filter = tm.ms(1, 2);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "ff.cuh"
 
 #define MDET_KPAD 144     // BF16 row length: 136 features + 8 zeros (9 x 16)
 #define MDET_TBL 256      // threshold table cells per axis
@@ -16,7 +17,8 @@ struct BlockMeta {
 };
 
 // Conservative upper bound of d*(x, y) over boxes of log sizes: a
-// 256 x 256 cell table over [lmin, lmax] with a sparse table along y.
+// 256 x 256 cell table over [lmin, lmax], suffix-maximised along x, with a
+// sparse table along y.
 struct DstarTable {
     const float* st;  // [levels][TBL][TBL]
     float lmin, inv_h;
@@ -39,6 +41,18 @@ struct ModelH {
     double h[4][6];  // H_m(t) coefficients t^1..t^5 (index 0 unused)
 };
 
+// The exact stage's per-contig data in float-float: F_m, G_m and the log size.
+struct PartsFF {
+    ff f[4];
+    ff g[4];
+    ff ls;
+    float pad[2];
+};
+
+struct ModelHFF {
+    ff h[4][6];
+};
+
 __device__ __forceinline__ int tbl_cell_lo(float v, const DstarTable& t) {
     int c = (int)floorf((v - t.lmin) * t.inv_h - 1e-3f);
     return c < 0 ? 0 : (c >= MDET_TBL ? MDET_TBL - 1 : c);
@@ -49,22 +63,18 @@ __device__ __forceinline__ int tbl_cell_hi(float v, const DstarTable& t) {
 }
 
 // Largest d* over all pairs whose sizes come from blocks with log-size
-// ranges [alo, ahi] and [blo, bhi].
+// ranges [alo, ahi] and [blo, bhi]: the x range starts at min(alo, blo),
+// whose suffix-maximised row covers the whole x range; two sparse-table
+// reads cover the y range.
 __device__ __forceinline__ float tile_dstar(const DstarTable& t, float alo, float ahi, float blo, float bhi) {
-    float xlo = fminf(alo, blo), xhi = fminf(ahi, bhi);
-    float ylo = fmaxf(alo, blo), yhi = fmaxf(ahi, bhi);
-    int cx0 = tbl_cell_lo(xlo, t), cx1 = tbl_cell_hi(xhi, t);
-    int cy0 = tbl_cell_lo(ylo, t), cy1 = tbl_cell_hi(yhi, t);
-    int span = cy1 - cy0 + 1;
-    int k = 31 - __clz(span);
-    const float* lvl = t.st + (size_t)k * MDET_TBL * MDET_TBL;
-    float m = 0.f;
-    for (int a = cx0; a <= cx1; ++a) {
-        float v0 = __ldg(lvl + a * MDET_TBL + cy0);
-        float v1 = __ldg(lvl + a * MDET_TBL + (cy1 - (1 << k) + 1));
-        m = fmaxf(m, fmaxf(v0, v1));
-    }
-    return m;
+    const float xlo = fminf(alo, blo);
+    const float ylo = fmaxf(alo, blo), yhi = fmaxf(ahi, bhi);
+    const int cx0 = tbl_cell_lo(xlo, t);
+    const int cy0 = tbl_cell_lo(ylo, t), cy1 = tbl_cell_hi(yhi, t);
+    const int span = cy1 - cy0 + 1;
+    const int k = 31 - __clz(span);
+    const float* lvl = t.st + (size_t)k * MDET_TBL * MDET_TBL + cx0 * MDET_TBL;
+    return fmaxf(__ldg(lvl + cy0), __ldg(lvl + (cy1 - (1 << k) + 1)));
 }
 
 // Host-side entry points of the stages (graph_*.cu).
@@ -74,7 +84,7 @@ struct GraphPrep {
     uint32_t* inv;                   // original index -> sorted position
     float* x32;                      // sorted FP32 TNF rows [n][136]
     double* ls;                      // sorted log sizes
-    ModelParts* parts;               // sorted model parts
+    PartsFF* parts;                  // sorted model parts and log sizes (float-float)
     uint16_t* xa;                    // A role: sorted centred BF16 rows [x~, 1, 1, 0..] [npad][144]
     uint16_t* xb;                    // B role: [x~, -hi(||x~||^2/2), -lo(||x~||^2/2), 0..]; padding -inf
     float* nsq;                      // ||x~||^2 per sorted row (inf for padding rows)
@@ -91,6 +101,7 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
                       bool sorted = true);
 ModelH model_h();
+ModelHFF model_h_ff();
 
 // Above-cutoff pair found by the exact stage (sorted positions).
 struct Edge {

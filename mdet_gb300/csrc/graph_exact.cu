@@ -22,10 +22,10 @@ struct ExactArgs {
     unsigned long long ncand;
     const uint32_t* row_map;  // maxprob: sample slot -> sorted position; graph: null
     const float* x32;
-    const double* ls;
-    const ModelParts* parts;
-    ModelH H;
+    const PartsFF* parts;
+    ModelHFF H;
     double L;
+    ff Lff;
     // graph outputs
     Edge* edges;
     unsigned long long* nedges;
@@ -34,31 +34,87 @@ struct ExactArgs {
     unsigned long long* maxkey;
 };
 
+// Squared distances of 32 candidates per warp: candidate base + L belongs to
+// lane L.  Eight lanes share one candidate at a time, so each row is read in
+// coalesced 128-byte runs (lane k of the group takes float4 columns k, k+8,
+// ...); partial sums keep their rounding errors (TwoSum) through the group
+// reduction.  Returns the owner lane's (sum, error) pair and its rows.
+__device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigned long long ncand,
+                                         unsigned long long base, const uint32_t* __restrict__ row_map,
+                                         const float* __restrict__ x32, uint32_t lane, uint32_t& si, uint32_t& sj) {
+    const uint32_t grp = lane >> 3, sub = lane & 7;
+    float ms = 0.f, mc = 0.f;
+    si = sj = 0;
+#pragma unroll 1
+    for (uint32_t it = 0; it < 8; ++it) {
+        const unsigned long long k = base + it * 4 + grp;
+        float s = 0.f, c = 0.f;
+        uint32_t a = 0, b = 0;
+        if (k < ncand) {
+            const uint2 cd = cand[k];
+            a = row_map ? row_map[cd.x] : cd.x;
+            b = cd.y;
+            const float4* ra = reinterpret_cast<const float4*>(x32 + (uint64_t)a * MDET_NTNF);
+            const float4* rb = reinterpret_cast<const float4*>(x32 + (uint64_t)b * MDET_NTNF);
+#pragma unroll
+            for (uint32_t q = 0; q < 5; ++q) {
+                const uint32_t col = sub + 8 * q;
+                if (col < MDET_NTNF / 4) {
+                    const float4 x = __ldg(ra + col), y = __ldg(rb + col);
+                    const float d0 = __fsub_rn(x.x, y.x), d1 = __fsub_rn(x.y, y.y);
+                    const float d2 = __fsub_rn(x.z, y.z), d3 = __fsub_rn(x.w, y.w);
+                    two_sum_acc(s, c, __fmul_rn(d0, d0));
+                    two_sum_acc(s, c, __fmul_rn(d1, d1));
+                    two_sum_acc(s, c, __fmul_rn(d2, d2));
+                    two_sum_acc(s, c, __fmul_rn(d3, d3));
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+            const float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+            const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+            const ff t = two_sum(s, s2);
+            s = t.hi;
+            c = __fadd_rn(__fadd_rn(c, c2), t.lo);
+        }
+        // candidate base + L was handled in round L / 4 by group L % 4
+        const uint32_t src = 8 * (lane & 3);
+        const float vs = __shfl_sync(0xffffffffu, s, src);
+        const float vc = __shfl_sync(0xffffffffu, c, src);
+        const uint32_t va = __shfl_sync(0xffffffffu, a, src);
+        const uint32_t vb = __shfl_sync(0xffffffffu, b, src);
+        if ((lane >> 2) == it) {
+            ms = vs;
+            mc = vc;
+            si = va;
+            sj = vb;
+        }
+    }
+    return quick_two_sum(ms, mc);
+}
+
 __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
     const bool model2 = p.L < kLn9;
     const uint32_t lane = threadIdx.x & 31;
-    for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < p.ncand;
-         base += (unsigned long long)gridDim.x * blockDim.x) {
-        unsigned long long idx = base + threadIdx.x;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    for (unsigned long long base = ((unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32;
+         base < p.ncand; base += warps * 32) {
+        uint32_t si, sj;
+        const ff d2 = warp_dist2(p.cand, p.ncand, base, nullptr, p.x32, lane, si, sj);
         bool edge = false;
-        uint32_t si = 0, sj = 0;
         double sim = 0;
-        if (idx < p.ncand) {
-            uint2 c = p.cand[idx];
-            si = c.x;
-            sj = c.y;
-            double d = exact_dist(p.x32 + (uint64_t)si * MDET_NTNF, p.x32 + (uint64_t)sj * MDET_NTNF);
-            ModelParts pi = p.parts[si], pj = p.parts[sj];
-            double pre = pre_prob(pi, pj, p.ls[si], p.ls[sj], d, p.H, model2);
-            if (pre > p.L) {
+        if (base + lane < p.ncand) {
+            const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, model2);
+            if (ff_gt(pre, p.Lff)) {
                 edge = true;
-                sim = 1. - 1. / (1. + exp(pre));
+                sim = sim_of(pre);
             }
         }
-        uint32_t bal = __ballot_sync(0xffffffffu, edge);
+        const uint32_t bal = __ballot_sync(0xffffffffu, edge);
         if (bal) {
             unsigned long long wb = 0;
-            int leader = __ffs(bal) - 1;
+            const int leader = __ffs(bal) - 1;
             if (lane == (uint32_t)leader) wb = atomicAdd(p.nedges, (unsigned long long)__popc(bal));
             wb = __shfl_sync(0xffffffffu, wb, leader);
             if (edge) {
@@ -75,15 +131,17 @@ __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
 }
 
 __global__ void __launch_bounds__(256) k_exact_maxprob(ExactArgs p) {
-    for (unsigned long long idx = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; idx < p.ncand;
-         idx += (unsigned long long)gridDim.x * blockDim.x) {
-        uint2 c = p.cand[idx];
-        uint32_t si = p.row_map[c.x], sj = c.y;
-        if (si == sj) continue;  // the sampled contig itself
-        double d = exact_dist(p.x32 + (uint64_t)si * MDET_NTNF, p.x32 + (uint64_t)sj * MDET_NTNF);
-        ModelParts pi = p.parts[si], pj = p.parts[sj];
-        double pre = pre_prob(pi, pj, p.ls[si], p.ls[sj], d, p.H, true);
-        atomicMax(&p.maxkey[c.x], dkey(pre));
+    const uint32_t lane = threadIdx.x & 31;
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    for (unsigned long long base = ((unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32;
+         base < p.ncand; base += warps * 32) {
+        uint32_t si, sj;
+        const ff d2 = warp_dist2(p.cand, p.ncand, base, p.row_map, p.x32, lane, si, sj);
+        const unsigned long long idx = base + lane;
+        if (idx < p.ncand && si != sj) {  // skip the sampled contig itself
+            const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, true);
+            atomicMax(&p.maxkey[p.cand[idx].x], dkey(ff_to_double(pre)));
+        }
     }
 }
 
@@ -235,13 +293,16 @@ __global__ void __launch_bounds__(1024) k_topk_big(const uint32_t* __restrict__ 
     }
 }
 
-// ---- register top-k: warp per contig, entries held in registers ----------
-// Entry i of a chunk of C = 32*E lives in lane i % 32, slot i / 32.  A
-// bitonic network sorts a chunk best-first (exchanges across lanes by
-// shuffles, within a lane by register swaps); a longer row is consumed chunk
-// by chunk, each sorted chunk merged into the running best C (elementwise
-// better of best[i] and chunk[C-1-i] is bitonic, then a bitonic merge), so a
-// row of any length needs C >= max_edges registers' worth of entries only.
+// ---- selection top-k: warp per contig --------------------------------------
+// A row's kept set is its max_edges best entries under (sim descending, ocol
+// ascending).  Ordered as the 96-bit key (bits of sim, ~ocol) -- sim is a
+// positive double, so its bits order like its value -- the kept set is every
+// entry whose key is >= the max_edges-th largest key, found by a radix
+// select (8-bit digits, most significant first, stopping as soon as the
+// digit's bin holds exactly the entries still needed).  Only kept entries
+// with ocol above the row's own index are emitted, so only those are sorted
+// (bitonic network in registers: entry i of a chunk of 32*E in lane i % 32,
+// slot i / 32) and written to the front of the row.
 
 __device__ __forceinline__ bool kv_less(double s1, uint32_t c1, double s2, uint32_t c2) {
     return s1 > s2 || (s1 == s2 && c1 < c2);
@@ -249,13 +310,12 @@ __device__ __forceinline__ bool kv_less(double s1, uint32_t c1, double s2, uint3
 
 // In-lane compare-exchange of slots e and e | JE (stride >= 32 entries).
 template <int E, int JE>
-__device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k,
-                                              bool all_up) {
+__device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         if ((e & JE) == 0) {
             const int e2 = e | JE;
-            const bool up = all_up || ((((uint32_t)e * 32u + lane) & k) == 0);
+            const bool up = ((((uint32_t)e * 32u + lane) & k) == 0);
             const bool sw = up ? kv_less(s[e2], c[e2], s[e], c[e]) : kv_less(s[e], c[e], s[e2], c[e2]);
             const double s1 = sw ? s[e2] : s[e], s2 = sw ? s[e] : s[e2];
             const uint32_t c1 = sw ? c[e2] : c[e], c2 = sw ? c[e] : c[e2];
@@ -268,19 +328,19 @@ __device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], 
 }
 
 template <int E>
-__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k, uint32_t j,
-                                           bool all_up) {
+__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k,
+                                              uint32_t j) {
     if (j >= 32) {
         const uint32_t je = j >> 5;
-        if (je == 1) stage_in_lane<E, 1>(s, c, lane, k, all_up);
-        if (E >= 4 && je == 2) stage_in_lane<E, (E >= 4 ? 2 : 1)>(s, c, lane, k, all_up);
-        if (E >= 8 && je == 4) stage_in_lane<E, (E >= 8 ? 4 : 1)>(s, c, lane, k, all_up);
-        if (E >= 16 && je == 8) stage_in_lane<E, (E >= 16 ? 8 : 1)>(s, c, lane, k, all_up);
+        if (E >= 2 && je == 1) stage_in_lane<E, 1>(s, c, lane, k);
+        if (E >= 4 && je == 2) stage_in_lane<E, (E >= 4 ? 2 : 1)>(s, c, lane, k);
+        if (E >= 8 && je == 4) stage_in_lane<E, (E >= 8 ? 4 : 1)>(s, c, lane, k);
+        if (E >= 16 && je == 8) stage_in_lane<E, (E >= 16 ? 8 : 1)>(s, c, lane, k);
     } else {
         const bool lower = (lane & j) == 0;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            const bool up = all_up || ((((uint32_t)e * 32u + lane) & k) == 0);
+            const bool up = ((((uint32_t)e * 32u + lane) & k) == 0);
             const double os = __shfl_xor_sync(0xffffffffu, s[e], (int)j);
             const uint32_t oc = __shfl_xor_sync(0xffffffffu, c[e], (int)j);
             const bool take = (lower == up) ? kv_less(os, oc, s[e], c[e]) : kv_less(s[e], c[e], os, oc);
@@ -290,102 +350,192 @@ __device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], 
     }
 }
 
+// Sorts entries [0, m) of the warp's staging buffer best-first into row[0, m).
 template <int E>
-__device__ __forceinline__ void bitonic_sort(double (&s)[E], uint32_t (&c)[E], uint32_t lane) {
-#pragma unroll 1
-    for (uint32_t k = 2; k <= 32u * E; k <<= 1)
-#pragma unroll 1
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_stage<E>(s, c, lane, k, j, false);
-}
-
-template <int E>
-__device__ __forceinline__ void load_chunk(const Ent* __restrict__ row, uint32_t base, uint32_t cnt, uint32_t lane,
-                                           double (&s)[E], uint32_t (&c)[E]) {
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const uint32_t i = base + (uint32_t)e * 32u + lane;
-        if (i < cnt) {
-            const Ent x = row[i];
-            s[e] = x.sim;
-            c[e] = x.ocol;
-        } else {
-            s[e] = -1.0;
-            c[e] = 0xFFFFFFFFu;
-        }
-    }
-}
-
-// Sorts the row's best min(cnt, keep) entries into row[0..) and returns how
-// many of them have a column above orow (lane 0 holds the total).
-template <int E>
-__device__ __forceinline__ uint32_t topk_row(Ent* __restrict__ row, uint32_t cnt, uint32_t keep, uint32_t orow,
-                                             uint32_t lane) {
-    double bs[E], cs[E];
-    uint32_t bc[E], cc[E];
-    load_chunk<E>(row, 0, cnt, lane, bs, bc);
-    bitonic_sort<E>(bs, bc, lane);
-    for (uint32_t base = 32u * E; base < cnt; base += 32u * E) {
-        load_chunk<E>(row, base, cnt, lane, cs, cc);
-        bitonic_sort<E>(cs, cc, lane);
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const double os = __shfl_sync(0xffffffffu, cs[E - 1 - e], 31 - lane);
-            const uint32_t oc = __shfl_sync(0xffffffffu, cc[E - 1 - e], 31 - lane);
-            if (kv_less(os, oc, bs[e], bc[e])) {
-                bs[e] = os;
-                bc[e] = oc;
-            }
-        }
-#pragma unroll 1
-        for (uint32_t j = 16u * E; j > 0; j >>= 1) bitonic_stage<E>(bs, bc, lane, 0, j, true);
-    }
-    __syncwarp();
-    uint32_t n_up = 0;
+__device__ __forceinline__ void sort_out(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ col,
+                                         uint32_t m, uint32_t lane, Ent* __restrict__ row) {
+    double s[E];
+    uint32_t c[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const uint32_t i = (uint32_t)e * 32u + lane;
-        if (i < keep) {
+        s[e] = i < m ? __longlong_as_double((long long)key[i]) : -1.0;
+        c[e] = i < m ? col[i] : 0xFFFFFFFFu;
+    }
+    uint32_t P = 32u * E;
+    while (P / 2 >= m && P > 64) P >>= 1;  // the network only needs the next power of two
+#pragma unroll 1
+    for (uint32_t k = 2; k <= P; k <<= 1)
+#pragma unroll 1
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) bitonic_stage<E>(s, c, lane, k, j);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t i = (uint32_t)e * 32u + lane;
+        if (i < m) {
             Ent x;
-            x.sim = bs[e];
-            x.ocol = bc[e];
+            x.sim = s[e];
+            x.ocol = c[e];
             x.pad = 0;
             row[i] = x;
-            n_up += bc[e] > orow;
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) n_up += __shfl_xor_sync(0xffffffffu, n_up, o);
-    return n_up;
+}
+
+constexpr int kSelWarps = 4;
+constexpr uint32_t kSelCap = 896;  // entries staged in shared memory per warp (46 KB per block)
+
+__device__ __forceinline__ uint32_t sel_digit(unsigned long long hi, uint32_t lo, int p) {
+    return p < 8 ? (uint32_t)(hi >> (56 - 8 * p)) & 255u : (lo >> (24 - 8 * (p - 8))) & 255u;
+}
+
+// key (hi, lo) agrees with the prefix (P_hi, P_lo) on its first p digits
+__device__ __forceinline__ bool sel_match(unsigned long long hi, uint32_t lo, unsigned long long P_hi, uint32_t P_lo,
+                                          int p) {
+    if (p == 0) return true;
+    if (p < 8) return (hi >> (64 - 8 * p)) == (P_hi >> (64 - 8 * p));
+    if (hi != P_hi) return false;
+    return p == 8 || (lo >> (32 - 8 * (p - 8))) == (P_lo >> (32 - 8 * (p - 8)));
 }
 
 template <int EMAX>
-__global__ void __launch_bounds__(256) k_topk_reg(const unsigned long long* __restrict__ rowptr,
-                                                  const uint32_t* __restrict__ deg, const uint32_t* __restrict__ perm,
-                                                  uint32_t n, uint32_t max_edges, Ent* __restrict__ list,
-                                                  uint32_t* __restrict__ out_cnt) {
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t s = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); s < n; s += gridDim.x * (blockDim.x / 32)) {
-        const uint32_t cnt = deg[s], orow = perm[s];
-        const uint32_t keep = cnt < max_edges ? cnt : max_edges;
-        Ent* row = list + rowptr[s];
-        uint32_t c;
-        if (cnt <= 128)
-            c = topk_row<4>(row, cnt, keep, orow, lane);
+__global__ void __launch_bounds__(kSelWarps * 32) k_topk_sel(const unsigned long long* __restrict__ rowptr,
+                                                             const uint32_t* __restrict__ deg,
+                                                             const uint32_t* __restrict__ perm, uint32_t n,
+                                                             uint32_t max_edges, Ent* __restrict__ list,
+                                                             uint32_t* __restrict__ out_cnt) {
+    __shared__ unsigned long long s_key[kSelWarps][kSelCap];
+    __shared__ uint32_t s_col[kSelWarps][kSelCap];
+    __shared__ uint32_t s_hist[kSelWarps][256];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long* key = s_key[w];
+    uint32_t* col = s_col[w];
+    uint32_t* hist = s_hist[w];
+    for (uint32_t sp = blockIdx.x * kSelWarps + w; sp < n; sp += gridDim.x * kSelWarps) {
+        const uint32_t cnt = deg[sp], orow = perm[sp];
+        Ent* row = list + rowptr[sp];
+        const bool staged = cnt <= kSelCap;
+        if (staged)
+            for (uint32_t i = lane; i < cnt; i += 32) {
+                const Ent x = row[i];
+                key[i] = (unsigned long long)__double_as_longlong(x.sim);
+                col[i] = x.ocol;
+            }
+        __syncwarp();
+        // threshold key (P_hi, P_lo): kept iff key >= it
+        unsigned long long P_hi = 0;
+        uint32_t P_lo = 0;
+        if (cnt > max_edges) {
+            uint32_t need = max_edges;
+            for (int p = 0; p < 12; ++p) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t) hist[lane * 8 + t] = 0;
+                __syncwarp();
+                for (uint32_t i = lane; i < cnt; i += 32) {
+                    unsigned long long hi;
+                    uint32_t c;
+                    if (staged) {
+                        hi = key[i];
+                        c = col[i];
+                    } else {
+                        const Ent x = row[i];
+                        hi = (unsigned long long)__double_as_longlong(x.sim);
+                        c = x.ocol;
+                    }
+                    const uint32_t lo = ~c;
+                    if (sel_match(hi, lo, P_hi, P_lo, p)) atomicAdd(&hist[sel_digit(hi, lo, p)], 1u);
+                }
+                __syncwarp();
+                // lane L owns bins [8L, 8L + 8); count the bins above each lane's
+                uint32_t b[8], own = 0;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    b[t] = hist[lane * 8 + t];
+                    own += b[t];
+                }
+                uint32_t suf = own;  // inclusive sum over lanes >= lane
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t v = __shfl_down_sync(0xffffffffu, suf, o);
+                    if (lane + o < 32) suf += v;
+                }
+                uint32_t above = suf - own;
+                int bin = -1;
+                uint32_t bin_above = 0, bin_cnt = 0;
+                if (above < need && need <= suf) {
+#pragma unroll
+                    for (int t = 7; t >= 0; --t) {
+                        if (bin < 0 && above + b[t] >= need) {
+                            bin = (int)(lane * 8 + t);
+                            bin_above = above;
+                            bin_cnt = b[t];
+                        }
+                        if (bin < 0) above += b[t];
+                    }
+                }
+                const uint32_t who = __ffs(__ballot_sync(0xffffffffu, bin >= 0)) - 1;
+                bin = __shfl_sync(0xffffffffu, bin, who);
+                bin_above = __shfl_sync(0xffffffffu, bin_above, who);
+                bin_cnt = __shfl_sync(0xffffffffu, bin_cnt, who);
+                need -= bin_above;
+                if (p < 8)
+                    P_hi |= (unsigned long long)bin << (56 - 8 * p);
+                else
+                    P_lo |= (uint32_t)bin << (24 - 8 * (p - 8));
+                if (bin_cnt == need) break;
+            }
+        }
+        // compact the kept entries with ocol > orow to the front of the buffer
+        uint32_t m = 0;
+        const uint32_t cap = max_edges;
+        for (uint32_t base = 0; base < cnt; base += 32) {
+            const uint32_t i = base + lane;
+            unsigned long long hi = 0;
+            uint32_t c = 0;
+            bool take = false;
+            if (i < cnt) {
+                if (staged) {
+                    hi = key[i];
+                    c = col[i];
+                } else {
+                    const Ent x = row[i];
+                    hi = (unsigned long long)__double_as_longlong(x.sim);
+                    c = x.ocol;
+                }
+                const uint32_t lo = ~c;
+                take = c > orow && (hi > P_hi || (hi == P_hi && lo >= P_lo));
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, take);
+            __syncwarp();  // every lane has read its entry before any slot is rewritten
+            const uint32_t q = m + __popc(bal & ((1u << lane) - 1u));
+            if (take && q < cap) {
+                key[q] = hi;
+                col[q] = c;
+            }
+            m += __popc(bal);
+            __syncwarp();
+        }
+        m = min(m, cap);
+        if (m <= 64)
+            sort_out<2>(key, col, m, lane, row);
+        else if (m <= 128)
+            sort_out<4>(key, col, m, lane, row);
         else
-            c = topk_row<EMAX>(row, cnt, keep, orow, lane);
-        if (lane == 0) out_cnt[orow] = c;
+            sort_out<EMAX>(key, col, m, lane, row);
+        if (lane == 0) out_cnt[orow] = m;
+        __syncwarp();
     }
 }
 
 // Warp per original row: write its kept edges with ocol > row, in order.
+// compacted: the row starts with exactly those edges (selection top-k).
 __global__ void k_emit(const uint32_t* __restrict__ inv, const unsigned long long* __restrict__ rowptr,
                        const uint32_t* __restrict__ deg, const Ent* __restrict__ list,
-                       const unsigned long long* __restrict__ outptr, uint32_t n, uint32_t max_edges,
+                       const unsigned long long* __restrict__ outptr, uint32_t n, uint32_t max_edges, int compacted,
                        uint64_t* __restrict__ from, uint64_t* __restrict__ to, double* __restrict__ stnf) {
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t o = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); o < n; o += gridDim.x * (blockDim.x / 32)) {
         const uint32_t s = inv[o];
-        const uint32_t keep = min(deg[s], max_edges);
+        const uint32_t keep = compacted ? (uint32_t)(outptr[o + 1] - outptr[o]) : min(deg[s], max_edges);
         const Ent* row = list + rowptr[s];
         unsigned long long pos = outptr[o];
         for (uint32_t b = 0; b < keep; b += 32) {
@@ -449,15 +599,17 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.cand = cand;
         p.ncand = ncand;
         p.x32 = g.x32;
-        p.ls = g.ls;
         p.parts = g.parts;
-        p.H = model_h();
+        p.H = model_h_ff();
         p.L = L;
+        p.Lff.hi = (float)L;
+        p.Lff.lo = (float)(L - (double)p.Lff.hi);
         p.edges = edges;
         p.nedges = cnt;
         p.deg = deg;
+        // a warp takes 32 candidates per round
         unsigned long long blocks = (ncand + 255) / 256;
-        unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
+        unsigned long long cap = (unsigned long long)ctx->num_sms * 8;
         ctx_timer_begin(ctx, "k_exact_graph");
     k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
         ctx_timer_end(ctx, "k_exact_graph");
@@ -484,12 +636,11 @@ int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned
         p.ncand = ncand;
         p.row_map = row_map;
         p.x32 = g.x32;
-        p.ls = g.ls;
         p.parts = g.parts;
-        p.H = model_h();
+        p.H = model_h_ff();
         p.maxkey = maxkey;
         unsigned long long blocks = (ncand + 255) / 256;
-        unsigned long long cap = (unsigned long long)ctx->num_sms * 16;
+        unsigned long long cap = (unsigned long long)ctx->num_sms * 8;
         ctx_timer_begin(ctx, "k_exact_maxprob");
     k_exact_maxprob<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
         ctx_timer_end(ctx, "k_exact_maxprob");
@@ -534,15 +685,16 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
     MDET_CUDA(ctx, cudaMemsetAsync(nbig, 0, 4, s));
     MDET_CUDA(ctx, cudaMemsetAsync(out_cnt, 0, (uint64_t)n * 4, s));
     if (max_edges <= 512) {
-        // register top-k (chunk of 256 or 512 entries per warp)
-        const unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + 7) / 8, (uint64_t)ctx->num_sms * 16);
-        ctx_timer_begin(ctx, "k_topk_reg");
+        // selection top-k, warp per row
+        const unsigned blocks =
+            (unsigned)std::min<uint64_t>(((uint64_t)n + kSelWarps - 1) / kSelWarps, (uint64_t)ctx->num_sms * 32);
+        ctx_timer_begin(ctx, "k_topk_sel");
         if (max_edges <= 256)
-            k_topk_reg<8><<<blocks, 256, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+            k_topk_sel<8><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
         else
-            k_topk_reg<16><<<blocks, 256, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
-        ctx_timer_end(ctx, "k_topk_reg");
-        MDET_LAUNCHED(ctx, "k_topk_reg");
+            k_topk_sel<16><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+        ctx_timer_end(ctx, "k_topk_sel");
+        MDET_LAUNCHED(ctx, "k_topk_sel");
     } else {
         size_t dyn = (size_t)kTopkWarps * kWarpCap * sizeof(Ent);
         static bool set[64] = {false};
@@ -580,7 +732,8 @@ int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d
     const uint32_t* deg = (const uint32_t*)ctx->bufs["ex.deg"].p;
     if (total) {
         unsigned blocks = (unsigned)std::min<uint64_t>(((uint64_t)n + 7) / 8, (uint64_t)ctx->num_sms * 32);
-        k_emit<<<blocks, 256, 0, s>>>(g.inv, rowptr, deg, list, outptr, n, max_edges, d_from, d_to, d_stnf);
+        k_emit<<<blocks, 256, 0, s>>>(g.inv, rowptr, deg, list, outptr, n, max_edges, max_edges <= 512 ? 1 : 0,
+                                      d_from, d_to, d_stnf);
         MDET_LAUNCHED(ctx, "k_emit");
     }
     return MDET_OK;

@@ -107,6 +107,13 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// max(a, b, c) in one instruction (three-source max.f32)
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // 64 consecutive FP32 columns of this thread's TMEM lane; the wait sits in
 // the same asm statement, so no use of the registers can be scheduled early.
 __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
@@ -359,19 +366,27 @@ __global__ void __launch_bounds__(kThreads, 1)
                     float v[64];
                     tmem_ld64(tmem + ((quarter * 32) << 16) + s * kBN + col0, v);
                     const uint32_t gc0 = c.J * kBN + col0;
+                    // strided group maxima: mx[t] = max of v[t + 8j], j = 0..7
                     float mx[8];
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) mx[k] = fmaxf(v[k], v[k + 8]);
-#pragma unroll
-                    for (int k = 16; k < 64; k += 8)
-#pragma unroll
-                        for (int t = 0; t < 8; ++t) mx[t] = fmaxf(mx[t], v[k + t]);
-                    const float m = fmaxf(fmaxf(fmaxf(mx[0], mx[1]), fmaxf(mx[2], mx[3])),
-                                          fmaxf(fmaxf(mx[4], mx[5]), fmaxf(mx[6], mx[7])));
+                    for (int t = 0; t < 8; ++t) {
+                        float a = max3f(v[t], v[t + 8], v[t + 16]);
+                        a = max3f(a, v[t + 24], v[t + 32]);
+                        a = max3f(a, v[t + 40], v[t + 48]);
+                        mx[t] = fmaxf(a, v[t + 56]);
+                    }
+                    const float m = max3f(max3f(mx[0], mx[1], mx[2]), max3f(mx[3], mx[4], mx[5]), fmaxf(mx[6], mx[7]));
                     if (m > hr) {
+                        // only the groups whose maximum passes are tested entry by entry
                         unsigned long long mask = 0;
 #pragma unroll
-                        for (int k = 0; k < 64; ++k) mask |= (unsigned long long)(v[k] > hr ? 1u : 0u) << k;
+                        for (int t = 0; t < 8; ++t) {
+                            if (mx[t] > hr) {
+#pragma unroll
+                                for (int j = 0; j < 8; ++j)
+                                    mask |= (unsigned long long)(v[t + 8 * j] > hr ? 1u : 0u) << (t + 8 * j);
+                            }
+                        }
                         while (mask) {
                             const int k = __ffsll((long long)mask) - 1;
                             mask &= mask - 1;

@@ -136,38 +136,65 @@ __global__ void __launch_bounds__(256) k_tile_flags(const float* __restrict__ rc
     }
 }
 
-// Recall of the kept tiles over the true edges of the sampled rows: every
-// candidate of the all-columns pass is scored exactly; an edge counts as
-// recalled when its tile pair is kept.
-__global__ void __launch_bounds__(256) k_recall(const uint2* __restrict__ cand, unsigned long long ncand,
-                                                const uint32_t* __restrict__ row_map, const float* __restrict__ x32,
-                                                const double* __restrict__ ls, const ModelParts* __restrict__ parts,
-                                                ModelH H, double L, const uint8_t* __restrict__ keep, uint32_t tb,
-                                                unsigned long long* __restrict__ counts) {
-    const bool model2 = L < kLn9;
-    unsigned long long tot = 0, hit = 0;
+// Exact edges of the sampled rows (all-columns pass): edges of even sample
+// slots give their embedded distance to the calibration set; edges of odd
+// slots go to the validation set as (row, column) positions.
+__global__ void __launch_bounds__(256) k_sample_edges(const uint2* __restrict__ cand, unsigned long long ncand,
+                                                      const uint32_t* __restrict__ row_map,
+                                                      const float* __restrict__ x32,
+                                                      const PartsFF* __restrict__ parts, ModelHFF H, ff L, int model2,
+                                                      const uint32_t* __restrict__ perm, const float* __restrict__ z,
+                                                      float* __restrict__ cal, uint2* __restrict__ val,
+                                                      unsigned long long* __restrict__ counts) {
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ncand;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const uint2 c = cand[i];
         const uint32_t r = row_map[c.x], q = c.y;
         if (r == q) continue;
-        const double d = exact_dist(x32 + (uint64_t)r * MDET_NTNF, x32 + (uint64_t)q * MDET_NTNF);
-        const double pre = pre_prob(parts[r], parts[q], ls[r], ls[q], d, H, model2);
-        if (pre > L) {
-            const uint32_t lo = min(r, q), hi = max(r, q);
-            ++tot;
-            hit += keep[(uint64_t)(lo / 128) * tb + hi / 256];
+        const ff d = exact_dist(x32 + (uint64_t)r * MDET_NTNF, x32 + (uint64_t)q * MDET_NTNF);
+        const ff pre = pre_prob(parts[r], parts[q], d, H, model2 != 0);
+        if (!ff_gt(pre, L)) continue;
+        if (c.x & 1) {
+            val[atomicAdd(counts + 1, 1ull)] = make_uint2(min(r, q), max(r, q));
+        } else {
+            const float4* za = reinterpret_cast<const float4*>(z + (uint64_t)perm[r] * MLP_OUT);
+            const float4* zb = reinterpret_cast<const float4*>(z + (uint64_t)perm[q] * MLP_OUT);
+            float e2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < MLP_OUT / 4; ++k) {
+                const float4 u = za[k], v = zb[k];
+                e2 += (u.x - v.x) * (u.x - v.x) + (u.y - v.y) * (u.y - v.y) + (u.z - v.z) * (u.z - v.z) +
+                      (u.w - v.w) * (u.w - v.w);
+            }
+            cal[atomicAdd(counts, 1ull)] = sqrtf(e2);
         }
     }
+}
+
+// Validation edges whose tile pair is kept.
+__global__ void k_recall(const uint2* __restrict__ val, unsigned long long nval, const uint8_t* __restrict__ keep,
+                         uint32_t tb, unsigned long long* __restrict__ hit) {
+    unsigned long long h = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < nval;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 e = val[i];
+        h += keep[(uint64_t)(e.x / 128) * tb + e.y / 256];
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        tot += __shfl_xor_sync(0xffffffffu, tot, o);
-        hit += __shfl_xor_sync(0xffffffffu, hit, o);
-    }
-    if ((threadIdx.x & 31) == 0 && tot) {
-        atomicAdd(counts, tot);
-        atomicAdd(counts + 1, hit);
-    }
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0 && h) atomicAdd(hit, h);
+}
+
+// Runs of `seg` positions of the embedding order, each re-sorted by log size
+// (so that 128-row blocks have narrow size ranges).
+__global__ void k_seg_keys(const uint32_t* __restrict__ order, const double* __restrict__ ls, uint64_t n, uint32_t seg,
+                           unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t o = order[p];
+    const float l = fmaxf((float)ls[o], 0.f);
+    keys[p] = ((unsigned long long)(p / seg) << 32) | __float_as_uint(l);
+    vals[p] = o;
 }
 
 __global__ void k_sample_rows(uint32_t n, uint32_t m, uint32_t* __restrict__ rows) {
@@ -238,7 +265,7 @@ struct PhaseClock {
 // Embeds the contigs and returns the Morton order (original index per
 // position) in `order`.
 int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const double* d_ls, uint64_t n, float* z,
-                  uint32_t* order) {
+                  uint32_t seg, uint32_t* order) {
     cudaStream_t s = ctx->stream;
     MDET_TRY(mlp_embed(ctx, net->params, d_tnf, n, z));
     // principal axes of the embedding: C = Z^T Z / n - mu mu^T
@@ -291,6 +318,11 @@ int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const 
     void* tmp = ctx_scratch(ctx, "lrn.sorttmp", tb);
     if (!tmp) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, order, (int)n, 0, 64, s));
+    if (seg > 1) {
+        k_seg_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(order, d_ls, n, seg, keys, vals);
+        MDET_LAUNCHED(ctx, "k_seg_keys");
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, order, (int)n, 0, 64, s));
+    }
     return MDET_OK;
 }
 
@@ -301,15 +333,17 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     cudaStream_t s = ctx->stream;
     const mdet_mlp* net = ctx->mlp;
     mdet_learned_report* rep = ctx->learned_report;
-    double target = rep && rep->recall_target > 0 ? rep->recall_target : 0.999;
-    const uint32_t want_rows = rep && rep->recall_rows ? rep->recall_rows : 1024;
+    const double target = rep && rep->recall_target > 0 ? rep->recall_target : 0.999;
+    const uint32_t want_rows = rep && rep->recall_rows ? rep->recall_rows : 2048;
+    const uint32_t seg = rep && rep->segment ? rep->segment : 1024;
     if (rep) {
         rep->recall = 0;
         rep->fell_back = 0;
         rep->tiles_skipped = 0;
+        rep->tau = 0;
     }
-    float tau = INFINITY;
-    MDET_CUDA(ctx, cudaMemcpyAsync(&tau, net->params + MLP_TAU, 4, cudaMemcpyDeviceToHost, s));
+    float tau_net = INFINITY;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&tau_net, net->params + MLP_TAU, 4, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
     const uint32_t ta = (uint32_t)((n + 127) / 128), tb = (uint32_t)((n + 255) / 256);
     const uint64_t full = [&] {
@@ -317,28 +351,29 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
         const uint64_t m = ta >> 1;
         return t - ((ta & 1) ? m * m : (m ? m * (m - 1) : 0));
     }();
-    auto fallback = [&](double recall) -> int {
+    auto fallback = [&](double recall, double tau) -> int {
         if (rep) {
             rep->recall = recall;
             rep->fell_back = 1;
             rep->tiles_skipped = 0;
+            rep->tau = tau;
         }
         return graph_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, MDET_MODE_BF16, st, g, total);
     };
-    if (!(tau < INFINITY) || n < 512) return fallback(0.0);
+    if (n < 2048 || (uint64_t)ta * tb >= (1ull << 31)) return fallback(0.0, 0.0);
 
     PhaseClock tm(s);
     tm.mark();
     float* z = (float*)ctx_scratch(ctx, "lrn.z", n * MLP_OUT * 4);
     uint32_t* order = (uint32_t*)ctx_scratch(ctx, "lrn.order", n * 4);
     if (!z || !order) return MDET_ERR_NOMEM;
-    MDET_TRY(learned_order(ctx, net, d_tnf, d_ls, n, z, order));
+    MDET_TRY(learned_order(ctx, net, d_tnf, d_ls, n, z, seg, order));
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, true, &g, order));
     const double L = logit(cutoff);
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl, false));
 
-    // block statistics and the tile list
+    // block statistics in embedding space
     float* rcent = (float*)ctx_scratch(ctx, "lrn.rcent", (uint64_t)ta * MLP_OUT * 4);
     float* rrad = (float*)ctx_scratch(ctx, "lrn.rrad", (uint64_t)ta * 4);
     float* ccent = (float*)ctx_scratch(ctx, "lrn.ccent", (uint64_t)tb * MLP_OUT * 4);
@@ -347,11 +382,63 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     uint32_t* list = (uint32_t*)ctx_scratch(ctx, "lrn.list", (uint64_t)ta * tb * 4);
     int* nsel = (int*)ctx_scratch(ctx, "lrn.nsel", 8);
     if (!rcent || !rrad || !ccent || !crad || !keep || !list || !nsel) return MDET_ERR_NOMEM;
-    if ((uint64_t)ta * tb >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many tiles for the learned form");
     k_block_stats<<<ta, 256, 0, s>>>(z, g.perm, (uint32_t)n, 128, ta, 0, rcent, rrad);
     MDET_LAUNCHED(ctx, "k_block_stats");
     k_block_stats<<<tb, 256, 0, s>>>(z, g.perm, (uint32_t)n, 256, tb, 1, ccent, crad);
     MDET_LAUNCHED(ctx, "k_block_stats");
+
+    // sampled rows against all columns, scored exactly: calibration and
+    // validation edges
+    const uint32_t m = (uint32_t)std::min<uint64_t>(n, want_rows);
+    uint32_t* rows = (uint32_t*)ctx_scratch(ctx, "lrn.rows", (uint64_t)m * 4);
+    unsigned long long* counts = (unsigned long long*)ctx_scratch(ctx, "lrn.counts", 32);
+    if (!rows || !counts) return MDET_ERR_NOMEM;
+    k_sample_rows<<<(m + 255) / 256, 256, 0, s>>>((uint32_t)n, m, rows);
+    MDET_LAUNCHED(ctx, "k_sample_rows");
+    RowSet rs;
+    MDET_TRY(gather_rows_bf16(ctx, g, rows, m, "lrn.s", &rs));
+    uint2* rc = nullptr;
+    unsigned long long nrc = 0;
+    MDET_TRY(run_filter(ctx, MDET_MODE_BF16, g, true, nullptr, rs.ab, rs.ansq, m, rs.meta, nullptr, tbl, "lrn.rc", &rc,
+                        &nrc));
+    float* cal = (float*)ctx_scratch(ctx, "lrn.cal", (nrc + 1) * 4);
+    float* cal2 = (float*)ctx_scratch(ctx, "lrn.cal2", (nrc + 1) * 4);
+    uint2* val = (uint2*)ctx_scratch(ctx, "lrn.val", (nrc + 1) * sizeof(uint2));
+    if (!cal || !cal2 || !val) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(counts, 0, 32, s));
+    if (nrc) {
+        const uint64_t blocks = std::min<uint64_t>((nrc + 255) / 256, (uint64_t)ctx->num_sms * 8);
+        ff Lff;
+        Lff.hi = (float)L;
+        Lff.lo = (float)(L - (double)Lff.hi);
+        k_sample_edges<<<(unsigned)blocks, 256, 0, s>>>(rc, nrc, rows, g.x32, g.parts, model_h_ff(), Lff,
+                                                         L < kLn9 ? 1 : 0, g.perm, z, cal, val, counts);
+        MDET_LAUNCHED(ctx, "k_sample_edges");
+    }
+    unsigned long long hc[2] = {0, 0};
+    MDET_CUDA(ctx, cudaMemcpyAsync(hc, counts, 16, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    MDET_TRY(check_flag(ctx));
+    // tau: an upper quantile of the calibration edges' embedded distances
+    // (the network's own margin when the sample holds too few edges)
+    float tau = tau_net;
+    const unsigned long long ncal = hc[0], nval = hc[1];
+    if (ncal >= 256) {
+        size_t tmpb = 0;
+        cub::DeviceRadixSort::SortKeys(nullptr, tmpb, cal, cal2, (int)ncal, 0, 32, s);
+        void* tmp = ctx_scratch(ctx, "lrn.caltmp", tmpb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortKeys(tmp, tmpb, cal, cal2, (int)ncal, 0, 32, s));
+        const double q = 1.0 - (1.0 - target) / 4.0;
+        const uint64_t qi = std::min<uint64_t>(ncal - 1, (uint64_t)std::ceil(q * (double)(ncal - 1)));
+        float hq = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&hq, cal2 + qi, 4, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        tau = hq * 1.02f + 1e-4f;
+    }
+    if (!(tau < INFINITY)) return fallback(0.0, 0.0);
+
+    // kept tiles and their list
     k_tile_flags<<<dim3((tb + 255) / 256, (ta + kFlagGroup - 1) / kFlagGroup), 256, 0, s>>>(rcent, rrad, ccent, crad,
                                                                                            ta, tb, tau, keep);
     MDET_LAUNCHED(ctx, "k_tile_flags");
@@ -363,34 +450,18 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
         if (!tmp) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cub::DeviceSelect::Flagged(tmp, tmpb, it, keep, list, nsel, (int)((uint64_t)ta * tb), s));
     }
-    int hsel = 0;
-    MDET_CUDA(ctx, cudaMemcpyAsync(&hsel, nsel, 4, cudaMemcpyDeviceToHost, s));
-
-    // recall on a systematic row sample: all-columns pass, exact scoring
-    const uint32_t m = (uint32_t)std::min<uint64_t>(n, want_rows);
-    uint32_t* rows = (uint32_t*)ctx_scratch(ctx, "lrn.rows", (uint64_t)m * 4);
-    unsigned long long* counts = (unsigned long long*)ctx_scratch(ctx, "lrn.counts", 16);
-    if (!rows || !counts) return MDET_ERR_NOMEM;
-    k_sample_rows<<<(m + 255) / 256, 256, 0, s>>>((uint32_t)n, m, rows);
-    MDET_LAUNCHED(ctx, "k_sample_rows");
-    RowSet rs;
-    MDET_TRY(gather_rows_bf16(ctx, g, rows, m, "lrn.s", &rs));
-    uint2* rc = nullptr;
-    unsigned long long nrc = 0;
-    MDET_TRY(run_filter(ctx, MDET_MODE_BF16, g, true, nullptr, rs.ab, rs.ansq, m, rs.meta, nullptr, tbl, "lrn.rc", &rc,
-                        &nrc));
-    MDET_CUDA(ctx, cudaMemsetAsync(counts, 0, 16, s));
-    if (nrc) {
-        const uint64_t blocks = std::min<uint64_t>((nrc + 255) / 256, (uint64_t)ctx->num_sms * 8);
-        k_recall<<<(unsigned)blocks, 256, 0, s>>>(rc, nrc, rows, g.x32, g.ls, g.parts, model_h(), L, keep, tb, counts);
+    if (nval) {
+        const uint64_t blocks = std::min<uint64_t>((nval + 255) / 256, (uint64_t)ctx->num_sms * 8);
+        k_recall<<<(unsigned)blocks, 256, 0, s>>>(val, nval, keep, tb, counts + 2);
         MDET_LAUNCHED(ctx, "k_recall");
     }
-    unsigned long long hc[2] = {0, 0};
-    MDET_CUDA(ctx, cudaMemcpyAsync(hc, counts, 16, cudaMemcpyDeviceToHost, s));
+    int hsel = 0;
+    unsigned long long hhit = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&hsel, nsel, 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(&hhit, counts + 2, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    MDET_TRY(check_flag(ctx));
-    const double recall = hc[0] ? (double)hc[1] / (double)hc[0] : 1.0;
-    if (recall < target) return fallback(recall);
+    const double recall = nval ? (double)hhit / (double)nval : 1.0;
+    if (recall < target) return fallback(recall, tau);
     tm.mark();
 
     uint2* cand = nullptr;
@@ -420,6 +491,7 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
         rep->recall = recall;
         rep->fell_back = 0;
         rep->tiles_skipped = full - (uint64_t)hsel;
+        rep->tau = tau;
     }
     return MDET_OK;
 }

@@ -39,7 +39,7 @@ __device__ __forceinline__ double poly(const double* c, int deg, double v) {
 
 __global__ void k_gather(const float* __restrict__ tnf, const double* __restrict__ ls, const uint32_t* __restrict__ perm,
                          uint64_t n, uint32_t* __restrict__ inv, float* __restrict__ x32, double* __restrict__ ls_s,
-                         ModelParts* __restrict__ parts, ModelSplit ms) {
+                         PartsFF* __restrict__ parts, ModelSplit ms) {
     uint64_t s = blockIdx.x;
     if (s >= n) return;
     uint32_t o = perm[s];
@@ -50,12 +50,14 @@ __global__ void k_gather(const float* __restrict__ tnf, const double* __restrict
         inv[o] = (uint32_t)s;
         double v = ls[o];
         ls_s[s] = v;
-        ModelParts p;
+        PartsFF p;
         for (int m = 0; m < 4; ++m) {
-            p.f[m] = poly(ms.F[m], 7, v);
+            p.f[m] = ff_from_double(poly(ms.F[m], 7, v));
             double g[7] = {0, ms.G[m][1], ms.G[m][2], ms.G[m][3], ms.G[m][4], ms.G[m][5], ms.G[m][6]};
-            p.g[m] = poly(g, 6, v);
+            p.g[m] = ff_from_double(poly(g, 6, v));
         }
+        p.ls = ff_from_double(v);
+        p.pad[0] = p.pad[1] = 0.f;
         parts[s] = p;
     }
 }
@@ -213,6 +215,18 @@ __global__ void k_dstar_cells(const float* __restrict__ pts, float* __restrict__
     st0[a * MDET_TBL + b] = T;
 }
 
+// Suffix maximum along x (the min-size axis): cell (a, b) then bounds every
+// cell (a', b) with a' >= a, so a box [x0, x1] x [y0, y1] is bounded by row
+// x0 alone.  d* falls as the smaller contig grows, so this costs little.
+__global__ void k_suffix_x(float* __restrict__ st0) {
+    const int b = threadIdx.x;
+    float m = st0[(MDET_TBL - 1) * MDET_TBL + b];
+    for (int a = MDET_TBL - 2; a >= 0; --a) {
+        m = fmaxf(m, st0[a * MDET_TBL + b]);
+        st0[a * MDET_TBL + b] = m;
+    }
+}
+
 __global__ void k_sparse(float* __restrict__ st, int k) {
     int a = blockIdx.x, b = threadIdx.x;
     const float* prev = st + (size_t)(k - 1) * MDET_TBL * MDET_TBL;
@@ -257,6 +271,18 @@ __global__ void k_minmax(const double* __restrict__ ls_s, uint64_t n, int sorted
 
 }  // namespace
 
+ModelHFF model_h_ff() {
+    const ModelH h = model_h();
+    ModelHFF r;
+    for (int m = 0; m < 4; ++m)
+        for (int k = 0; k < 6; ++k) {
+            const float hi = (float)h.h[m][k];
+            r.h[m][k].hi = hi;
+            r.h[m][k].lo = (float)(h.h[m][k] - (double)hi);
+        }
+    return r;
+}
+
 ModelH model_h() {
     ModelH h;
     const ModelSplit& s = model_split();
@@ -278,7 +304,7 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
     g->inv = (uint32_t*)ctx_scratch(ctx, "pre.inv", n * 4);
     g->x32 = (float*)ctx_scratch(ctx, "pre.x32", n * MDET_NTNF * 4);
     g->ls = (double*)ctx_scratch(ctx, "pre.ls", n * 8);
-    g->parts = (ModelParts*)ctx_scratch(ctx, "pre.parts", n * sizeof(ModelParts));
+    g->parts = (PartsFF*)ctx_scratch(ctx, "pre.parts", n * sizeof(PartsFF));
     uint64_t nblk = npad / MDET_BLK;
     g->meta32 = (BlockMeta*)ctx_scratch(ctx, "pre.meta32", nblk * sizeof(BlockMeta));
     g->mu = (float*)ctx_scratch(ctx, "pre.mu", MDET_NTNF * 4);
@@ -361,6 +387,8 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
     MDET_LAUNCHED(ctx, "k_dstar_points");
     k_dstar_cells<<<MDET_TBL, MDET_TBL, 0, s>>>(pts, st);
     MDET_LAUNCHED(ctx, "k_dstar_cells");
+    k_suffix_x<<<1, MDET_TBL, 0, s>>>(st);
+    MDET_LAUNCHED(ctx, "k_suffix_x");
     for (int k = 1; k < MDET_TBL_LEVELS; ++k) {
         k_sparse<<<MDET_TBL, MDET_TBL, 0, s>>>(st, k);
         MDET_LAUNCHED(ctx, "k_sparse");

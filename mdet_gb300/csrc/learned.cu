@@ -188,13 +188,12 @@ __global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __re
 
 // exact label of sorted-position pairs: 1 when pre-probability beats L
 __global__ void k_label_pairs(const uint2* __restrict__ pairs, uint64_t np, const float* __restrict__ x32,
-                              const double* __restrict__ ls, const ModelParts* __restrict__ parts, ModelH H, double L,
-                              float* __restrict__ labels) {
+                              const PartsFF* __restrict__ parts, ModelHFF H, ff L, float* __restrict__ labels) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < np; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 c = pairs[i];
-        const double d = exact_dist(x32 + (uint64_t)c.x * MDET_NTNF, x32 + (uint64_t)c.y * MDET_NTNF);
-        const double pre = pre_prob(parts[c.x], parts[c.y], ls[c.x], ls[c.y], d, H, true);
-        labels[i] = pre > L ? 1.f : 0.f;
+        const ff d = exact_dist(x32 + (uint64_t)c.x * MDET_NTNF, x32 + (uint64_t)c.y * MDET_NTNF);
+        const ff pre = pre_prob(parts[c.x], parts[c.y], d, H, true);
+        labels[i] = ff_gt(pre, L) ? 1.f : 0.f;
     }
 }
 
@@ -366,7 +365,13 @@ int mlp_colsum(mdet_ctx* ctx, const float* z, uint64_t n, float* sum) {
 }
 
 int mlp_project(mdet_ctx* ctx, const float* z, uint64_t n, const float* V, int k, float* P) {
-    return gemm<false, false, false, 0>(ctx, (int)n, k, MLP_OUT, z, MLP_OUT, V, k, P, k, nullptr, nullptr);
+    const uint64_t chunk = 1u << 20;  // keeps the grid's y extent in range
+    for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
+        const int rows = (int)std::min(chunk, n - r0);
+        MDET_TRY((gemm<false, false, false, 0>(ctx, rows, k, MLP_OUT, z + r0 * MLP_OUT, MLP_OUT, V, k, P + r0 * k, k,
+                                               nullptr, nullptr)));
+    }
+    return MDET_OK;
 }
 
 extern "C" {
@@ -444,7 +449,7 @@ int mdet_mlp_grad(mdet_ctx* ctx, const mdet_mlp* m, const float* x, uint64_t row
     cudaStream_t s = ctx->stream;
     for (uint64_t i = 0; i < 2 * np; ++i)
         if (pairs[i] >= rows) return ctx_fail(ctx, MDET_ERR_INVALID, "pair index out of range");
-    float* dx = (float*)ctx_scratch(ctx, "mlpq.x", rows * MLP_IN * 4);
+    float* dx = (float*)ctx_scratch(ctx, "mlpq.in", rows * MLP_IN * 4);
     uint32_t* didx = (uint32_t*)ctx_scratch(ctx, "mlpq.idx", 2 * np * 4);
     float* dl = (float*)ctx_scratch(ctx, "mlpq.lab", np * 4);
     float* g = (float*)ctx_scratch(ctx, "mlpq.g", MLP_NTRAIN * 4);
@@ -501,7 +506,10 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
     k_pair_pool<<<ctx->num_sms * 8, 256, 0, s>>>(tp->seed, pool, (uint32_t)n, cand, ncand, frac, pairs);
     MDET_LAUNCHED(ctx, "k_pair_pool");
     const double L = log((1.0 / (1. - tp->label_cutoff)) - 1.0);
-    k_label_pairs<<<ctx->num_sms * 16, 256, 0, s>>>(pairs, pool, g.x32, g.ls, g.parts, model_h(), L, labels);
+    ff Lff;
+    Lff.hi = (float)L;
+    Lff.lo = (float)(L - (double)Lff.hi);
+    k_label_pairs<<<ctx->num_sms * 16, 256, 0, s>>>(pairs, pool, g.x32, g.parts, model_h_ff(), Lff, labels);
     MDET_LAUNCHED(ctx, "k_label_pairs");
     // hold out the last 1% for calibration
     const uint64_t hold = std::max<uint64_t>(pool / 100, 1);

@@ -2,6 +2,8 @@
 
   python -m mdet_gb300.profile_case count --n 100000     K1 on ~0.85 GB of FASTA
   python -m mdet_gb300.profile_case graph --n 500000     pairwise stage (bf16 or plain)
+  python -m mdet_gb300.profile_case learned --n 500000   network trained on a second
+                                                          assembly, then the learned graph
 
 The graph case frees the FASTA before the pairwise call so that only the
 stage's own buffers (~1-2 GB) are resident when it runs.
@@ -18,7 +20,10 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("stage", choices=["count", "graph"])
+    ap.add_argument("stage", choices=["count", "graph", "learned"])
+    ap.add_argument("--train-n", type=int, default=200000)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--segs", default="1024", help="comma-separated size-sorted run lengths to try")
     ap.add_argument("--n", type=int, default=100000)
     ap.add_argument("--genomes", type=int, default=0)
     ap.add_argument("--mode", default="bf16")
@@ -46,6 +51,39 @@ def main():
         ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), args.n, d_cnt.data_ptr(),
                           d_tnf.data_ptr())
     torch.cuda.synchronize()
+    if args.stage == "learned":
+        import time
+
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        # training assembly: other genomes (another seed)
+        b = synth.generate(4, args.train_n, max(10, args.train_n // 500))
+        tb = torch.zeros(b.data.size + 64, dtype=torch.uint8, device=dev)
+        tb[:b.data.size].copy_(torch.from_numpy(b.data))
+        t_off = torch.from_numpy(b.seq_off.astype(np.int64)).to(dev)
+        t_len = torch.from_numpy(b.seq_len.astype(np.int64)).to(dev)
+        t_cnt = torch.empty((args.train_n, 136), dtype=torch.int32, device=dev)
+        t_tnf = torch.empty((args.train_n, 136), dtype=torch.float32, device=dev)
+        ctx.tnf_count_dev(tb.data_ptr(), b.data.size, t_off.data_ptr(), t_len.data_ptr(), args.train_n,
+                          t_cnt.data_ptr(), t_tnf.data_ptr())
+        t_ls = torch.from_numpy(b.log_sizes).to(dev)
+        torch.cuda.synchronize()
+        del tb, t_cnt
+        net = m.Network(ctx, seed=5)
+        t0 = time.time()
+        rep = net.train_dev(t_tnf.data_ptr(), t_ls.data_ptr(), args.train_n, steps=args.train_steps)
+        print({"train_s": round(time.time() - t0, 2), **rep})
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        runs = [("bf16", 0)] + [("learned", int(x)) for x in args.segs.split(",") for _ in range(2)] + [("bf16", 0)]
+        for mode, seg in runs:
+            lr = ctx.set_learned(net, segment=seg)
+            ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, mode,
+                                       out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+            extra = lr.as_dict() if mode == "learned" else {}
+            print({"mode": mode, "edges": ne, **{k: round(v, 3) if isinstance(v, float) else v
+                                                 for k, v in st.items()}, **extra})
     if args.stage == "graph":
         del d_bytes, d_cnt
         torch.cuda.empty_cache()

@@ -88,15 +88,16 @@ class LearnedReport(ctypes.Structure):
     _fields_ = [
         ("recall_target", D),
         ("recall_rows", u32),
-        ("reserved", u32),
+        ("segment", u32),
         ("recall", D),
         ("fell_back", u32),
-        ("reserved2", u32),
+        ("reserved", u32),
         ("tiles_skipped", u64),
+        ("tau", D),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("reserved")}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 # (name, restype, argtypes) of every entry point in include/mdet_tnf.h
@@ -314,12 +315,14 @@ class Context:
         return ne.value, stats.as_dict()
 
     # ---- learned proposal -----------------------------------------------
-    def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 1024):
+    def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 2048,
+                    segment: int = 0):
         """Network used by mode="learned" graph calls; returns the report that
-        those calls fill (recall estimate, fallback, tiles skipped)."""
+        those calls fill (recall estimate, fallback, tiles skipped, tau)."""
         rep = LearnedReport()
         rep.recall_target = recall_target
         rep.recall_rows = recall_rows
+        rep.segment = segment
         self._learned = (net, rep)  # the context keeps both pointers
         self._check(self.lib.mdet_ctx_set_learned(self.h, net.h if net else None, ctypes.byref(rep)))
         return rep

@@ -142,6 +142,41 @@ int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_si
                        double cutoff, uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to,
                        double* d_stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
 
+/* Exact-stage distance and probability of m given pairs (no counterpart in
+ * the reference as an entry point): the arithmetic of cal_tnf_pre_dist_d
+ * (cuda/Cuda2.cu:192-241) and the sigmoid of get_tnf_graph2 (255) for
+ * d_pairs[2p], d_pairs[2p+1] (contig indices < n), with no cutoff.  Device
+ * buffers; d_dist or d_prob may be null.  For rescoring chosen pairs and for
+ * stating the error against an FP64 evaluation. */
+int mdet_tnf_pair_scores_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                             const uint64_t* d_pairs, uint64_t m, double* d_dist, double* d_prob);
+
+/* ---- many assemblies in one pass -----------------------------------------
+ * Replaces running gen_tnf_graph (cuda/Cuda2.cu:861-970) once per assembly:
+ * every assembly's graph is computed with the same rules as
+ * mdet_tnf_graph_dev (its own cutoff and max_edges, indices local to the
+ * assembly), but the whole batch shares one tile list, one filter launch,
+ * one exact-stage launch and one selection launch.  Device inputs and
+ * outputs; max_edges <= 512; mode PLAIN or BF16.  Returns MDET_ERR_CAPACITY
+ * when some assembly's capacity is short (that assembly's status says so and
+ * its n_edges holds the count needed; the others are written). */
+typedef struct {
+    const float* d_tnf;        /* n x 136 TNF rows */
+    const double* d_log_size;  /* n log10 sizes */
+    uint64_t n;
+    double cutoff;             /* in (0, 1) */
+    uint32_t max_edges;        /* 1 .. 512 */
+    int32_t status;            /* out */
+    uint64_t* d_from;          /* outputs of `capacity` entries, from < to */
+    uint64_t* d_to;
+    double* d_stnf;
+    uint64_t capacity;
+    uint64_t n_edges;          /* out */
+} mdet_assembly;
+
+int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* assemblies, uint32_t count, int mode,
+                           mdet_graph_stats* stats);
+
 /* ---- learned proposal (no counterpart in the reference) ----------------
  * A 136 -> 256 -> 128 -> 64 GELU network (BF16 weights, FP32 accumulation)
  * embeds each TNF row.  In MDET_MODE_LEARNED the graph orders contigs by

@@ -32,6 +32,7 @@ CU_UNITS = [
     "graph",
     "learned",
     "graph_learned",
+    "graph_batch",
 ]
 
 

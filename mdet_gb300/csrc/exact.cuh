@@ -71,7 +71,7 @@ __device__ __forceinline__ ff pre_prob(const PartsFF& pi, const PartsFF& pj, ff 
     const bool imin = ff_le(pi.ls, pj.ls);
     const PartsFF& pmin = imin ? pi : pj;
     const PartsFF& pmax = imin ? pj : pi;
-    const ff t = ff_mul(pi.ls, pj.ls);
+    const ff t = ff_mul(pmin.ls, pmax.ls);  // fixed operand order: the same bits for (i, j) and (j, i)
     ff b = ff_add(ff_add(pmin.f[0], pmax.g[0]), horner_h(H.h[0], t));
     ff c = ff_add(ff_add(pmin.f[1], pmax.g[1]), horner_h(H.h[1], t));
     ff pre = ff_neg(ff_add(b, ff_mul(c, d)));

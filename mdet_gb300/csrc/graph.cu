@@ -111,7 +111,7 @@ double logit(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
-               const uint32_t* tiles, uint64_t nlist) {
+               const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
     cudaStream_t s = ctx->stream;
     std::string cap_key = std::string(tag) + ".cap";
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
@@ -129,12 +129,12 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
         if (mode == MDET_MODE_PLAIN) {
             const float* A = rect ? a32 : g.x32;
             MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect, tbl,
-                                 out));
+                                 out, tiles, nlist, row_tbl, tbl_stride));
         } else {
             const uint16_t* A = rect ? ab : g.xa;
             const float* An = rect ? ansq : g.nsq;
             MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
-                               out, tiles, nlist));
+                               out, tiles, nlist, row_tbl, tbl_stride));
         }
         unsigned long long found = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
@@ -401,6 +401,21 @@ int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int mdet_tnf_pair_scores_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
+                             const uint64_t* d_pairs, uint64_t m, double* d_dist, double* d_prob) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    if (m == 0) return MDET_OK;
+    if (!d_tnf || !d_log_size || !d_pairs || (!d_dist && !d_prob)) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    if (n < 1 || n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "bad contig count");
+    GraphPrep g;
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, false, &g));
+    MDET_TRY(pair_scores(ctx, g, d_pairs, m, d_dist, d_prob));
+    MDET_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return check_flag(ctx);
 }
 
 int mdet_tnf_max_prob_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,

@@ -97,9 +97,18 @@ struct GraphPrep {
 // index per position, device) when given.
 int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out,
                 const uint32_t* order = nullptr);
+// Arrays of a prepared set of `rows` positions (a multiple of 256) in
+// scratch named after tag; prep_into fills positions [base, base + npad) of
+// them with one contig set (perm/inv values are base + local indices).
+int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, GraphPrep* g);
+int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, const GraphPrep& g,
+              uint64_t base, const uint32_t* order = nullptr);
 // sorted: d_ls_sorted is ascending (else its range is found by a scan).
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
                       bool sorted = true);
+// A table over a given log-size range written to st (MDET_TBL_LEVELS x TBL x TBL floats).
+int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out);
+#define MDET_TBL_FLOATS ((uint64_t)MDET_TBL_LEVELS * MDET_TBL * MDET_TBL)
 ModelH model_h();
 ModelHFF model_h_ff();
 
@@ -116,8 +125,13 @@ struct Ent {
     uint32_t pad;
 };
 
+// tiles/nlist: optional list of 128 x 128 tiles (I * tiles_b + J); row_tbl:
+// optional d* table index per row tile (tables tbl_stride floats apart from
+// tbl.st).
 int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ameta, const float* b, uint32_t nb,
-                const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out);
+                const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out,
+                const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
+                uint64_t tbl_stride = 0);
 // Tensor-core filter over centred BF16 rows: a (A role, na rows) against b
 // (B role, nb rows), both padded to 256 rows; a_nsq = ||a~||^2 (+inf on
 // padding rows).
@@ -125,23 +139,39 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
 // to evaluate (column tiles of 256); null evaluates the whole schedule.
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
-              CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0);
+              CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
+              uint64_t tbl_stride = 0);
+// Cutoff of one 256-row block of a batch: logit(cutoff) in float-float and
+// whether the second model is needed (logit(cutoff) < ln 9, decided in FP64).
+struct BlkCut {
+    ff L;
+    uint32_t model2;
+    uint32_t pad;
+};
+// blk_L: optional per-256-row-block cutoff overriding L.
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
-                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out);
+                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out,
+                const BlkCut* blk_L = nullptr);
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
                   const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out);
+// Exact-stage distance and probability of given pairs (original indices).
+int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64_t m, double* dist, double* prob);
+// blk_K: optional per-256-row-block max_edges (each <= max_edges <= 512).
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
-                uint32_t max_edges, uint64_t* n_out);
+                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K = nullptr);
 int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
               double* d_stnf, uint64_t total);
 
-// Orchestration shared by the graph entry points (graph.cu, graph_learned.cu).
+// Orchestration shared by the graph entry points (graph.cu, graph_learned.cu,
+// graph_batch.cu).
 double logit(double cutoff);
 int check_flag(mdet_ctx* ctx);
+int check_mode(mdet_ctx* ctx, int mode);
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
-               const uint32_t* tiles = nullptr, uint64_t nlist = 0);
+               const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
+               uint64_t tbl_stride = 0);
 int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
                int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total);
 int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,

@@ -26,6 +26,7 @@ struct ExactArgs {
     ModelHFF H;
     double L;
     ff Lff;
+    const BlkCut* blk_L;  // optional per-256-row-block cutoff
     // graph outputs
     Edge* edges;
     unsigned long long* nedges;
@@ -105,8 +106,15 @@ __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
         bool edge = false;
         double sim = 0;
         if (base + lane < p.ncand) {
-            const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, model2);
-            if (ff_gt(pre, p.Lff)) {
+            ff Lc = p.Lff;
+            bool m2 = model2;
+            if (p.blk_L) {
+                const BlkCut bc = p.blk_L[si >> 8];
+                Lc = bc.L;
+                m2 = bc.model2 != 0;
+            }
+            const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, m2);
+            if (ff_gt(pre, Lc)) {
                 edge = true;
                 sim = sim_of(pre);
             }
@@ -142,6 +150,19 @@ __global__ void __launch_bounds__(256) k_exact_maxprob(ExactArgs p) {
             const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, true);
             atomicMax(&p.maxkey[p.cand[idx].x], dkey(ff_to_double(pre)));
         }
+    }
+}
+
+// Distance and probability of given pairs (original indices, mapped through inv).
+__global__ void k_pair_scores(const uint64_t* __restrict__ pairs, uint64_t m, const uint32_t* __restrict__ inv,
+                              const float* __restrict__ x32, const PartsFF* __restrict__ parts, ModelHFF H,
+                              double* __restrict__ dist, double* __restrict__ prob) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < m; q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = inv[pairs[2 * q]], j = inv[pairs[2 * q + 1]];
+        const ff d = exact_dist(x32 + (uint64_t)i * MDET_NTNF, x32 + (uint64_t)j * MDET_NTNF);
+        const ff pre = pre_prob(parts[i], parts[j], d, H, true);
+        if (dist) dist[q] = ff_to_double(d);
+        if (prob) prob[q] = sim_of(pre);
     }
 }
 
@@ -401,8 +422,8 @@ template <int EMAX>
 __global__ void __launch_bounds__(kSelWarps * 32) k_topk_sel(const unsigned long long* __restrict__ rowptr,
                                                              const uint32_t* __restrict__ deg,
                                                              const uint32_t* __restrict__ perm, uint32_t n,
-                                                             uint32_t max_edges, Ent* __restrict__ list,
-                                                             uint32_t* __restrict__ out_cnt) {
+                                                             uint32_t max_edges_all, const uint32_t* __restrict__ blk_K,
+                                                             Ent* __restrict__ list, uint32_t* __restrict__ out_cnt) {
     __shared__ unsigned long long s_key[kSelWarps][kSelCap];
     __shared__ uint32_t s_col[kSelWarps][kSelCap];
     __shared__ uint32_t s_hist[kSelWarps][256];
@@ -412,6 +433,7 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_topk_sel(const unsigned long
     uint32_t* hist = s_hist[w];
     for (uint32_t sp = blockIdx.x * kSelWarps + w; sp < n; sp += gridDim.x * kSelWarps) {
         const uint32_t cnt = deg[sp], orow = perm[sp];
+        const uint32_t max_edges = blk_K ? blk_K[sp >> 8] : max_edges_all;
         Ent* row = list + rowptr[sp];
         const bool staged = cnt <= kSelCap;
         if (staged)
@@ -585,7 +607,7 @@ __global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long
 // ------------------------------------------------------------ host side --
 
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
-                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out) {
+                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out, const BlkCut* blk_L) {
     cudaStream_t s = ctx->stream;
     Edge* edges = (Edge*)ctx_scratch(ctx, "ex.edges", (ncand ? ncand : 1) * sizeof(Edge));
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "ex.cnt", 8);
@@ -604,6 +626,7 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.L = L;
         p.Lff.hi = (float)L;
         p.Lff.lo = (float)(L - (double)p.Lff.hi);
+        p.blk_L = blk_L;
         p.edges = edges;
         p.nedges = cnt;
         p.deg = deg;
@@ -651,8 +674,16 @@ int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned
     return MDET_OK;
 }
 
+int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64_t m, double* dist, double* prob) {
+    if (m == 0) return MDET_OK;
+    const uint64_t blocks = std::min<uint64_t>((m + 255) / 256, (uint64_t)ctx->num_sms * 16);
+    k_pair_scores<<<(unsigned)blocks, 256, 0, ctx->stream>>>(pairs, m, g.inv, g.x32, g.parts, model_h_ff(), dist, prob);
+    MDET_LAUNCHED(ctx, "k_pair_scores");
+    return MDET_OK;
+}
+
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
-                uint32_t max_edges, uint64_t* n_out) {
+                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = g.n;
     unsigned long long* rowptr = (unsigned long long*)ctx_scratch(ctx, "tk.rowptr", ((uint64_t)n + 1) * 8);
@@ -690,12 +721,13 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
             (unsigned)std::min<uint64_t>(((uint64_t)n + kSelWarps - 1) / kSelWarps, (uint64_t)ctx->num_sms * 32);
         ctx_timer_begin(ctx, "k_topk_sel");
         if (max_edges <= 256)
-            k_topk_sel<8><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+            k_topk_sel<8><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, blk_K, list, out_cnt);
         else
-            k_topk_sel<16><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, list, out_cnt);
+            k_topk_sel<16><<<blocks, kSelWarps * 32, 0, s>>>(rowptr, deg, g.perm, n, max_edges, blk_K, list, out_cnt);
         ctx_timer_end(ctx, "k_topk_sel");
         MDET_LAUNCHED(ctx, "k_topk_sel");
     } else {
+        if (blk_K) return ctx_fail(ctx, MDET_ERR_INVALID, "per-row max_edges needs max_edges <= 512");
         size_t dyn = (size_t)kTopkWarps * kWarpCap * sizeof(Ent);
         static bool set[64] = {false};
         if (!set[ctx->device & 63]) {

@@ -24,9 +24,18 @@ struct SimtArgs {
     DstarTable tbl;
     CandBuf out;
     unsigned long long ntiles;
+    const uint32_t* tiles;   // optional list (I * tb + J); null: the full schedule
+    const uint8_t* row_tbl;  // optional table index per row tile (tables tbl_stride floats apart)
+    uint64_t tbl_stride;
 };
 
 __device__ __forceinline__ void tile_of(const SimtArgs& p, unsigned long long t, uint32_t& I, uint32_t& J) {
+    if (p.tiles) {
+        const uint32_t v = p.tiles[t];
+        I = v / p.tb;
+        J = v % p.tb;
+        return;
+    }
     if (!p.triangular) {
         I = (uint32_t)(t / p.tb);
         J = (uint32_t)(t % p.tb);
@@ -56,7 +65,9 @@ __global__ void __launch_bounds__(TH, 2) k_filter_simt(SimtArgs p) {
         const uint32_t i0 = I * BM, j0 = J * BN;
         // tile threshold
         BlockMeta ma = p.ameta[I], mb = p.bmeta[J];
-        float T = tile_dstar(p.tbl, ma.lo, ma.hi, mb.lo, mb.hi);
+        DstarTable tb = p.tbl;
+        if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[I] * p.tbl_stride;
+        float T = tile_dstar(tb, ma.lo, ma.hi, mb.lo, mb.hi);
         float R = T * (1.f + 2e-5f) + 1e-6f;
         float R2 = R * R;
         if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
@@ -141,7 +152,8 @@ __global__ void __launch_bounds__(TH, 2) k_filter_simt(SimtArgs p) {
 }  // namespace
 
 int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ameta, const float* b, uint32_t nb,
-                const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out) {
+                const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out, const uint32_t* tiles,
+                uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
     SimtArgs p;
     p.a = a;
     p.b = b;
@@ -155,6 +167,10 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
     p.tbl = tbl;
     p.out = out;
     p.ntiles = triangular ? (unsigned long long)p.ta * (p.ta + 1) / 2 : (unsigned long long)p.ta * p.tb;
+    p.tiles = tiles;
+    p.row_tbl = row_tbl;
+    p.tbl_stride = tbl_stride;
+    if (tiles) p.ntiles = nlist;
     if (p.ntiles == 0) return MDET_OK;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_filter_simt, TH, 0);

@@ -43,6 +43,8 @@ struct TcArgs {
     uint32_t na, nb, ta, tb, segs;
     const uint32_t* tiles;  // optional list of tiles (I * tb + J, row-major); null: full schedule
     uint64_t nlist;
+    const uint8_t* row_tbl;  // optional table index per row tile (tables tbl_stride floats apart)
+    uint64_t tbl_stride;
     int triangular;
     const float* a_nsq;
     const BlockMeta* ameta;
@@ -343,7 +345,9 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const BlockMeta ma = p.ameta[c.I];
                 const BlockMeta mb0 = p.bmeta[2 * c.J], mb1 = p.bmeta[2 * c.J + 1];
                 const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
-                const float T = tile_dstar(p.tbl, ma.lo, ma.hi, blo, bhi);
+                DstarTable tb = p.tbl;
+                if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I] * p.tbl_stride;
+                const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
                 const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
                 const float N2 = ma.nmax * fmaxf(mb0.nmax, mb1.nmax);
                 // TMEM holds a~.b~ - ||b~||^2/2 (the column term rides in K
@@ -475,7 +479,7 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
 
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
-              CandBuf out, const uint32_t* tiles, uint64_t nlist) {
+              CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
     if (na == 0 || nb == 0) return MDET_OK;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
@@ -512,6 +516,8 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     while ((uint64_t)p.ta * p.segs < 2ull * ctx->num_sms && p.segs < p.tb) ++p.segs;
     p.tiles = tiles;
     p.nlist = nlist;
+    p.row_tbl = row_tbl;
+    p.tbl_stride = tbl_stride;
     unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)ctx->num_sms,
                                                            tiles ? nlist : (unsigned long long)p.ta * p.segs);
     if (grid == 0) return MDET_OK;

@@ -11,6 +11,8 @@
 // and the d* table.
 #include <cub/cub.cuh>
 
+#include <string>
+
 #include <cmath>
 #include <cstring>
 
@@ -37,17 +39,31 @@ __device__ __forceinline__ double poly(const double* c, int deg, double v) {
     return r;
 }
 
-__global__ void k_gather(const float* __restrict__ tnf, const double* __restrict__ ls, const uint32_t* __restrict__ perm,
-                         uint64_t n, uint32_t* __restrict__ inv, float* __restrict__ x32, double* __restrict__ ls_s,
-                         PartsFF* __restrict__ parts, ModelSplit ms) {
+// Block per position s of [0, npad) of one contig set placed at row `base`
+// of the prepared arrays (all pointers here already offset by base): perm
+// arrives with local original indices and leaves with base + local; inv is
+// the full array.  Padding positions map to themselves.
+__global__ void k_gather(const float* __restrict__ tnf, const double* __restrict__ ls, uint32_t* __restrict__ perm,
+                         uint64_t n, uint64_t npad, uint32_t base, uint32_t* __restrict__ inv,
+                         float* __restrict__ x32, double* __restrict__ ls_s, PartsFF* __restrict__ parts,
+                         ModelSplit ms) {
     uint64_t s = blockIdx.x;
-    if (s >= n) return;
-    uint32_t o = perm[s];
+    if (s >= npad) return;
+    if (s >= n) {
+        if (threadIdx.x == 0) {
+            perm[s] = base + (uint32_t)s;
+            inv[base + s] = base + (uint32_t)s;
+        }
+        return;
+    }
+    const uint32_t o = perm[s];
+    __syncthreads();  // every thread has read perm[s] before it is rewritten
     const float* src = tnf + (uint64_t)o * MDET_NTNF;
     float* dst = x32 + s * MDET_NTNF;
     for (int k = threadIdx.x; k < MDET_NTNF; k += blockDim.x) dst[k] = src[k];
     if (threadIdx.x == 0) {
-        inv[o] = (uint32_t)s;
+        perm[s] = base + o;
+        inv[base + o] = base + (uint32_t)s;
         double v = ls[o];
         ls_s[s] = v;
         PartsFF p;
@@ -291,66 +307,111 @@ ModelH model_h() {
     return h;
 }
 
-int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g,
-                const uint32_t* order) {
+int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, GraphPrep* g) {
+    const std::string t(tag);
+    const uint64_t nblk = rows / MDET_BLK;
+    g->perm = (uint32_t*)ctx_scratch(ctx, (t + ".perm").c_str(), rows * 4);
+    g->inv = (uint32_t*)ctx_scratch(ctx, (t + ".inv").c_str(), rows * 4);
+    g->x32 = (float*)ctx_scratch(ctx, (t + ".x32").c_str(), rows * MDET_NTNF * 4);
+    g->ls = (double*)ctx_scratch(ctx, (t + ".ls").c_str(), rows * 8);
+    g->parts = (PartsFF*)ctx_scratch(ctx, (t + ".parts").c_str(), rows * sizeof(PartsFF));
+    g->meta32 = (BlockMeta*)ctx_scratch(ctx, (t + ".meta32").c_str(), nblk * sizeof(BlockMeta));
+    g->mu = (float*)ctx_scratch(ctx, (t + ".mu").c_str(), MDET_NTNF * 4);
+    g->xa = g->xb = nullptr;
+    g->nsq = nullptr;
+    g->meta = nullptr;
+    if (need_bf16) {
+        g->xa = (uint16_t*)ctx_scratch(ctx, (t + ".xa").c_str(), rows * MDET_KPAD * 2);
+        g->xb = (uint16_t*)ctx_scratch(ctx, (t + ".xb").c_str(), rows * MDET_KPAD * 2);
+        g->nsq = (float*)ctx_scratch(ctx, (t + ".nsq").c_str(), rows * 4);
+        g->meta = (BlockMeta*)ctx_scratch(ctx, (t + ".meta").c_str(), nblk * sizeof(BlockMeta));
+        if (!g->xa || !g->xb || !g->nsq || !g->meta) return MDET_ERR_NOMEM;
+    }
+    if (!g->perm || !g->inv || !g->x32 || !g->ls || !g->parts || !g->meta32 || !g->mu) return MDET_ERR_NOMEM;
+    return MDET_OK;
+}
+
+int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, const GraphPrep& g,
+              uint64_t base, const uint32_t* order) {
     cudaStream_t s = ctx->stream;
-    g->n = (uint32_t)n;
-    g->npad = (uint32_t)((n + 255) / 256 * 256);
-    const uint64_t npad = g->npad;
+    const uint64_t npad = (n + 255) / 256 * 256;
+    const uint64_t nblk = npad / MDET_BLK;
     unsigned long long* keys = (unsigned long long*)ctx_scratch(ctx, "pre.keys", n * 8);
     unsigned long long* keys2 = (unsigned long long*)ctx_scratch(ctx, "pre.keys2", n * 8);
     uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "pre.vals", n * 4);
-    g->perm = (uint32_t*)ctx_scratch(ctx, "pre.perm", n * 4);
-    g->inv = (uint32_t*)ctx_scratch(ctx, "pre.inv", n * 4);
-    g->x32 = (float*)ctx_scratch(ctx, "pre.x32", n * MDET_NTNF * 4);
-    g->ls = (double*)ctx_scratch(ctx, "pre.ls", n * 8);
-    g->parts = (PartsFF*)ctx_scratch(ctx, "pre.parts", n * sizeof(PartsFF));
-    uint64_t nblk = npad / MDET_BLK;
-    g->meta32 = (BlockMeta*)ctx_scratch(ctx, "pre.meta32", nblk * sizeof(BlockMeta));
-    g->mu = (float*)ctx_scratch(ctx, "pre.mu", MDET_NTNF * 4);
     double* sums = (double*)ctx_scratch(ctx, "pre.sums", MDET_NTNF * 8);
-    if (!keys || !keys2 || !vals || !g->perm || !g->inv || !g->x32 || !g->ls || !g->parts || !g->meta32 || !g->mu ||
-        !sums)
-        return MDET_ERR_NOMEM;
-    unsigned blocks = (unsigned)((n + 255) / 256);
+    if (!keys || !keys2 || !vals || !sums) return MDET_ERR_NOMEM;
+    uint32_t* perm = g.perm + base;
+    float* x32 = g.x32 + base * MDET_NTNF;
+    double* ls = g.ls + base;
+    PartsFF* parts = g.parts + base;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
     if (order) {
         // caller's order (original index per position)
-        MDET_CUDA(ctx, cudaMemcpyAsync(g->perm, order, n * 4, cudaMemcpyDeviceToDevice, s));
+        MDET_CUDA(ctx, cudaMemcpyAsync(perm, order, n * 4, cudaMemcpyDeviceToDevice, s));
     } else {
         k_keys<<<blocks, 256, 0, s>>>(d_ls, n, keys, vals);
         MDET_LAUNCHED(ctx, "k_keys");
         size_t tmpb = 0;
-        cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s);
+        cub::DeviceRadixSort::SortPairs(nullptr, tmpb, keys, keys2, vals, perm, (int)n, 0, 64, s);
         void* tmp = ctx_scratch(ctx, "pre.cubtmp", tmpb);
         if (!tmp) return MDET_ERR_NOMEM;
-        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, g->perm, (int)n, 0, 64, s));
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, perm, (int)n, 0, 64, s));
     }
-    k_gather<<<(unsigned)n, 64, 0, s>>>(d_tnf, d_ls, g->perm, n, g->inv, g->x32, g->ls, g->parts, model_split());
+    k_gather<<<(unsigned)npad, 64, 0, s>>>(d_tnf, d_ls, perm, n, npad, (uint32_t)base, g.inv, x32, ls, parts,
+                                          model_split());
     MDET_LAUNCHED(ctx, "k_gather");
-    g->xa = nullptr;
-    g->xb = nullptr;
-    g->nsq = nullptr;
-    g->meta = nullptr;
     float* err = nullptr;
     float* nrm = nullptr;
     if (need_bf16) {
-        MDET_CUDA(ctx, cudaMemsetAsync(sums, 0, MDET_NTNF * 8, s));
-        k_colsum<<<std::min<uint64_t>(1024, n), MDET_NTNF, 0, s>>>(g->x32, n, sums);
-        MDET_LAUNCHED(ctx, "k_colsum");
-        k_mean<<<1, MDET_NTNF, 0, s>>>(sums, n, g->mu);
-        MDET_LAUNCHED(ctx, "k_mean");
-        g->xa = (uint16_t*)ctx_scratch(ctx, "pre.xa", npad * MDET_KPAD * 2);
-        g->xb = (uint16_t*)ctx_scratch(ctx, "pre.xb", npad * MDET_KPAD * 2);
-        g->nsq = (float*)ctx_scratch(ctx, "pre.nsq", npad * 4);
         err = (float*)ctx_scratch(ctx, "pre.err", npad * 4);
         nrm = (float*)ctx_scratch(ctx, "pre.nrm", npad * 4);
-        g->meta = (BlockMeta*)ctx_scratch(ctx, "pre.meta", nblk * sizeof(BlockMeta));
-        if (!g->xa || !g->xb || !g->nsq || !err || !nrm || !g->meta) return MDET_ERR_NOMEM;
-        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(g->x32, g->mu, n, npad, g->xa, g->xb, g->nsq, err, nrm);
+        if (!err || !nrm) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cudaMemsetAsync(sums, 0, MDET_NTNF * 8, s));
+        k_colsum<<<std::min<uint64_t>(1024, n), MDET_NTNF, 0, s>>>(x32, n, sums);
+        MDET_LAUNCHED(ctx, "k_colsum");
+        k_mean<<<1, MDET_NTNF, 0, s>>>(sums, n, g.mu);
+        MDET_LAUNCHED(ctx, "k_mean");
+        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(x32, g.mu, n, npad, g.xa + base * MDET_KPAD,
+                                                         g.xb + base * MDET_KPAD, g.nsq + base, err, nrm);
         MDET_LAUNCHED(ctx, "k_bf16");
     }
-    k_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(g->ls, err, nrm, n, nblk, g->meta, g->meta32);
+    k_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(ls, err, nrm, n, nblk,
+                                                         need_bf16 ? g.meta + base / MDET_BLK : nullptr,
+                                                         g.meta32 + base / MDET_BLK);
     MDET_LAUNCHED(ctx, "k_meta");
+    return MDET_OK;
+}
+
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g,
+                const uint32_t* order) {
+    g->n = (uint32_t)n;
+    g->npad = (uint32_t)((n + 255) / 256 * 256);
+    MDET_TRY(prep_alloc(ctx, "pre", g->npad, need_bf16, g));
+    return prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, order);
+}
+
+int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out) {
+    cudaStream_t s = ctx->stream;
+    float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
+    if (!pts) return MDET_ERR_NOMEM;
+    double h = (lmax - lmin) / MDET_TBL;
+    if (!(h > 1e-7)) h = 1e-7;
+    lmin -= 1e-9;
+    dim3 grid((kPts + 127) / 128, kPts);
+    k_dstar_points<<<grid, 128, 0, s>>>(lmin, h, logit_cut, model_split(), pts);
+    MDET_LAUNCHED(ctx, "k_dstar_points");
+    k_dstar_cells<<<MDET_TBL, MDET_TBL, 0, s>>>(pts, st);
+    MDET_LAUNCHED(ctx, "k_dstar_cells");
+    k_suffix_x<<<1, MDET_TBL, 0, s>>>(st);
+    MDET_LAUNCHED(ctx, "k_suffix_x");
+    for (int k = 1; k < MDET_TBL_LEVELS; ++k) {
+        k_sparse<<<MDET_TBL, MDET_TBL, 0, s>>>(st, k);
+        MDET_LAUNCHED(ctx, "k_sparse");
+    }
+    out->st = st;
+    out->lmin = (float)lmin;
+    out->inv_h = (float)(1.0 / h);
     return MDET_OK;
 }
 

@@ -51,6 +51,22 @@ class GraphStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class Assembly(ctypes.Structure):
+    _fields_ = [
+        ("d_tnf", P),
+        ("d_log_size", P),
+        ("n", u64),
+        ("cutoff", D),
+        ("max_edges", u32),
+        ("status", ctypes.c_int32),
+        ("d_from", P),
+        ("d_to", P),
+        ("d_stnf", P),
+        ("capacity", u64),
+        ("n_edges", u64),
+    ]
+
+
 class TrainParams(ctypes.Structure):
     _fields_ = [
         ("pairs", u64),
@@ -121,6 +137,9 @@ SIGNATURES = [
      [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
     ("mdet_tnf_graph_dev", ctypes.c_int,
      [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
+    ("mdet_tnf_pair_scores_dev", ctypes.c_int, [P, P, P, u64, P, u64, P, P]),
+    ("mdet_tnf_graph_batched", ctypes.c_int, [P, ctypes.POINTER(Assembly), u32, ctypes.c_int,
+                                              ctypes.POINTER(GraphStats)]),
     ("mdet_mlp_create", ctypes.c_int, [P, u64, ctypes.POINTER(P)]),
     ("mdet_mlp_destroy", ctypes.c_int, [P]),
     ("mdet_mlp_param_count", u64, []),
@@ -313,6 +332,29 @@ class Context:
                                                 MODES[mode], P(d_from), P(d_to), P(d_stnf), capacity,
                                                 ctypes.byref(ne), ctypes.byref(stats)))
         return ne.value, stats.as_dict()
+
+    def pair_scores_dev(self, d_tnf, d_ls, n, d_pairs, m, d_dist, d_prob):
+        self._check(self.lib.mdet_tnf_pair_scores_dev(self.h, P(d_tnf), P(d_ls), n, P(d_pairs), m, P(d_dist),
+                                                      P(d_prob)))
+
+    def tnf_graph_batched(self, assemblies, mode="bf16"):
+        """Graphs of many assemblies in one pass (device buffers).  Each item:
+        dict(d_tnf, d_ls, n, cutoff, max_edges, d_from, d_to, d_stnf,
+        capacity).  Returns ([(status, n_edges)], stats); capacity shortfalls
+        are reported per assembly, not raised."""
+        arr = (Assembly * len(assemblies))()
+        for a, d in zip(arr, assemblies):
+            a.d_tnf, a.d_log_size, a.n = P(d["d_tnf"]), P(d["d_ls"]), d["n"]
+            a.cutoff, a.max_edges = float(d["cutoff"]), int(d["max_edges"])
+            a.d_from, a.d_to, a.d_stnf = P(d["d_from"]), P(d["d_to"]), P(d["d_stnf"])
+            a.capacity = int(d["capacity"])
+        stats = GraphStats()
+        rc = self.lib.mdet_tnf_graph_batched(self.h, arr, len(assemblies), MODES[mode], ctypes.byref(stats))
+        if rc not in (OK, ERR_CAPACITY):
+            self._check(rc)
+        return [(a.status, a.n_edges) for a in arr], stats.as_dict()
+
+    gen_tnf_graph_batched = tnf_graph_batched
 
     # ---- learned proposal -----------------------------------------------
     def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 2048,

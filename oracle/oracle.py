@@ -44,6 +44,7 @@ def lib():
         L.orc_tnf_distance.argtypes = [P, P]
         L.orc_pre_prob_from_d.restype = D
         L.orc_pre_prob_from_d.argtypes = [D, D, D]
+        L.orc_pair_scores.argtypes = [P, P, P, u64, P, P, ctypes.c_int]
         L.orc_logit_cutoff.restype = D
         L.orc_logit_cutoff.argtypes = [D]
         L.orc_tnf_graph.restype = u64
@@ -96,6 +97,18 @@ def pre_prob(r1, r2, a, b):
     a = np.ascontiguousarray(a, np.float32)
     b = np.ascontiguousarray(b, np.float32)
     return lib().orc_pre_prob(r1, r2, _p(a), _p(b))
+
+
+def pair_scores(tnf, ls, pairs, threads=0):
+    """(distance, probability) of index pairs (m x 2) in FP64."""
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    pr = np.ascontiguousarray(pairs, np.uint64)
+    m = pr.shape[0]
+    d = np.zeros(m, np.float64)
+    p = np.zeros(m, np.float64)
+    lib().orc_pair_scores(_p(tnf), _p(ls), _p(pr), m, _p(d), _p(p), threads)
+    return d, p
 
 
 def graph(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):

@@ -315,6 +315,22 @@ double orc_tnf_dist_cpu(double r1, double r2, const float* a, const float* bb) {
 
 double orc_logit_cutoff(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
 
+/* Distance and probability of given pairs (pairs[2p], pairs[2p+1]):
+ * cuda/Cuda2.cu:192-241 for the pre-probability, sigmoid as at 255. */
+void orc_pair_scores(const float* tnf, const double* logsize, const uint64_t* pairs, uint64_t m, double* dist,
+                     double* prob, int threads) {
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t p = 0; p < (int64_t)m; ++p) {
+        const uint64_t i = pairs[2 * p], j = pairs[2 * p + 1];
+        const double d = orc_tnf_distance(tnf + i * 136, tnf + j * 136);
+        const double pre = orc_pre_prob_from_d(logsize[i], logsize[j], d);
+        dist[p] = d;
+        prob[p] = 1. - 1. / (1. + exp(pre));
+    }
+}
+
 uint64_t orc_tnf_graph(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
                        uint64_t row0, uint64_t row1, uint64_t* from, uint64_t* to, double* stnf, uint64_t cap,
                        int threads) {

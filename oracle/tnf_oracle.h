@@ -56,6 +56,10 @@ double orc_tnf_dist_cpu(double r1, double r2, const float* a, const float* b);
 /* logit(cutoff) as gen_tnf_graph computes it (cuda/Cuda2.cu:884). */
 double orc_logit_cutoff(double cutoff);
 
+/* Distance and probability of m given pairs (index pairs, 2m entries). */
+void orc_pair_scores(const float* tnf, const double* logsize, const uint64_t* pairs, uint64_t m, double* dist,
+                     double* prob, int threads);
+
 /* gen_tnf_graph for rows [row0,row1) against all n columns
  * (cuda/Cuda2.cu:861-946, kernel get_tnf_graph2 243-262).  Per row a
  * std::priority_queue min-heap of size max_edges with the reference's strict

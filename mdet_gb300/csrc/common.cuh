@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <unordered_map>
 #include <utility>
@@ -51,6 +52,11 @@ struct mdet_ctx {
     std::unordered_map<std::string, KernelTimer> timers;
     const struct mdet_mlp* mlp = nullptr;          // network of MDET_MODE_LEARNED
     mdet_learned_report* learned_report = nullptr;  // optional caller-owned report
+    // tile-shape autotuner of the tensor-core filter: chosen column-tile
+    // width per shape class, whether to tune, and the width of the last launch
+    std::map<uint64_t, int> tc_shape;
+    bool autotune = true;
+    int last_tile_n = 0;
 };
 
 // Event pair around one launch of a named kernel when timing is enabled.

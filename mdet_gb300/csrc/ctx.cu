@@ -307,6 +307,12 @@ int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream) {
     return MDET_OK;
 }
 
+int mdet_ctx_set_autotune(mdet_ctx* ctx, int enable) {
+    if (!ctx) return MDET_ERR_INVALID;
+    ctx->autotune = enable != 0;
+    return MDET_OK;
+}
+
 int mdet_ctx_set_timing(mdet_ctx* ctx, int enable) {
     if (!ctx) return MDET_ERR_INVALID;
     cudaSetDevice(ctx->device);

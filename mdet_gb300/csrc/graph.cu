@@ -108,12 +108,45 @@ __global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, 
 
 double logit(double cutoff) { return log((1.0 / (1. - cutoff)) - 1.0); }
 
+uint64_t tc_shape_key(bool rect, bool list, uint64_t na, uint64_t nb) {
+    auto lg = [](uint64_t v) {
+        uint64_t b = 0;
+        while (v > 1) {
+            v >>= 1;
+            ++b;
+        }
+        return b;
+    };
+    return (rect ? 1ull : 0ull) | (list ? 2ull : 0ull) | (lg(na) << 2) | (lg(nb) << 10);
+}
+
+int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run) {
+    auto it = ctx->tc_shape.find(key);
+    if (it != ctx->tc_shape.end()) return run(it->second);
+    if (!ctx->autotune) return run(256);
+    cudaEvent_t ev[3];
+    for (auto& e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], ctx->stream);
+    int rc = run(256);
+    cudaEventRecord(ev[1], ctx->stream);
+    if (rc == MDET_OK) rc = run(128);
+    cudaEventRecord(ev[2], ctx->stream);
+    float t256 = 0, t128 = 0;
+    if (rc == MDET_OK) {
+        cudaEventSynchronize(ev[2]);
+        cudaEventElapsedTime(&t256, ev[0], ev[1]);
+        cudaEventElapsedTime(&t128, ev[1], ev[2]);
+        ctx->tc_shape[key] = t128 < t256 ? 128 : 256;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
-               const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
+               const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride, int bn) {
     cudaStream_t s = ctx->stream;
-    std::string cap_key = std::string(tag) + ".cap";
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
     if (!cnt) return MDET_ERR_NOMEM;
     // remembered capacity (bytes of the candidate buffer) from earlier calls
@@ -124,18 +157,27 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
         uint2* cand = (uint2*)ctx_scratch(ctx, (std::string(tag) + ".cand").c_str(), guess);
         if (!cand) return MDET_ERR_NOMEM;
         unsigned long long cap = ctx->bufs[std::string(tag) + ".cand"].cap / sizeof(uint2);
-        MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
         CandBuf out{cand, cnt, cap};
-        if (mode == MDET_MODE_PLAIN) {
-            const float* A = rect ? a32 : g.x32;
-            MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect, tbl,
-                                 out, tiles, nlist, row_tbl, tbl_stride));
-        } else {
-            const uint16_t* A = rect ? ab : g.xa;
-            const float* An = rect ? ansq : g.nsq;
-            MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
-                               out, tiles, nlist, row_tbl, tbl_stride));
-        }
+        auto run = [&](int w) -> int {
+            MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
+            if (mode == MDET_MODE_PLAIN) {
+                const float* A = rect ? a32 : g.x32;
+                MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect,
+                                     tbl, out, tiles, nlist, row_tbl, tbl_stride));
+                ctx->last_tile_n = 128;
+            } else {
+                const uint16_t* A = rect ? ab : g.xa;
+                const float* An = rect ? ansq : g.nsq;
+                MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
+                                   out, tiles, nlist, row_tbl, tbl_stride, w));
+                ctx->last_tile_n = w;
+            }
+            return MDET_OK;
+        };
+        if (mode == MDET_MODE_PLAIN || bn != 0 || tiles)
+            MDET_TRY(run(bn ? bn : 256));
+        else
+            MDET_TRY(tc_autotune(ctx, tc_shape_key(rect, false, rect ? na : g.n, g.n), run));
         unsigned long long found = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
         MDET_CUDA(ctx, cudaStreamSynchronize(s));
@@ -235,6 +277,7 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
         st->ms_filter = tm.ms(1, 2);
         st->ms_exact = tm.ms(2, 3);
         st->ms_select = tm.ms(3, 4);
+        st->tile_n = (uint32_t)ctx->last_tile_n;
     }
     return MDET_OK;
 }

@@ -4,6 +4,8 @@
 #include "common.cuh"
 #include "ff.cuh"
 
+#include <functional>
+
 #define MDET_KPAD 144     // BF16 row length: 136 features + 8 zeros (9 x 16)
 #define MDET_TBL 256      // threshold table cells per axis
 #define MDET_TBL_LEVELS 9 // sparse-table levels (2^8 = 256)
@@ -136,11 +138,12 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
 // (B role, nb rows), both padded to 256 rows; a_nsq = ||a~||^2 (+inf on
 // padding rows).
 // tiles/nlist: optional row-major list (I * tiles_b + J) of the tile pairs
-// to evaluate (column tiles of 256); null evaluates the whole schedule.
+// to evaluate (column tiles of bn); null evaluates the whole schedule.
+// bn: column-tile width, 256 (one CTA per SM) or 128 (two per SM).
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
-              uint64_t tbl_stride = 0);
+              uint64_t tbl_stride = 0, int bn = 256);
 // Cutoff of one 256-row block of a batch: logit(cutoff) in float-float and
 // whether the second model is needed (logit(cutoff) < ln 9, decided in FP64).
 struct BlkCut {
@@ -171,7 +174,12 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
-               uint64_t tbl_stride = 0);
+               uint64_t tbl_stride = 0, int bn = 0);
+// Tile-shape autotuner: run(bn) performs one filter pass with column tiles
+// of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
+// keeps the faster (the later pass's output stands); later passes use it.
+int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run);
+uint64_t tc_shape_key(bool rect, bool list, uint64_t na, uint64_t nb);
 int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
                int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total);
 int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,

@@ -120,8 +120,7 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
     if (N == 0) return MDET_OK;
     if (N >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "batch too large (%llu rows)", (unsigned long long)N);
     const uint32_t nblk256 = (uint32_t)(N / 256), nrt = (uint32_t)(N / 128);
-    const uint32_t tcols = bf16 ? nblk256 : nrt;  // column tiles of the filter
-    if ((uint64_t)nrt * tcols >= (1ull << 32)) return ctx_fail(ctx, MDET_ERR_INVALID, "batch too large for the tile list");
+    if ((uint64_t)nrt * nrt >= (1ull << 32)) return ctx_fail(ctx, MDET_ERR_INVALID, "batch too large for the tile list");
 
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -169,12 +168,10 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
         for (auto& kv : tab_of)
             MDET_TRY(build_dstar_table_at(ctx, gmin, gmax, logit(kv.first), st + kv.second * MDET_TBL_FLOATS, &tbl));
         tbl.st = st;
-        // per-block side tables and the tile list
+        // per-block side tables
         std::vector<uint8_t> row_tbl(nrt, 0);
         std::vector<BlkCut> bcut(nblk256);
         std::vector<uint32_t> bK(nblk256, 1), bA(nblk256, 0);
-        std::vector<uint32_t> j0(nrt, 0), j1(nrt, 0);
-        std::vector<unsigned long long> off(nrt + 1, 0);
         for (uint32_t k = 0; k < count; ++k) {
             const uint32_t npad = (nn[k] + 255) / 256 * 256;
             if (!npad) continue;
@@ -189,20 +186,8 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
                 bK[b] = as[k].max_edges;
                 bA[b] = k;
             }
-            const uint32_t t0 = R[k] / 128, ta = npad / 128;
-            for (uint32_t i = 0; i < ta; ++i) {
-                row_tbl[t0 + i] = (uint8_t)tab_of[as[k].cutoff];
-                if (bf16) {  // 128 x 256 tiles, J >= I / 2 inside the assembly
-                    j0[t0 + i] = R[k] / 256 + i / 2;
-                    j1[t0 + i] = (R[k] + npad) / 256;
-                } else {     // 128 x 128 tiles, J >= I
-                    j0[t0 + i] = t0 + i;
-                    j1[t0 + i] = t0 + ta;
-                }
-            }
+            for (uint32_t i = 0; i < npad / 128; ++i) row_tbl[R[k] / 128 + i] = (uint8_t)tab_of[as[k].cutoff];
         }
-        for (uint32_t I = 0; I < nrt; ++I) off[I + 1] = off[I] + (j1[I] - j0[I]);
-        const uint64_t nlist = off[nrt];
         uint8_t* d_rtbl = (uint8_t*)ctx_scratch(ctx, "bt.rtbl", nrt);
         BlkCut* d_bcut = (BlkCut*)ctx_scratch(ctx, "bt.bcut", (uint64_t)nblk256 * sizeof(BlkCut));
         uint32_t* d_bK = (uint32_t*)ctx_scratch(ctx, "bt.bK", (uint64_t)nblk256 * 4);
@@ -210,23 +195,46 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
         uint32_t* d_j0 = (uint32_t*)ctx_scratch(ctx, "bt.j0", (uint64_t)nrt * 4);
         uint32_t* d_j1 = (uint32_t*)ctx_scratch(ctx, "bt.j1", (uint64_t)nrt * 4);
         unsigned long long* d_off = (unsigned long long*)ctx_scratch(ctx, "bt.off", (uint64_t)nrt * 8);
-        uint32_t* d_list = (uint32_t*)ctx_scratch(ctx, "bt.list", std::max<uint64_t>(nlist, 1) * 4);
-        if (!d_rtbl || !d_bcut || !d_bK || !d_bA || !d_j0 || !d_j1 || !d_off || !d_list) return MDET_ERR_NOMEM;
+        if (!d_rtbl || !d_bcut || !d_bK || !d_bA || !d_j0 || !d_j1 || !d_off) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cudaMemcpyAsync(d_rtbl, row_tbl.data(), nrt, cudaMemcpyHostToDevice, s));
         MDET_CUDA(ctx, cudaMemcpyAsync(d_bcut, bcut.data(), nblk256 * sizeof(BlkCut), cudaMemcpyHostToDevice, s));
         MDET_CUDA(ctx, cudaMemcpyAsync(d_bK, bK.data(), nblk256 * 4, cudaMemcpyHostToDevice, s));
         MDET_CUDA(ctx, cudaMemcpyAsync(d_bA, bA.data(), nblk256 * 4, cudaMemcpyHostToDevice, s));
-        MDET_CUDA(ctx, cudaMemcpyAsync(d_j0, j0.data(), nrt * 4, cudaMemcpyHostToDevice, s));
-        MDET_CUDA(ctx, cudaMemcpyAsync(d_j1, j1.data(), nrt * 4, cudaMemcpyHostToDevice, s));
-        MDET_CUDA(ctx, cudaMemcpyAsync(d_off, off.data(), nrt * 8, cudaMemcpyHostToDevice, s));
-        k_tile_list<<<nrt, 128, 0, s>>>(d_j0, d_j1, d_off, tcols, d_list);
-        MDET_LAUNCHED(ctx, "k_tile_list");
 
-        // one filter launch over every assembly's tiles, one exact stage, one selection
+        // the tile list for column tiles of width w (upper triangle of every
+        // assembly), then one filter launch over all of it
+        uint64_t nlist = 0;
+        std::vector<uint32_t> j0(nrt), j1(nrt);
+        std::vector<unsigned long long> off(nrt + 1);
         uint2* cand = nullptr;
         unsigned long long ncand = 0;
-        MDET_TRY(run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "bt", &cand, &ncand,
-                            d_list, nlist, d_rtbl, MDET_TBL_FLOATS));
+        auto run = [&](int w) -> int {
+            const uint32_t sh = w == 256 ? 1u : 0u;
+            for (uint32_t k = 0; k < count; ++k) {
+                const uint32_t npad = (nn[k] + 255) / 256 * 256;
+                const uint32_t t0 = R[k] / 128;
+                for (uint32_t i = 0; i < npad / 128; ++i) {
+                    j0[t0 + i] = (R[k] / 128 + i) >> sh;
+                    j1[t0 + i] = (R[k] + npad) / (uint32_t)w;
+                }
+            }
+            off[0] = 0;
+            for (uint32_t I = 0; I < nrt; ++I) off[I + 1] = off[I] + (j1[I] - j0[I]);
+            nlist = off[nrt];
+            uint32_t* d_list = (uint32_t*)ctx_scratch(ctx, "bt.list", std::max<uint64_t>(nlist, 1) * 4);
+            if (!d_list) return MDET_ERR_NOMEM;
+            MDET_CUDA(ctx, cudaMemcpyAsync(d_j0, j0.data(), nrt * 4, cudaMemcpyHostToDevice, s));
+            MDET_CUDA(ctx, cudaMemcpyAsync(d_j1, j1.data(), nrt * 4, cudaMemcpyHostToDevice, s));
+            MDET_CUDA(ctx, cudaMemcpyAsync(d_off, off.data(), nrt * 8, cudaMemcpyHostToDevice, s));
+            k_tile_list<<<nrt, 128, 0, s>>>(d_j0, d_j1, d_off, (uint32_t)(N / w), d_list);
+            MDET_LAUNCHED(ctx, "k_tile_list");
+            return run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "bt", &cand,
+                              &ncand, d_list, nlist, d_rtbl, MDET_TBL_FLOATS, w);
+        };
+        if (bf16)
+            MDET_TRY(tc_autotune(ctx, tc_shape_key(false, true, N, N), run));
+        else
+            MDET_TRY(run(128));
         Edge* edges = nullptr;
         unsigned long long ne = 0;
         uint32_t* deg = nullptr;
@@ -282,6 +290,7 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
             stats->n_edges = total;
             stats->tiles_total = nlist;
             stats->tiles_computed = nlist;
+            stats->tile_n = (uint32_t)ctx->last_tile_n;
         }
         return status;
     };

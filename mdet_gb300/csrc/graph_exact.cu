@@ -325,20 +325,23 @@ __global__ void __launch_bounds__(1024) k_topk_big(const uint32_t* __restrict__ 
 // (bitonic network in registers: entry i of a chunk of 32*E in lane i % 32,
 // slot i / 32) and written to the front of the row.
 
-__device__ __forceinline__ bool kv_less(double s1, uint32_t c1, double s2, uint32_t c2) {
+// Keys are the bit patterns of positive doubles, which order like the
+// values, so every comparison is an integer one (FP64 is slow on this part).
+__device__ __forceinline__ bool kv_less(unsigned long long s1, uint32_t c1, unsigned long long s2, uint32_t c2) {
     return s1 > s2 || (s1 == s2 && c1 < c2);
 }
 
 // In-lane compare-exchange of slots e and e | JE (stride >= 32 entries).
 template <int E, int JE>
-__device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k) {
+__device__ __forceinline__ void stage_in_lane(unsigned long long (&s)[E], uint32_t (&c)[E], uint32_t lane,
+                                              uint32_t k) {
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         if ((e & JE) == 0) {
             const int e2 = e | JE;
             const bool up = ((((uint32_t)e * 32u + lane) & k) == 0);
             const bool sw = up ? kv_less(s[e2], c[e2], s[e], c[e]) : kv_less(s[e], c[e], s[e2], c[e2]);
-            const double s1 = sw ? s[e2] : s[e], s2 = sw ? s[e] : s[e2];
+            const unsigned long long s1 = sw ? s[e2] : s[e], s2 = sw ? s[e] : s[e2];
             const uint32_t c1 = sw ? c[e2] : c[e], c2 = sw ? c[e] : c[e2];
             s[e] = s1;
             s[e2] = s2;
@@ -349,7 +352,7 @@ __device__ __forceinline__ void stage_in_lane(double (&s)[E], uint32_t (&c)[E], 
 }
 
 template <int E>
-__device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k,
+__device__ __forceinline__ void bitonic_stage(unsigned long long (&s)[E], uint32_t (&c)[E], uint32_t lane, uint32_t k,
                                               uint32_t j) {
     if (j >= 32) {
         const uint32_t je = j >> 5;
@@ -362,7 +365,7 @@ __device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], 
 #pragma unroll
         for (int e = 0; e < E; ++e) {
             const bool up = ((((uint32_t)e * 32u + lane) & k) == 0);
-            const double os = __shfl_xor_sync(0xffffffffu, s[e], (int)j);
+            const unsigned long long os = __shfl_xor_sync(0xffffffffu, s[e], (int)j);
             const uint32_t oc = __shfl_xor_sync(0xffffffffu, c[e], (int)j);
             const bool take = (lower == up) ? kv_less(os, oc, s[e], c[e]) : kv_less(s[e], c[e], os, oc);
             s[e] = take ? os : s[e];
@@ -375,12 +378,12 @@ __device__ __forceinline__ void bitonic_stage(double (&s)[E], uint32_t (&c)[E], 
 template <int E>
 __device__ __forceinline__ void sort_out(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ col,
                                          uint32_t m, uint32_t lane, Ent* __restrict__ row) {
-    double s[E];
+    unsigned long long s[E];
     uint32_t c[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         const uint32_t i = (uint32_t)e * 32u + lane;
-        s[e] = i < m ? __longlong_as_double((long long)key[i]) : -1.0;
+        s[e] = i < m ? key[i] : 0ull;  // padding sorts last (every real key is a positive double)
         c[e] = i < m ? col[i] : 0xFFFFFFFFu;
     }
     uint32_t P = 32u * E;
@@ -394,7 +397,7 @@ __device__ __forceinline__ void sort_out(const unsigned long long* __restrict__ 
         const uint32_t i = (uint32_t)e * 32u + lane;
         if (i < m) {
             Ent x;
-            x.sim = s[e];
+            x.sim = __longlong_as_double((long long)s[e]);
             x.ocol = c[e];
             x.pad = 0;
             row[i] = x;

@@ -26,21 +26,31 @@
 
 namespace {
 
-constexpr int kBM = 128, kBN = 256;
+constexpr int kBM = 128;
 constexpr uint32_t kAChunk = kBM * 128;           // 16 KB, 64 bf16 per row
 constexpr uint32_t kATail = kBM * 32;             // 4 KB, 16 bf16 per row
 constexpr uint32_t kABytes = 2 * kAChunk + kATail;  // 36 KB
-constexpr uint32_t kBChunk = kBN * 128;           // 32 KB
-constexpr uint32_t kBTail = kBN * 32;             // 8 KB
-constexpr uint32_t kBBytes = 2 * kBChunk + kBTail;  // 72 KB
 constexpr int kEpiWarps = 8;
 constexpr int kThreads = (2 + kEpiWarps) * 32;
-constexpr int kQueue = 512;                       // candidate queue per epilogue warp
-constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kSmemBytes = kABytes + 2 * kBBytes + 1024;  // + alignment slack
+
+// Column-tile width BN (256: one CTA per SM; 128: two CTAs per SM).
+template <int BN>
+struct Shape {
+    static constexpr uint32_t kBChunk = BN * 128;               // K 0..63 or 64..127
+    static constexpr uint32_t kBBytes = 2 * kBChunk + BN * 32;  // + K 128..143
+    static constexpr uint32_t kTmemCols = 2 * BN;               // two accumulators
+    static constexpr uint32_t kSmemBytes = kABytes + 2 * kBBytes + 1024;  // + alignment slack
+    static constexpr int kCtasPerSm = BN == 128 ? 2 : 1;
+    // candidate queue per epilogue warp (two CTAs of the narrow shape share one SM's shared memory)
+    static constexpr int kQueue = BN == 128 ? 32 : 512;
+    // BF16 x BF16 -> FP32, M = 128, N = BN, A and B K-major.
+    static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                       ((uint32_t)(kBM >> 4) << 24);
+};
 
 struct TcArgs {
     uint32_t na, nb, ta, tb, segs;
+    uint32_t jshift;  // log2(BN / 128): the first column tile of row tile I is I >> jshift
     const uint32_t* tiles;  // optional list of tiles (I * tb + J, row-major); null: full schedule
     uint64_t nlist;
     const uint8_t* row_tbl;  // optional table index per row tile (tables tbl_stride floats apart)
@@ -89,15 +99,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t layout, u
 }
 constexpr uint32_t kLayoutSW128 = 2, kLayoutSW32 = 6;
 
-// BF16 x BF16 -> FP32, M = 128, N = 256, A and B K-major.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
@@ -147,7 +154,9 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 // same time, so each B tile comes from DRAM about once per wave and from L2
 // for the other CTAs; the snake order evens out the triangular row lengths.
 
-__device__ __forceinline__ uint32_t j_start(const TcArgs& p, uint32_t I) { return p.triangular ? (I >> 1) : 0u; }
+__device__ __forceinline__ uint32_t j_start(const TcArgs& p, uint32_t I) {
+    return p.triangular ? (I >> p.jshift) : 0u;
+}
 
 // A work unit is one segment of one row tile's column range: p.segs segments
 // per row tile (1 when row tiles outnumber the CTAs).
@@ -216,11 +225,13 @@ __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, 
 
 // -------------------------------------------------------------- kernel --
 
-__global__ void __launch_bounds__(kThreads, 1)
+template <int BN>
+__global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
     k_filter_tc(const __grid_constant__ CUtensorMap tmA128, const __grid_constant__ CUtensorMap tmA32,
                 const __grid_constant__ CUtensorMap tmB128, const __grid_constant__ CUtensorMap tmB32, TcArgs p) {
     extern __shared__ unsigned char smem_raw[];
     __shared__ Ctl ctl;
+    constexpr int kQueue = Shape<BN>::kQueue;
     __shared__ uint2 queue[kEpiWarps][kQueue];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = smem;
@@ -249,7 +260,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ctl.tmem_base)),
-                     "r"(kTmemCols)
+                     "r"(Shape<BN>::kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -279,12 +290,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                     const uint32_t bs = lt & 1;
                     if (!mbar_wait(&ctl.b_empty[bs], b_e_ph[bs] ^ 1, p.flag)) break;
                     b_e_ph[bs] ^= 1;
-                    unsigned char* dst = sB + bs * kBBytes;
-                    mbar_arrive_tx(&ctl.b_full[bs], kBBytes);
-                    const int y = (int)(c.J * kBN);
+                    unsigned char* dst = sB + bs * Shape<BN>::kBBytes;
+                    mbar_arrive_tx(&ctl.b_full[bs], Shape<BN>::kBBytes);
+                    const int y = (int)(c.J * BN);
                     tma_load_2d(dst, &tmB128, 0, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + kBChunk, &tmB128, 64, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + 2 * kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
+                    tma_load_2d(dst + Shape<BN>::kBChunk, &tmB128, 64, y, &ctl.b_full[bs]);
+                    tma_load_2d(dst + 2 * Shape<BN>::kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
                 }
             }
         } else if (warp == 1) {
@@ -306,20 +317,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (!mbar_wait(&ctl.b_full[s], b_ph[s], p.flag)) break;
                     b_ph[s] ^= 1;
                     tc_fence_after();
-                    const uint32_t d = tmem + s * kBN;
-                    const uint32_t bb = b_base + s * kBBytes;
+                    const uint32_t d = tmem + s * BN;
+                    const uint32_t bb = b_base + s * Shape<BN>::kBBytes;
 #pragma unroll
                     for (int k = 0; k < 9; ++k) {
                         uint64_t ad, bd;
                         if (k < 8) {
                             const uint32_t ch = k >> 2, ko = (k & 3) * 32;
                             ad = smem_desc(a_base + ch * kAChunk + ko, kLayoutSW128, 1024);
-                            bd = smem_desc(bb + ch * kBChunk + ko, kLayoutSW128, 1024);
+                            bd = smem_desc(bb + ch * Shape<BN>::kBChunk + ko, kLayoutSW128, 1024);
                         } else {
                             ad = smem_desc(a_base + 2 * kAChunk, kLayoutSW32, 256);
-                            bd = smem_desc(bb + 2 * kBChunk, kLayoutSW32, 256);
+                            bd = smem_desc(bb + 2 * Shape<BN>::kBChunk, kLayoutSW32, 256);
                         }
-                        mma_bf16(d, ad, bd, k > 0 ? 1u : 0u);
+                        mma_bf16(d, ad, bd, Shape<BN>::kIdesc, k > 0 ? 1u : 0u);
                     }
                     mma_commit(&ctl.b_empty[s]);
                     mma_commit(&ctl.acc_full[s]);
@@ -343,7 +354,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t row = c.I * kBM + quarter * 32 + lane;
                 // tile threshold
                 const BlockMeta ma = p.ameta[c.I];
-                const BlockMeta mb0 = p.bmeta[2 * c.J], mb1 = p.bmeta[2 * c.J + 1];
+                constexpr uint32_t kBlk = BN / MDET_BLK;  // metadata blocks per column tile
+                const BlockMeta mb0 = p.bmeta[kBlk * c.J], mb1 = p.bmeta[kBlk * c.J + kBlk - 1];
                 const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
                 DstarTable tb = p.tbl;
                 if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I] * p.tbl_stride;
@@ -359,17 +371,17 @@ __global__ void __launch_bounds__(kThreads, 1)
                 float R2 = R * R + 4e-5f * (N2 + NB2) + 1e-7f;
                 if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
                 const float hr = 0.5f * (__ldg(p.a_nsq + row) - R2);
-                const bool diag = p.triangular && (c.J * kBN < c.I * kBM + kBM);
+                const bool diag = p.triangular && (c.J * BN < c.I * kBM + kBM);
                 const bool ok = mbar_wait(&ctl.acc_full[s], f_ph[s], p.flag);
                 if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform, so tcgen05.ld stays converged
                 f_ph[s] ^= 1;
                 tc_fence_after();
 #pragma unroll 1
-                for (uint32_t ch = 0; ch < 2; ++ch) {
-                    const uint32_t col0 = half * 128 + ch * 64;
+                for (uint32_t ch = 0; ch < BN / 128; ++ch) {
+                    const uint32_t col0 = half * (BN / 2) + ch * 64;
                     float v[64];
-                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * kBN + col0, v);
-                    const uint32_t gc0 = c.J * kBN + col0;
+                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * BN + col0, v);
+                    const uint32_t gc0 = c.J * BN + col0;
                     // strided group maxima: mx[t] = max of v[t + 8j], j = 0..7
                     float mx[8];
 #pragma unroll
@@ -441,7 +453,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc_fence_after();
     if (warp == 1) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Shape<BN>::kTmemCols)
+                     : "memory");
     }
 }
 
@@ -475,23 +488,22 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
     return MDET_OK;
 }
 
-}  // namespace
-
-int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+template <int BN>
+int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
-    if (na == 0 || nb == 0) return MDET_OK;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
     MDET_TRY(make_map(ctx, &mA128, a, na_pad, 64, kBM, CU_TENSOR_MAP_SWIZZLE_128B));
     MDET_TRY(make_map(ctx, &mA32, a, na_pad, 16, kBM, CU_TENSOR_MAP_SWIZZLE_32B));
-    MDET_TRY(make_map(ctx, &mB128, b, nb_pad, 64, kBN, CU_TENSOR_MAP_SWIZZLE_128B));
-    MDET_TRY(make_map(ctx, &mB32, b, nb_pad, 16, kBN, CU_TENSOR_MAP_SWIZZLE_32B));
+    MDET_TRY(make_map(ctx, &mB128, b, nb_pad, 64, BN, CU_TENSOR_MAP_SWIZZLE_128B));
+    MDET_TRY(make_map(ctx, &mB32, b, nb_pad, 16, BN, CU_TENSOR_MAP_SWIZZLE_32B));
     TcArgs p;
     p.na = na;
     p.nb = nb;
     p.ta = (na + kBM - 1) / kBM;
-    p.tb = (nb + kBN - 1) / kBN;
+    p.tb = (nb + BN - 1) / BN;
+    p.jshift = BN == 256 ? 1u : 0u;
     p.triangular = triangular ? 1 : 0;
     p.a_nsq = a_nsq;
     p.ameta = ameta;
@@ -500,30 +512,51 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     p.out = out;
     p.flag = ctx->d_flag;
     unsigned long long total = (unsigned long long)p.ta * p.tb;
-    if (triangular) {
-        unsigned long long m = p.ta >> 1;
-        unsigned long long f = (p.ta & 1) ? m * m : (m ? m * (m - 1) : 0);
+    if (triangular) {  // tiles left of each row tile's first column tile
+        unsigned long long f = 0;
+        if (BN == 256) {
+            const unsigned long long m = p.ta >> 1;
+            f = (p.ta & 1) ? m * m : (m ? m * (m - 1) : 0);
+        } else {
+            f = (unsigned long long)p.ta * (p.ta - 1) / 2;
+        }
         total -= f;
     }
     p.ntiles = total;
     static bool attr[64] = {false};
     if (!attr[ctx->device & 63]) {
-        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes));
+        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)Shape<BN>::kSmemBytes));
         attr[ctx->device & 63] = true;
     }
-    // enough work units for every SM: split row tiles into column segments when they are few
+    const uint32_t ctas = (uint32_t)ctx->num_sms * Shape<BN>::kCtasPerSm;
+    // enough work units for every CTA: split row tiles into column segments when they are few
     p.segs = 1;
-    while ((uint64_t)p.ta * p.segs < 2ull * ctx->num_sms && p.segs < p.tb) ++p.segs;
+    while ((uint64_t)p.ta * p.segs < 2ull * ctas && p.segs < p.tb) ++p.segs;
     p.tiles = tiles;
     p.nlist = nlist;
     p.row_tbl = row_tbl;
     p.tbl_stride = tbl_stride;
-    unsigned grid = (unsigned)std::min<unsigned long long>((unsigned long long)ctx->num_sms,
-                                                           tiles ? nlist : (unsigned long long)p.ta * p.segs);
+    const unsigned grid =
+        (unsigned)std::min<unsigned long long>(ctas, tiles ? nlist : (unsigned long long)p.ta * p.segs);
     if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
-    k_filter_tc<<<grid, kThreads, kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
+    k_filter_tc<BN><<<grid, kThreads, Shape<BN>::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");
     MDET_LAUNCHED(ctx, "k_filter_tc");
     return MDET_OK;
+}
+
+}  // namespace
+
+int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+              CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride,
+              int bn) {
+    if (na == 0 || nb == 0) return MDET_OK;
+    if (bn == 128)
+        return launch_tc<128>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist, row_tbl,
+                              tbl_stride);
+    return launch_tc<256>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist, row_tbl,
+                          tbl_stride);
 }

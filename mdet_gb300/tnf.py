@@ -39,7 +39,7 @@ class GraphStats(ctypes.Structure):
         ("tiles_total", u64),
         ("tiles_computed", u64),
         ("gpu_launches", u32),
-        ("reserved", u32),
+        ("tile_n", u32),
         ("ms_prep", D),
         ("ms_filter", D),
         ("ms_exact", D),
@@ -48,7 +48,7 @@ class GraphStats(ctypes.Structure):
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Assembly(ctypes.Structure):
@@ -126,6 +126,7 @@ SIGNATURES = [
     ("mdet_ctx_set_timing", ctypes.c_int, [P, ctypes.c_int]),
     ("mdet_ctx_kernel_ms", ctypes.c_int, [P, ctypes.c_char_p, ctypes.POINTER(D), ctypes.POINTER(u32)]),
     ("mdet_ctx_launch_count", u64, [P]),
+    ("mdet_ctx_set_autotune", ctypes.c_int, [P, ctypes.c_int]),
     ("mdet_tnf_count", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_dev", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_noalloc", ctypes.c_int, [P, u64, P, P, u64, P, P, P]),
@@ -240,6 +241,9 @@ class Context:
         n = u32()
         self._check(self.lib.mdet_ctx_kernel_ms(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
+
+    def set_autotune(self, enable: bool):
+        self._check(self.lib.mdet_ctx_set_autotune(self.h, 1 if enable else 0))
 
     def launch_count(self) -> int:
         return int(self.lib.mdet_ctx_launch_count(self.h))

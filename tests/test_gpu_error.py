@@ -2,7 +2,10 @@
 probability of 10^6 seeded random pairs plus every pair within 1e-3 of the
 cutoff or of its row's top-k cutoff, on a 2*10^4-contig, 50-genome set.
 The exact stage carries its sums in float-float (about 48 significant
-bits), so both errors stay near 1e-14; the bound asserted is 1e-12."""
+bits).  The distance error stays near 1e-14.  The logistic model sums
+polynomial terms of magnitude ~1e5-1e6 down to values of order 10, so even
+an FP64 evaluation carries absolute errors near 1e-10 in the
+pre-probability; the probability bound asserted is 1e-9."""
 import os
 import sys
 
@@ -61,4 +64,4 @@ def test_exact_stage_error_vs_fp64(gpu_ctx):
           f"max |d err| {ed.max():.3e}, max rel d err {(ed / np.maximum(od, 1e-300)).max():.3e}, "
           f"max |p err| {ep.max():.3e}")
     assert ed.max() <= 1e-12
-    assert ep.max() <= 1e-12
+    assert ep.max() <= 1e-9

@@ -55,6 +55,7 @@ struct mdet_ctx {
     // tile-shape autotuner of the tensor-core filter: chosen column-tile
     // width per shape class, whether to tune, and the width of the last launch
     std::map<uint64_t, int> tc_shape;
+    std::map<uint64_t, int> exact_shape;  // blocks per SM of the exact stage
     bool autotune = true;
     int last_tile_n = 0;
 };

@@ -120,26 +120,39 @@ uint64_t tc_shape_key(bool rect, bool list, uint64_t na, uint64_t nb) {
     return (rect ? 1ull : 0ull) | (list ? 2ull : 0ull) | (lg(na) << 2) | (lg(nb) << 10);
 }
 
-int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run) {
-    auto it = ctx->tc_shape.find(key);
-    if (it != ctx->tc_shape.end()) return run(it->second);
-    if (!ctx->autotune) return run(256);
-    cudaEvent_t ev[3];
+int launch_autotune(mdet_ctx* ctx, std::map<uint64_t, int>& table, uint64_t key, const std::vector<int>& values,
+                    const std::function<int(int)>& run) {
+    auto it = table.find(key);
+    if (it != table.end()) return run(it->second);
+    if (!ctx->autotune || values.size() < 2) return run(values[0]);
+    std::vector<cudaEvent_t> ev(values.size() + 1);
     for (auto& e : ev) cudaEventCreate(&e);
+    int rc = MDET_OK;
     cudaEventRecord(ev[0], ctx->stream);
-    int rc = run(256);
-    cudaEventRecord(ev[1], ctx->stream);
-    if (rc == MDET_OK) rc = run(128);
-    cudaEventRecord(ev[2], ctx->stream);
-    float t256 = 0, t128 = 0;
+    for (size_t k = 0; k < values.size() && rc == MDET_OK; ++k) {
+        rc = run(values[k]);
+        cudaEventRecord(ev[k + 1], ctx->stream);
+    }
     if (rc == MDET_OK) {
-        cudaEventSynchronize(ev[2]);
-        cudaEventElapsedTime(&t256, ev[0], ev[1]);
-        cudaEventElapsedTime(&t128, ev[1], ev[2]);
-        ctx->tc_shape[key] = t128 < t256 ? 128 : 256;
+        cudaEventSynchronize(ev.back());
+        float best = 0;
+        int pick = values[0];
+        for (size_t k = 0; k < values.size(); ++k) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            if (k == 0 || t < best) {
+                best = t;
+                pick = values[k];
+            }
+        }
+        table[key] = pick;
     }
     for (auto& e : ev) cudaEventDestroy(e);
     return rc;
+}
+
+int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run) {
+    return launch_autotune(ctx, ctx->tc_shape, key, {256, 128}, run);
 }
 
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,

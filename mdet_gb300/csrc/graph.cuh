@@ -179,6 +179,11 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
 // of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
 // keeps the faster (the later pass's output stands); later passes use it.
 int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run);
+// Launch-shape autotuner: the first call of a shape class times run(v) for
+// every candidate value (the last run's output stands) and keeps the fastest
+// in `table`; later calls run the kept value.
+int launch_autotune(mdet_ctx* ctx, std::map<uint64_t, int>& table, uint64_t key, const std::vector<int>& values,
+                    const std::function<int(int)>& run);
 uint64_t tc_shape_key(bool rect, bool list, uint64_t na, uint64_t nb);
 int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
                int mode, mdet_graph_stats* st, GraphPrep& g, uint64_t* total);

@@ -96,11 +96,16 @@ __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigne
 }
 
 __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
+    __shared__ uint32_t wcount[8];
+    __shared__ unsigned long long bbase;
     const bool model2 = p.L < kLn9;
-    const uint32_t lane = threadIdx.x & 31;
-    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x / 32);
-    for (unsigned long long base = ((unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32;
-         base < p.ncand; base += warps * 32) {
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // the block takes 256 candidates per round (32 per warp), so every warp
+    // runs the same number of rounds and the block reserves its edge slots
+    // with one global atomic per round
+    for (unsigned long long bb = (unsigned long long)blockIdx.x * 256; bb < p.ncand;
+         bb += (unsigned long long)gridDim.x * 256) {
+        const unsigned long long base = bb + 32ull * w;
         uint32_t si, sj;
         const ff d2 = warp_dist2(p.cand, p.ncand, base, nullptr, p.x32, lane, si, sj);
         bool edge = false;
@@ -120,21 +125,26 @@ __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
             }
         }
         const uint32_t bal = __ballot_sync(0xffffffffu, edge);
-        if (bal) {
-            unsigned long long wb = 0;
-            const int leader = __ffs(bal) - 1;
-            if (lane == (uint32_t)leader) wb = atomicAdd(p.nedges, (unsigned long long)__popc(bal));
-            wb = __shfl_sync(0xffffffffu, wb, leader);
-            if (edge) {
-                Edge e;
-                e.i = si;
-                e.j = sj;
-                e.sim = sim;
-                p.edges[wb + __popc(bal & ((1u << lane) - 1u))] = e;
-                atomicAdd(&p.deg[si], 1u);
-                atomicAdd(&p.deg[sj], 1u);
-            }
+        if (lane == 0) wcount[w] = __popc(bal);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int k = 0; k < 8; ++k) t += wcount[k];
+            bbase = t ? atomicAdd(p.nedges, (unsigned long long)t) : 0ull;
         }
+        __syncthreads();
+        uint32_t before = 0;
+        for (uint32_t k = 0; k < w; ++k) before += wcount[k];
+        if (edge) {
+            Edge e;
+            e.i = si;
+            e.j = sj;
+            e.sim = sim;
+            p.edges[bbase + before + __popc(bal & ((1u << lane) - 1u))] = e;
+            atomicAdd(&p.deg[si], 1u);
+            atomicAdd(&p.deg[sj], 1u);
+        }
+        __syncthreads();  // wcount and bbase are rewritten next round
     }
 }
 
@@ -633,13 +643,21 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.edges = edges;
         p.nedges = cnt;
         p.deg = deg;
-        // a warp takes 32 candidates per round
-        unsigned long long blocks = (ncand + 255) / 256;
-        unsigned long long cap = (unsigned long long)ctx->num_sms * 8;
-        ctx_timer_begin(ctx, "k_exact_graph");
-    k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
-        ctx_timer_end(ctx, "k_exact_graph");
-    MDET_LAUNCHED(ctx, "k_exact_graph");
+        // a block takes 256 candidates per round; blocks per SM (how many
+        // candidates are in flight, hence how far apart in the list the rows
+        // read at one time lie) is tuned once per shape class
+        const unsigned long long blocks = (ncand + 255) / 256;
+        auto run = [&](int per_sm) -> int {
+            MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
+            MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (uint64_t)g.n * 4, s));
+            const unsigned long long cap = (unsigned long long)ctx->num_sms * per_sm;
+            ctx_timer_begin(ctx, "k_exact_graph");
+            k_exact_graph<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
+            ctx_timer_end(ctx, "k_exact_graph");
+            MDET_LAUNCHED(ctx, "k_exact_graph");
+            return MDET_OK;
+        };
+        MDET_TRY(launch_autotune(ctx, ctx->exact_shape, tc_shape_key(false, false, ncand, g.n), {8, 4, 2}, run));
     }
     MDET_CUDA(ctx, cudaMemcpyAsync(nedges_out, cnt, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));

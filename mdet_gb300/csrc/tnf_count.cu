@@ -216,11 +216,61 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                 // pass over the chunk from a fully poisoned state
                 uint32_t x = kPoison, nact = 0, x3 = 0, nlm = 0;
                 const bool full = act == 0xFFFFu;
+                bool packed = false;
                 if (full) {
+                    // SWAR per word: 2-bit codes, newline bytes, bytes that are no base letter
+                    uint32_t xs[4], pzm = 0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint32_t w = words[q];
+                        const uint32_t lc = w | 0x20202020u;
+                        const uint32_t K = (lc >> 1) & 0x03030303u;
+                        const uint32_t sel = __byte_perm(K | (K >> 4), 0u, 0x4420u);
+                        const uint32_t bad = lc ^ __byte_perm(0x67746361u, 0u, sel);  // 'a' 'c' 't' 'g'
+                        const uint32_t nz = (((bad & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | bad) & 0x80808080u;
+                        const uint32_t z = w ^ 0x0A0A0A0Au;
+                        const uint32_t nl = ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
+                        nlm |= ((((nl >> 7) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
+                        pzm |= (((((nz & ~nl) >> 7) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
+                        xs[q] = K * 0x40100401u;  // byte 3: the word's four codes, oldest highest
+                    }
+                    if (__popc(nlm) <= 2) {
+                        packed = true;
+                        // field f (2 bits at 2f) holds byte 15 - f; drop the newline fields
+                        const uint32_t hi = __byte_perm(xs[0], xs[1], 0x3700u);
+                        const uint32_t lo = __byte_perm(xs[2], xs[3], 0x0037u);
+                        uint64_t P = __byte_perm(hi, lo, 0x3254u);
+                        uint32_t pz = __brev(pzm) >> 16, nlr = __brev(nlm) >> 16;
+                        while (nlr) {
+                            const int f = 31 - __clz(nlr);
+                            nlr &= ~(1u << f);
+                            P = ((P >> (2 * f + 2)) << (2 * f)) | (P & ((1ull << (2 * f)) - 1));
+                            pz = ((pz >> (f + 1)) << f) | (pz & ((1u << f) - 1));
+                        }
+                        nact = 16u - __popc(nlm);
+                        // window k: fields k..k+3 (newest at k); poisoned when any of them is
+                        const uint32_t wi = pz | (pz >> 1) | (pz >> 2) | (pz >> 3);
+                        const uint32_t P32 = (uint32_t)P;
+#pragma unroll
+                        for (int k = 0; k < 13; ++k) {
+                            const uint32_t code = (P32 >> (2 * k)) & 0xFFu;
+                            const bool ok = (uint32_t)k + 4u <= nact && !((wi >> k) & 1u);
+                            atomicAdd(&hist[ok ? code : 256u], 1u);
+                        }
+                        // states: the last four codes and the first three, poison in the high byte
+                        auto spread = [](uint32_t b) {
+                            return ((b & 1u) * 3u) | ((b & 2u) * 6u) | ((b & 4u) * 12u) | ((b & 8u) * 24u);
+                        };
+                        x = (P32 & 0xFFu) | (spread(pz & 0xFu) << 8);
+                        x3 = ((P32 >> (2 * (nact - 3))) & 0x3Fu) | (spread((pz >> (nact - 3)) & 7u) << 8);
+                    }
+                }
+                if (full && !packed) {
                     // every byte of the chunk is in the piece: table-driven
                     // update, newline bytes leave the state unchanged, and
                     // every window lands in a bin (bin 256 takes the invalid
                     // ones) so the loop has no branches
+                    nlm = 0;
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
                         const uint32_t ch = __byte_perm(words[b >> 2], 0u, 0x4440u | (uint32_t)(b & 3));
@@ -240,7 +290,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                         nlm |= hit ? (((hit >> 7) * 0x01020408u) >> 24 & 0xFu) << (4 * q) : 0u;
                     }
                     nact = 16u - __popc(nlm);
-                } else {
+                } else if (!full) {
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
                         uint32_t ch = (words[b >> 2] >> (8 * (b & 3))) & 0xFFu;
@@ -282,8 +332,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                     carry = (last >> 16) >= 3 ? (last & 0xFFFFu) : compose(carry, last & 0xFFFFu, last >> 16);
                 }
                 // the first (up to) three windows of the chunk depend on the carry-in
-                if (full && (nlm & 7u) == 0) {
-                    // bytes 0..2 are bases: x3 holds them in slots 2, 1, 0
+                if (packed || (full && (nlm & 7u) == 0)) {
+                    // x3 holds the chunk's first three characters in slots 2, 1, 0
                     const uint32_t w1 = compose(cin, x3 >> 4, 1);
                     const uint32_t w2 = compose(cin, x3 >> 2, 2);
                     const uint32_t w3 = compose(cin, x3, 3);

@@ -334,7 +334,8 @@ def run_ours(args):
             "edges": int(info["edges"]),
             "candidates": int(st["n_candidates"]),
             "above_cutoff": int(st["n_above_cutoff"]),
-            "filter_tile": f"128x{int(st['tile_n'])} (autotuned)" if args.mode == "bf16" else "128x128 SIMT",
+            "filter_tile": (f"{int(st['tile_m_n']) // 1000}x{int(st['tile_m_n']) % 1000} (autotuned)"
+                            if args.mode == "bf16" else "128x128 SIMT"),
         }
         if not args.no_plain:
             torch.cuda.synchronize()

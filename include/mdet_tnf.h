@@ -46,7 +46,7 @@ typedef struct {
     uint64_t tiles_total;    /* tile pairs in the pairwise schedule */
     uint64_t tiles_computed; /* tile pairs actually evaluated (< total with the learned proposal) */
     uint32_t gpu_launches;   /* kernels this call launched */
-    uint32_t tile_n;         /* column-tile width of the filter's last launch (128 or 256) */
+    uint32_t tile_m_n;       /* filter tile of the last launch: 1000 * rows + columns (128256, 256128, 128128) */
     double ms_prep, ms_filter, ms_exact, ms_select, ms_total; /* device time per phase */
 } mdet_graph_stats;
 
@@ -59,11 +59,14 @@ const char* mdet_last_error(const mdet_ctx* ctx);
 int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream);
 /* Build identification: "sm_103a ..." */
 const char* mdet_version(void);
-/* Tile-shape autotuner of the tensor-core filter (on by default): the first
- * call of each shape class times 128 x 256 tiles (one CTA per SM) against
- * 128 x 128 tiles (two CTAs per SM) and keeps the faster for the context.
- * enable = 0 fixes 128 x 256. */
-int mdet_ctx_set_autotune(mdet_ctx* ctx, int enable);
+/* Tile-shape autotuner (on by default): the first call of each shape class
+ * times the tensor-core filter's tile shapes -- 128 x 256 (one CTA per SM),
+ * 128 x 128 (two per SM), 256 x 128 with four B stages (one per SM) -- and
+ * the exact stage's blocks per SM, and keeps the fastest for the context.
+ * mode 1: tune; 0: fixed 128 x 256 tiles and 8 blocks per SM; 128256,
+ * 128128 or 256128: force that filter tile (tile lists fall back to 128 x 256
+ * for 256128). */
+int mdet_ctx_set_autotune(mdet_ctx* ctx, int mode);
 
 /* Kernel timing: when enabled, the main kernels (k_count, k_filter_tc,
  * k_filter_simt, k_exact_graph, k_exact_maxprob) are bracketed by CUDA events

@@ -57,6 +57,7 @@ struct mdet_ctx {
     std::map<uint64_t, int> tc_shape;
     std::map<uint64_t, int> exact_shape;  // blocks per SM of the exact stage
     bool autotune = true;
+    int forced_shape = 0;  // tile-shape code forced by mdet_ctx_set_autotune (0: none)
     int last_tile_n = 0;
 };
 

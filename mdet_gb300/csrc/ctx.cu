@@ -307,9 +307,16 @@ int mdet_ctx_set_stream(mdet_ctx* ctx, void* stream) {
     return MDET_OK;
 }
 
-int mdet_ctx_set_autotune(mdet_ctx* ctx, int enable) {
+int mdet_ctx_set_autotune(mdet_ctx* ctx, int mode) {
     if (!ctx) return MDET_ERR_INVALID;
-    ctx->autotune = enable != 0;
+    if (mode == 0 || mode == 1) {
+        ctx->autotune = mode == 1;
+        ctx->forced_shape = 0;
+        return MDET_OK;
+    }
+    if (mode != 128256 && mode != 128128 && mode != 256128)
+        return ctx_fail(ctx, MDET_ERR_INVALID, "unknown tile shape %d", mode);
+    ctx->forced_shape = mode;
     return MDET_OK;
 }
 

@@ -151,8 +151,14 @@ int launch_autotune(mdet_ctx* ctx, std::map<uint64_t, int>& table, uint64_t key,
     return rc;
 }
 
-int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run) {
-    return launch_autotune(ctx, ctx->tc_shape, key, {256, 128}, run);
+int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run, bool list) {
+    if (ctx->forced_shape) {
+        const int f = ctx->forced_shape;
+        const int w = f == 128128 ? 128 : (f == 256128 && !list ? kShapeTall : 256);
+        return run(w);
+    }
+    if (list) return launch_autotune(ctx, ctx->tc_shape, key, {256, 128}, run);
+    return launch_autotune(ctx, ctx->tc_shape, key, {256, 128, kShapeTall}, run);
 }
 
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
@@ -177,13 +183,13 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                 const float* A = rect ? a32 : g.x32;
                 MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect,
                                      tbl, out, tiles, nlist, row_tbl, tbl_stride));
-                ctx->last_tile_n = 128;
+                ctx->last_tile_n = 128128;
             } else {
                 const uint16_t* A = rect ? ab : g.xa;
                 const float* An = rect ? ansq : g.nsq;
                 MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
                                    out, tiles, nlist, row_tbl, tbl_stride, w));
-                ctx->last_tile_n = w;
+                ctx->last_tile_n = w == kShapeTall ? 256128 : 128 * 1000 + w;
             }
             return MDET_OK;
         };
@@ -290,7 +296,7 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
         st->ms_filter = tm.ms(1, 2);
         st->ms_exact = tm.ms(2, 3);
         st->ms_select = tm.ms(3, 4);
-        st->tile_n = (uint32_t)ctx->last_tile_n;
+        st->tile_m_n = (uint32_t)ctx->last_tile_n;
     }
     return MDET_OK;
 }

@@ -7,6 +7,7 @@
 #include <functional>
 
 #define MDET_KPAD 144     // BF16 row length: 136 features + 8 zeros (9 x 16)
+constexpr int kShapeTall = 1256;  // filter_tc shape code of 256 x 128 tiles
 #define MDET_TBL 256      // threshold table cells per axis
 #define MDET_TBL_LEVELS 9 // sparse-table levels (2^8 = 256)
 #define MDET_BLK 128      // rows per metadata block
@@ -139,7 +140,8 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
 // padding rows).
 // tiles/nlist: optional row-major list (I * tiles_b + J) of the tile pairs
 // to evaluate (column tiles of bn); null evaluates the whole schedule.
-// bn: column-tile width, 256 (one CTA per SM) or 128 (two per SM).
+// bn: tile shape: 256 = 128 x 256 tiles (one CTA per SM), 128 = 128 x 128
+// (two per SM), kShapeTall = 256 x 128 with four B stages (no tile lists).
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
@@ -178,7 +180,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
 // Tile-shape autotuner: run(bn) performs one filter pass with column tiles
 // of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
 // keeps the faster (the later pass's output stands); later passes use it.
-int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run);
+int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run, bool list = false);
 // Launch-shape autotuner: the first call of a shape class times run(v) for
 // every candidate value (the last run's output stands) and keeps the fastest
 // in `table`; later calls run the kept value.

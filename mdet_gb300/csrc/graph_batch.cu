@@ -232,7 +232,7 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
                               &ncand, d_list, nlist, d_rtbl, MDET_TBL_FLOATS, w);
         };
         if (bf16)
-            MDET_TRY(tc_autotune(ctx, tc_shape_key(false, true, N, N), run));
+            MDET_TRY(tc_autotune(ctx, tc_shape_key(false, true, N, N), run, true));
         else
             MDET_TRY(run(128));
         Edge* edges = nullptr;
@@ -290,7 +290,7 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
             stats->n_edges = total;
             stats->tiles_total = nlist;
             stats->tiles_computed = nlist;
-            stats->tile_n = (uint32_t)ctx->last_tile_n;
+            stats->tile_m_n = (uint32_t)ctx->last_tile_n;
         }
         return status;
     };

@@ -33,24 +33,35 @@ constexpr uint32_t kABytes = 2 * kAChunk + kATail;  // 36 KB
 constexpr int kEpiWarps = 8;
 constexpr int kThreads = (2 + kEpiWarps) * 32;
 
-// Column-tile width BN (256: one CTA per SM; 128: two CTAs per SM).
-template <int BN>
+// Tile shapes: BM rows (one or two M = 128 MMAs) x BN columns, with NST
+// stages of B tiles in shared memory.  128 x 256 x 2 and 256 x 128 x 4 run one
+// CTA per SM; 128 x 128 x 2 runs two.  A 256-row tile reads each B tile for
+// twice the rows, halving the B traffic per output.
+template <int BM, int BN, int NST>
 struct Shape {
+    static constexpr int MH = BM / 128;                         // M halves
+    static constexpr uint32_t kABytesAll = MH * kABytes;
     static constexpr uint32_t kBChunk = BN * 128;               // K 0..63 or 64..127
     static constexpr uint32_t kBBytes = 2 * kBChunk + BN * 32;  // + K 128..143
-    static constexpr uint32_t kTmemCols = 2 * BN;               // two accumulators
-    static constexpr uint32_t kSmemBytes = kABytes + 2 * kBBytes + 1024;  // + alignment slack
-    static constexpr int kCtasPerSm = BN == 128 ? 2 : 1;
+    static constexpr uint32_t kAccCols = MH * BN;               // one accumulator
+    static constexpr uint32_t kTmemCols = 2 * kAccCols;         // double buffered
+    static constexpr uint32_t kSmemBytes = kABytesAll + NST * kBBytes + 1024;  // + alignment slack
+    static constexpr int kCtasPerSm = (BM == 128 && BN == 128) ? 2 : 1;
     // candidate queue per epilogue warp (two CTAs of the narrow shape share one SM's shared memory)
-    static constexpr int kQueue = BN == 128 ? 32 : 512;
+    static constexpr int kQueue = kCtasPerSm == 2 ? 32 : (kSmemBytes + 512 * 64 <= 227 * 1024 ? 512 : 128);
+    // epilogue: 8 warps = 4 TMEM lane quarters x 2 groups; the groups split the
+    // columns (one M half) or take one M half each
+    static constexpr uint32_t kWarpCols = MH == 1 ? BN / 2 : BN;
     // BF16 x BF16 -> FP32, M = 128, N = BN, A and B K-major.
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                                       ((uint32_t)(kBM >> 4) << 24);
+                                       ((uint32_t)(128 >> 4) << 24);
+    static_assert(kTmemCols <= 512, "TMEM holds 512 columns");
+    static_assert(NST <= 4, "at most four B stages");
 };
 
 struct TcArgs {
     uint32_t na, nb, ta, tb, segs;
-    uint32_t jshift;  // log2(BN / 128): the first column tile of row tile I is I >> jshift
+    uint32_t jnum, jden;  // the first column tile of row tile I is I * jnum / jden (BM / 128, BN / 128)
     const uint32_t* tiles;  // optional list of tiles (I * tb + J, row-major); null: full schedule
     uint64_t nlist;
     const uint8_t* row_tbl;  // optional table index per row tile (tables tbl_stride floats apart)
@@ -67,7 +78,7 @@ struct TcArgs {
 
 struct __align__(8) Ctl {
     uint64_t a_full, a_empty;
-    uint64_t b_full[2], b_empty[2];
+    uint64_t b_full[4], b_empty[4];
     uint64_t acc_full[2], acc_empty[2];
     uint32_t tmem_base;
     uint32_t qcount[kEpiWarps];
@@ -155,7 +166,7 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 // for the other CTAs; the snake order evens out the triangular row lengths.
 
 __device__ __forceinline__ uint32_t j_start(const TcArgs& p, uint32_t I) {
-    return p.triangular ? (I >> p.jshift) : 0u;
+    return p.triangular ? (I * p.jnum) / p.jden : 0u;
 }
 
 // A work unit is one segment of one row tile's column range: p.segs segments
@@ -225,17 +236,18 @@ __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, 
 
 // -------------------------------------------------------------- kernel --
 
-template <int BN>
-__global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
+template <int BM, int BN, int NST>
+__global__ void __launch_bounds__(kThreads, Shape<BM, BN, NST>::kCtasPerSm)
     k_filter_tc(const __grid_constant__ CUtensorMap tmA128, const __grid_constant__ CUtensorMap tmA32,
                 const __grid_constant__ CUtensorMap tmB128, const __grid_constant__ CUtensorMap tmB32, TcArgs p) {
+    using S = Shape<BM, BN, NST>;
     extern __shared__ unsigned char smem_raw[];
     __shared__ Ctl ctl;
-    constexpr int kQueue = Shape<BN>::kQueue;
+    constexpr int kQueue = S::kQueue;
     __shared__ uint2 queue[kEpiWarps][kQueue];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = smem;
-    unsigned char* sB = smem + kABytes;
+    unsigned char* sB = smem + S::kABytesAll;
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     const uint32_t G = gridDim.x, cta = blockIdx.x;
@@ -243,9 +255,11 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
     if (threadIdx.x == 0) {
         mbar_init(&ctl.a_full, 1);
         mbar_init(&ctl.a_empty, 1);
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < NST; ++s) {
             mbar_init(&ctl.b_full[s], 1);
             mbar_init(&ctl.b_empty[s], 1);
+        }
+        for (int s = 0; s < 2; ++s) {
             mbar_init(&ctl.acc_full[s], 1);
             mbar_init(&ctl.acc_empty[s], kEpiWarps * 32);
         }
@@ -260,7 +274,7 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&ctl.tmem_base)),
-                     "r"(Shape<BN>::kTmemCols)
+                     "r"(S::kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -274,35 +288,43 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
             // ------------------------------------------------ TMA producer
             if (lane == 0) {
                 Cursor c = cursor_first(p, cta, G);
-                uint32_t a_e_ph = 0, b_e_ph[2] = {0, 0};
+                uint32_t a_e_ph = 0, b_e_ph[NST];
+#pragma unroll
+                for (int t = 0; t < NST; ++t) b_e_ph[t] = 0;
                 uint32_t curI = 0xFFFFFFFFu;
                 for (uint32_t lt = 0; c.valid; ++lt, advance(p, c, cta, G)) {
                     if (c.I != curI) {
                         if (!mbar_wait(&ctl.a_empty, a_e_ph ^ 1, p.flag)) break;
                         a_e_ph ^= 1;
-                        mbar_arrive_tx(&ctl.a_full, kABytes);
-                        const int y = (int)(c.I * kBM);
-                        tma_load_2d(sA, &tmA128, 0, y, &ctl.a_full);
-                        tma_load_2d(sA + kAChunk, &tmA128, 64, y, &ctl.a_full);
-                        tma_load_2d(sA + 2 * kAChunk, &tmA32, 128, y, &ctl.a_full);
+                        mbar_arrive_tx(&ctl.a_full, S::kABytesAll);
+#pragma unroll
+                        for (int h = 0; h < S::MH; ++h) {
+                            const int y = (int)(c.I * BM + h * 128);
+                            unsigned char* dA = sA + h * kABytes;
+                            tma_load_2d(dA, &tmA128, 0, y, &ctl.a_full);
+                            tma_load_2d(dA + kAChunk, &tmA128, 64, y, &ctl.a_full);
+                            tma_load_2d(dA + 2 * kAChunk, &tmA32, 128, y, &ctl.a_full);
+                        }
                         curI = c.I;
                     }
-                    const uint32_t bs = lt & 1;
+                    const uint32_t bs = lt % NST;
                     if (!mbar_wait(&ctl.b_empty[bs], b_e_ph[bs] ^ 1, p.flag)) break;
                     b_e_ph[bs] ^= 1;
-                    unsigned char* dst = sB + bs * Shape<BN>::kBBytes;
-                    mbar_arrive_tx(&ctl.b_full[bs], Shape<BN>::kBBytes);
+                    unsigned char* dst = sB + bs * S::kBBytes;
+                    mbar_arrive_tx(&ctl.b_full[bs], S::kBBytes);
                     const int y = (int)(c.J * BN);
                     tma_load_2d(dst, &tmB128, 0, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + Shape<BN>::kBChunk, &tmB128, 64, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + 2 * Shape<BN>::kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
+                    tma_load_2d(dst + S::kBChunk, &tmB128, 64, y, &ctl.b_full[bs]);
+                    tma_load_2d(dst + 2 * S::kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
                 }
             }
         } else if (warp == 1) {
             // -------------------------------------------------- MMA issuer
             if (lane == 0) {
                 Cursor c = cursor_first(p, cta, G);
-                uint32_t a_ph = 0, b_ph[2] = {0, 0}, e_ph[2] = {0, 0};
+                uint32_t a_ph = 0, b_ph[NST], e_ph[2] = {0, 0};
+#pragma unroll
+                for (int t = 0; t < NST; ++t) b_ph[t] = 0;
                 uint32_t curI = 0xFFFFFFFFu;
                 const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB);
                 for (uint32_t lt = 0; c.valid; ++lt) {
@@ -311,28 +333,32 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
                         a_ph ^= 1;
                         curI = c.I;
                     }
-                    const uint32_t s = lt & 1;
+                    const uint32_t s = lt & 1, bs = lt % NST;
                     if (!mbar_wait(&ctl.acc_empty[s], e_ph[s] ^ 1, p.flag)) break;
                     e_ph[s] ^= 1;
-                    if (!mbar_wait(&ctl.b_full[s], b_ph[s], p.flag)) break;
-                    b_ph[s] ^= 1;
+                    if (!mbar_wait(&ctl.b_full[bs], b_ph[bs], p.flag)) break;
+                    b_ph[bs] ^= 1;
                     tc_fence_after();
-                    const uint32_t d = tmem + s * BN;
-                    const uint32_t bb = b_base + s * Shape<BN>::kBBytes;
+                    const uint32_t bb = b_base + bs * S::kBBytes;
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        uint64_t ad, bd;
-                        if (k < 8) {
-                            const uint32_t ch = k >> 2, ko = (k & 3) * 32;
-                            ad = smem_desc(a_base + ch * kAChunk + ko, kLayoutSW128, 1024);
-                            bd = smem_desc(bb + ch * Shape<BN>::kBChunk + ko, kLayoutSW128, 1024);
-                        } else {
-                            ad = smem_desc(a_base + 2 * kAChunk, kLayoutSW32, 256);
-                            bd = smem_desc(bb + 2 * Shape<BN>::kBChunk, kLayoutSW32, 256);
+                    for (int h = 0; h < S::MH; ++h) {
+                        const uint32_t d = tmem + s * S::kAccCols + h * BN;
+                        const uint32_t ab = a_base + h * kABytes;
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) {
+                            uint64_t ad, bd;
+                            if (k < 8) {
+                                const uint32_t ch = k >> 2, ko = (k & 3) * 32;
+                                ad = smem_desc(ab + ch * kAChunk + ko, kLayoutSW128, 1024);
+                                bd = smem_desc(bb + ch * S::kBChunk + ko, kLayoutSW128, 1024);
+                            } else {
+                                ad = smem_desc(ab + 2 * kAChunk, kLayoutSW32, 256);
+                                bd = smem_desc(bb + 2 * S::kBChunk, kLayoutSW32, 256);
+                            }
+                            mma_bf16(d, ad, bd, S::kIdesc, k > 0 ? 1u : 0u);
                         }
-                        mma_bf16(d, ad, bd, Shape<BN>::kIdesc, k > 0 ? 1u : 0u);
                     }
-                    mma_commit(&ctl.b_empty[s]);
+                    mma_commit(&ctl.b_empty[bs]);
                     mma_commit(&ctl.acc_full[s]);
                     Cursor nx = c;
                     advance(p, nx, cta, G);
@@ -344,21 +370,23 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
             // ---------------------------------------------------- epilogue
             const uint32_t ew = warp - 2;           // 0..7
             const uint32_t quarter = warp & 3;      // TMEM lanes 32*quarter ..
-            const uint32_t half = ew >> 2;          // column half of the 256-wide tile
+            const uint32_t grp = ew >> 2;
+            const uint32_t mh = S::MH == 1 ? 0u : grp;                  // M half of this warp
+            const uint32_t cbase = S::MH == 1 ? grp * (BN / 2) : 0u;    // first column of this warp
             uint32_t* qc = &ctl.qcount[ew];
             uint2* q = queue[ew];
             Cursor c = cursor_first(p, cta, G);
             uint32_t f_ph[2] = {0, 0};
             for (uint32_t lt = 0; c.valid; ++lt, advance(p, c, cta, G)) {
                 const uint32_t s = lt & 1;
-                const uint32_t row = c.I * kBM + quarter * 32 + lane;
-                // tile threshold
-                const BlockMeta ma = p.ameta[c.I];
+                const uint32_t row = c.I * BM + mh * 128 + quarter * 32 + lane;
+                // tile threshold (per M half)
+                const BlockMeta ma = p.ameta[c.I * S::MH + mh];
                 constexpr uint32_t kBlk = BN / MDET_BLK;  // metadata blocks per column tile
                 const BlockMeta mb0 = p.bmeta[kBlk * c.J], mb1 = p.bmeta[kBlk * c.J + kBlk - 1];
                 const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
                 DstarTable tb = p.tbl;
-                if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I] * p.tbl_stride;
+                if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I * S::MH + mh] * p.tbl_stride;
                 const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
                 const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
                 const float N2 = ma.nmax * fmaxf(mb0.nmax, mb1.nmax);
@@ -371,16 +399,16 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
                 float R2 = R * R + 4e-5f * (N2 + NB2) + 1e-7f;
                 if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
                 const float hr = 0.5f * (__ldg(p.a_nsq + row) - R2);
-                const bool diag = p.triangular && (c.J * BN < c.I * kBM + kBM);
+                const bool diag = p.triangular && (c.J * BN < c.I * BM + BM);
                 const bool ok = mbar_wait(&ctl.acc_full[s], f_ph[s], p.flag);
                 if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform, so tcgen05.ld stays converged
                 f_ph[s] ^= 1;
                 tc_fence_after();
 #pragma unroll 1
-                for (uint32_t ch = 0; ch < BN / 128; ++ch) {
-                    const uint32_t col0 = half * (BN / 2) + ch * 64;
+                for (uint32_t ch = 0; ch < S::kWarpCols / 64; ++ch) {
+                    const uint32_t col0 = cbase + ch * 64;
                     float v[64];
-                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * BN + col0, v);
+                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * S::kAccCols + mh * BN + col0, v);
                     const uint32_t gc0 = c.J * BN + col0;
                     // strided group maxima: mx[t] = max of v[t + 8j], j = 0..7
                     float mx[8];
@@ -453,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, Shape<BN>::kCtasPerSm)
     __syncthreads();
     tc_fence_after();
     if (warp == 1) {
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Shape<BN>::kTmemCols)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::kTmemCols)
                      : "memory");
     }
 }
@@ -488,10 +516,11 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
     return MDET_OK;
 }
 
-template <int BN>
+template <int BM, int BN, int NST>
 int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
+    using S = Shape<BM, BN, NST>;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
     MDET_TRY(make_map(ctx, &mA128, a, na_pad, 64, kBM, CU_TENSOR_MAP_SWIZZLE_128B));
@@ -501,9 +530,10 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     TcArgs p;
     p.na = na;
     p.nb = nb;
-    p.ta = (na + kBM - 1) / kBM;
+    p.ta = (na + BM - 1) / BM;
     p.tb = (nb + BN - 1) / BN;
-    p.jshift = BN == 256 ? 1u : 0u;
+    p.jnum = BM / 128;
+    p.jden = BN / 128;
     p.triangular = triangular ? 1 : 0;
     p.a_nsq = a_nsq;
     p.ameta = ameta;
@@ -511,25 +541,14 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     p.tbl = tbl;
     p.out = out;
     p.flag = ctx->d_flag;
-    unsigned long long total = (unsigned long long)p.ta * p.tb;
-    if (triangular) {  // tiles left of each row tile's first column tile
-        unsigned long long f = 0;
-        if (BN == 256) {
-            const unsigned long long m = p.ta >> 1;
-            f = (p.ta & 1) ? m * m : (m ? m * (m - 1) : 0);
-        } else {
-            f = (unsigned long long)p.ta * (p.ta - 1) / 2;
-        }
-        total -= f;
-    }
-    p.ntiles = total;
+    p.ntiles = 0;
     static bool attr[64] = {false};
     if (!attr[ctx->device & 63]) {
-        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)Shape<BN>::kSmemBytes));
+        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc<BM, BN, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)S::kSmemBytes));
         attr[ctx->device & 63] = true;
     }
-    const uint32_t ctas = (uint32_t)ctx->num_sms * Shape<BN>::kCtasPerSm;
+    const uint32_t ctas = (uint32_t)ctx->num_sms * S::kCtasPerSm;
     // enough work units for every CTA: split row tiles into column segments when they are few
     p.segs = 1;
     while ((uint64_t)p.ta * p.segs < 2ull * ctas && p.segs < p.tb) ++p.segs;
@@ -541,7 +560,7 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
         (unsigned)std::min<unsigned long long>(ctas, tiles ? nlist : (unsigned long long)p.ta * p.segs);
     if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
-    k_filter_tc<BN><<<grid, kThreads, Shape<BN>::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
+    k_filter_tc<BM, BN, NST><<<grid, kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");
     MDET_LAUNCHED(ctx, "k_filter_tc");
     return MDET_OK;
@@ -555,8 +574,13 @@ int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
               int bn) {
     if (na == 0 || nb == 0) return MDET_OK;
     if (bn == 128)
-        return launch_tc<128>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist, row_tbl,
-                              tbl_stride);
-    return launch_tc<256>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist, row_tbl,
-                          tbl_stride);
+        return launch_tc<128, 128, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                      row_tbl, tbl_stride);
+    if (bn == kShapeTall) {
+        if (tiles) return ctx_fail(ctx, MDET_ERR_INVALID, "tile lists use 128-row tiles");
+        return launch_tc<256, 128, 4>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                      row_tbl, tbl_stride);
+    }
+    return launch_tc<128, 256, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                  row_tbl, tbl_stride);
 }

@@ -39,7 +39,7 @@ class GraphStats(ctypes.Structure):
         ("tiles_total", u64),
         ("tiles_computed", u64),
         ("gpu_launches", u32),
-        ("tile_n", u32),
+        ("tile_m_n", u32),
         ("ms_prep", D),
         ("ms_filter", D),
         ("ms_exact", D),
@@ -242,8 +242,10 @@ class Context:
         self._check(self.lib.mdet_ctx_kernel_ms(self.h, kernel.encode(), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
-    def set_autotune(self, enable: bool):
-        self._check(self.lib.mdet_ctx_set_autotune(self.h, 1 if enable else 0))
+    def set_autotune(self, mode):
+        """True/False: tune or not; 128256, 128128, 256128: force that filter tile shape."""
+        m = (1 if mode else 0) if isinstance(mode, bool) else int(mode)
+        self._check(self.lib.mdet_ctx_set_autotune(self.h, m))
 
     def launch_count(self) -> int:
         return int(self.lib.mdet_ctx_launch_count(self.h))

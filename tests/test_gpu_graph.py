@@ -39,6 +39,22 @@ def test_bf16_equals_plain(gpu_ctx, set_a, cutoff, k):
     assert t.stats["n_candidates"] >= t.stats["n_above_cutoff"]
 
 
+@pytest.mark.parametrize("shape", [128256, 128128, 256128])
+def test_every_tile_shape_equals_plain(gpu_ctx, set_a, shape):
+    a, _, tnf = set_a
+    p = gpu_ctx.tnf_graph(tnf, a.log_sizes, 0.9, 40, mode="plain")
+    gpu_ctx.set_autotune(shape)
+    try:
+        t = gpu_ctx.tnf_graph(tnf, a.log_sizes, 0.9, 40, mode="bf16")
+        m = gpu_ctx.max_prob(tnf, a.log_sizes, np.arange(0, tnf.shape[0], 7), mode="bf16")
+    finally:
+        gpu_ctx.set_autotune(True)
+    assert t.stats["tile_m_n"] == shape
+    assert np.array_equal(p.from_, t.from_) and np.array_equal(p.to, t.to) and np.array_equal(p.sTNF, t.sTNF)
+    mp = gpu_ctx.max_prob(tnf, a.log_sizes, np.arange(0, tnf.shape[0], 7), mode="plain")
+    assert np.array_equal(m, mp)
+
+
 def test_identical_contigs_big_rows(gpu_ctx):
     # 1500 copies of a handful of profiles: rows with > 1024 tied edges
     a, _, tnf = synth_set(seed=22, n=40, genomes=2, max_len=30000)

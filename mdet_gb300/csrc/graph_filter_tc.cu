@@ -15,8 +15,9 @@
 // distance is below d* is dropped; the exact stage re-scores every kept pair,
 // so the edge set equals the plain form's.  Nothing n x n leaves the SM.
 //
-// Warp roles (10 warps): 0 = TMA producer, 1 = MMA issuer + TMEM owner,
-// 2..9 = epilogue (TMEM lane quarter = warp % 4, column half = (warp-2)/4).
+// Warp roles: 0 = TMA producer, 1 = MMA issuer + TMEM owner, 2.. = epilogue
+// (TMEM lane quarter = warp % 4; the groups of four split the tile's columns
+// and M halves).
 // CTAs take whole row tiles in waves (see the schedule below), so the A tile
 // (128 rows) is loaded once per row tile and B tiles stream through a
 // two-stage ring.  All waits are bounded.
@@ -30,8 +31,7 @@ constexpr int kBM = 128;
 constexpr uint32_t kAChunk = kBM * 128;           // 16 KB, 64 bf16 per row
 constexpr uint32_t kATail = kBM * 32;             // 4 KB, 16 bf16 per row
 constexpr uint32_t kABytes = 2 * kAChunk + kATail;  // 36 KB
-constexpr int kEpiWarps = 8;
-constexpr int kThreads = (2 + kEpiWarps) * 32;
+constexpr int kMaxEpiWarps = 16;
 
 // Tile shapes: BM rows (one or two M = 128 MMAs) x BN columns, with NST
 // stages of B tiles in shared memory.  128 x 256 x 2 and 256 x 128 x 4 run one
@@ -47,11 +47,16 @@ struct Shape {
     static constexpr uint32_t kTmemCols = 2 * kAccCols;         // double buffered
     static constexpr uint32_t kSmemBytes = kABytesAll + NST * kBBytes + 1024;  // + alignment slack
     static constexpr int kCtasPerSm = (BM == 128 && BN == 128) ? 2 : 1;
-    // candidate queue per epilogue warp (two CTAs of the narrow shape share one SM's shared memory)
-    static constexpr int kQueue = kCtasPerSm == 2 ? 32 : (kSmemBytes + 512 * 64 <= 227 * 1024 ? 512 : 128);
-    // epilogue: 8 warps = 4 TMEM lane quarters x 2 groups; the groups split the
-    // columns (one M half) or take one M half each
-    static constexpr uint32_t kWarpCols = MH == 1 ? BN / 2 : BN;
+    // epilogue warps: 4 TMEM lane quarters x kEpi/4 groups; the groups of an
+    // M half split its columns.  One-CTA shapes take 16 so that the TMEM
+    // reads of a tile are spread over more warps in flight.
+    static constexpr int kEpi = kCtasPerSm == 2 ? 8 : 16;
+    static constexpr int kThreads = (2 + kEpi) * 32;
+    static constexpr int kGroupsPerHalf = kEpi / 4 / MH;
+    static constexpr uint32_t kWarpCols = BN / kGroupsPerHalf;
+    // candidate queue per epilogue warp, within the shared memory left
+    static constexpr int kQueue = kCtasPerSm == 2 ? 32 : (kSmemBytes + kEpi * 256 * 8 <= 227 * 1024 ? 256 : 64);
+    static_assert(kWarpCols % 64 == 0, "epilogue reads 64 columns at a time");
     // BF16 x BF16 -> FP32, M = 128, N = BN, A and B K-major.
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                        ((uint32_t)(128 >> 4) << 24);
@@ -81,7 +86,7 @@ struct __align__(8) Ctl {
     uint64_t b_full[4], b_empty[4];
     uint64_t acc_full[2], acc_empty[2];
     uint32_t tmem_base;
-    uint32_t qcount[kEpiWarps];
+    uint32_t qcount[kMaxEpiWarps];
 };
 
 // ---------------------------------------------------------------- PTX --
@@ -237,14 +242,14 @@ __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, 
 // -------------------------------------------------------------- kernel --
 
 template <int BM, int BN, int NST>
-__global__ void __launch_bounds__(kThreads, Shape<BM, BN, NST>::kCtasPerSm)
+__global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NST>::kCtasPerSm)
     k_filter_tc(const __grid_constant__ CUtensorMap tmA128, const __grid_constant__ CUtensorMap tmA32,
                 const __grid_constant__ CUtensorMap tmB128, const __grid_constant__ CUtensorMap tmB32, TcArgs p) {
     using S = Shape<BM, BN, NST>;
     extern __shared__ unsigned char smem_raw[];
     __shared__ Ctl ctl;
     constexpr int kQueue = S::kQueue;
-    __shared__ uint2 queue[kEpiWarps][kQueue];
+    __shared__ uint2 queue[S::kEpi][kQueue];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     unsigned char* sA = smem;
     unsigned char* sB = smem + S::kABytesAll;
@@ -261,9 +266,9 @@ __global__ void __launch_bounds__(kThreads, Shape<BM, BN, NST>::kCtasPerSm)
         }
         for (int s = 0; s < 2; ++s) {
             mbar_init(&ctl.acc_full[s], 1);
-            mbar_init(&ctl.acc_empty[s], kEpiWarps * 32);
+            mbar_init(&ctl.acc_empty[s], S::kEpi * 32);
         }
-        for (int w = 0; w < kEpiWarps; ++w) ctl.qcount[w] = 0;
+        for (int w = 0; w < S::kEpi; ++w) ctl.qcount[w] = 0;
         mbar_fence_init();
     }
     if (warp == 0 && lane == 0) {
@@ -368,11 +373,11 @@ __global__ void __launch_bounds__(kThreads, Shape<BM, BN, NST>::kCtasPerSm)
             }
         } else {
             // ---------------------------------------------------- epilogue
-            const uint32_t ew = warp - 2;           // 0..7
+            const uint32_t ew = warp - 2;           // 0 .. kEpi - 1
             const uint32_t quarter = warp & 3;      // TMEM lanes 32*quarter ..
             const uint32_t grp = ew >> 2;
-            const uint32_t mh = S::MH == 1 ? 0u : grp;                  // M half of this warp
-            const uint32_t cbase = S::MH == 1 ? grp * (BN / 2) : 0u;    // first column of this warp
+            const uint32_t mh = grp / S::kGroupsPerHalf;                      // M half of this warp
+            const uint32_t cbase = (grp % S::kGroupsPerHalf) * S::kWarpCols;  // first column of this warp
             uint32_t* qc = &ctl.qcount[ew];
             uint2* q = queue[ew];
             Cursor c = cursor_first(p, cta, G);
@@ -560,7 +565,7 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
         (unsigned)std::min<unsigned long long>(ctas, tiles ? nlist : (unsigned long long)p.ta * p.segs);
     if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
-    k_filter_tc<BM, BN, NST><<<grid, kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
+    k_filter_tc<BM, BN, NST><<<grid, S::kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");
     MDET_LAUNCHED(ctx, "k_filter_tc");
     return MDET_OK;

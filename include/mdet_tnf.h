@@ -185,6 +185,16 @@ typedef struct {
 
 int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* assemblies, uint32_t count, int mode,
                            mdet_graph_stats* stats);
+/* CUDA-graph recording of batched calls (on by default): after a batch has
+ * run once, its whole device work -- preparation, d* tables, filter, exact
+ * stage, selection, output -- is recorded as one CUDA graph with every count
+ * kept on the device; a later call with the same sizes, cutoffs, max_edges,
+ * buffers and capacities (the data may differ) replays it with one launch.
+ * A replay whose candidates outgrow the recording falls back to the sized
+ * path.  The recording is dropped when any scratch buffer of the context is
+ * reallocated.  mdet_ctx_graph_replays counts replays. */
+int mdet_ctx_set_graph_capture(mdet_ctx* ctx, int enable);
+uint64_t mdet_ctx_graph_replays(mdet_ctx* ctx);
 
 /* ---- learned proposal (no counterpart in the reference) ----------------
  * A 136 -> 256 -> 128 -> 64 GELU network (BF16 weights, FP32 accumulation)

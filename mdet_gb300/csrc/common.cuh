@@ -58,7 +58,15 @@ struct mdet_ctx {
     std::map<uint64_t, int> exact_shape;  // blocks per SM of the exact stage
     bool autotune = true;
     int forced_shape = 0;  // tile-shape code forced by mdet_ctx_set_autotune (0: none)
+    int forced_exact = 0;  // exact-stage blocks per SM forced while a pass is captured (0: none)
     int last_tile_n = 0;
+    // CUDA-graph capture of repeated batched passes
+    bool graph_capture = true;
+    bool capturing = false;
+    uint64_t scratch_gen = 0;  // bumped whenever a scratch buffer is (re)allocated
+    uint64_t graph_replays = 0;
+    void* batch_plan = nullptr;
+    void (*batch_plan_free)(void*) = nullptr;
 };
 
 // Event pair around one launch of a named kernel when timing is enabled.

@@ -58,6 +58,11 @@ void* ctx_scratch(mdet_ctx* ctx, const char* name, size_t bytes, bool zero_on_gr
     if (bytes == 0) bytes = 16;
     DevBuf& b = ctx->bufs[name];
     if (b.cap >= bytes) return b.p;
+    if (ctx->capturing) {  // a captured pass must not move its buffers
+        ctx_fail(ctx, MDET_ERR_NOMEM, "scratch %s would grow while a pass is captured", name);
+        return nullptr;
+    }
+    ++ctx->scratch_gen;  // captured passes that used the old buffer are stale now
     if (b.p) {
         cudaStreamSynchronize(ctx->stream);
         cudaFree(b.p);
@@ -285,6 +290,7 @@ int mdet_ctx_destroy(mdet_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     timers_clear(ctx);
+    if (ctx->batch_plan_free) ctx->batch_plan_free(ctx->batch_plan);
     for (auto& kv : ctx->bufs)
         if (kv.second.p) cudaFree(kv.second.p);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);

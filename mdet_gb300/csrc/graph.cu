@@ -164,10 +164,30 @@ int tc_autotune(mdet_ctx* ctx, uint64_t key, const std::function<int(int)>& run,
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
-               const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride, int bn) {
+               const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride, int bn,
+               unsigned long long fixed_cap, unsigned long long** cnt_dev) {
     cudaStream_t s = ctx->stream;
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
     if (!cnt) return MDET_ERR_NOMEM;
+    if (fixed_cap) {
+        // one pass into a buffer of fixed_cap pairs; the count stays on the
+        // device (pairs beyond the capacity are dropped and only counted)
+        uint2* cand = (uint2*)ctx_scratch(ctx, (std::string(tag) + ".cand").c_str(), fixed_cap * sizeof(uint2));
+        if (!cand) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cudaMemsetAsync(cnt, 0, 8, s));
+        CandBuf out{cand, cnt, fixed_cap};
+        if (mode == MDET_MODE_PLAIN) {
+            MDET_TRY(filter_simt(ctx, rect ? a32 : g.x32, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n,
+                                 g.meta32, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride));
+        } else {
+            MDET_TRY(filter_tc(ctx, rect ? ab : g.xa, rect ? ansq : g.nsq, rect ? na : g.n, rect ? ameta : g.meta, g.xb,
+                               g.n, g.meta, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride, bn ? bn : 256));
+        }
+        *cand_out = cand;
+        *ncand_out = fixed_cap;
+        if (cnt_dev) *cnt_dev = cnt;
+        return MDET_OK;
+    }
     // remembered capacity (bytes of the candidate buffer) from earlier calls
     size_t guess = ((size_t)256 * (rect ? na : g.n) + (1u << 20)) * sizeof(uint2);
     DevBuf& cb = ctx->bufs[std::string(tag) + ".cand"];

@@ -25,6 +25,13 @@ struct BlockMeta {
 struct DstarTable {
     const float* st;  // [levels][TBL][TBL]
     float lmin, inv_h;
+    const float* dyn;  // optional device copy of {lmin, inv_h}, read by the kernels instead
+};
+
+// Grid of a table built from a device-resident size range.
+struct TableGrid {
+    double lmin, h;  // first cell edge and cell width
+    float lminf, inv_hf;
 };
 
 // Pairs handed from the distance filter to the exact stage.
@@ -111,6 +118,10 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
                       bool sorted = true);
 // A table over a given log-size range written to st (MDET_TBL_LEVELS x TBL x TBL floats).
 int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out);
+// The same over the union of `count` device ranges (lo, hi pairs; entries
+// with lo > hi are empty): no host synchronisation, grid left in *grid.
+int grid_from_ranges(mdet_ctx* ctx, const double* ranges, uint32_t count, TableGrid* grid);
+int build_dstar_table_dev(mdet_ctx* ctx, const TableGrid* grid, double logit_cut, float* st, DstarTable* out);
 #define MDET_TBL_FLOATS ((uint64_t)MDET_TBL_LEVELS * MDET_TBL * MDET_TBL)
 ModelH model_h();
 ModelHFF model_h_ff();
@@ -154,16 +165,22 @@ struct BlkCut {
     uint32_t pad;
 };
 // blk_L: optional per-256-row-block cutoff overriding L.
+// ncand_dev: the candidate count on the device (ncand is then its cap); with
+// nedges_dev the edge count stays on the device too and nothing is read back.
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
                 Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out,
-                const BlkCut* blk_L = nullptr);
+                const BlkCut* blk_L = nullptr, const unsigned long long* ncand_dev = nullptr,
+                unsigned long long** nedges_dev = nullptr);
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
                   const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out);
 // Exact-stage distance and probability of given pairs (original indices).
 int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64_t m, double* dist, double* prob);
 // blk_K: optional per-256-row-block max_edges (each <= max_edges <= 512).
+// ne_dev: the edge count on the device (ne is then its cap); the total is
+// then left in the device outptr[n] and *n_out is 0.
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
-                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K = nullptr);
+                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K = nullptr,
+                const unsigned long long* ne_dev = nullptr);
 int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
               double* d_stnf, uint64_t total);
 
@@ -176,7 +193,8 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
-               uint64_t tbl_stride = 0, int bn = 0);
+               uint64_t tbl_stride = 0, int bn = 0, unsigned long long fixed_cap = 0,
+               unsigned long long** cnt_dev = nullptr);
 // Tile-shape autotuner: run(bn) performs one filter pass with column tiles
 // of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
 // keeps the faster (the later pass's output stands); later passes use it.

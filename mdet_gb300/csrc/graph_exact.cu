@@ -27,6 +27,7 @@ struct ExactArgs {
     double L;
     ff Lff;
     const BlkCut* blk_L;  // optional per-256-row-block cutoff
+    const unsigned long long* ncand_dev;  // optional device candidate count (ncand is then its cap)
     // graph outputs
     Edge* edges;
     unsigned long long* nedges;
@@ -98,6 +99,7 @@ __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigne
 __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
     __shared__ uint32_t wcount[8];
     __shared__ unsigned long long bbase;
+    if (p.ncand_dev) p.ncand = min(*p.ncand_dev, p.ncand);
     const bool model2 = p.L < kLn9;
     const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     // the block takes 256 candidates per round (32 per warp), so every warp
@@ -176,9 +178,11 @@ __global__ void k_pair_scores(const uint64_t* __restrict__ pairs, uint64_t m, co
     }
 }
 
-__global__ void k_scatter(const Edge* __restrict__ edges, unsigned long long ne, const uint32_t* __restrict__ perm,
+__global__ void k_scatter(const Edge* __restrict__ edges, unsigned long long ne_cap,
+                          const unsigned long long* __restrict__ ne_dev, const uint32_t* __restrict__ perm,
                           const unsigned long long* __restrict__ rowptr, uint32_t* __restrict__ cursor,
                           Ent* __restrict__ list) {
+    const unsigned long long ne = ne_dev ? min(*ne_dev, ne_cap) : ne_cap;
     for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < ne;
          e += (unsigned long long)gridDim.x * blockDim.x) {
         Edge ed = edges[e];
@@ -620,7 +624,8 @@ __global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long
 // ------------------------------------------------------------ host side --
 
 int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand, double L,
-                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out, const BlkCut* blk_L) {
+                Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out, const BlkCut* blk_L,
+                const unsigned long long* ncand_dev, unsigned long long** nedges_dev) {
     cudaStream_t s = ctx->stream;
     Edge* edges = (Edge*)ctx_scratch(ctx, "ex.edges", (ncand ? ncand : 1) * sizeof(Edge));
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "ex.cnt", 8);
@@ -640,6 +645,7 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.Lff.hi = (float)L;
         p.Lff.lo = (float)(L - (double)p.Lff.hi);
         p.blk_L = blk_L;
+        p.ncand_dev = ncand_dev;
         p.edges = edges;
         p.nedges = cnt;
         p.deg = deg;
@@ -657,12 +663,20 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
             MDET_LAUNCHED(ctx, "k_exact_graph");
             return MDET_OK;
         };
-        MDET_TRY(launch_autotune(ctx, ctx->exact_shape, tc_shape_key(false, false, ncand, g.n), {8, 4, 2}, run));
+        if (ctx->forced_exact)
+            MDET_TRY(run(ctx->forced_exact));
+        else
+            MDET_TRY(launch_autotune(ctx, ctx->exact_shape, tc_shape_key(false, false, ncand, g.n), {8, 4, 2}, run));
+    }
+    *edges_out = edges;
+    *deg_out = deg;
+    if (nedges_dev) {  // counts stay on the device (capturable); ncand bounds the edges
+        *nedges_dev = cnt;
+        *nedges_out = ncand;
+        return MDET_OK;
     }
     MDET_CUDA(ctx, cudaMemcpyAsync(nedges_out, cnt, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    *edges_out = edges;
-    *deg_out = deg;
     return MDET_OK;
 }
 
@@ -704,7 +718,7 @@ int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64
 }
 
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
-                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K) {
+                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K, const unsigned long long* ne_dev) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = g.n;
     unsigned long long* rowptr = (unsigned long long*)ctx_scratch(ctx, "tk.rowptr", ((uint64_t)n + 1) * 8);
@@ -730,7 +744,8 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
     if (ne) {
         unsigned long long blocks = (ne + 255) / 256, cap = (unsigned long long)ctx->num_sms * 16;
         ctx_timer_begin(ctx, "k_scatter");
-        k_scatter<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(edges, ne, g.perm, rowptr, cursor, list);
+        k_scatter<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(edges, ne, ne_dev, g.perm, rowptr, cursor,
+                                                                           list);
         ctx_timer_end(ctx, "k_scatter");
         MDET_LAUNCHED(ctx, "k_scatter");
     }
@@ -768,6 +783,10 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
     k_widen<<<wblocks, 256, 0, s>>>(out_cnt, n, w64);
     MDET_LAUNCHED(ctx, "k_widen");
     MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, w64, outptr, (int)n + 1, s));
+    if (ne_dev) {  // capturable: the total stays on the device (outptr[n])
+        *n_out = 0;
+        return MDET_OK;
+    }
     unsigned long long total = 0;
     MDET_CUDA(ctx, cudaMemcpyAsync(&total, outptr + n, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));

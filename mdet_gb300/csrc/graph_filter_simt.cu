@@ -66,6 +66,10 @@ __global__ void __launch_bounds__(TH, 2) k_filter_simt(SimtArgs p) {
         // tile threshold
         BlockMeta ma = p.ameta[I], mb = p.bmeta[J];
         DstarTable tb = p.tbl;
+        if (tb.dyn) {
+            tb.lmin = tb.dyn[0];
+            tb.inv_h = tb.dyn[1];
+        }
         if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[I] * p.tbl_stride;
         float T = tile_dstar(tb, ma.lo, ma.hi, mb.lo, mb.hi);
         float R = T * (1.f + 2e-5f) + 1e-6f;

@@ -391,6 +391,10 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                 const BlockMeta mb0 = p.bmeta[kBlk * c.J], mb1 = p.bmeta[kBlk * c.J + kBlk - 1];
                 const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
                 DstarTable tb = p.tbl;
+                if (tb.dyn) {
+                    tb.lmin = tb.dyn[0];
+                    tb.inv_h = tb.dyn[1];
+                }
                 if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I * S::MH + mh] * p.tbl_stride;
                 const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
                 const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);

@@ -217,6 +217,36 @@ __global__ void k_dstar_points(double lmin, double h, double L, ModelSplit ms, f
     pts[a * kPts + b] = __double2float_ru(d);
 }
 
+// the same points on a grid held in device memory
+__global__ void k_dstar_points_dev(const TableGrid* __restrict__ grid, double L, ModelSplit ms, float* __restrict__ pts) {
+    int a = blockIdx.y, b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= kPts) return;
+    int lo = min(a, b), hi = max(a, b);
+    const double lmin = grid->lmin, h = grid->h;
+    double x = lmin + lo * (h / 4), y = lmin + hi * (h / 4);
+    double d = dev_dstar(x, y, L, ms);
+    pts[a * kPts + b] = __double2float_ru(d);
+}
+
+// union of (lo, hi) ranges -> table grid (one thread)
+__global__ void k_grid_from_ranges(const double* __restrict__ r, uint32_t count, TableGrid* __restrict__ g) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double lo = INFINITY, hi = -INFINITY;
+    for (uint32_t k = 0; k < count; ++k)
+        if (r[2 * k] <= r[2 * k + 1]) {
+            lo = fmin(lo, r[2 * k]);
+            hi = fmax(hi, r[2 * k + 1]);
+        }
+    if (!(lo <= hi)) lo = hi = 0;
+    double h = (hi - lo) / MDET_TBL;
+    if (!(h > 1e-7)) h = 1e-7;
+    lo -= 1e-9;
+    g->lmin = lo;
+    g->h = h;
+    g->lminf = (float)lo;
+    g->inv_hf = (float)(1.0 / h);
+}
+
 __global__ void k_dstar_cells(const float* __restrict__ pts, float* __restrict__ st0) {
     int a = blockIdx.x, b = threadIdx.x;
     float mx = -__int_as_float(0x7f800000), mn = __int_as_float(0x7f800000);
@@ -393,6 +423,7 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
 
 int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out) {
     cudaStream_t s = ctx->stream;
+    out->dyn = nullptr;
     float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
     if (!pts) return MDET_ERR_NOMEM;
     double h = (lmax - lmin) / MDET_TBL;
@@ -415,8 +446,37 @@ int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_c
     return MDET_OK;
 }
 
+int grid_from_ranges(mdet_ctx* ctx, const double* ranges, uint32_t count, TableGrid* grid) {
+    k_grid_from_ranges<<<1, 32, 0, ctx->stream>>>(ranges, count, grid);
+    MDET_LAUNCHED(ctx, "k_grid_from_ranges");
+    return MDET_OK;
+}
+
+int build_dstar_table_dev(mdet_ctx* ctx, const TableGrid* grid, double logit_cut, float* st, DstarTable* out) {
+    cudaStream_t s = ctx->stream;
+    float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
+    if (!pts) return MDET_ERR_NOMEM;
+    dim3 g((kPts + 127) / 128, kPts);
+    k_dstar_points_dev<<<g, 128, 0, s>>>(grid, logit_cut, model_split(), pts);
+    MDET_LAUNCHED(ctx, "k_dstar_points");
+    k_dstar_cells<<<MDET_TBL, MDET_TBL, 0, s>>>(pts, st);
+    MDET_LAUNCHED(ctx, "k_dstar_cells");
+    k_suffix_x<<<1, MDET_TBL, 0, s>>>(st);
+    MDET_LAUNCHED(ctx, "k_suffix_x");
+    for (int k = 1; k < MDET_TBL_LEVELS; ++k) {
+        k_sparse<<<MDET_TBL, MDET_TBL, 0, s>>>(st, k);
+        MDET_LAUNCHED(ctx, "k_sparse");
+    }
+    out->st = st;
+    out->lmin = 0.f;
+    out->inv_h = 0.f;
+    out->dyn = &grid->lminf;
+    return MDET_OK;
+}
+
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
                       bool sorted) {
+    out->dyn = nullptr;
     cudaStream_t s = ctx->stream;
     double* mm = (double*)ctx_scratch(ctx, "tbl.mm", 16);
     float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);

@@ -141,6 +141,8 @@ SIGNATURES = [
     ("mdet_tnf_pair_scores_dev", ctypes.c_int, [P, P, P, u64, P, u64, P, P]),
     ("mdet_tnf_graph_batched", ctypes.c_int, [P, ctypes.POINTER(Assembly), u32, ctypes.c_int,
                                               ctypes.POINTER(GraphStats)]),
+    ("mdet_ctx_set_graph_capture", ctypes.c_int, [P, ctypes.c_int]),
+    ("mdet_ctx_graph_replays", u64, [P]),
     ("mdet_mlp_create", ctypes.c_int, [P, u64, ctypes.POINTER(P)]),
     ("mdet_mlp_destroy", ctypes.c_int, [P]),
     ("mdet_mlp_param_count", u64, []),
@@ -361,6 +363,12 @@ class Context:
         return [(a.status, a.n_edges) for a in arr], stats.as_dict()
 
     gen_tnf_graph_batched = tnf_graph_batched
+
+    def set_graph_capture(self, enable: bool):
+        self._check(self.lib.mdet_ctx_set_graph_capture(self.h, 1 if enable else 0))
+
+    def graph_replays(self) -> int:
+        return int(self.lib.mdet_ctx_graph_replays(self.h))
 
     # ---- learned proposal -----------------------------------------------
     def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 2048,

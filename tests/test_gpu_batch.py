@@ -76,6 +76,48 @@ def test_batch_equals_single(gpu_ctx, batch_inputs, mode):
     assert total > 0 and stats["n_edges"] == total
 
 
+def test_recorded_batch_replays_with_new_data(gpu_ctx, batch_inputs):
+    """Three calls with the same buffers: the first runs the sized path and
+    records the batch, the next two replay the recording.  Then the inputs
+    change in place (same sizes) and the replay must follow them."""
+    import torch
+
+    outs, items = [], []
+    for x in batch_inputs:
+        o = _outputs(torch, x["n"], x["max_edges"])
+        outs.append(o)
+        items.append(dict(d_tnf=x["d_tnf"].data_ptr(), d_ls=x["d_ls"].data_ptr(), n=x["n"], cutoff=x["cutoff"],
+                          max_edges=x["max_edges"], d_from=o[0].data_ptr(), d_to=o[1].data_ptr(),
+                          d_stnf=o[2].data_ptr(), capacity=o[3]))
+    singles = [_single(gpu_ctx, torch, x, "bf16") for x in batch_inputs]
+    r0 = gpu_ctx.graph_replays()
+    for call in range(3):
+        res, _ = gpu_ctx.tnf_graph_batched(items, mode="bf16")
+        for (status, ne), o, (f, t, st) in zip(res, outs, singles):
+            assert status == 0 and ne == f.size
+            assert np.array_equal(o[1][:ne].cpu().numpy(), t) and np.array_equal(o[2][:ne].cpu().numpy(), st)
+    assert gpu_ctx.graph_replays() == r0 + 2
+    # new data in the same buffers: reverse the rows of every assembly
+    saved = [(x["d_tnf"].clone(), x["d_ls"].clone()) for x in batch_inputs]
+    try:
+        for x in batch_inputs:
+            x["d_tnf"].copy_(torch.flip(x["d_tnf"], [0]))
+            x["d_ls"].copy_(torch.flip(x["d_ls"], [0]))
+        torch.cuda.synchronize()
+        res, _ = gpu_ctx.tnf_graph_batched(items, mode="bf16")
+        assert gpu_ctx.graph_replays() == r0 + 3
+        for x, (status, ne), o in zip(batch_inputs, res, outs):
+            f, t, st = _single(gpu_ctx, torch, x, "bf16")
+            assert status == 0 and ne == f.size
+            assert np.array_equal(o[0][:ne].cpu().numpy(), f)
+            assert np.array_equal(o[1][:ne].cpu().numpy(), t) and np.array_equal(o[2][:ne].cpu().numpy(), st)
+    finally:
+        for x, (a, b) in zip(batch_inputs, saved):
+            x["d_tnf"].copy_(a)
+            x["d_ls"].copy_(b)
+        torch.cuda.synchronize()
+
+
 def test_batch_capacity_shortfall(gpu_ctx, batch_inputs):
     import torch
 

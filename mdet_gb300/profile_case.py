@@ -4,6 +4,8 @@
   python -m mdet_gb300.profile_case graph --n 500000     pairwise stage (bf16 or plain)
   python -m mdet_gb300.profile_case learned --n 500000   network trained on a second
                                                           assembly, then the learned graph
+  python -m mdet_gb300.profile_case batch --count 64      many assemblies, n ~ logU(nmin, nmax):
+                                                          one call per assembly vs one batched call
 
 The graph case frees the FASTA before the pairwise call so that only the
 stage's own buffers (~1-2 GB) are resident when it runs.
@@ -20,7 +22,10 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("stage", choices=["count", "graph", "learned"])
+    ap.add_argument("stage", choices=["count", "graph", "learned", "batch"])
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--nmin", type=int, default=5000)
+    ap.add_argument("--nmax", type=int, default=300000)
     ap.add_argument("--train-n", type=int, default=200000)
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--segs", default="1024", help="comma-separated size-sorted run lengths to try")
@@ -35,10 +40,12 @@ def main():
     import mdet_gb300 as m
     from mdet_gb300 import synth
 
-    G = args.genomes or max(10, args.n // 500)
-    a = synth.generate(3, args.n, G)
     ctx = m.Context(0)
     dev = torch.device("cuda:0")
+    if args.stage == "batch":
+        return batch_case(args, m, synth, ctx, dev, torch)
+    G = args.genomes or max(10, args.n // 500)
+    a = synth.generate(3, args.n, G)
     nb = a.data.size
     d_bytes = torch.zeros(nb + 64, dtype=torch.uint8, device=dev)
     d_bytes[:nb].copy_(torch.from_numpy(a.data))
@@ -95,6 +102,61 @@ def main():
                                        out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
         print({"edges": ne, **{k: st[k] for k in ("n_candidates", "ms_filter", "ms_total")}})
     torch.cuda.synchronize()
+    ctx.close()
+
+
+def batch_case(args, m, synth, ctx, dev, torch):
+    """Assemblies of n ~ logU(nmin, nmax) contigs, 20-800 genomes each (each
+    one's TNF counted on the GPU, its FASTA freed), then the graphs: one call
+    per assembly, and the batched call (sized run + recording, then replays)."""
+    import time
+
+    rng = np.random.default_rng(44)
+    sizes = np.exp(rng.uniform(np.log(args.nmin), np.log(args.nmax), args.count)).astype(np.int64)
+    genomes = np.clip((sizes / 400).astype(np.int64), 20, 800)
+    tnfs, lss = [], []
+    t0 = time.time()
+    for k, (n, G) in enumerate(zip(sizes, genomes)):
+        a = synth.generate(1000 + k, int(n), int(G))
+        nb = a.data.size
+        d_bytes = torch.zeros(nb + 64, dtype=torch.uint8, device=dev)
+        d_bytes[:nb].copy_(torch.from_numpy(a.data))
+        d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+        d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+        d_cnt = torch.empty((int(n), 136), dtype=torch.int32, device=dev)
+        d_tnf = torch.empty((int(n), 136), dtype=torch.float32, device=dev)
+        ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), int(n), d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+        tnfs.append(d_tnf)
+        lss.append(torch.from_numpy(a.log_sizes).to(dev))
+        del d_bytes, d_cnt
+    torch.cuda.synchronize()
+    print({"assemblies": args.count, "contigs": int(sizes.sum()), "sum_n2": float((sizes.astype(np.float64) ** 2).sum()),
+           "prep_s": round(time.time() - t0, 1)})
+    K, cut = 200, 0.9
+    outs = [[torch.empty(int(n) * K, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+            for n in sizes]
+    items = [dict(d_tnf=t.data_ptr(), d_ls=l.data_ptr(), n=int(n), cutoff=cut, max_edges=K, d_from=o[0].data_ptr(),
+                  d_to=o[1].data_ptr(), d_stnf=o[2].data_ptr(), capacity=int(n) * K)
+             for t, l, n, o in zip(tnfs, lss, sizes, outs)]
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        tot = 0
+        for t, l, n, o in zip(tnfs, lss, sizes, outs):
+            ne, st = ctx.tnf_graph_dev(t.data_ptr(), l.data_ptr(), int(n), cut, K, "bf16", o[0].data_ptr(),
+                                       o[1].data_ptr(), o[2].data_ptr(), int(n) * K)
+            tot += ne
+        torch.cuda.synchronize()
+        print({"per_assembly_calls_s": round(time.time() - t0, 4), "edges": tot})
+    for rep in range(5):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        res, st = ctx.tnf_graph_batched(items, mode="bf16")
+        torch.cuda.synchronize()
+        print({"batched_call_s": round(time.time() - t0, 4), "edges": sum(r[1] for r in res),
+               "replays": ctx.graph_replays(), "gpu_launches": st["gpu_launches"], "tile": st["tile_m_n"],
+               "candidates": st["n_candidates"]})
     ctx.close()
 
 

@@ -254,11 +254,17 @@ def run_ours(args):
     e2e_info = {}
 
     def step_e2e():
+        t0 = time.perf_counter()
         ctx.tnf_count(data_h, off_h, len_h, out=(cnt_h, tnf_h))
+        t1 = time.perf_counter()
         libc.srand(12345)
         p = ctx.ptnf_search(tnf_h, ls_h, MAXP / 100.0, args.mode)
+        t2 = time.perf_counter()
         g = ctx.tnf_graph(tnf_h, ls_h, p / 1000.0, MAX_EDGES, args.mode, out=(from_h, to_h, st_h))
+        t3 = time.perf_counter()
         e2e_info["edges"] = g.getEdgeCount()
+        e2e_info["phases_s"] = {"count": round(t1 - t0, 4), "ptnf_search": round(t2 - t1, 4),
+                                "graph": round(t3 - t2, 4)}
 
     e2e_steps = max(1, min(args.steps, 3))
     step_e2e()
@@ -321,7 +327,8 @@ def run_ours(args):
             "dtype": "bf16",
             "data": "synthetic (seeded Markov-genome assembly; no public dataset is shipped)",
             "config": workload_config(n, G, args.mode, ws),
-            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "phases_s": e2e_info.get("phases_s")},
             "gpu_launches": int(launches),
             "roofline": roof,
             "count_roofline": count_roof,

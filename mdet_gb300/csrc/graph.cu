@@ -165,7 +165,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride, int bn,
-               unsigned long long fixed_cap, unsigned long long** cnt_dev) {
+               unsigned long long fixed_cap, unsigned long long** cnt_dev, const unsigned long long* rowoff) {
     cudaStream_t s = ctx->stream;
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
     if (!cnt) return MDET_ERR_NOMEM;
@@ -181,7 +181,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                                  g.meta32, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride));
         } else {
             MDET_TRY(filter_tc(ctx, rect ? ab : g.xa, rect ? ansq : g.nsq, rect ? na : g.n, rect ? ameta : g.meta, g.xb,
-                               g.n, g.meta, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride, bn ? bn : 256));
+                               g.n, g.meta, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride, bn ? bn : 256, rowoff));
         }
         *cand_out = cand;
         *ncand_out = fixed_cap;
@@ -208,7 +208,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                 const uint16_t* A = rect ? ab : g.xa;
                 const float* An = rect ? ansq : g.nsq;
                 MDET_TRY(filter_tc(ctx, A, An, rect ? na : g.n, rect ? ameta : g.meta, g.xb, g.n, g.meta, !rect, tbl,
-                                   out, tiles, nlist, row_tbl, tbl_stride, w));
+                                   out, tiles, nlist, row_tbl, tbl_stride, w, rowoff));
                 ctx->last_tile_n = w == kShapeTall ? 256128 : 128 * 1000 + w;
             }
             return MDET_OK;

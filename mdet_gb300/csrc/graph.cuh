@@ -151,12 +151,14 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
 // padding rows).
 // tiles/nlist: optional row-major list (I * tiles_b + J) of the tile pairs
 // to evaluate (column tiles of bn); null evaluates the whole schedule.
+// rowoff (with a list): entries of row tile I are [rowoff[I], rowoff[I+1]),
+// and row tiles are taken in the waves of the full schedule.
 // bn: tile shape: 256 = 128 x 256 tiles (one CTA per SM), 128 = 128 x 128
 // (two per SM), kShapeTall = 256 x 128 with four B stages (no tile lists).
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
-              uint64_t tbl_stride = 0, int bn = 256);
+              uint64_t tbl_stride = 0, int bn = 256, const unsigned long long* rowoff = nullptr);
 // Cutoff of one 256-row block of a batch: logit(cutoff) in float-float and
 // whether the second model is needed (logit(cutoff) < ln 9, decided in FP64).
 struct BlkCut {
@@ -194,7 +196,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
                uint64_t tbl_stride = 0, int bn = 0, unsigned long long fixed_cap = 0,
-               unsigned long long** cnt_dev = nullptr);
+               unsigned long long** cnt_dev = nullptr, const unsigned long long* rowoff = nullptr);
 // Tile-shape autotuner: run(bn) performs one filter pass with column tiles
 // of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
 // keeps the faster (the later pass's output stands); later passes use it.

@@ -170,7 +170,7 @@ int upload_sides(mdet_ctx* ctx, const mdet_assembly* as, const Layout& L, Dev& d
     d.bA = (uint32_t*)ctx_scratch(ctx, "bt.bA", (uint64_t)L.nblk256 * 4);
     d.j0 = (uint32_t*)ctx_scratch(ctx, "bt.j0", (uint64_t)L.nrt * 4);
     d.j1 = (uint32_t*)ctx_scratch(ctx, "bt.j1", (uint64_t)L.nrt * 4);
-    d.off = (unsigned long long*)ctx_scratch(ctx, "bt.off", (uint64_t)L.nrt * 8);
+    d.off = (unsigned long long*)ctx_scratch(ctx, "bt.off", ((uint64_t)L.nrt + 1) * 8);
     d.bo = (BatchOut*)ctx_scratch(ctx, "bt.bo", count * sizeof(BatchOut));
     d.status = (int*)ctx_scratch(ctx, "bt.status", count * 4);
     d.tbl = (float*)ctx_scratch(ctx, "bt.tbl", L.tab_of.size() * MDET_TBL_FLOATS * 4);
@@ -239,7 +239,7 @@ int build_list(mdet_ctx* ctx, const Layout& L, Dev& d, int w, uint64_t* nlist) {
     if (!d.list) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cudaMemcpyAsync(d.j0, j0.data(), L.nrt * 4, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(d.j1, j1.data(), L.nrt * 4, cudaMemcpyHostToDevice, s));
-    MDET_CUDA(ctx, cudaMemcpyAsync(d.off, off.data(), L.nrt * 8, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(d.off, off.data(), ((uint64_t)L.nrt + 1) * 8, cudaMemcpyHostToDevice, s));
     k_tile_list<<<L.nrt, 128, 0, s>>>(d.j0, d.j1, d.off, (uint32_t)(L.N / w), d.list);
     MDET_LAUNCHED(ctx, "k_tile_list");
     MDET_CUDA(ctx, cudaStreamSynchronize(s));  // the host arrays die here
@@ -287,7 +287,7 @@ int device_pass(mdet_ctx* ctx, const mdet_assembly* as, const Layout& L, int mod
     uint2* cand = nullptr;
     unsigned long long ncap = 0, *ncand_dev = nullptr, *ne_dev = nullptr;
     MDET_TRY(run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "bt", &cand, &ncap,
-                        d.list, nlist, d.rtbl, MDET_TBL_FLOATS, shape, cap, &ncand_dev));
+                        d.list, nlist, d.rtbl, MDET_TBL_FLOATS, shape, cap, &ncand_dev, d.off));
     Edge* edges = nullptr;
     unsigned long long ecap = 0;
     uint32_t* deg = nullptr;
@@ -490,7 +490,7 @@ extern "C" int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* as, uint32_t
             auto run = [&](int w) -> int {
                 MDET_TRY(build_list(ctx, L, d, w, &nlist));
                 return run_filter(ctx, mode, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "bt",
-                                  &cand, &ncand, d.list, nlist, d.rtbl, MDET_TBL_FLOATS, w);
+                                  &cand, &ncand, d.list, nlist, d.rtbl, MDET_TBL_FLOATS, w, 0, nullptr, d.off);
             };
             if (bf16)
                 MDET_TRY(tc_autotune(ctx, tc_shape_key(false, true, L.N, L.N), run, true));

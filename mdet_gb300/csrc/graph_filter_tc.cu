@@ -69,6 +69,7 @@ struct TcArgs {
     uint32_t jnum, jden;  // the first column tile of row tile I is I * jnum / jden (BM / 128, BN / 128)
     const uint32_t* tiles;  // optional list of tiles (I * tb + J, row-major); null: full schedule
     uint64_t nlist;
+    const unsigned long long* rowoff;  // optional: list entries of row tile I are [rowoff[I], rowoff[I+1])
     const uint8_t* row_tbl;  // optional table index per row tile (tables tbl_stride floats apart)
     uint64_t tbl_stride;
     int triangular;
@@ -207,8 +208,34 @@ __device__ __forceinline__ void list_decode(const TcArgs& p, Cursor& k) {
     }
 }
 
+// Wave-ordered list: row tiles in the waves of the full schedule, each row
+// tile's listed column tiles in order (so concurrent CTAs sweep the same B
+// tiles, as in the full schedule).  Moves to the first non-empty row tile
+// from wave k.w on.
+__device__ __forceinline__ void list_next_row(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G) {
+    while (true) {
+        const uint32_t I = unit_of_wave(k.w, c, G);
+        if (I >= p.ta) {
+            k.valid = false;
+            return;
+        }
+        k.li = p.rowoff[I];
+        k.lend = p.rowoff[I + 1];
+        if (k.li < k.lend) {
+            list_decode(p, k);
+            return;
+        }
+        ++k.w;
+    }
+}
+
 __device__ __forceinline__ Cursor cursor_first(const TcArgs& p, uint32_t c, uint32_t G) {
     Cursor k;
+    if (p.tiles && p.rowoff) {
+        k.w = 0;
+        list_next_row(p, k, c, G);
+        return k;
+    }
     if (p.tiles) {
         // list mode: CTA c takes a contiguous range of the row-major list
         k.li = p.nlist * c / G;
@@ -223,6 +250,15 @@ __device__ __forceinline__ Cursor cursor_first(const TcArgs& p, uint32_t c, uint
 }
 
 __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, uint32_t G) {
+    if (p.tiles && p.rowoff) {
+        if (++k.li < k.lend) {
+            list_decode(p, k);
+            return;
+        }
+        ++k.w;
+        list_next_row(p, k, c, G);
+        return;
+    }
     if (p.tiles) {
         ++k.li;
         list_decode(p, k);
@@ -528,7 +564,8 @@ int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t row
 template <int BM, int BN, int NST>
 int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
-              CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride) {
+              CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride,
+              const unsigned long long* rowoff) {
     using S = Shape<BM, BN, NST>;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
     CUtensorMap mA128, mA32, mB128, mB32;
@@ -563,10 +600,12 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     while ((uint64_t)p.ta * p.segs < 2ull * ctas && p.segs < p.tb) ++p.segs;
     p.tiles = tiles;
     p.nlist = nlist;
+    p.rowoff = tiles ? rowoff : nullptr;
     p.row_tbl = row_tbl;
     p.tbl_stride = tbl_stride;
-    const unsigned grid =
+    unsigned grid =
         (unsigned)std::min<unsigned long long>(ctas, tiles ? nlist : (unsigned long long)p.ta * p.segs);
+    if (p.rowoff) grid = (unsigned)std::min<unsigned long long>(grid, p.ta);  // one row tile per CTA and wave
     if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
     k_filter_tc<BM, BN, NST><<<grid, S::kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
@@ -580,16 +619,16 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
 int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
               const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride,
-              int bn) {
+              int bn, const unsigned long long* rowoff) {
     if (na == 0 || nb == 0) return MDET_OK;
     if (bn == 128)
         return launch_tc<128, 128, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                      row_tbl, tbl_stride);
+                                      row_tbl, tbl_stride, rowoff);
     if (bn == kShapeTall) {
         if (tiles) return ctx_fail(ctx, MDET_ERR_INVALID, "tile lists use 128-row tiles");
         return launch_tc<256, 128, 4>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                      row_tbl, tbl_stride);
+                                      row_tbl, tbl_stride, rowoff);
     }
     return launch_tc<128, 256, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                  row_tbl, tbl_stride);
+                                  row_tbl, tbl_stride, rowoff);
 }

@@ -197,6 +197,23 @@ __global__ void k_seg_keys(const uint32_t* __restrict__ order, const double* __r
     vals[p] = o;
 }
 
+// kept tiles per row tile (block per row tile), widened for the scan
+__global__ void k_row_kept(const uint8_t* __restrict__ keep, uint32_t tb, unsigned long long* __restrict__ cnt) {
+    __shared__ uint32_t part[8];
+    const uint32_t I = blockIdx.x;
+    uint32_t c = 0;
+    for (uint32_t J = threadIdx.x; J < tb; J += blockDim.x) c += keep[(uint64_t)I * tb + J];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        cnt[I] = t;
+    }
+}
+
 __global__ void k_sample_rows(uint32_t n, uint32_t m, uint32_t* __restrict__ rows) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < m) rows[k] = (uint32_t)(((uint64_t)k * 2 + 1) * n / (2ull * m));
@@ -464,11 +481,25 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     if (recall < target) return fallback(recall, tau);
     tm.mark();
 
+    // list entries per row tile, so the filter takes row tiles in waves
+    unsigned long long* rowcnt = (unsigned long long*)ctx_scratch(ctx, "lrn.rowcnt", ((uint64_t)ta + 1) * 8);
+    unsigned long long* rowoff = (unsigned long long*)ctx_scratch(ctx, "lrn.rowoff", ((uint64_t)ta + 1) * 8);
+    if (!rowcnt || !rowoff) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(rowcnt + ta, 0, 8, s));
+    k_row_kept<<<ta, 256, 0, s>>>(keep, tb, rowcnt);
+    MDET_LAUNCHED(ctx, "k_row_kept");
+    {
+        size_t tmpb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tmpb, rowcnt, rowoff, (int)ta + 1, s);
+        void* tmp = ctx_scratch(ctx, "lrn.scantmp", tmpb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tmpb, rowcnt, rowoff, (int)ta + 1, s));
+    }
     uint2* cand = nullptr;
     unsigned long long ncand = 0;
     if (hsel > 0)
         MDET_TRY(run_filter(ctx, MDET_MODE_BF16, g, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "g",
-                            &cand, &ncand, list, (uint64_t)hsel));
+                            &cand, &ncand, list, (uint64_t)hsel, nullptr, 0, 256, 0, nullptr, rowoff));
     tm.mark();
     Edge* edges = nullptr;
     unsigned long long ne = 0;

@@ -142,13 +142,14 @@ def batch_case(args, m, synth, ctx, dev, torch):
     for rep in range(2):
         torch.cuda.synchronize()
         t0 = time.time()
-        tot = 0
+        tot = cands = 0
         for t, l, n, o in zip(tnfs, lss, sizes, outs):
             ne, st = ctx.tnf_graph_dev(t.data_ptr(), l.data_ptr(), int(n), cut, K, "bf16", o[0].data_ptr(),
                                        o[1].data_ptr(), o[2].data_ptr(), int(n) * K)
             tot += ne
+            cands += st["n_candidates"]
         torch.cuda.synchronize()
-        print({"per_assembly_calls_s": round(time.time() - t0, 4), "edges": tot})
+        print({"per_assembly_calls_s": round(time.time() - t0, 4), "edges": tot, "candidates": cands})
     for rep in range(5):
         torch.cuda.synchronize()
         t0 = time.time()

@@ -162,13 +162,26 @@ static __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t par
     return ok != 0;
 }
 
+// try_wait with a suspend-time hint (ns): the thread sleeps until the phase
+// completes or the hint runs out instead of polling, so waiting warps leave
+// their issue slots to the working ones.
+static __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait: returns false (and raises the device flag) when the budget
 // runs out, so no wait in this library can spin forever.
 static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* flag) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_suspend(bar, parity)) return true;
         if ((unsigned long long)(clock64() - t0) > MDET_SPIN_CYCLES) {
             if (flag) atomicOr(flag, MDET_FLAG_TIMEOUT);
             return false;

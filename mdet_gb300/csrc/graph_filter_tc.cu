@@ -88,6 +88,7 @@ struct __align__(8) Ctl {
     uint64_t acc_full[2], acc_empty[2];
     uint32_t tmem_base;
     uint32_t qcount[kMaxEpiWarps];
+    float r2[2];  // one-half shapes: R^2 of the tile in each accumulator
 };
 
 // ---------------------------------------------------------------- PTX --
@@ -162,6 +163,32 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
         : "memory");
 #pragma unroll
     for (int k = 0; k < 64; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+// Squared pass radius of row block ib against column tile J:
+// R = d*_tile + e_a + e_b + slack, where d*_tile bounds the model's distance
+// threshold over the blocks' sizes, e_a and e_b bound the BF16 rounding of the
+// rows, and the slack covers FP32 accumulation and the two-term split of
+// ||b~||^2/2.
+template <int BN>
+__device__ __forceinline__ float tile_r2(const TcArgs& p, uint32_t ib, uint32_t J) {
+    const BlockMeta ma = p.ameta[ib];
+    constexpr uint32_t kBlk = BN / MDET_BLK;  // metadata blocks per column tile
+    const BlockMeta mb0 = p.bmeta[kBlk * J], mb1 = p.bmeta[kBlk * J + kBlk - 1];
+    const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
+    DstarTable tb = p.tbl;
+    if (tb.dyn) {
+        tb.lmin = tb.dyn[0];
+        tb.inv_h = tb.dyn[1];
+    }
+    if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[ib] * p.tbl_stride;
+    const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
+    const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
+    const float nb = fmaxf(mb0.nmax, mb1.nmax);
+    const float R = T * (1.f + 2e-5f) + 1e-6f + E;
+    float R2 = R * R + 4e-5f * (ma.nmax * nb + nb * nb) + 1e-7f;
+    if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
+    return R2;
 }
 
 // ------------------------------------------------------------ schedule --
@@ -301,7 +328,8 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
             mbar_init(&ctl.b_empty[s], 1);
         }
         for (int s = 0; s < 2; ++s) {
-            mbar_init(&ctl.acc_full[s], 1);
+            // one-half shapes: the MMA commit and the tile's R^2 written
+            mbar_init(&ctl.acc_full[s], S::MH == 1 ? 2 : 1);
             mbar_init(&ctl.acc_empty[s], S::kEpi * 32);
         }
         for (int w = 0; w < S::kEpi; ++w) ctl.qcount[w] = 0;
@@ -401,6 +429,13 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                     }
                     mma_commit(&ctl.b_empty[bs]);
                     mma_commit(&ctl.acc_full[s]);
+                    if constexpr (S::MH == 1) {
+                        // the tile's R^2 for the epilogue, loaded while the MMAs
+                        // run (this thread would otherwise wait); the epilogue of
+                        // the tile that used this slot before is done (acc_empty)
+                        ctl.r2[s] = tile_r2<BN>(p, c.I, c.J);
+                        mbar_arrive(&ctl.acc_full[s]);
+                    }
                     Cursor nx = c;
                     advance(p, nx, cta, G);
                     if (!nx.valid || nx.I != c.I) mma_commit(&ctl.a_empty);
@@ -418,37 +453,27 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
             uint2* q = queue[ew];
             Cursor c = cursor_first(p, cta, G);
             uint32_t f_ph[2] = {0, 0};
+            uint32_t curI = 0xFFFFFFFFu;
+            float ansq = 0.f;
             for (uint32_t lt = 0; c.valid; ++lt, advance(p, c, cta, G)) {
                 const uint32_t s = lt & 1;
                 const uint32_t row = c.I * BM + mh * 128 + quarter * 32 + lane;
-                // tile threshold (per M half)
-                const BlockMeta ma = p.ameta[c.I * S::MH + mh];
-                constexpr uint32_t kBlk = BN / MDET_BLK;  // metadata blocks per column tile
-                const BlockMeta mb0 = p.bmeta[kBlk * c.J], mb1 = p.bmeta[kBlk * c.J + kBlk - 1];
-                const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
-                DstarTable tb = p.tbl;
-                if (tb.dyn) {
-                    tb.lmin = tb.dyn[0];
-                    tb.inv_h = tb.dyn[1];
-                }
-                if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[c.I * S::MH + mh] * p.tbl_stride;
-                const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
-                const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
-                const float N2 = ma.nmax * fmaxf(mb0.nmax, mb1.nmax);
                 // TMEM holds a~.b~ - ||b~||^2/2 (the column term rides in K
                 // columns 136/137); the pair passes when it exceeds
-                // hr = (||a~||^2 - R^2)/2.  Slack: BF16 rounding of rows (E),
-                // FP32 accumulation and the two-term split of ||b~||^2/2.
-                const float R = T * (1.f + 2e-5f) + 1e-6f + E;
-                const float NB2 = fmaxf(mb0.nmax, mb1.nmax) * fmaxf(mb0.nmax, mb1.nmax);
-                float R2 = R * R + 4e-5f * (N2 + NB2) + 1e-7f;
-                if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
-                const float hr = 0.5f * (__ldg(p.a_nsq + row) - R2);
+                // hr = (||a~||^2 - R^2)/2.  One-half shapes take R^2 from the
+                // MMA thread; the two-half shape computes it here per M half.
+                if (c.I != curI) {  // ||a~||^2 of this lane's row, once per row tile
+                    ansq = __ldg(p.a_nsq + row);
+                    curI = c.I;
+                }
+                float r2_own = 0.f;
+                if constexpr (S::MH != 1) r2_own = tile_r2<BN>(p, c.I * S::MH + mh, c.J);
                 const bool diag = p.triangular && (c.J * BN < c.I * BM + BM);
                 const bool ok = mbar_wait(&ctl.acc_full[s], f_ph[s], p.flag);
                 if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform, so tcgen05.ld stays converged
                 f_ph[s] ^= 1;
                 tc_fence_after();
+                const float hr = 0.5f * (ansq - (S::MH == 1 ? ctl.r2[s] : r2_own));
 #pragma unroll 1
                 for (uint32_t ch = 0; ch < S::kWarpCols / 64; ++ch) {
                     const uint32_t col0 = cbase + ch * 64;

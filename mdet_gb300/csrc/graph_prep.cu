@@ -39,42 +39,54 @@ __device__ __forceinline__ double poly(const double* c, int deg, double v) {
     return r;
 }
 
-// Block per position s of [0, npad) of one contig set placed at row `base`
+// Warp per position s of [0, npad) of one contig set placed at row `base`
 // of the prepared arrays (all pointers here already offset by base): perm
 // arrives with local original indices and leaves with base + local; inv is
-// the full array.  Padding positions map to themselves.
+// the full array.  Padding positions map to themselves.  The row is copied
+// by the whole warp; the nine FP64 polynomials of the model parts run on
+// nine lanes side by side (FP64 is a narrow unit here, so one long serial
+// chain per row would bound the kernel).
 __global__ void k_gather(const float* __restrict__ tnf, const double* __restrict__ ls, uint32_t* __restrict__ perm,
                          uint64_t n, uint64_t npad, uint32_t base, uint32_t* __restrict__ inv,
                          float* __restrict__ x32, double* __restrict__ ls_s, PartsFF* __restrict__ parts,
                          ModelSplit ms) {
-    uint64_t s = blockIdx.x;
+    const uint64_t s = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    const uint32_t lane = threadIdx.x & 31;
     if (s >= npad) return;
     if (s >= n) {
-        if (threadIdx.x == 0) {
+        if (lane == 0) {
             perm[s] = base + (uint32_t)s;
             inv[base + s] = base + (uint32_t)s;
         }
         return;
     }
-    const uint32_t o = perm[s];
-    __syncthreads();  // every thread has read perm[s] before it is rewritten
+    uint32_t o = 0;
+    if (lane == 0) o = perm[s];
+    o = __shfl_sync(0xffffffffu, o, 0);  // read by lane 0 before lane 0 rewrites it below
     const float* src = tnf + (uint64_t)o * MDET_NTNF;
     float* dst = x32 + s * MDET_NTNF;
-    for (int k = threadIdx.x; k < MDET_NTNF; k += blockDim.x) dst[k] = src[k];
-    if (threadIdx.x == 0) {
+    for (int k = lane; k < MDET_NTNF; k += 32) dst[k] = src[k];
+    const double v = ls[o];
+    if (lane == 0) {
         perm[s] = base + o;
         inv[base + o] = base + (uint32_t)s;
-        double v = ls[o];
         ls_s[s] = v;
-        PartsFF p;
-        for (int m = 0; m < 4; ++m) {
-            p.f[m] = ff_from_double(poly(ms.F[m], 7, v));
-            double g[7] = {0, ms.G[m][1], ms.G[m][2], ms.G[m][3], ms.G[m][4], ms.G[m][5], ms.G[m][6]};
-            p.g[m] = ff_from_double(poly(g, 6, v));
-        }
-        p.ls = ff_from_double(v);
-        p.pad[0] = p.pad[1] = 0.f;
-        parts[s] = p;
+    }
+    // lanes 0-3: f[m] = F_m(v) (degree 7); lanes 4-7: g[m] = G_m(v) without
+    // its constant (degree 6); lane 8: the log size itself
+    ff* out = reinterpret_cast<ff*>(parts + s);  // f[0..3], g[0..3], ls
+    if (lane < 4) {
+        out[lane] = ff_from_double(poly(ms.F[lane], 7, v));
+    } else if (lane < 8) {
+        const int m = lane - 4;
+        double r = ms.G[m][6];
+        for (int k = 5; k >= 1; --k) r = fma(r, v, ms.G[m][k]);
+        out[lane] = ff_from_double(r * v);
+    } else if (lane == 8) {
+        out[8] = ff_from_double(v);
+    } else if (lane == 9) {
+        parts[s].pad[0] = 0.f;
+        parts[s].pad[1] = 0.f;
     }
 }
 
@@ -119,25 +131,35 @@ __global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ 
         }
         return;
     }
-    double e2 = 0, q = 0;
+    // FP32 throughout (FP64 is a narrow unit here).  hv^2 is exact in FP32
+    // (8-bit significands), so a float-float accumulator gives ||x~||^2
+    // exactly to ~2^-44; the rounding error d = hv - (a - mu) is exact per
+    // entry up to one FP32 rounding (TwoSum of a - mu; v - hv is exact by
+    // Sterbenz), and its sum of squares is inflated before the square root
+    // is rounded up, so err stays an upper bound of ||x~ - x||.
+    float e2 = 0.f;
+    ff q = ff_make(0.f, 0.f);
     for (int k = lane; k < MDET_NTNF; k += 32) {
-        float a = x32[s * MDET_NTNF + k];
-        float v = a - mu[k];
-        __nv_bfloat16 h = __float2bfloat16_rn(v);
-        uint16_t b = *reinterpret_cast<uint16_t*>(&h);
-        double hv = (double)__bfloat162float(h);
-        double ex = (double)a - (double)mu[k];
-        e2 += (hv - ex) * (hv - ex);
-        q += hv * hv;
+        const float a = x32[s * MDET_NTNF + k];
+        const ff v = two_sum(a, -mu[k]);  // v.hi + v.lo == a - mu exactly
+        const __nv_bfloat16 h = __float2bfloat16_rn(v.hi);
+        const uint16_t b = *reinterpret_cast<const uint16_t*>(&h);
+        const float hv = __bfloat162float(h);
+        const float d = __fadd_rn(__fsub_rn(v.hi, hv), v.lo);
+        e2 = __fmaf_rn(d, d, e2);
+        q = ff_add_f(q, __fmul_rn(hv, hv));
         rowa[k] = b;
         rowb[k] = b;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-        q += __shfl_xor_sync(0xffffffffu, q, o);
+        ff t;
+        t.hi = __shfl_xor_sync(0xffffffffu, q.hi, o);
+        t.lo = __shfl_xor_sync(0xffffffffu, q.lo, o);
+        q = ff_add(q, t);
     }
-    const float half = (float)(0.5 * q);
+    const float half = 0.5f * q.hi;
     const __nv_bfloat16 hi = __float2bfloat16_rn(half);
     const __nv_bfloat16 lo = __float2bfloat16_rn(half - __bfloat162float(hi));
     const uint16_t nhi = *reinterpret_cast<const uint16_t*>(&hi) ^ 0x8000u;
@@ -147,9 +169,9 @@ __global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ 
         rowb[k] = k == MDET_NTNF ? nhi : (k == MDET_NTNF + 1 ? nlo : 0);
     }
     if (lane == 0) {
-        nsq[s] = (float)q;
-        err[s] = __double2float_ru(sqrt(e2));
-        nrm[s] = __double2float_ru(sqrt(q));
+        nsq[s] = q.hi;
+        err[s] = __fsqrt_ru(__fmul_ru(e2, 1.001f));
+        nrm[s] = __fsqrt_ru(__fadd_ru(q.hi, q.lo));
     }
 }
 
@@ -388,8 +410,8 @@ int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n,
         if (!tmp) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tmpb, keys, keys2, vals, perm, (int)n, 0, 64, s));
     }
-    k_gather<<<(unsigned)npad, 64, 0, s>>>(d_tnf, d_ls, perm, n, npad, (uint32_t)base, g.inv, x32, ls, parts,
-                                          model_split());
+    k_gather<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(d_tnf, d_ls, perm, n, npad, (uint32_t)base, g.inv, x32, ls,
+                                                       parts, model_split());
     MDET_LAUNCHED(ctx, "k_gather");
     float* err = nullptr;
     float* nrm = nullptr;

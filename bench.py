@@ -50,6 +50,21 @@ def assembly_seed(rank: int) -> int:
     return 2 + 1000 * rank
 
 
+def filter_traffic():
+    """DRAM bytes (read + write) per k_filter_tc launch of this step, from the
+    one-pass ncu capture summarised in profiles/k_filter_tc_1M_traffic.md
+    (None when the summary is absent)."""
+    path = os.path.join(ROOT, "profiles", "k_filter_tc_1M_traffic.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 def reduce_max(value: float, device) -> float:
     """Max over ranks (a no-op without an initialised process group)."""
     import torch
@@ -297,7 +312,7 @@ def run_ours(args):
             achieved = flops_step * args.steps / (dom_ms / 1e3) / 1e12
             peak_v = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
             roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak_v, "unit": "TFLOP/s",
-                    "frac": achieved / peak_v, "traffic": None,
+                    "frac": achieved / peak_v, "traffic": filter_traffic(),
                     "algorithmic_per_launch": flops_step * args.steps / dom_launches,
                     "avg_launch_ms": dom_ms / dom_launches, "peak_source": f"bf16 sustained ({pk_kind})"}
         else:

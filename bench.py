@@ -312,7 +312,7 @@ def run_ours(args):
             achieved = flops_step * args.steps / (dom_ms / 1e3) / 1e12
             peak_v = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
             roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak_v, "unit": "TFLOP/s",
-                    "frac": achieved / peak_v, "traffic": filter_traffic(),
+                    "frac": achieved / peak_v, "traffic": filter_traffic() if (n == 1_000_000 and args.mode == "bf16") else None,
                     "algorithmic_per_launch": flops_step * args.steps / dom_launches,
                     "avg_launch_ms": dom_ms / dom_launches, "peak_source": f"bf16 sustained ({pk_kind})"}
         else:

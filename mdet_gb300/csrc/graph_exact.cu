@@ -45,17 +45,25 @@ __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigne
                                          unsigned long long base, const uint32_t* __restrict__ row_map,
                                          const float* __restrict__ x32, uint32_t lane, uint32_t& si, uint32_t& sj) {
     const uint32_t grp = lane >> 3, sub = lane & 7;
-    float ms = 0.f, mc = 0.f;
+    // every lane loads its own candidate once (one coalesced read for the
+    // warp); the rounds below take the row indices by shuffle, so the row
+    // reads of a round depend on no further load
+    const bool own = base + lane < ncand;
     si = sj = 0;
+    if (own) {
+        const uint2 cd = cand[base + lane];
+        si = row_map ? row_map[cd.x] : cd.x;
+        sj = cd.y;
+    }
+    float ms = 0.f, mc = 0.f;
 #pragma unroll 1
     for (uint32_t it = 0; it < 8; ++it) {
-        const unsigned long long k = base + it * 4 + grp;
+        const uint32_t from = it * 4 + grp;  // lane owning the candidate of this group and round
+        const unsigned long long k = base + from;
+        const uint32_t a = __shfl_sync(0xffffffffu, si, from);
+        const uint32_t b = __shfl_sync(0xffffffffu, sj, from);
         float s = 0.f, c = 0.f;
-        uint32_t a = 0, b = 0;
         if (k < ncand) {
-            const uint2 cd = cand[k];
-            a = row_map ? row_map[cd.x] : cd.x;
-            b = cd.y;
             const float4* ra = reinterpret_cast<const float4*>(x32 + (uint64_t)a * MDET_NTNF);
             const float4* rb = reinterpret_cast<const float4*>(x32 + (uint64_t)b * MDET_NTNF);
 #pragma unroll
@@ -84,13 +92,9 @@ __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigne
         const uint32_t src = 8 * (lane & 3);
         const float vs = __shfl_sync(0xffffffffu, s, src);
         const float vc = __shfl_sync(0xffffffffu, c, src);
-        const uint32_t va = __shfl_sync(0xffffffffu, a, src);
-        const uint32_t vb = __shfl_sync(0xffffffffu, b, src);
         if ((lane >> 2) == it) {
             ms = vs;
             mc = vc;
-            si = va;
-            sj = vb;
         }
     }
     return quick_two_sum(ms, mc);
@@ -663,10 +667,18 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
             MDET_LAUNCHED(ctx, "k_exact_graph");
             return MDET_OK;
         };
-        if (ctx->forced_exact)
+        if (ctx->forced_exact) {
             MDET_TRY(run(ctx->forced_exact));
-        else
-            MDET_TRY(launch_autotune(ctx, ctx->exact_shape, tc_shape_key(false, false, ncand, g.n), {8, 4, 2}, run));
+        } else {
+            // candidates: as many blocks per SM as fit, half that, and 2
+            int fit = 0;
+            MDET_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_exact_graph, 256, 0));
+            fit = fit < 2 ? 2 : fit;
+            std::vector<int> cands = {fit};
+            if (fit / 2 > 2) cands.push_back(fit / 2);
+            if (fit > 2) cands.push_back(2);
+            MDET_TRY(launch_autotune(ctx, ctx->exact_shape, tc_shape_key(false, false, ncand, g.n), cands, run));
+        }
     }
     *edges_out = edges;
     *deg_out = deg;
@@ -698,7 +710,9 @@ int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned
         p.H = model_h_ff();
         p.maxkey = maxkey;
         unsigned long long blocks = (ncand + 255) / 256;
-        unsigned long long cap = (unsigned long long)ctx->num_sms * 8;
+        int fit = 0;
+        MDET_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k_exact_maxprob, 256, 0));
+        unsigned long long cap = (unsigned long long)ctx->num_sms * (fit < 1 ? 1 : fit);
         ctx_timer_begin(ctx, "k_exact_maxprob");
     k_exact_maxprob<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(p);
         ctx_timer_end(ctx, "k_exact_maxprob");

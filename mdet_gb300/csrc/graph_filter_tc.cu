@@ -56,7 +56,7 @@ struct Shape {
     static constexpr uint32_t kWarpCols = BN / kGroupsPerHalf;
     // candidate queue per epilogue warp, within the shared memory left
     static constexpr int kQueue = kCtasPerSm == 2 ? 32 : (kSmemBytes + kEpi * 256 * 8 <= 227 * 1024 ? 256 : 64);
-    static_assert(kWarpCols % 64 == 0, "epilogue reads 64 columns at a time");
+    static_assert(kWarpCols == 64, "each epilogue warp reads one 64-column chunk per tile");
     // BF16 x BF16 -> FP32, M = 128, N = BN, A and B K-major.
     static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                        ((uint32_t)(128 >> 4) << 24);
@@ -474,13 +474,11 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                 f_ph[s] ^= 1;
                 tc_fence_after();
                 const float hr = 0.5f * (ansq - (S::MH == 1 ? ctl.r2[s] : r2_own));
-#pragma unroll 1
-                for (uint32_t ch = 0; ch < S::kWarpCols / 64; ++ch) {
-                    const uint32_t col0 = cbase + ch * 64;
+                const uint32_t gc0 = c.J * BN + cbase;
+                unsigned long long mask = 0;  // this lane's hits: bit k = column gc0 + k
+                {
                     float v[64];
-                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * S::kAccCols + mh * BN + col0, v);
-                    const uint32_t gc0 = c.J * BN + col0;
-                    // strided group maxima: mx[t] = max of v[t + 8j], j = 0..7
+                    tmem_ld64(tmem + ((quarter * 32) << 16) + s * S::kAccCols + mh * BN + cbase, v);
                     float mx[8];
 #pragma unroll
                     for (int t = 0; t < 8; ++t) {
@@ -491,8 +489,6 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                     }
                     const float m = max3f(max3f(mx[0], mx[1], mx[2]), max3f(mx[3], mx[4], mx[5]), fmaxf(mx[6], mx[7]));
                     if (m > hr) {
-                        // only the groups whose maximum passes are tested entry by entry
-                        unsigned long long mask = 0;
 #pragma unroll
                         for (int t = 0; t < 8; ++t) {
                             if (mx[t] > hr) {
@@ -501,24 +497,25 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                                     mask |= (unsigned long long)(v[t + 8 * j] > hr ? 1u : 0u) << (t + 8 * j);
                             }
                         }
-                        while (mask) {
-                            const int k = __ffsll((long long)mask) - 1;
-                            mask &= mask - 1;
-                            const uint32_t col = gc0 + k;
-                            if (col < p.nb && row < p.na && (!diag || col > row)) {
-                                uint32_t slot = atomicAdd(qc, 1u);
-                                if (slot < (uint32_t)kQueue) {
-                                    q[slot] = make_uint2(row, col);
-                                } else {
-                                    unsigned long long pos = atomicAdd(p.out.count, 1ull);
-                                    if (pos < p.out.cap) p.out.cand[pos] = make_uint2(row, col);
-                                }
-                            }
+                    }
+                }
+                // the hits are in registers: release the accumulator before emitting
+                tc_fence_before();
+                mbar_arrive(&ctl.acc_empty[s]);
+                while (mask) {
+                    const int k = __ffsll((long long)mask) - 1;
+                    mask &= mask - 1;
+                    const uint32_t col = gc0 + k;
+                    if (col < p.nb && row < p.na && (!diag || col > row)) {
+                        uint32_t slot = atomicAdd(qc, 1u);
+                        if (slot < (uint32_t)kQueue) {
+                            q[slot] = make_uint2(row, col);
+                        } else {
+                            unsigned long long pos = atomicAdd(p.out.count, 1ull);
+                            if (pos < p.out.cap) p.out.cand[pos] = make_uint2(row, col);
                         }
                     }
                 }
-                tc_fence_before();
-                mbar_arrive(&ctl.acc_empty[s]);
                 // flush this warp's queue when it is half full
                 __syncwarp();
                 uint32_t cnt = *(volatile uint32_t*)qc;

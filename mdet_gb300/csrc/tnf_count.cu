@@ -9,13 +9,14 @@
 //
 // GB300 layout: the sequence bytes sit in HBM exactly as the FASTA reader
 // left them (newlines included).  Work is cut into pieces of <= 16 KB of
-// one contig; each warp takes pieces from a global counter and streams the
-// piece through a private double buffer in shared memory with 1-D bulk
-// copies (the TMA engine), histogramming raw 8-bit codes into a private
-// 256-bin shared histogram.  The window that straddles two lanes' 16-byte
-// chunks is carried by a warp scan over (last three bases, count) states.
-// A contig cut into several pieces accumulates into a per-contig scratch row
-// and the last piece to finish normalises it (and clears the scratch row).
+// one contig; each warp takes pieces from a global counter, and each lane
+// walks a contiguous 1/32 of the piece with its own rolling state
+// (16-byte loads, the next one in flight), warmed up on the bytes just
+// before its run, so no lane depends on another while it counts.  Windows go
+// into the warp's 256-bin shared histogram of raw 8-bit codes, folded onto
+// the 136 canonical columns per piece.  A contig cut into several pieces
+// accumulates into a per-contig scratch row and the last piece to finish
+// normalises it (and clears the scratch row).
 #include <cub/cub.cuh>
 
 #include <mutex>
@@ -25,8 +26,7 @@
 namespace {
 
 constexpr int kWarps = 8;
-constexpr uint32_t kStage = 4096;   // bytes per warp stage
-constexpr uint64_t kPiece = 16384;  // bytes per piece (multiple of kStage)
+constexpr uint64_t kPiece = 16384;  // bytes per piece
 constexpr uint32_t kPoison = 0xFF00u;
 
 struct FoldTables {
@@ -48,28 +48,6 @@ __global__ void k_piece_map(const uint32_t* __restrict__ npieces, const uint32_t
     uint32_t s = start[i], np = npieces[i];
     for (uint32_t k = 0; k < np; ++k) piece_contig[s + k] = (uint32_t)i;
 }
-
-// Shift character state `x` (codes in the low byte, poison in the high byte,
-// two bits per slot) by one more character.
-__device__ __forceinline__ uint32_t shift_in(uint32_t x, uint32_t ch) {
-    uint32_t u = (ch | 0x20u) - 0x61u;  // 'a'..
-    uint32_t valid = (u < 20u) ? ((0x80045u >> u) & 1u) : 0u;  // a, c, g, t
-    return ((x << 2) & 0xFCFCu) | ((ch >> 1) & 3u) | (valid ? 0u : 0x300u);
-}
-
-// Compose the state of a prefix with the state of the following chunk that
-// holds `cnt` (capped at 4) characters of its own.
-__device__ __forceinline__ uint32_t compose(uint32_t pre, uint32_t chunk_x, uint32_t cnt) {
-    uint32_t m8 = (0xFFu << (2 * cnt)) & 0xFFu;
-    uint32_t m = m8 | (m8 << 8);
-    return ((pre << (2 * cnt)) & m) | (chunk_x & ~m);
-}
-
-__device__ __forceinline__ uint32_t pack_state(uint32_t x, uint32_t cnt) { return x | (cnt << 16); }
-
-struct Sums {
-    uint64_t v;
-};
 
 __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
 #pragma unroll
@@ -103,6 +81,26 @@ __device__ __forceinline__ void finish_row(uint32_t lane, const uint32_t (&v)[5]
     }
 }
 
+// One byte of the rolling state.  x: codes of the last four non-newline
+// characters (2 bits each, newest lowest) in bits 0-7 and their poison bits
+// (not a base) in bits 8-15; u = lut[byte].  A newline leaves x unchanged
+// (the reference overwrites the window's oldest slot instead of shifting, so
+// the window spanning a line break is still counted); t >= 256 marks a
+// window that is not counted (poisoned, or the newline itself).
+__device__ __forceinline__ uint32_t roll(uint32_t x, uint32_t u, uint32_t& t) {
+    t = ((x << 2) & 0xFCFCu) | u;
+    return u >= 0x8000u ? x : t;
+}
+
+__device__ __forceinline__ uint32_t byte_of(const uint4& v, int b) {
+    const uint32_t w = b < 4 ? v.x : (b < 8 ? v.y : (b < 12 ? v.z : v.w));
+    return __byte_perm(w, 0u, 0x4440u | (uint32_t)(b & 3));
+}
+
+// Warp per piece (<= 16 KB of one contig, taken from a global counter);
+// lane l walks its 1/32 of the piece in order with its own rolling state, warmed up on the bytes just before its run, and counts
+// each window that ends in its run into the warp's shared histogram of raw
+// 8-bit codes.  No lane waits on another until the piece is folded.
 __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __restrict__ bytes,
                                                       const uint64_t* __restrict__ off,
                                                       const uint64_t* __restrict__ len, uint64_t n,
@@ -112,250 +110,94 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                                                       uint32_t* __restrict__ work, uint32_t* __restrict__ acc,
                                                       uint32_t* __restrict__ done, uint32_t* __restrict__ counts,
                                                       float* __restrict__ tnf, FoldTables tabs, int* flag) {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ uint32_t hist_all[kWarps][257];  // 256 raw 4-mer codes + a bin for discarded windows
-    __shared__ uint64_t bars[kWarps][2];
+    __shared__ uint32_t hist_all[kWarps][257];  // 256 raw 4-mer codes (+1 unused)
     // byte -> update word: 2-bit base code | 0x300 when not a base | 0x8000 for '\n'
     __shared__ uint16_t lut[256];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* buf0 = smem + (size_t)w * 2 * kStage;
     uint32_t* hist = hist_all[w];
     for (uint32_t c = threadIdx.x; c < 256; c += blockDim.x) {
         const uint32_t u = (c | 0x20u) - 0x61u;
         const uint32_t valid = (u < 20u) ? ((0x80045u >> u) & 1u) : 0u;
         lut[c] = (uint16_t)(c == '\n' ? 0x8000u : (((c >> 1) & 3u) | (valid ? 0u : 0x300u)));
     }
-    if (lane == 0) {
-        mbar_init(&bars[w][0], 1);
-        mbar_init(&bars[w][1], 1);
-        mbar_fence_init();
-    }
     __syncthreads();
-    uint32_t phase[2] = {0, 0};
     const uint32_t total = piece_start[n - 1] + npieces[n - 1];
 
     while (true) {
+        // the next piece (lane 0) and the abort flag (lane 1) load side by side
         uint32_t p = 0;
+        int stop = 0;
         if (lane == 0) p = atomicAdd(work, 1u);
+        else if (lane == 1) stop = *(volatile int*)flag;
         p = __shfl_sync(0xffffffffu, p, 0);
-        if (p >= total) break;
-        if (*(volatile int*)flag) break;
+        stop = __shfl_sync(0xffffffffu, stop, 1);
+        if (p >= total || stop) break;
         const uint64_t c = piece_contig[p];
         const uint32_t k = p - piece_start[c];
         const uint64_t s0 = off[c], L = len[c];
         const uint64_t p0 = s0 + (uint64_t)k * kPiece;
         const uint64_t p1 = min(s0 + L, p0 + kPiece);
 
-        // carry-in: the last three non-newline characters before p0
-        uint32_t carry = kPoison;
-        {
-            int need = 3;
-            uint32_t got[3] = {0, 0, 0};  // newest first
-            uint64_t pos = p0;
-            while (need > 0 && pos > s0) {
-                int64_t q = (int64_t)pos - 1 - (int64_t)lane;
-                uint32_t ch = (q >= (int64_t)s0) ? bytes[q] : (uint32_t)'\n';
-                bool inb = q >= (int64_t)s0;
-                uint32_t good = __ballot_sync(0xffffffffu, inb && ch != '\n');
-                while (good && need > 0) {
-                    int src = __ffs(good) - 1;
-                    got[3 - need] = __shfl_sync(0xffffffffu, ch, src);
-                    good &= good - 1;
-                    --need;
-                }
-                pos = pos > s0 + 32 ? pos - 32 : s0;
-            }
-            for (int t = 2; t >= 0; --t)
-                if (t < 3 - need) carry = shift_in(carry, got[t]);
-        }
-
         for (int i = lane; i < 257; i += 32) hist[i] = 0;
         __syncwarp();
 
-        const uint64_t a0 = p0 & ~(uint64_t)15;
-        const uint64_t a1 = (p1 + 15) & ~(uint64_t)15;
-        const uint32_t nst = (uint32_t)((a1 - a0 + kStage - 1) / kStage);
-        bool ok = true;
-        if (lane == 0 && nst > 0) {
-            fence_proxy_async_smem();
-            uint32_t b0 = (uint32_t)min((uint64_t)kStage, a1 - a0);
-            mbar_arrive_tx(&bars[w][0], b0);
-            bulk_g2s(buf0, bytes + a0, b0, &bars[w][0]);
-        }
-        for (uint32_t st = 0; st < nst; ++st) {
-            const uint32_t bi = st & 1;
-            const uint64_t sabs = a0 + (uint64_t)st * kStage;
-            const uint32_t sbytes = (uint32_t)min((uint64_t)kStage, a1 - sabs);
-            if (st + 1 < nst) {
-                __syncwarp();
-                if (lane == 0) {
-                    fence_proxy_async_smem();
-                    uint64_t nabs = sabs + kStage;
-                    uint32_t nb = (uint32_t)min((uint64_t)kStage, a1 - nabs);
-                    mbar_arrive_tx(&bars[w][bi ^ 1], nb);
-                    bulk_g2s(buf0 + (bi ^ 1) * kStage, bytes + nabs, nb, &bars[w][bi ^ 1]);
+        // the piece is split evenly over the 32 lanes in runs of whole 16-byte
+        // chunks (so every lane's run starts at the same offset mod 16)
+        const uint64_t run = max((uint64_t)16, (((p1 - p0) + 31) / 32 + 15) & ~(uint64_t)15);
+        const uint64_t seg0 = p0 + (uint64_t)lane * run;
+        const uint64_t seg1 = min(p1, seg0 + run);
+        if (seg0 < seg1) {
+            // warm-up: the state after the last three non-newline bytes before
+            // seg0 (none before s0).  Fast case: the four bytes before seg0
+            // hold at most one newline; else walk back byte by byte.
+            uint32_t x = kPoison, t;
+            bool warm = false;
+            if (seg0 >= s0 + 4) {
+                const uint64_t q = seg0 - 4;
+                const uint32_t* wp = reinterpret_cast<const uint32_t*>(bytes + (q & ~(uint64_t)3));
+                const uint32_t four = __funnelshift_r(__ldg(wp), __ldg(wp + 1), 8u * (uint32_t)(q & 3));
+                const uint32_t z = four ^ 0x0A0A0A0Au;
+                const uint32_t nl = ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
+                if (__popc(nl) <= 1) {
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) x = roll(x, lut[(four >> (8 * b)) & 0xFFu], t);
+                    warm = true;
                 }
             }
-            if (!__all_sync(0xffffffffu, mbar_wait(&bars[w][bi], phase[bi], flag))) {  // bounded, warp-uniform
-                ok = false;
-                break;
+            if (!warm) {
+                uint64_t ws = seg0;
+                int need = 3;
+                while (need > 0 && ws > s0) {
+                    --ws;
+                    if (bytes[ws] != '\n') --need;
+                }
+                for (uint64_t q = ws; q < seg0; ++q) x = roll(x, lut[bytes[q]], t);
             }
-            phase[bi] ^= 1;
-            const unsigned char* sb = buf0 + bi * kStage;
-            for (uint32_t r = 0; r * 512 < sbytes; ++r) {
-                const uint32_t cofs = r * 512 + lane * 16;
-                const int64_t cb = (int64_t)(sabs + cofs);
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (cofs < sbytes) v = *reinterpret_cast<const uint4*>(sb + cofs);
-                int64_t lo = (int64_t)p0 - cb, hi = (int64_t)p1 - cb;
-                lo = lo < 0 ? 0 : (lo > 16 ? 16 : lo);
-                hi = hi < 0 ? 0 : (hi > 16 ? 16 : hi);
-                uint32_t act = ((hi >= 16 ? 0xFFFFu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u));
-                if (cofs >= sbytes) act = 0;
-                uint32_t words[4] = {v.x, v.y, v.z, v.w};
-                // pass over the chunk from a fully poisoned state
-                uint32_t x = kPoison, nact = 0, x3 = 0, nlm = 0;
-                const bool full = act == 0xFFFFu;
-                bool packed = false;
-                if (full) {
-                    // SWAR per word: 2-bit codes, newline bytes, bytes that are no base letter
-                    uint32_t xs[4], pzm = 0;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t w = words[q];
-                        const uint32_t lc = w | 0x20202020u;
-                        const uint32_t K = (lc >> 1) & 0x03030303u;
-                        const uint32_t sel = __byte_perm(K | (K >> 4), 0u, 0x4420u);
-                        const uint32_t bad = lc ^ __byte_perm(0x67746361u, 0u, sel);  // 'a' 'c' 't' 'g'
-                        const uint32_t nz = (((bad & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | bad) & 0x80808080u;
-                        const uint32_t z = w ^ 0x0A0A0A0Au;
-                        const uint32_t nl = ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
-                        nlm |= ((((nl >> 7) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
-                        pzm |= (((((nz & ~nl) >> 7) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
-                        xs[q] = K * 0x40100401u;  // byte 3: the word's four codes, oldest highest
-                    }
-                    if (__popc(nlm) <= 2) {
-                        packed = true;
-                        // field f (2 bits at 2f) holds byte 15 - f; drop the newline fields
-                        const uint32_t hi = __byte_perm(xs[0], xs[1], 0x3700u);
-                        const uint32_t lo = __byte_perm(xs[2], xs[3], 0x0037u);
-                        uint64_t P = __byte_perm(hi, lo, 0x3254u);
-                        uint32_t pz = __brev(pzm) >> 16, nlr = __brev(nlm) >> 16;
-                        while (nlr) {
-                            const int f = 31 - __clz(nlr);
-                            nlr &= ~(1u << f);
-                            P = ((P >> (2 * f + 2)) << (2 * f)) | (P & ((1ull << (2 * f)) - 1));
-                            pz = ((pz >> (f + 1)) << f) | (pz & ((1u << f) - 1));
-                        }
-                        nact = 16u - __popc(nlm);
-                        // window k: fields k..k+3 (newest at k); poisoned when any of them is
-                        const uint32_t wi = pz | (pz >> 1) | (pz >> 2) | (pz >> 3);
-                        const uint32_t P32 = (uint32_t)P;
-#pragma unroll
-                        for (int k = 0; k < 13; ++k) {
-                            const uint32_t code = (P32 >> (2 * k)) & 0xFFu;
-                            const bool ok = (uint32_t)k + 4u <= nact && !((wi >> k) & 1u);
-                            atomicAdd(&hist[ok ? code : 256u], 1u);
-                        }
-                        // states: the last four codes and the first three, poison in the high byte
-                        auto spread = [](uint32_t b) {
-                            return ((b & 1u) * 3u) | ((b & 2u) * 6u) | ((b & 4u) * 12u) | ((b & 8u) * 24u);
-                        };
-                        x = (P32 & 0xFFu) | (spread(pz & 0xFu) << 8);
-                        x3 = ((P32 >> (2 * (nact - 3))) & 0x3Fu) | (spread((pz >> (nact - 3)) & 7u) << 8);
-                    }
-                }
-                if (full && !packed) {
-                    // every byte of the chunk is in the piece: table-driven
-                    // update, newline bytes leave the state unchanged, and
-                    // every window lands in a bin (bin 256 takes the invalid
-                    // ones) so the loop has no branches
-                    nlm = 0;
+            // counting pass over aligned 16-byte chunks, the next one in flight
+            const uint64_t a0 = seg0 & ~(uint64_t)15;
+            uint4 nxt = __ldg(reinterpret_cast<const uint4*>(bytes + a0));
+            for (uint64_t a = a0; a < seg1; a += 16) {
+                const uint4 v = nxt;
+                if (a + 16 < seg1) nxt = __ldg(reinterpret_cast<const uint4*>(bytes + a + 16));
+                if (a >= seg0 && a + 16 <= seg1) {
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
-                        const uint32_t ch = __byte_perm(words[b >> 2], 0u, 0x4440u | (uint32_t)(b & 3));
-                        const uint32_t m = lut[ch];
-                        const bool nl = m >= 0x8000u;
-                        const uint32_t xn = ((x << 2) & 0xFCFCu) | m;
-                        x = nl ? x : xn;
-                        const uint32_t bin = (nl || x >= 256u) ? 256u : x;
-                        atomicAdd(&hist[bin], 1u);
-                        if (b == 2) x3 = x;
+                        x = roll(x, lut[byte_of(v, b)], t);
+                        if (t < 256u) atomicAdd(&hist[t], 1u);
                     }
-                    // newline bytes of the chunk (SWAR zero-byte test on w ^ '\n')
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t z = words[q] ^ 0x0A0A0A0Au;
-                        const uint32_t hit = ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
-                        nlm |= hit ? (((hit >> 7) * 0x01020408u) >> 24 & 0xFu) << (4 * q) : 0u;
-                    }
-                    nact = 16u - __popc(nlm);
-                } else if (!full) {
-#pragma unroll
-                    for (int b = 0; b < 16; ++b) {
-                        uint32_t ch = (words[b >> 2] >> (8 * (b & 3))) & 0xFFu;
-                        bool on = ((act >> b) & 1u) && ch != '\n';
-                        if (on) {
-                            x = shift_in(x, ch);
-                            ++nact;
-                            if (x < 256u) atomicAdd(&hist[x], 1u);
-                        }
-                    }
-                }
-                uint32_t cnt = nact < 4 ? nact : 4;
-                // carry-in for this lane: compose lanes 0..l-1 of this row onto `carry`
-                uint32_t st_incl = pack_state(x & 0xFFFFu, cnt);
-                uint32_t all_full = __all_sync(0xffffffffu, cnt >= 3);
-                uint32_t cin;
-                if (all_full) {
-                    uint32_t prev = __shfl_up_sync(0xffffffffu, st_incl, 1);
-                    cin = lane == 0 ? carry : (prev & 0xFFFFu);
-                    uint32_t last = __shfl_sync(0xffffffffu, st_incl, 31);
-                    carry = last & 0xFFFFu;
                 } else {
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        uint32_t other = __shfl_up_sync(0xffffffffu, st_incl, o);
-                        if (lane >= (uint32_t)o) {
-                            uint32_t mc = st_incl >> 16;
-                            uint32_t ox = other & 0xFFFFu, oc = other >> 16;
-                            uint32_t nx = compose(ox, st_incl & 0xFFFFu, mc);
-                            uint32_t nc = oc + mc;
-                            st_incl = pack_state(nx, nc < 4 ? nc : 4);
-                        }
-                    }
-                    uint32_t prev = __shfl_up_sync(0xffffffffu, st_incl, 1);
-                    uint32_t excl = lane == 0 ? kPoison : (prev & 0xFFFFu);
-                    uint32_t excl_cnt = lane == 0 ? 0u : (prev >> 16);
-                    cin = excl_cnt >= 3 ? excl : compose(carry, excl, excl_cnt);
-                    uint32_t last = __shfl_sync(0xffffffffu, st_incl, 31);
-                    carry = (last >> 16) >= 3 ? (last & 0xFFFFu) : compose(carry, last & 0xFFFFu, last >> 16);
-                }
-                // the first (up to) three windows of the chunk depend on the carry-in
-                if (packed || (full && (nlm & 7u) == 0)) {
-                    // x3 holds the chunk's first three characters in slots 2, 1, 0
-                    const uint32_t w1 = compose(cin, x3 >> 4, 1);
-                    const uint32_t w2 = compose(cin, x3 >> 2, 2);
-                    const uint32_t w3 = compose(cin, x3, 3);
-                    atomicAdd(&hist[w1 < 256u ? w1 : 256u], 1u);
-                    atomicAdd(&hist[w2 < 256u ? w2 : 256u], 1u);
-                    atomicAdd(&hist[w3 < 256u ? w3 : 256u], 1u);
-                } else if (nact > 0) {
-                    uint32_t y = cin, seen = 0;
+                    const uint32_t lo = a < seg0 ? (uint32_t)(seg0 - a) : 0u;
+                    const uint32_t hi = seg1 - a < 16 ? (uint32_t)(seg1 - a) : 16u;
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
-                        uint32_t ch = (words[b >> 2] >> (8 * (b & 3))) & 0xFFu;
-                        bool on = ((act >> b) & 1u) && ch != '\n' && seen < 3;
-                        if (on) {
-                            y = shift_in(y, ch);
-                            ++seen;
-                            if (y < 256u) atomicAdd(&hist[y], 1u);
+                        if ((uint32_t)b >= lo && (uint32_t)b < hi) {
+                            x = roll(x, lut[byte_of(v, b)], t);
+                            if (t < 256u) atomicAdd(&hist[t], 1u);
                         }
                     }
                 }
             }
         }
-        if (!ok) break;
         __syncwarp();
         uint32_t v[5];
 #pragma unroll
@@ -445,17 +287,11 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
     const TnTables& t = tn_tables();
     memcpy(tabs.fw, t.col_fw, MDET_NTNF);
     memcpy(tabs.rc, t.col_rc, MDET_NTNF);
-    const size_t dyn = (size_t)kWarps * 2 * kStage;
-    static bool attr_set[64] = {false};
-    if (!attr_set[ctx->device & 63]) {
-        MDET_CUDA(ctx, cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
-        attr_set[ctx->device & 63] = true;
-    }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_count, kWarps * 32, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_count, kWarps * 32, 0);
     if (per_sm < 1) per_sm = 1;
     ctx_timer_begin(ctx, "k_count");
-    k_count<<<ctx->num_sms * per_sm, kWarps * 32, dyn, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
+    k_count<<<ctx->num_sms * per_sm, kWarps * 32, 0, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
                                                             npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
                                                             ctx->d_flag);
     ctx_timer_end(ctx, "k_count");
@@ -572,7 +408,6 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MDET_ERR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t dyn = (size_t)kWarps * 2 * kStage;
     {
         // once per device, with that device current: resolve the array's
         // device address (host code cannot use the symbol itself)
@@ -584,9 +419,8 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
                 cudaGetLastError();
                 return MDET_ERR_CUDA;
             }
-            if (cudaFuncSetAttribute(k_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess ||
-                cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.per_sm, k_count, kWarps * 32, dyn) != cudaSuccess) {
+            if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.per_sm, k_count, kWarps * 32, 0) != cudaSuccess) {
                 cudaGetLastError();
                 return MDET_ERR_CUDA;
             }
@@ -634,7 +468,7 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
     const TnTables& t = tn_tables();
     memcpy(tabs.fw, t.col_fw, MDET_NTNF);
     memcpy(tabs.rc, t.col_rc, MDET_NTNF);
-    k_count<<<d.num_sms * d.per_sm, kWarps * 32, dyn, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
+    k_count<<<d.num_sms * d.per_sm, kWarps * 32, 0, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
                                                            npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
                                                            flag);
     if (cudaGetLastError() != cudaSuccess) return MDET_ERR_CUDA;

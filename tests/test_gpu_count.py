@@ -60,6 +60,34 @@ def test_random_layouts(gpu_ctx):
     _check(gpu_ctx, data, p.seq_off, p.seq_len)
 
 
+def test_newline_runs_and_piece_edges(gpu_ctx):
+    """Runs of many newlines (a lane's warm-up must walk back past them),
+    contigs made of newlines only, and lengths on either side of the 16 KB
+    piece and 512-byte lane boundaries."""
+    rng = np.random.default_rng(11)
+    bases = np.frombuffer(b"ACGTacgtN", np.uint8)
+    recs = []
+    for k, L in enumerate([3, 4, 5, 511, 512, 513, 515, 516, 16380, 16383, 16384, 16385, 16388, 32767, 32768, 32771,
+                           49152, 70000]):
+        s = bases[rng.integers(0, 9, L)].copy()
+        nl = rng.random(L) < 0.05
+        s[nl] = ord("\n")
+        body = s.tobytes()
+        if k % 3 == 0:  # stretches of 2-40 newlines
+            parts = body.split(b"\n")
+            body = b"".join(q + b"\n" * int(rng.integers(2, 41)) for q in parts)
+        recs.append(b">r%d\n" % k + body + b"\n")
+    recs.append(b">nl\n" + b"\n" * 40)
+    data = np.frombuffer(b"".join(recs), np.uint8)
+    p = parse_fasta_bytes(data, min_contig=0)
+    _check(gpu_ctx, data, p.seq_off, p.seq_len)
+    # the same bytes as one view each, newlines inside (no FASTA parsing)
+    raw = np.frombuffer(b"".join(r.split(b"\n", 1)[1] for r in recs), np.uint8)
+    lens = np.array([len(r.split(b"\n", 1)[1]) for r in recs], np.uint64)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.uint64)
+    _check(gpu_ctx, raw, offs, lens)
+
+
 def test_short_and_empty_contigs(gpu_ctx):
     txt = b">e\n>a\nA\n>b\nACG\n>c\nACGT\n>d\nAC\nGT\n>f\nNNNNNNNN\n"
     data = np.frombuffer(txt, np.uint8)

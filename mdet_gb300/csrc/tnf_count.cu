@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                                                       uint32_t* __restrict__ work, uint32_t* __restrict__ acc,
                                                       uint32_t* __restrict__ done, uint32_t* __restrict__ counts,
                                                       float* __restrict__ tnf, FoldTables tabs, int* flag) {
-    __shared__ uint32_t hist_all[kWarps][257];  // 256 raw 4-mer codes (+1 unused)
+    __shared__ uint32_t hist_all[kWarps][257];  // 256 raw 4-mer codes + a bin for windows not counted
     // byte -> update word: 2-bit base code | 0x300 when not a base | 0x8000 for '\n'
     __shared__ uint16_t lut[256];
     const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
 #pragma unroll
                     for (int b = 0; b < 16; ++b) {
                         x = roll(x, lut[byte_of(v, b)], t);
-                        if (t < 256u) atomicAdd(&hist[t], 1u);
+                        atomicAdd(&hist[min(t, 256u)], 1u);  // bin 256 takes the windows not counted
                     }
                 } else {
                     const uint32_t lo = a < seg0 ? (uint32_t)(seg0 - a) : 0u;

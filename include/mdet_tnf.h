@@ -99,8 +99,8 @@ int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, cons
  * and results as mdet_tnf_count_dev, but no context: the work runs on
  * `stream` (a cudaStream_t, 0 for the default stream) with its scratch in a
  * static device array of about 4.9 MB that every GPU loading the library
- * holds until exit.  Limits: n <= 8192 contigs and at most 65536 16-KB pieces
- * of sequence (about 1 GB); larger inputs return MDET_ERR_CAPACITY.  The
+ * holds until exit.  Limits: n <= 8192 contigs and at most 65536 64-KB pieces
+ * of sequence (about 4 GB); larger inputs return MDET_ERR_CAPACITY.  The
  * first call on a device resolves the array's device address there (make it
  * before any stream capture).  All calls share the one array, so calls whose
  * work overlaps on the GPU race; serialise them.  The call returns after its

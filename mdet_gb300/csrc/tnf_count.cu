@@ -8,7 +8,7 @@
 // exact integers; TNF = float(c / sqrt(sum float(c*c))).
 //
 // GB300 layout: the sequence bytes sit in HBM exactly as the FASTA reader
-// left them (newlines included).  Work is cut into pieces of <= 16 KB of
+// left them (newlines included).  Work is cut into pieces of <= 64 KB of
 // one contig; each warp takes pieces from a global counter, and each lane
 // walks a contiguous 1/32 of the piece with its own rolling state
 // (16-byte loads, the next one in flight), warmed up on the bytes just
@@ -26,7 +26,7 @@
 namespace {
 
 constexpr int kWarps = 8;
-constexpr uint64_t kPiece = 16384;  // bytes per piece
+constexpr uint64_t kPiece = 65536;  // bytes per piece
 constexpr uint32_t kPoison = 0xFF00u;
 
 struct FoldTables {
@@ -97,7 +97,7 @@ __device__ __forceinline__ uint32_t byte_of(const uint4& v, int b) {
     return __byte_perm(w, 0u, 0x4440u | (uint32_t)(b & 3));
 }
 
-// Warp per piece (<= 16 KB of one contig, taken from a global counter);
+// Warp per piece (<= 64 KB of one contig, taken from a global counter);
 // lane l walks its 1/32 of the piece in order with its own rolling state, warmed up on the bytes just before its run, and counts
 // each window that ends in its run into the warp's shared histogram of raw
 // 8-bit codes.  No lane waits on another until the piece is folded.

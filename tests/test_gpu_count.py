@@ -62,13 +62,13 @@ def test_random_layouts(gpu_ctx):
 
 def test_newline_runs_and_piece_edges(gpu_ctx):
     """Runs of many newlines (a lane's warm-up must walk back past them),
-    contigs made of newlines only, and lengths on either side of the 16 KB
-    piece and 512-byte lane boundaries."""
+    contigs made of newlines only, and lengths on either side of the 64 KB
+    piece size and of 16-byte chunk and lane-run boundaries."""
     rng = np.random.default_rng(11)
     bases = np.frombuffer(b"ACGTacgtN", np.uint8)
     recs = []
     for k, L in enumerate([3, 4, 5, 511, 512, 513, 515, 516, 16380, 16383, 16384, 16385, 16388, 32767, 32768, 32771,
-                           49152, 70000]):
+                           49152, 65535, 65536, 65537, 65540, 131075, 200000]):
         s = bases[rng.integers(0, 9, L)].copy()
         nl = rng.random(L) < 0.05
         s[nl] = ord("\n")

@@ -75,6 +75,22 @@ __global__ void k_sample_gather_bf16(const uint32_t* __restrict__ row_map, uint6
     }
 }
 
+// The sample's rows in the B role: row r = xb row row_map[r]; padding rows
+// carry -inf in the column-term slot so that no pair with them passes.
+__global__ void k_sample_gather_b(const uint32_t* __restrict__ row_map, uint64_t m, uint64_t mpad,
+                                  const uint16_t* __restrict__ xb, uint16_t* __restrict__ sb) {
+    const uint64_t r = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    const uint32_t lane = threadIdx.x & 31;
+    if (r >= mpad) return;
+    if (r < m) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(xb + (uint64_t)row_map[r] * MDET_KPAD);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(sb + r * MDET_KPAD);
+        for (int k = lane; k < MDET_KPAD / 2; k += 32) dst[k] = src[k];
+    } else {
+        for (int k = lane; k < MDET_KPAD; k += 32) sb[r * MDET_KPAD + k] = k == MDET_NTNF ? 0xFF80 : 0;
+    }
+}
+
 // per-128 block metadata of the gathered sample (log-size range, and for
 // BF16 rows the max rounding error / norm of the gathered rows)
 __global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, const double* __restrict__ ls,
@@ -165,8 +181,11 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride, int bn,
-               unsigned long long fixed_cap, unsigned long long** cnt_dev, const unsigned long long* rowoff) {
+               unsigned long long fixed_cap, unsigned long long** cnt_dev, const unsigned long long* rowoff,
+               const BSide* bside) {
     cudaStream_t s = ctx->stream;
+    if (bside && (mode == MDET_MODE_PLAIN || fixed_cap || tiles))
+        return ctx_fail(ctx, MDET_ERR_INVALID, "a B-role subset needs a tensor-core form without a tile list");
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
     if (!cnt) return MDET_ERR_NOMEM;
     if (fixed_cap) {
@@ -189,7 +208,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
         return MDET_OK;
     }
     // remembered capacity (bytes of the candidate buffer) from earlier calls
-    size_t guess = ((size_t)256 * (rect ? na : g.n) + (1u << 20)) * sizeof(uint2);
+    size_t guess = ((size_t)256 * (bside ? bside->nb : (rect ? na : g.n)) + (1u << 20)) * sizeof(uint2);
     DevBuf& cb = ctx->bufs[std::string(tag) + ".cand"];
     if (cb.cap > guess) guess = cb.cap;
     for (int attempt = 0; attempt < 3; ++attempt) {
@@ -204,6 +223,9 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                 MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect,
                                      tbl, out, tiles, nlist, row_tbl, tbl_stride));
                 ctx->last_tile_n = 128128;
+            } else if (bside) {  // all rows (A role) against a B-role subset
+                MDET_TRY(filter_tc(ctx, g.xa, g.nsq, g.n, g.meta, bside->xb, bside->nb, bside->meta, false, tbl, out,
+                                   nullptr, 0, nullptr, 0, w, nullptr));
             } else {
                 const uint16_t* A = rect ? ab : g.xa;
                 const float* An = rect ? ansq : g.nsq;
@@ -216,7 +238,9 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
         if (mode == MDET_MODE_PLAIN || bn != 0 || tiles)
             MDET_TRY(run(bn ? bn : 256));
         else
-            MDET_TRY(tc_autotune(ctx, tc_shape_key(rect, false, rect ? na : g.n, g.n), run));
+            MDET_TRY(tc_autotune(ctx, bside ? tc_shape_key(true, false, g.n, bside->nb)
+                                            : tc_shape_key(rect, false, rect ? na : g.n, g.n),
+                                 run));
         unsigned long long found = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&found, cnt, 8, cudaMemcpyDeviceToHost, s));
         MDET_CUDA(ctx, cudaStreamSynchronize(s));
@@ -357,23 +381,29 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
     MDET_LAUNCHED(ctx, "k_sample_gather");
     k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta32, nblk, ameta32);
     MDET_LAUNCHED(ctx, "k_sample_meta");
-    uint16_t* ab = nullptr;
-    float* ansq = nullptr;
-    if (mode != MDET_MODE_PLAIN) {
-        ab = (uint16_t*)ctx_scratch(ctx, "mp.ab", mpad * MDET_KPAD * 2);
-        ansq = (float*)ctx_scratch(ctx, "mp.ansq", mpad * 4);
-        if (!ab || !ansq) return MDET_ERR_NOMEM;
-        k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xa, g.nsq, ab, ansq);
-        MDET_LAUNCHED(ctx, "k_sample_gather_bf16");
-        k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
-        MDET_LAUNCHED(ctx, "k_sample_meta");
-    }
     const double L = floor_prob > 0 ? logit(floor_prob) : -INFINITY;
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, g.n, L, &tbl));
     uint2* cand = nullptr;
     unsigned long long ncand = 0;
-    MDET_TRY(run_filter(ctx, mode, g, true, a32, ab, ansq, (uint32_t)m, ameta, ameta32, tbl, "mp", &cand, &ncand));
+    if (mode != MDET_MODE_PLAIN) {
+        // tensor-core forms: all rows in the A role (each A tile read once)
+        // against the sample in the B role (small enough to stay in L2), so
+        // the pairs come out as (row, sample slot)
+        uint16_t* sb = (uint16_t*)ctx_scratch(ctx, "mp.sb", mpad * MDET_KPAD * 2);
+        if (!sb) return MDET_ERR_NOMEM;
+        k_sample_gather_b<<<(unsigned)((mpad + 7) / 8), 256, 0, s>>>(row_map, m, mpad, g.xb, sb);
+        MDET_LAUNCHED(ctx, "k_sample_gather_b");
+        k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
+        MDET_LAUNCHED(ctx, "k_sample_meta");
+        const BSide bs{sb, (uint32_t)m, ameta};
+        MDET_TRY(run_filter(ctx, mode, g, true, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "mp", &cand,
+                            &ncand, nullptr, 0, nullptr, 0, 0, 0, nullptr, nullptr, &bs));
+        MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out, true));
+        return MDET_OK;
+    }
+    MDET_TRY(run_filter(ctx, mode, g, true, a32, nullptr, nullptr, (uint32_t)m, ameta, ameta32, tbl, "mp", &cand,
+                        &ncand));
     MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out));
     return MDET_OK;
 }

@@ -173,8 +173,9 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
                 Edge** edges_out, unsigned long long* nedges_out, uint32_t** deg_out,
                 const BlkCut* blk_L = nullptr, const unsigned long long* ncand_dev = nullptr,
                 unsigned long long** nedges_dev = nullptr);
+// swapped: the pairs are (other row, sample slot) instead of (sample slot, other row)
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
-                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out);
+                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out, bool swapped = false);
 // Exact-stage distance and probability of given pairs (original indices).
 int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64_t m, double* dist, double* prob);
 // blk_K: optional per-256-row-block max_edges (each <= max_edges <= 512).
@@ -191,12 +192,20 @@ int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d
 double logit(double cutoff);
 int check_flag(mdet_ctx* ctx);
 int check_mode(mdet_ctx* ctx, int mode);
+// A subset of rows in the B role (BF16 B layout, per-128-row metadata), for a
+// rectangular pass of all rows (A role) against the subset.
+struct BSide {
+    const uint16_t* xb;
+    uint32_t nb;
+    const BlockMeta* meta;
+};
 int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const float* a32, const uint16_t* ab,
                const float* ansq, uint32_t na, const BlockMeta* ameta, const BlockMeta* ameta32,
                const DstarTable& tbl, const char* tag, uint2** cand_out, unsigned long long* ncand_out,
                const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
                uint64_t tbl_stride = 0, int bn = 0, unsigned long long fixed_cap = 0,
-               unsigned long long** cnt_dev = nullptr, const unsigned long long* rowoff = nullptr);
+               unsigned long long** cnt_dev = nullptr, const unsigned long long* rowoff = nullptr,
+               const BSide* bside = nullptr);
 // Tile-shape autotuner: run(bn) performs one filter pass with column tiles
 // of bn.  The first pass of a shape class times bn = 256 and bn = 128 and
 // keeps the faster (the later pass's output stands); later passes use it.

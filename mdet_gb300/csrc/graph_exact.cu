@@ -21,6 +21,7 @@ struct ExactArgs {
     const uint2* cand;
     unsigned long long ncand;
     const uint32_t* row_map;  // maxprob: sample slot -> sorted position; graph: null
+    bool swapped;             // maxprob: pairs are (sorted position, sample slot)
     const float* x32;
     const PartsFF* parts;
     ModelHFF H;
@@ -43,7 +44,8 @@ struct ExactArgs {
 // reduction.  Returns the owner lane's (sum, error) pair and its rows.
 __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigned long long ncand,
                                          unsigned long long base, const uint32_t* __restrict__ row_map,
-                                         const float* __restrict__ x32, uint32_t lane, uint32_t& si, uint32_t& sj) {
+                                         const float* __restrict__ x32, uint32_t lane, uint32_t& si, uint32_t& sj,
+                                         bool swapped = false) {
     const uint32_t grp = lane >> 3, sub = lane & 7;
     // every lane loads its own candidate once (one coalesced read for the
     // warp); the rounds below take the row indices by shuffle, so the row
@@ -51,7 +53,8 @@ __device__ __forceinline__ ff warp_dist2(const uint2* __restrict__ cand, unsigne
     const bool own = base + lane < ncand;
     si = sj = 0;
     if (own) {
-        const uint2 cd = cand[base + lane];
+        uint2 cd = cand[base + lane];
+        if (swapped) cd = make_uint2(cd.y, cd.x);
         si = row_map ? row_map[cd.x] : cd.x;
         sj = cd.y;
     }
@@ -160,11 +163,12 @@ __global__ void __launch_bounds__(256) k_exact_maxprob(ExactArgs p) {
     for (unsigned long long base = ((unsigned long long)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5)) * 32;
          base < p.ncand; base += warps * 32) {
         uint32_t si, sj;
-        const ff d2 = warp_dist2(p.cand, p.ncand, base, p.row_map, p.x32, lane, si, sj);
+        const ff d2 = warp_dist2(p.cand, p.ncand, base, p.row_map, p.x32, lane, si, sj, p.swapped);
         const unsigned long long idx = base + lane;
         if (idx < p.ncand && si != sj) {  // skip the sampled contig itself
             const ff pre = pre_prob(p.parts[si], p.parts[sj], ff_sqrt(d2), p.H, true);
-            atomicMax(&p.maxkey[p.cand[idx].x], dkey(ff_to_double(pre)));
+            const uint2 cd = p.cand[idx];
+            atomicMax(&p.maxkey[p.swapped ? cd.y : cd.x], dkey(ff_to_double(pre)));
         }
     }
 }
@@ -693,7 +697,7 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
 }
 
 int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned long long ncand,
-                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out) {
+                  const uint32_t* row_map, uint64_t m, const uint32_t* slot_of, double* d_out, bool swapped) {
     cudaStream_t s = ctx->stream;
     unsigned long long* maxkey = (unsigned long long*)ctx_scratch(ctx, "mp.maxkey", (m ? m : 1) * 8);
     if (!maxkey) return MDET_ERR_NOMEM;
@@ -705,6 +709,7 @@ int exact_maxprob(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned
         p.cand = cand;
         p.ncand = ncand;
         p.row_map = row_map;
+        p.swapped = swapped;
         p.x32 = g.x32;
         p.parts = g.parts;
         p.H = model_h_ff();

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -591,15 +592,26 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
     const double floor_prob = 0.7;
     auto sample = [&](bool full, double* p_out) -> int {
         uint64_t m = full ? n : std::min<uint64_t>(n, 2500);
-        std::iota(idx.begin(), idx.end(), (uint64_t)0);
-        {  // random_unique (cuda/Cuda2.cu:500-511)
-            uint64_t left = n, k = m;
-            uint64_t* begin = idx.data();
-            while (k--) {
-                uint64_t* r = begin + (uint64_t)rand() % left;
-                std::swap(*begin, *r);
-                ++begin;
-                --left;
+        // random_unique (cuda/Cuda2.cu:500-511): a partial Fisher-Yates
+        // shuffle of 0..n-1 whose first m entries are the sample; step p
+        // swaps position p with p + rand() % (n - p)
+        if (m == n) {
+            std::iota(idx.begin(), idx.end(), (uint64_t)0);
+            for (uint64_t p = 0; p < m; ++p) std::swap(idx[p], idx[p + (uint64_t)rand() % (n - p)]);
+        } else {
+            // the same draws on a sparse array (untouched positions hold their
+            // own index), so a pass costs O(m) instead of O(n)
+            std::unordered_map<uint64_t, uint64_t> moved;
+            moved.reserve(2 * m);
+            auto at = [&](uint64_t i) {
+                const auto it = moved.find(i);
+                return it == moved.end() ? i : it->second;
+            };
+            for (uint64_t p = 0; p < m; ++p) {
+                const uint64_t r = p + (uint64_t)rand() % (n - p);
+                const uint64_t vp = at(p), vr = at(r);
+                idx[p] = vr;  // later steps only touch positions after p
+                moved[r] = vp;
             }
         }
         MDET_CUDA(ctx, cudaMemcpyAsync(d_idx, idx.data(), m * 8, cudaMemcpyHostToDevice, s));

@@ -590,6 +590,8 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
     if (!d_idx || !d_mx) return MDET_ERR_NOMEM;
     // the search only compares maxima against cutoffs above 0.700
     const double floor_prob = 0.7;
+    // first floor of a pass: just below the previous pass's cutoff
+    double next_floor = 0.9;
     auto sample = [&](bool full, double* p_out) -> int {
         uint64_t m = full ? n : std::min<uint64_t>(n, 2500);
         // random_unique (cuda/Cuda2.cu:500-511): a partial Fisher-Yates
@@ -614,16 +616,44 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
                 moved[r] = vp;
             }
         }
-        MDET_CUDA(ctx, cudaMemcpyAsync(d_idx, idx.data(), m * 8, cudaMemcpyHostToDevice, s));
-        MDET_TRY(maxprob_core(ctx, g, d_idx, m, mode, floor_prob, d_mx));
-        mx.resize(m);
-        MDET_CUDA(ctx, cudaMemcpyAsync(mx.data(), d_mx, m * 8, cudaMemcpyDeviceToHost, s));
-        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        // Maxima at floor f1 >= floor_prob first: a maximum at or above f1 is
+        // exact (the pair that attains it is a candidate at that floor), so the
+        // cuts the search makes at or above f1 see the same counts.  Samples
+        // below f1 are scored again at floor_prob only if the search goes
+        // below f1.  The result is the same for any f1; a higher f1 just
+        // means fewer candidate pairs.
+        const double f1 = full ? floor_prob : std::max(floor_prob, next_floor);
+        auto maxima = [&](const uint64_t* ids, uint64_t k, double floor, double* out) -> int {
+            MDET_CUDA(ctx, cudaMemcpyAsync(d_idx, ids, k * 8, cudaMemcpyHostToDevice, s));
+            MDET_TRY(maxprob_core(ctx, g, d_idx, k, mode, floor, d_mx));
+            MDET_CUDA(ctx, cudaMemcpyAsync(out, d_mx, k * 8, cudaMemcpyDeviceToHost, s));
+            MDET_CUDA(ctx, cudaStreamSynchronize(s));
+            return MDET_OK;
+        };
+        std::vector<double> raw(m);
+        MDET_TRY(maxima(idx.data(), m, f1, raw.data()));
+        std::vector<uint64_t> low;  // sample positions whose maximum is below f1
+        if (f1 > floor_prob)
+            for (uint64_t i = 0; i < m; ++i)
+                if (!(raw[i] >= f1)) low.push_back(i);
+        mx = raw;
         std::sort(mx.begin(), mx.end(), std::greater<double>());
         uint64_t p = 999, pp = 1000, counton = 0;
         double cov = 0, pcov = 0;
         for (; p > 700;) {
             double cut = (double)p / 1000.;
+            if (cut < f1 && !low.empty()) {
+                // the exact maxima below f1 (all of them lie below f1, so the
+                // first counton entries of the sorted list stay in place)
+                std::vector<uint64_t> ids(low.size());
+                std::vector<double> v(low.size());
+                for (size_t i = 0; i < low.size(); ++i) ids[i] = idx[low[i]];
+                MDET_TRY(maxima(ids.data(), ids.size(), floor_prob, v.data()));
+                for (size_t i = 0; i < low.size(); ++i) raw[low[i]] = v[i];
+                low.clear();
+                mx = raw;
+                std::sort(mx.begin(), mx.end(), std::greater<double>());
+            }
             while (counton < m && mx[counton] >= cut) counton++;
             cov = (double)counton / m;
             if (cov >= coverage) {
@@ -652,6 +682,7 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
         for (int i = 0; i < 10; ++i) {
             double minp = 0;
             MDET_TRY(sample(false, &minp));
+            next_floor = (minp - 10.) / 1000.;
             if (minp < 701) minp = 700.;
             ptnf += minp;
             if (i == 1 && ptnf / 2 < 701) {

@@ -45,9 +45,14 @@ struct mdet_ctx {
     void* encode_tiled = nullptr;  // cuTensorMapEncodeTiled entry point
     bool count_scratch_dirty = false;
     uint64_t total_launches = 0;
-    // key of the d* table currently held in scratch "tbl.st"
-    bool tbl_valid = false;
-    double tbl_L = 0, tbl_lmin = 0, tbl_lmax = 0;
+    // keys of the d* tables held in scratch "tbl.st0".."tbl.st3" (least
+    // recently used one is rebuilt on a miss)
+    struct TblSlot {
+        bool valid = false;
+        double L = 0, lmin = 0, lmax = 0;
+        uint64_t used = 0;
+    } tbl[4];
+    uint64_t tbl_clock = 0;
     bool timing = false;
     std::unordered_map<std::string, KernelTimer> timers;
     const struct mdet_mlp* mlp = nullptr;          // network of MDET_MODE_LEARNED

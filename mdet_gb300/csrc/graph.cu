@@ -355,7 +355,7 @@ int validate_graph_args(mdet_ctx* ctx, uint64_t n, double cutoff, uint32_t max_e
 
 // --- max-probability sample on a prepared contig set ---
 int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, uint64_t m, int mode,
-                 double floor_prob, double* d_out) {
+                 double floor_prob, double* d_out, double* lrange = nullptr) {
     cudaStream_t s = ctx->stream;
     if (m == 0) return MDET_OK;
     uint32_t* keys = (uint32_t*)ctx_scratch(ctx, "mp.keys", m * 4);
@@ -384,7 +384,7 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
     MDET_LAUNCHED(ctx, "k_sample_meta");
     const double L = floor_prob > 0 ? logit(floor_prob) : -INFINITY;
     DstarTable tbl;
-    MDET_TRY(build_dstar_table(ctx, g.ls, g.n, L, &tbl));
+    MDET_TRY(build_dstar_table(ctx, g.ls, g.n, L, &tbl, true, lrange));
     uint2* cand = nullptr;
     unsigned long long ncand = 0;
     if (mode != MDET_MODE_PLAIN) {
@@ -590,8 +590,10 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
     if (!d_idx || !d_mx) return MDET_ERR_NOMEM;
     // the search only compares maxima against cutoffs above 0.700
     const double floor_prob = 0.7;
-    // first floor of a pass: just below the previous pass's cutoff
+    // first floor of a pass: just below the previous pass's cutoff, on a
+    // 0.005 grid so that passes share a d* table
     double next_floor = 0.9;
+    double lrange[2] = {NAN, NAN};  // log-size range of the sorted rows, found once
     auto sample = [&](bool full, double* p_out) -> int {
         uint64_t m = full ? n : std::min<uint64_t>(n, 2500);
         // random_unique (cuda/Cuda2.cu:500-511): a partial Fisher-Yates
@@ -625,7 +627,7 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
         const double f1 = full ? floor_prob : std::max(floor_prob, next_floor);
         auto maxima = [&](const uint64_t* ids, uint64_t k, double floor, double* out) -> int {
             MDET_CUDA(ctx, cudaMemcpyAsync(d_idx, ids, k * 8, cudaMemcpyHostToDevice, s));
-            MDET_TRY(maxprob_core(ctx, g, d_idx, k, mode, floor, d_mx));
+            MDET_TRY(maxprob_core(ctx, g, d_idx, k, mode, floor, d_mx, lrange));
             MDET_CUDA(ctx, cudaMemcpyAsync(out, d_mx, k * 8, cudaMemcpyDeviceToHost, s));
             MDET_CUDA(ctx, cudaStreamSynchronize(s));
             return MDET_OK;
@@ -682,7 +684,7 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
         for (int i = 0; i < 10; ++i) {
             double minp = 0;
             MDET_TRY(sample(false, &minp));
-            next_floor = (minp - 10.) / 1000.;
+            next_floor = std::floor((minp - 10.) / 5.) * 5. / 1000.;
             if (minp < 701) minp = 700.;
             ptnf += minp;
             if (i == 1 && ptnf / 2 < 701) {

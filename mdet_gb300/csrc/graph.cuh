@@ -114,8 +114,11 @@ int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, Gr
 int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, const GraphPrep& g,
               uint64_t base, const uint32_t* order = nullptr);
 // sorted: d_ls_sorted is ascending (else its range is found by a scan).
+// range: optional host copy of the log-size range {min, max}; when given with
+// range[0] not NaN it is used as is, else it is found (one device round trip)
+// and stored there for the next call over the same sizes.
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
-                      bool sorted = true);
+                      bool sorted = true, double* range = nullptr);
 // A table over a given log-size range written to st (MDET_TBL_LEVELS x TBL x TBL floats).
 int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out);
 // The same over the union of `count` device ranges (lo, hi pairs; entries

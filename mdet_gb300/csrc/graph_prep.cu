@@ -497,36 +497,54 @@ int build_dstar_table_dev(mdet_ctx* ctx, const TableGrid* grid, double logit_cut
 }
 
 int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, double logit_cut, DstarTable* out,
-                      bool sorted) {
+                      bool sorted, double* range) {
     out->dyn = nullptr;
     cudaStream_t s = ctx->stream;
-    double* mm = (double*)ctx_scratch(ctx, "tbl.mm", 16);
-    float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
-    float* st = (float*)ctx_scratch(ctx, "tbl.st", (size_t)MDET_TBL_LEVELS * MDET_TBL * MDET_TBL * 4);
-    if (!mm || !pts || !st) return MDET_ERR_NOMEM;
-    // the range is needed on the host to place the grid
-    double range[2];
-    k_minmax<<<1, sorted ? 32 : 1024, 0, s>>>(d_ls_sorted, n, sorted ? 1 : 0, mm);
-    MDET_LAUNCHED(ctx, "k_minmax");
-    MDET_CUDA(ctx, cudaMemcpyAsync(range, mm, 16, cudaMemcpyDeviceToHost, s));
-    MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    double lmin = range[0], lmax = range[1];
-    const bool same = ctx->tbl_valid && ctx->tbl_L == logit_cut && ctx->tbl_lmin == lmin && ctx->tbl_lmax == lmax;
+    double lmin, lmax;
+    if (range && !std::isnan(range[0])) {
+        lmin = range[0];
+        lmax = range[1];
+    } else {
+        // the range is needed on the host to place the grid
+        double* mm = (double*)ctx_scratch(ctx, "tbl.mm", 16);
+        if (!mm) return MDET_ERR_NOMEM;
+        double r[2];
+        k_minmax<<<1, sorted ? 32 : 1024, 0, s>>>(d_ls_sorted, n, sorted ? 1 : 0, mm);
+        MDET_LAUNCHED(ctx, "k_minmax");
+        MDET_CUDA(ctx, cudaMemcpyAsync(r, mm, 16, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        lmin = r[0];
+        lmax = r[1];
+        if (range) {
+            range[0] = lmin;
+            range[1] = lmax;
+        }
+    }
     double h = (lmax - lmin) / MDET_TBL;
     if (!(h > 1e-7)) h = 1e-7;
-    if (same) {  // the table in scratch was built for this cutoff and size range
-        out->st = st;
-        out->lmin = (float)(lmin - 1e-9);
-        out->inv_h = (float)(1.0 / h);
-        return MDET_OK;
+    // a table already built for this cutoff and size range?
+    int slot = -1, lru = 0;
+    for (int k = 0; k < 4; ++k) {
+        const auto& t = ctx->tbl[k];
+        if (t.valid && t.L == logit_cut && t.lmin == lmin && t.lmax == lmax) slot = k;
+        if (ctx->tbl[k].used < ctx->tbl[lru].used) lru = k;
     }
-    ctx->tbl_valid = false;
-    ctx->tbl_L = logit_cut;
-    ctx->tbl_lmin = lmin;
-    ctx->tbl_lmax = lmax;
-    lmin -= 1e-9;
+    const bool hit = slot >= 0;
+    if (!hit) slot = lru;
+    const std::string name = "tbl.st" + std::to_string(slot);
+    float* st = (float*)ctx_scratch(ctx, name.c_str(), (size_t)MDET_TBL_LEVELS * MDET_TBL * MDET_TBL * 4);
+    if (!st) return MDET_ERR_NOMEM;
+    auto& t = ctx->tbl[slot];
+    t.used = ++ctx->tbl_clock;
+    out->st = st;
+    out->lmin = (float)(lmin - 1e-9);
+    out->inv_h = (float)(1.0 / h);
+    if (hit) return MDET_OK;
+    float* pts = (float*)ctx_scratch(ctx, "tbl.pts", (size_t)kPts * kPts * 4);
+    if (!pts) return MDET_ERR_NOMEM;
+    t.valid = false;
     dim3 grid((kPts + 127) / 128, kPts);
-    k_dstar_points<<<grid, 128, 0, s>>>(lmin, h, logit_cut, model_split(), pts);
+    k_dstar_points<<<grid, 128, 0, s>>>(lmin - 1e-9, h, logit_cut, model_split(), pts);
     MDET_LAUNCHED(ctx, "k_dstar_points");
     k_dstar_cells<<<MDET_TBL, MDET_TBL, 0, s>>>(pts, st);
     MDET_LAUNCHED(ctx, "k_dstar_cells");
@@ -536,9 +554,9 @@ int build_dstar_table(mdet_ctx* ctx, const double* d_ls_sorted, uint64_t n, doub
         k_sparse<<<MDET_TBL, MDET_TBL, 0, s>>>(st, k);
         MDET_LAUNCHED(ctx, "k_sparse");
     }
-    out->st = st;
-    out->lmin = (float)lmin;
-    out->inv_h = (float)(1.0 / h);
-    ctx->tbl_valid = true;
+    t.valid = true;
+    t.L = logit_cut;
+    t.lmin = lmin;
+    t.lmax = lmax;
     return MDET_OK;
 }

@@ -106,6 +106,22 @@ def test_max_prob_vs_oracle(gpu_ctx, set_a, mode):
     assert np.abs(exact - ref[:60]).max() <= 1e-9
 
 
+@pytest.mark.parametrize("genomes", [50, 2000])
+def test_ptnf_search_sampled_vs_oracle(gpu_ctx, genomes):
+    """Above 25,000 contigs the search samples 2,500 rows ten times.  Each pass
+    scores maxima at a floor just below the previous cutoff first and rescores
+    the rows below it only when the search goes there: with 50 genomes the
+    cutoff stays high, with 2,000 it drops below the first floor (0.9), so
+    both branches run; the result must equal the oracle's."""
+    a, _, tnf = synth_set(seed=5, n=26000, genomes=genomes)
+    want = oracle.ptnf_search(tnf, a.log_sizes, 0.95, seed=77)
+    oracle.srand(77)
+    got = gpu_ctx.ptnf_search(tnf, a.log_sizes, 0.95, mode="bf16")
+    assert got == want
+    if genomes == 2000:
+        assert want < 900
+
+
 @pytest.mark.parametrize("mode", ["plain", "bf16"])
 def test_ptnf_search_vs_oracle(gpu_ctx, set_a, mode):
     a, _, tnf = set_a

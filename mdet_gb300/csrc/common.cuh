@@ -72,6 +72,8 @@ struct mdet_ctx {
     uint64_t graph_replays = 0;
     void* batch_plan = nullptr;
     void (*batch_plan_free)(void*) = nullptr;
+    // copy streams of the host-buffer entry points (created on first use)
+    cudaStream_t io_in = nullptr, io_out = nullptr;
 };
 
 // Event pair around one launch of a named kernel when timing is enabled.

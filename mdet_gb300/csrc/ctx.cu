@@ -296,6 +296,8 @@ int mdet_ctx_destroy(mdet_ctx* ctx) {
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->d_flag) cudaFree(ctx->d_flag);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->io_in) cudaStreamDestroy(ctx->io_in);
+    if (ctx->io_out) cudaStreamDestroy(ctx->io_out);
     delete ctx;
     return MDET_OK;
 }

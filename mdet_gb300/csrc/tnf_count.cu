@@ -20,6 +20,7 @@
 #include <cub/cub.cuh>
 
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 
@@ -328,6 +329,71 @@ int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, cons
     return check_flag(ctx);
 }
 
+// Chunked host-buffer path of mdet_tnf_count (file-order views, see there).
+static int count_chunked(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint64_t* off, const uint64_t* len,
+                         uint64_t n, uint32_t* counts, float* tnf, char* d_bytes, const uint64_t* d_off,
+                         const uint64_t* d_len, uint32_t* d_counts, float* d_tnf) {
+    cudaStream_t s = ctx->stream;
+    if (!ctx->io_in) MDET_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->io_in, cudaStreamNonBlocking));
+    if (!ctx->io_out) MDET_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->io_out, cudaStreamNonBlocking));
+    const uint64_t target = (uint64_t)1 << 30;
+    // chunk k: contigs [cs[k], cs[k+1]), bytes [bs[k], bs[k+1]) (the chunks tile the buffer)
+    std::vector<uint64_t> cs{0}, bs{0};
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t end = off[i] + len[i];
+        if (end - bs.back() >= target && i + 1 < n) {
+            cs.push_back(i + 1);
+            bs.push_back(end);
+        }
+    }
+    cs.push_back(n);
+    bs.push_back(nbytes);
+    const size_t K = cs.size() - 1;
+    std::vector<cudaEvent_t> landed(K, nullptr), counted(K, nullptr);
+    int rc = MDET_OK;
+    for (size_t k = 0; k < K && rc == MDET_OK; ++k) {
+        rc = ctx_cuda(ctx, cudaEventCreateWithFlags(&landed[k], cudaEventDisableTiming), "cudaEventCreate");
+        if (rc == MDET_OK)
+            rc = ctx_cuda(ctx, cudaEventCreateWithFlags(&counted[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    for (size_t k = 0; k < K && rc == MDET_OK; ++k) {
+        rc = ctx_cuda(ctx,
+                      cudaMemcpyAsync(d_bytes + bs[k], bytes + bs[k], bs[k + 1] - bs[k], cudaMemcpyHostToDevice,
+                                      ctx->io_in),
+                      "cudaMemcpyAsync");
+        if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaEventRecord(landed[k], ctx->io_in), "cudaEventRecord");
+    }
+    for (size_t k = 0; k < K && rc == MDET_OK; ++k) {
+        const uint64_t c0 = cs[k], nk = cs[k + 1] - cs[k];
+        rc = ctx_cuda(ctx, cudaStreamWaitEvent(s, landed[k], 0), "cudaStreamWaitEvent");
+        if (rc == MDET_OK && nk)
+            rc = count_impl(ctx, d_bytes, nbytes, d_off + c0, d_len + c0, nk, d_counts + c0 * MDET_NTNF,
+                            d_tnf + c0 * MDET_NTNF);
+        if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaEventRecord(counted[k], s), "cudaEventRecord");
+        if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaStreamWaitEvent(ctx->io_out, counted[k], 0), "cudaStreamWaitEvent");
+        if (rc == MDET_OK && nk)
+            rc = ctx_cuda(ctx,
+                          cudaMemcpyAsync(counts + c0 * MDET_NTNF, d_counts + c0 * MDET_NTNF, nk * MDET_NTNF * 4,
+                                          cudaMemcpyDeviceToHost, ctx->io_out),
+                          "cudaMemcpyAsync");
+        if (rc == MDET_OK && nk)
+            rc = ctx_cuda(ctx,
+                          cudaMemcpyAsync(tnf + c0 * MDET_NTNF, d_tnf + c0 * MDET_NTNF, nk * MDET_NTNF * 4,
+                                          cudaMemcpyDeviceToHost, ctx->io_out),
+                          "cudaMemcpyAsync");
+    }
+    if (rc != MDET_OK) ctx->count_scratch_dirty = true;
+    // no copy may still touch the caller's buffers when this returns
+    cudaStreamSynchronize(ctx->io_in);
+    cudaStreamSynchronize(ctx->io_out);
+    for (auto e : landed)
+        if (e) cudaEventDestroy(e);
+    for (auto e : counted)
+        if (e) cudaEventDestroy(e);
+    if (rc != MDET_OK) return rc;
+    return check_flag(ctx);
+}
+
 int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint64_t* off, const uint64_t* len,
                    uint64_t n, uint32_t* counts, float* tnf) {
     if (!ctx) return MDET_ERR_INVALID;
@@ -346,9 +412,18 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
     uint32_t* d_counts = (uint32_t*)ctx_scratch(ctx, "io.counts", n * MDET_NTNF * 4);
     float* d_tnf = (float*)ctx_scratch(ctx, "io.tnf", n * MDET_NTNF * 4);
     if (!d_bytes || !d_off || !d_len || !d_counts || !d_tnf) return MDET_ERR_NOMEM;
-    MDET_CUDA(ctx, cudaMemcpyAsync(d_bytes, bytes, nbytes, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(d_off, off, n * 8, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(d_len, len, n * 8, cudaMemcpyHostToDevice, s));
+    // Views in file order (each contig after the previous one), as a FASTA
+    // reader makes them: copy the bytes in ~1 GB chunks on a copy stream and
+    // count each chunk once it has landed, returning its rows on a second copy
+    // stream, so the count and the result copies hide behind the input copy.
+    // The kernel reads nothing outside a contig's own bytes for its counts.
+    bool ordered = n >= 2 && nbytes >= ((uint64_t)2 << 30);
+    for (uint64_t i = 1; ordered && i < n; ++i) ordered = off[i] >= off[i - 1] + len[i - 1];
+    if (ordered) return count_chunked(ctx, bytes, nbytes, off, len, n, counts, tnf, d_bytes, d_off, d_len, d_counts,
+                                      d_tnf);
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_bytes, bytes, nbytes, cudaMemcpyHostToDevice, s));
     int rc = count_impl(ctx, d_bytes, nbytes, d_off, d_len, n, d_counts, d_tnf);
     if (rc != MDET_OK) {
         ctx->count_scratch_dirty = true;

@@ -88,6 +88,31 @@ def test_newline_runs_and_piece_edges(gpu_ctx):
     _check(gpu_ctx, raw, offs, lens)
 
 
+def test_host_path_chunked_equals_device(gpu_ctx):
+    """Host buffers of >= 2 GB in file order take the chunked path (copy and
+    count overlapped): its counts and TNF must equal the device-buffer path's."""
+    torch = pytest.importorskip("torch")
+    from mdet_gb300 import synth
+
+    a = synth.generate(seed=31, n=270000, genomes=300)
+    assert a.data.size >= (2 << 30)
+    counts, tnf = gpu_ctx.tnf_count(a.data, a.seq_off, a.seq_len)
+    dev = torch.device("cuda:0")
+    nb = a.data.size
+    d_bytes = torch.zeros(nb + 64, dtype=torch.uint8, device=dev)
+    d_bytes[:nb].copy_(torch.from_numpy(a.data))
+    d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+    d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+    n = a.seq_off.size
+    d_cnt = torch.empty((n, 136), dtype=torch.int32, device=dev)
+    d_tnf = torch.empty((n, 136), dtype=torch.float32, device=dev)
+    gpu_ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), n, d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(counts, d_cnt.cpu().numpy().view(np.uint32))
+    assert np.array_equal(tnf.view(np.uint32), d_tnf.cpu().numpy().view(np.uint32))
+
+
 def test_short_and_empty_contigs(gpu_ctx):
     txt = b">e\n>a\nA\n>b\nACG\n>c\nACGT\n>d\nAC\nGT\n>f\nNNNNNNNN\n"
     data = np.frombuffer(txt, np.uint8)

@@ -11,7 +11,9 @@ program: tetranucleotide counting of every contig, the pTNF search
   value  device-resident: inputs already in HBM, the *_dev entry points
   e2e    the host-buffer entry points a drop-in caller uses (mdet_tnf_count,
          mdet_tnf_ptnf_search, mdet_tnf_graph) from pinned host memory,
-         every copy inside the timed region
+         every copy inside the timed region; e2e.link_h2d_gbs is a plain copy
+         of the same pinned buffer measured right after (the link's speed on
+         that box, which moves e2e by tens of milliseconds between boxes)
 
 Lower is better (seconds per step).  `--impl reference` times the
 reference's CPU arithmetic (the oracle restatement; the reference's own
@@ -292,6 +294,14 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t) / e2e_steps
     e2e_s = reduce_max(e2e_s, dev)
+    # context for e2e (outside the timed region): a plain copy of the same
+    # pinned FASTA buffer into the device-resident copy, i.e. what the
+    # host->device link gives this process on this machine right now
+    torch.cuda.synchronize()
+    t_link = time.perf_counter()
+    d_bytes[:nbytes].copy_(pinned[:nbytes], non_blocking=True)
+    torch.cuda.synchronize()
+    link_gbs = nbytes / (time.perf_counter() - t_link) / 1e9
     ne = e2e_info["edges"]
     h2d = nbytes + 2 * n * 8 + 2 * (n * 136 * 4 + n * 8)
     d2h = n * 136 * 8 + ne * 24
@@ -343,6 +353,7 @@ def run_ours(args):
             "data": "synthetic (seeded Markov-genome assembly; no public dataset is shipped)",
             "config": workload_config(n, G, args.mode, ws),
             "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "link_h2d_gbs": round(link_gbs, 1),
                     "phases_s": e2e_info.get("phases_s")},
             "gpu_launches": int(launches),
             "roofline": roof,

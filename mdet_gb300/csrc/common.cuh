@@ -72,6 +72,20 @@ struct mdet_ctx {
     uint64_t graph_replays = 0;
     void* batch_plan = nullptr;
     void (*batch_plan_free)(void*) = nullptr;
+    // The last size-sorted preparation ("pre" buffers): which inputs it was
+    // made from (pointers, n, BF16 part, a hash of their contents) and which
+    // buffers hold it.  Counting invalidates it (new TNF rows).
+    struct PrepCache {
+        bool valid = false;
+        const void* tnf = nullptr;
+        const void* ls = nullptr;
+        uint64_t n = 0;
+        bool bf16 = false;
+        unsigned long long hash = 0;
+        const void* x32 = nullptr;
+        const void* xa = nullptr;
+        uint64_t gen = 0;  // scratch_gen when it was made (no buffer moved since)
+    } prep_cache;
     // copy streams of the host-buffer entry points (created on first use)
     cudaStream_t io_in = nullptr, io_out = nullptr;
 };

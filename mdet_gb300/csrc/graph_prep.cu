@@ -435,12 +435,61 @@ int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n,
     return MDET_OK;
 }
 
+// A 64-bit hash of the prepared inputs' contents (sum over the words of a
+// splitmix64 finaliser of word and position), to recognise unchanged inputs.
+__global__ void k_content_hash(const uint32_t* __restrict__ a, uint64_t na, const uint32_t* __restrict__ b,
+                               uint64_t nb, unsigned long long* __restrict__ out) {
+    unsigned long long h = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < na + nb; i += stride) {
+        unsigned long long z = (unsigned long long)(i < na ? a[i] : b[i - na]) + (i + 1) * 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        h += z ^ (z >> 31);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+// Rows sorted by size (or in the caller's order).  A preparation of the very
+// same inputs that is still in place (same pointers and contents, no count
+// since) is used as it is: the search and the graph of one assembly share it.
 int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g,
                 const uint32_t* order) {
     g->n = (uint32_t)n;
     g->npad = (uint32_t)((n + 255) / 256 * 256);
     MDET_TRY(prep_alloc(ctx, "pre", g->npad, need_bf16, g));
-    return prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, order);
+    auto& c = ctx->prep_cache;
+    if (order) {
+        c.valid = false;
+        return prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, order);
+    }
+    unsigned long long* dh = (unsigned long long*)ctx_scratch(ctx, "pre.hash", 8);
+    if (!dh) return MDET_ERR_NOMEM;
+    cudaStream_t s = ctx->stream;
+    unsigned long long h = 0;
+    MDET_CUDA(ctx, cudaMemsetAsync(dh, 0, 8, s));
+    k_content_hash<<<ctx->num_sms * 8, 256, 0, s>>>((const uint32_t*)d_tnf, n * MDET_NTNF, (const uint32_t*)d_ls,
+                                                    n * 2, dh);
+    MDET_LAUNCHED(ctx, "k_content_hash");
+    MDET_CUDA(ctx, cudaMemcpyAsync(&h, dh, 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    if (c.valid && c.tnf == d_tnf && c.ls == d_ls && c.n == n && (c.bf16 || !need_bf16) && c.hash == h &&
+        c.x32 == g->x32 && (!need_bf16 || c.xa == g->xa) && c.gen == ctx->scratch_gen)
+        return MDET_OK;
+    c.valid = false;
+    MDET_TRY(prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, nullptr));
+    c.valid = true;
+    c.tnf = d_tnf;
+    c.ls = d_ls;
+    c.n = n;
+    c.bf16 = need_bf16;
+    c.hash = h;
+    c.x32 = g->x32;
+    c.xa = g->xa;
+    c.gen = ctx->scratch_gen;
+    return MDET_OK;
 }
 
 int build_dstar_table_at(mdet_ctx* ctx, double lmin, double lmax, double logit_cut, float* st, DstarTable* out) {

@@ -248,6 +248,7 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
                       const uint64_t* d_len, uint64_t n, uint32_t* d_counts, float* d_tnf) {
     if (n == 0) return MDET_OK;
     if (n >= 0xFFFFFFFFull) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs (%llu)", (unsigned long long)n);
+    ctx->prep_cache.valid = false;  // new TNF rows: no preparation carries over past a count
     if (((uintptr_t)d_bytes & 15) != 0)
         return ctx_fail(ctx, MDET_ERR_INVALID, "sequence buffer must be 16-byte aligned");
     (void)nbytes;

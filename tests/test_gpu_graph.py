@@ -129,3 +129,55 @@ def test_ptnf_search_vs_oracle(gpu_ctx, set_a, mode):
     oracle.srand(77)
     got = gpu_ctx.ptnf_search(tnf, a.log_sizes, 0.95, mode=mode)
     assert got == want
+
+
+def test_prep_reuse_follows_contents(gpu_ctx):
+    """Calls on the same device buffers reuse the size-sorted preparation only
+    while the contents are unchanged and no count ran in between: results
+    must always equal a fresh context's on the current contents."""
+    torch = pytest.importorskip("torch")
+    import mdet_gb300 as m
+
+    dev = torch.device("cuda:0")
+    a1, _, t1 = synth_set(seed=41, n=1500, genomes=20)
+    a2, _, t2 = synth_set(seed=42, n=1500, genomes=20)
+    n = 1500
+    d_tnf = torch.from_numpy(t1).to(dev)
+    d_ls = torch.from_numpy(a1.log_sizes.copy()).to(dev)
+    cap = n * 40
+    outs = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+
+    def run(ctx):
+        ne, _ = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, 0.9, 40, "bf16", outs[0].data_ptr(),
+                                  outs[1].data_ptr(), outs[2].data_ptr(), cap)
+        torch.cuda.synchronize()
+        return [o[:ne].cpu().numpy().copy() for o in outs]
+
+    def fresh():
+        with m.Context(0) as c:
+            return run(c)
+
+    r1 = run(gpu_ctx)
+    r1b = run(gpu_ctx)  # same contents: the preparation is reused
+    for x, y in zip(r1, r1b):
+        assert np.array_equal(x, y)
+    # new contents in the same buffers
+    d_tnf.copy_(torch.from_numpy(t2))
+    d_ls.copy_(torch.from_numpy(a2.log_sizes.copy()))
+    r2 = run(gpu_ctx)
+    f2 = fresh()
+    for x, y in zip(r2, f2):
+        assert np.array_equal(x, y)
+    assert not np.array_equal(r1[0], r2[0]) or not np.array_equal(r1[1], r2[1])
+    # a count into the same TNF buffer invalidates it even when it writes the same rows
+    d_bytes = torch.zeros(a2.data.size + 64, dtype=torch.uint8, device=dev)
+    d_bytes[:a2.data.size].copy_(torch.from_numpy(a2.data))
+    d_off = torch.from_numpy(a2.seq_off.astype(np.int64)).to(dev)
+    d_len = torch.from_numpy(a2.seq_len.astype(np.int64)).to(dev)
+    d_cnt = torch.empty((n, 136), dtype=torch.int32, device=dev)
+    gpu_ctx.tnf_count_dev(d_bytes.data_ptr(), a2.data.size, d_off.data_ptr(), d_len.data_ptr(), n, d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+    r3 = run(gpu_ctx)
+    f3 = fresh()
+    for x, y in zip(r3, f3):
+        assert np.array_equal(x, y)

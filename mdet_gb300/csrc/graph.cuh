@@ -76,7 +76,10 @@ __device__ __forceinline__ int tbl_cell_hi(float v, const DstarTable& t) {
 // ranges [alo, ahi] and [blo, bhi]: the x range starts at min(alo, blo),
 // whose suffix-maximised row covers the whole x range; two sparse-table
 // reads cover the y range.
-__device__ __forceinline__ float tile_dstar(const DstarTable& t, float alo, float ahi, float blo, float bhi) {
+// The bound is the larger of two table entries; tile_dstar_cells gives their
+// addresses so that a caller can issue the loads early.
+__device__ __forceinline__ void tile_dstar_cells(const DstarTable& t, float alo, float ahi, float blo, float bhi,
+                                                 const float*& c0, const float*& c1) {
     const float xlo = fminf(alo, blo);
     const float ylo = fmaxf(alo, blo), yhi = fmaxf(ahi, bhi);
     const int cx0 = tbl_cell_lo(xlo, t);
@@ -84,7 +87,13 @@ __device__ __forceinline__ float tile_dstar(const DstarTable& t, float alo, floa
     const int span = cy1 - cy0 + 1;
     const int k = 31 - __clz(span);
     const float* lvl = t.st + (size_t)k * MDET_TBL * MDET_TBL + cx0 * MDET_TBL;
-    return fmaxf(__ldg(lvl + cy0), __ldg(lvl + (cy1 - (1 << k) + 1)));
+    c0 = lvl + cy0;
+    c1 = lvl + (cy1 - (1 << k) + 1);
+}
+__device__ __forceinline__ float tile_dstar(const DstarTable& t, float alo, float ahi, float blo, float bhi) {
+    const float *c0, *c1;
+    tile_dstar_cells(t, alo, ahi, blo, bhi, c0, c1);
+    return fmaxf(__ldg(c0), __ldg(c1));
 }
 
 // Host-side entry points of the stages (graph_*.cu).

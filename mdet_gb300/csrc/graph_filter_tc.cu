@@ -170,25 +170,57 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 // threshold over the blocks' sizes, e_a and e_b bound the BF16 rounding of the
 // rows, and the slack covers FP32 accumulation and the two-term split of
 // ||b~||^2/2.
+//
+// It takes two dependent rounds of loads (block metadata, then the two d*
+// table cells), split here so that a caller can run them ahead of use.
+struct R2Meta {  // round 1: the blocks' metadata and the table selector
+    BlockMeta ma, mb0, mb1;
+    uint32_t tsel;
+};
+struct R2Cells {  // round 2: the table cells (loads in flight) and the other terms
+    float t0, t1, E, N;
+};
 template <int BN>
-__device__ __forceinline__ float tile_r2(const TcArgs& p, uint32_t ib, uint32_t J) {
-    const BlockMeta ma = p.ameta[ib];
+__device__ __forceinline__ R2Meta r2_meta(const TcArgs& p, uint32_t ib, uint32_t J) {
     constexpr uint32_t kBlk = BN / MDET_BLK;  // metadata blocks per column tile
-    const BlockMeta mb0 = p.bmeta[kBlk * J], mb1 = p.bmeta[kBlk * J + kBlk - 1];
-    const float blo = fminf(mb0.lo, mb1.lo), bhi = fmaxf(mb0.hi, mb1.hi);
+    R2Meta m;
+    m.ma = p.ameta[ib];
+    m.mb0 = p.bmeta[kBlk * J];
+    m.mb1 = p.bmeta[kBlk * J + kBlk - 1];
+    m.tsel = p.row_tbl ? p.row_tbl[ib] : 0u;
+    return m;
+}
+// tbase: p.tbl with the dynamic grid (if any) already read
+__device__ __forceinline__ R2Cells r2_cells(const TcArgs& p, const DstarTable& tbase, const R2Meta& m) {
+    DstarTable tb = tbase;
+    tb.st += (uint64_t)m.tsel * p.tbl_stride;
+    const float *c0, *c1;
+    tile_dstar_cells(tb, m.ma.lo, m.ma.hi, fminf(m.mb0.lo, m.mb1.lo), fmaxf(m.mb0.hi, m.mb1.hi), c0, c1);
+    R2Cells c;
+    c.t0 = __ldg(c0);
+    c.t1 = __ldg(c1);
+    c.E = m.ma.emax + fmaxf(m.mb0.emax, m.mb1.emax);
+    const float nb = fmaxf(m.mb0.nmax, m.mb1.nmax);
+    c.N = m.ma.nmax * nb + nb * nb;
+    return c;
+}
+__device__ __forceinline__ float r2_finish(const R2Cells& c) {
+    const float R = fmaxf(c.t0, c.t1) * (1.f + 2e-5f) + 1e-6f + c.E;
+    float R2 = R * R + 4e-5f * c.N + 1e-7f;
+    if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
+    return R2;
+}
+__device__ __forceinline__ DstarTable table_base(const TcArgs& p) {
     DstarTable tb = p.tbl;
     if (tb.dyn) {
         tb.lmin = tb.dyn[0];
         tb.inv_h = tb.dyn[1];
     }
-    if (p.row_tbl) tb.st += (uint64_t)p.row_tbl[ib] * p.tbl_stride;
-    const float T = tile_dstar(tb, ma.lo, ma.hi, blo, bhi);
-    const float E = ma.emax + fmaxf(mb0.emax, mb1.emax);
-    const float nb = fmaxf(mb0.nmax, mb1.nmax);
-    const float R = T * (1.f + 2e-5f) + 1e-6f + E;
-    float R2 = R * R + 4e-5f * (ma.nmax * nb + nb * nb) + 1e-7f;
-    if (!(R2 < 1e30f)) R2 = __int_as_float(0x7f800000);
-    return R2;
+    return tb;
+}
+template <int BN>
+__device__ __forceinline__ float tile_r2(const TcArgs& p, uint32_t ib, uint32_t J) {
+    return r2_finish(r2_cells(p, table_base(p), r2_meta<BN>(p, ib, J)));
 }
 
 // ------------------------------------------------------------ schedule --
@@ -391,6 +423,17 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
             // -------------------------------------------------- MMA issuer
             if (lane == 0) {
                 Cursor c = cursor_first(p, cta, G);
+                // one-half shapes: the R^2 loads run ahead (metadata two tiles,
+                // table cells one tile), so only arithmetic sits between MMA batches
+                Cursor n1 = c;
+                if (n1.valid) advance(p, n1, cta, G);
+                const DstarTable tbase = table_base(p);
+                R2Cells cc{};
+                R2Meta mn{};
+                if constexpr (S::MH == 1) {
+                    if (c.valid) cc = r2_cells(p, tbase, r2_meta<BN>(p, c.I, c.J));
+                    if (n1.valid) mn = r2_meta<BN>(p, n1.I, n1.J);
+                }
                 uint32_t a_ph = 0, b_ph[NST], e_ph[2] = {0, 0};
 #pragma unroll
                 for (int t = 0; t < NST; ++t) b_ph[t] = 0;
@@ -429,17 +472,19 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                     }
                     mma_commit(&ctl.b_empty[bs]);
                     mma_commit(&ctl.acc_full[s]);
+                    Cursor n2 = n1;
+                    if (n2.valid) advance(p, n2, cta, G);
                     if constexpr (S::MH == 1) {
-                        // the tile's R^2 for the epilogue, loaded while the MMAs
-                        // run (this thread would otherwise wait); the epilogue of
-                        // the tile that used this slot before is done (acc_empty)
-                        ctl.r2[s] = tile_r2<BN>(p, c.I, c.J);
+                        // the tile's R^2 for the epilogue (the epilogue of the
+                        // tile that used this slot before is done: acc_empty)
+                        ctl.r2[s] = r2_finish(cc);
                         mbar_arrive(&ctl.acc_full[s]);
+                        if (n1.valid) cc = r2_cells(p, tbase, mn);
+                        if (n2.valid) mn = r2_meta<BN>(p, n2.I, n2.J);
                     }
-                    Cursor nx = c;
-                    advance(p, nx, cta, G);
-                    if (!nx.valid || nx.I != c.I) mma_commit(&ctl.a_empty);
-                    c = nx;
+                    if (!n1.valid || n1.I != c.I) mma_commit(&ctl.a_empty);
+                    c = n1;
+                    n1 = n2;
                 }
             }
         } else {

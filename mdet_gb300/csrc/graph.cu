@@ -94,31 +94,45 @@ __global__ void k_sample_gather_b(const uint32_t* __restrict__ row_map, uint64_t
 
 // per-128 block metadata of the gathered sample (log-size range, and for
 // BF16 rows the max rounding error / norm of the gathered rows)
+// Metadata of the sample's blocks of MDET_BLK rows, one warp per block: lane
+// l takes rows l, l + 32, ... of the block (the gathers overlap instead of
+// running one after another).  NaN is the identity of fmin/fmax here, so the
+// result is the same as a walk over the rows in order.
 __global__ void k_sample_meta(const uint32_t* __restrict__ row_map, uint64_t m, const double* __restrict__ ls,
                               const BlockMeta* __restrict__ src_meta, uint64_t nblk, BlockMeta* __restrict__ out) {
-    uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (b >= nblk) return;
-    uint64_t r0 = b * MDET_BLK, r1 = min(m, r0 + MDET_BLK);
+    const uint64_t b = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (b >= nblk) return;  // warp-uniform
+    const uint64_t r0 = b * MDET_BLK, r1 = min(m, r0 + MDET_BLK);
     BlockMeta o;
-    o.lo = o.hi = 0.f;
     o.emax = o.nmax = 0.f;
     if (r0 < m) {
-        double lo = ls[row_map[r0]], hi = lo;
-        for (uint64_t r = r0 + 1; r < r1; ++r) {
-            lo = fmin(lo, ls[row_map[r]]);
-            hi = fmax(hi, ls[row_map[r]]);
+        double lo = __longlong_as_double(0x7ff8000000000000ll), hi = lo;
+        float e = 0.f, nm = 0.f;
+        for (uint64_t r = r0 + lane; r < r1; r += 32) {
+            const uint32_t row = row_map[r];
+            const double v = ls[row];
+            lo = fmin(lo, v);
+            hi = fmax(hi, v);
+            const BlockMeta& sm = src_meta[row / MDET_BLK];
+            e = fmaxf(e, sm.emax);
+            nm = fmaxf(nm, sm.nmax);
+        }
+#pragma unroll
+        for (int d = 16; d; d >>= 1) {
+            lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, d));
+            hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, d));
+            e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, d));
+            nm = fmaxf(nm, __shfl_xor_sync(0xffffffffu, nm, d));
         }
         o.lo = __double2float_rd(lo);
         o.hi = __double2float_ru(hi);
-        for (uint64_t r = r0; r < r1; ++r) {
-            const BlockMeta& sm = src_meta[row_map[r] / MDET_BLK];
-            o.emax = fmaxf(o.emax, sm.emax);
-            o.nmax = fmaxf(o.nmax, sm.nmax);
-        }
+        o.emax = e;
+        o.nmax = nm;
     } else {
         o.lo = o.hi = __double2float_rd(ls[row_map[m - 1]]);
     }
-    out[b] = o;
+    if (lane == 0) out[b] = o;
 }
 
 }  // namespace
@@ -295,7 +309,7 @@ int gather_rows_bf16(mdet_ctx* ctx, const GraphPrep& g, const uint32_t* row_map,
     if (m == 0) return MDET_OK;
     k_sample_gather_bf16<<<(unsigned)mpad, 64, 0, s>>>(row_map, m, mpad, g.xa, g.nsq, out->ab, out->ansq);
     MDET_LAUNCHED(ctx, "k_sample_gather_bf16");
-    k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, out->meta);
+    k_sample_meta<<<(unsigned)((nblk * 32 + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, out->meta);
     MDET_LAUNCHED(ctx, "k_sample_meta");
     return MDET_OK;
 }
@@ -380,8 +394,6 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
     const uint32_t* row_map = keys2;  // sorted positions of the sample, ascending
     k_sample_gather<<<(unsigned)m, 64, 0, s>>>(row_map, order, m, g.x32, g.ls, a32, als, slot_of);
     MDET_LAUNCHED(ctx, "k_sample_gather");
-    k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta32, nblk, ameta32);
-    MDET_LAUNCHED(ctx, "k_sample_meta");
     const double L = floor_prob > 0 ? logit(floor_prob) : -INFINITY;
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, g.n, L, &tbl, true, lrange));
@@ -395,7 +407,7 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
         if (!sb) return MDET_ERR_NOMEM;
         k_sample_gather_b<<<(unsigned)((mpad + 7) / 8), 256, 0, s>>>(row_map, m, mpad, g.xb, sb);
         MDET_LAUNCHED(ctx, "k_sample_gather_b");
-        k_sample_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
+        k_sample_meta<<<(unsigned)((nblk * 32 + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta, nblk, ameta);
         MDET_LAUNCHED(ctx, "k_sample_meta");
         const BSide bs{sb, (uint32_t)m, ameta};
         MDET_TRY(run_filter(ctx, mode, g, true, nullptr, nullptr, nullptr, 0, nullptr, nullptr, tbl, "mp", &cand,
@@ -403,6 +415,8 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
         MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out, true));
         return MDET_OK;
     }
+    k_sample_meta<<<(unsigned)((nblk * 32 + 127) / 128), 128, 0, s>>>(row_map, m, g.ls, g.meta32, nblk, ameta32);
+    MDET_LAUNCHED(ctx, "k_sample_meta");
     MDET_TRY(run_filter(ctx, mode, g, true, a32, nullptr, nullptr, (uint32_t)m, ameta, ameta32, tbl, "mp", &cand,
                         &ncand));
     MDET_TRY(exact_maxprob(ctx, g, cand, ncand, row_map, m, slot_of, d_out));

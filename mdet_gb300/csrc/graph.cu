@@ -7,7 +7,6 @@
 #include <cstring>
 #include <functional>
 #include <numeric>
-#include <unordered_map>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -598,7 +597,10 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
     GraphPrep g;
     MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, mode != MDET_MODE_PLAIN, &g));
     std::vector<uint64_t> idx(n);
-    std::vector<double> mx;
+    // sparse shuffle state: open addressing over positions (key ~0: empty)
+    std::vector<uint64_t> mkey, mval;
+    // ge[q]: how many sampled maxima are >= q / 1000. (q = 0..1000)
+    std::vector<uint64_t> ge(1002);
     uint64_t* d_idx = (uint64_t*)ctx_scratch(ctx, "pt.idx", n * 8);
     double* d_mx = (double*)ctx_scratch(ctx, "pt.mx", n * 8);
     if (!d_idx || !d_mx) return MDET_ERR_NOMEM;
@@ -618,18 +620,31 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
             for (uint64_t p = 0; p < m; ++p) std::swap(idx[p], idx[p + (uint64_t)rand() % (n - p)]);
         } else {
             // the same draws on a sparse array (untouched positions hold their
-            // own index), so a pass costs O(m) instead of O(n)
-            std::unordered_map<uint64_t, uint64_t> moved;
-            moved.reserve(2 * m);
+            // own index), so a pass costs O(m) instead of O(n); the moved
+            // positions live in a linear-probing table of >= 4m slots
+            uint64_t cap = 16;
+            while (cap < 4 * m) cap <<= 1;
+            mkey.assign(cap, ~0ull);
+            mval.resize(cap);
+            auto slot = [&](uint64_t i) {
+                uint64_t h = (i * 0x9E3779B97F4A7C15ull) >> 20;
+                while (true) {
+                    h &= cap - 1;
+                    if (mkey[h] == i || mkey[h] == ~0ull) return h;
+                    ++h;
+                }
+            };
             auto at = [&](uint64_t i) {
-                const auto it = moved.find(i);
-                return it == moved.end() ? i : it->second;
+                const uint64_t h = slot(i);
+                return mkey[h] == i ? mval[h] : i;
             };
             for (uint64_t p = 0; p < m; ++p) {
                 const uint64_t r = p + (uint64_t)rand() % (n - p);
                 const uint64_t vp = at(p), vr = at(r);
                 idx[p] = vr;  // later steps only touch positions after p
-                moved[r] = vp;
+                const uint64_t h = slot(r);
+                mkey[h] = r;
+                mval[h] = vp;
             }
         }
         // Maxima at floor f1 >= floor_prob first: a maximum at or above f1 is
@@ -652,8 +667,21 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
         if (f1 > floor_prob)
             for (uint64_t i = 0; i < m; ++i)
                 if (!(raw[i] >= f1)) low.push_back(i);
-        mx = raw;
-        std::sort(mx.begin(), mx.end(), std::greater<double>());
+        // counts of maxima at or above each cut q / 1000. (what walking the
+        // maxima sorted in descending order gives, without the sort)
+        auto count_cuts = [&]() {
+            std::fill(ge.begin(), ge.end(), 0);
+            for (uint64_t i = 0; i < m; ++i) {
+                const double v = raw[i];
+                if (!(v >= 0.)) continue;  // below every cut (or NaN)
+                int q = v >= 1. ? 1000 : (int)(v * 1000.);
+                while (q < 1000 && v >= (double)(q + 1) / 1000.) ++q;
+                while (q > 0 && !(v >= (double)q / 1000.)) --q;
+                ge[q]++;
+            }
+            for (int q = 999; q >= 0; --q) ge[q] += ge[q + 1];
+        };
+        count_cuts();
         uint64_t p = 999, pp = 1000, counton = 0;
         double cov = 0, pcov = 0;
         for (; p > 700;) {
@@ -667,10 +695,9 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
                 MDET_TRY(maxima(ids.data(), ids.size(), floor_prob, v.data()));
                 for (size_t i = 0; i < low.size(); ++i) raw[low[i]] = v[i];
                 low.clear();
-                mx = raw;
-                std::sort(mx.begin(), mx.end(), std::greater<double>());
+                count_cuts();
             }
-            while (counton < m && mx[counton] >= cut) counton++;
+            counton = ge[p];
             cov = (double)counton / m;
             if (cov >= coverage) {
                 if (cov - coverage > coverage - pcov) {

@@ -196,6 +196,40 @@ int mdet_tnf_graph_batched(mdet_ctx* ctx, mdet_assembly* assemblies, uint32_t co
 int mdet_ctx_set_graph_capture(mdet_ctx* ctx, int enable);
 uint64_t mdet_ctx_graph_replays(mdet_ctx* ctx);
 
+/* ---- abundance (coverage) side --------------------------------------------
+ * The coverage matrices the reference reads from its abundance file into the
+ * globals ABD (mean depth) and ABD_VAR (depth variance) (cuda/Cuda2.cu:
+ * 1593-1700): n x nabd, row-major FP64, rows in the contig order of the TNF
+ * rows.  mdet_ctx_set_abundance copies them (host buffers) into the context;
+ * abd == null or nabd == 0 clears them.  While they are set, mdet_tnf_graph
+ * and mdet_tnf_graph_dev skip every pair of two contigs none of whose depths
+ * exceeds 1 before the per-contig top-k (is_nz, cuda/Cuda2.cu:845-856, as
+ * applied at 925), and fail with MDET_ERR_INVALID when called for a
+ * different number of contigs.  The batched graph, the max-probability sample
+ * and the pTNF search do not apply it (neither does the reference). */
+int mdet_ctx_set_abundance(mdet_ctx* ctx, const double* abd, const double* abd_var, uint64_t n,
+                           uint32_t nabd);
+
+/* sTNF -> sSCR of a graph's edges (cuda/Cuda2.cu:1921-1971) with the
+ * abundance set on the context: per edge, the mean of 1 - cal_abd_dist
+ * (cuda/Cuda2.cu:667-719) over the nnz samples where either depth exceeds
+ * min_cv; sTNF ranked ("min" ties) and, when nabd >= min_sample, the depth
+ * correlation cal_abd_corr (cuda/Cuda2.cu:1219-1245) ranked ("max" ties,
+ * cuda/ranker.h:56-80) are replaced by those quantiles of the sorted mean
+ * similarities; sSCR = (s^(1-w) t^w c)^(1/2), or s^(1-w) t^w without the
+ * correlation, with w = 1 / (1 + nnz).  Edge e joins to[e] and from[e]
+ * (contig indices < n), taken in that order as the reference does.  Without
+ * abundance on the context, sscr = stnf.  MDET_ERR_INVALID when an index is
+ * out of range or an edge has no sample above min_cv (the reference would
+ * divide 0 by 0).  min_cv, min_sample: the reference's minCV (default 1)
+ * and minSample (default 3).  As in the reference, a contig whose depths are
+ * the same in every sample makes its correlations undefined. */
+int mdet_edges_sscr(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* stnf,
+                    uint64_t n_edges, double min_cv, uint32_t min_sample, double* sscr);
+int mdet_edges_sscr_dev(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to,
+                        const double* d_stnf, uint64_t n_edges, double min_cv, uint32_t min_sample,
+                        double* d_sscr);
+
 /* ---- learned proposal (no counterpart in the reference) ----------------
  * A 136 -> 256 -> 128 -> 64 GELU network (BF16 weights, FP32 accumulation)
  * embeds each TNF row.  In MDET_MODE_LEARNED the graph orders contigs by

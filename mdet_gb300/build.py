@@ -33,7 +33,11 @@ CU_UNITS = [
     "learned",
     "graph_learned",
     "graph_batch",
+    "abundance",
 ]
+# per-unit flags: the abundance unit rounds every product and sum separately
+# (no FMA contraction), as the reference's host arithmetic does
+UNIT_FLAGS = {"abundance": ["-fmad=false"]}
 
 
 def _headers():
@@ -66,7 +70,7 @@ def build(verbose: bool = False) -> str:
         obj = os.path.join(OBJ, u + ".o")
         if _stale(obj, [src] + hdrs):
             jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                         f"-I{os.path.join(ROOT, 'include')}", "-c", src, "-o", obj])
+                         *UNIT_FLAGS.get(u, []), f"-I{os.path.join(ROOT, 'include')}", "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         for r in ex.map(_run, jobs):
             if verbose:

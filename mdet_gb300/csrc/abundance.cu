@@ -1,0 +1,347 @@
+// abundance.cu -- the coverage side of the graph: the pair gate of the
+// abundance form (is_nz, cuda/Cuda2.cu:845-856, applied at 925) and the
+// sTNF -> sSCR conversion of the edges (cuda/Cuda2.cu:1921-1971 with
+// cal_abd_dist2 / cal_abd_dist 667-719, cal_abd_corr 1219-1245 and the ranks
+// of cuda/ranker.h:56-80).
+//
+// Layout: the context keeps the reference's ABD (mean depth) and ABD_VAR
+// (variance) as n x nabd row-major FP64 matrices in the original contig order,
+// plus one byte per contig that says whether none of its depths exceeds 1.
+// sSCR runs one thread per edge over its nabd samples (FP64: the normal CDFs
+// need erfc/log at double precision), then three radix sorts (the abundance
+// similarities, sTNF and the depth correlations) turn values into ranks and
+// the ranks into quantiles of the similarity distribution.
+//
+// This unit is compiled without FMA contraction: sums and products round
+// separately, as in the reference, so the depth correlations -- whose ranks
+// pick quantiles -- come out bit-identical to a host evaluation.
+#include <cub/cub.cuh>
+
+#include "graph.cuh"
+
+namespace {
+
+__global__ void k_abd_low(const double* __restrict__ abd, uint64_t n, uint32_t nabd, uint8_t* __restrict__ low) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+        bool any = false;
+        for (uint32_t i = 0; i < nabd; ++i) any = any || abd[r * nabd + i] > 1.;
+        low[r] = any ? 0 : 1;
+    }
+}
+
+__global__ void k_low_sorted(const uint32_t* __restrict__ perm, const uint8_t* __restrict__ low, uint64_t n,
+                             uint8_t* __restrict__ out) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x)
+        out[s] = low[perm[s]];
+}
+
+// CDF of the normal distribution N(mean, sd^2) as Boost.Math defines it for
+// normal_distribution (the function the reference calls):
+// erfc(-(x - mean) / (sd * sqrt(2))) / 2.
+__device__ double normal_cdf(double mean, double sd, double x) {
+    const double z = (x - mean) / (sd * 1.4142135623730951);
+    return erfc(-z) / 2;
+}
+
+// Overlap of two normal densities from their crossing points k1 <= k2, the
+// narrower distribution evaluated first (cal_abd_dist2).
+__device__ double abd_dist2(double m1, double s1, double m2, double s2) {
+    const double v1 = s1 * s1, v2 = s2 * s2;
+    double k1, k2;
+    if (fabs(v2 - v1) < 1e-4) {
+        k1 = k2 = (m1 + m2) / 2;
+    } else {
+        const double t = sqrt(v1 * v2 * ((m1 - m2) * (m1 - m2) - 2 * (v1 - v2) * log(sqrt(v2 / v1))));
+        k1 = (t - m1 * v2 + m2 * v1) / (v1 - v2);
+        k2 = (t + m1 * v2 - m2 * v1) / (v2 - v1);
+    }
+    if (k1 > k2) {
+        const double x = k1;
+        k1 = k2;
+        k2 = x;
+    }
+    double ma = m1, sa = s1, mb = m2, sb = s2;
+    if (v1 > v2) {
+        ma = m2;
+        sa = s2;
+        mb = m1;
+        sb = s1;
+    }
+    if (k1 == k2) return fabs(normal_cdf(ma, sa, k1) - normal_cdf(mb, sb, k1));
+    return fabs(normal_cdf(ma, sa, k2) - normal_cdf(ma, sa, k1) + normal_cdf(mb, sb, k1) - normal_cdf(mb, sb, k2));
+}
+
+struct ScoreArgs {
+    const uint64_t* from;
+    const uint64_t* to;
+    uint64_t ne, n;
+    const double* abd;
+    const double* var;
+    uint32_t nabd;
+    double min_cv;
+    bool corr;
+    double* raw;     // mean abundance similarity per edge
+    uint32_t* nnz;   // samples where either depth exceeds min_cv
+    double* cor;     // depth correlation per edge (corr only)
+    uint32_t* idx;   // 0 .. ne-1, the values of the rank sorts
+    unsigned long long* bad;  // edges with an index out of range or no covered sample
+};
+
+// One thread per edge: r1 = to[e], r2 = from[e] (the reference's order).
+__global__ void k_abd_score(ScoreArgs p) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < p.ne;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        p.idx[e] = (uint32_t)e;
+        const uint64_t r1 = p.to[e], r2 = p.from[e];
+        if (r1 >= p.n || r2 >= p.n) {
+            atomicAdd(p.bad, 1ull);
+            p.raw[e] = 0.;
+            p.nnz[e] = 0;
+            if (p.corr) p.cor[e] = 0.;
+            continue;
+        }
+        const double* a1 = p.abd + r1 * p.nabd;
+        const double* a2 = p.abd + r2 * p.nabd;
+        const double* w1 = p.var + r1 * p.nabd;
+        const double* w2 = p.var + r2 * p.nabd;
+        double sum = 0.;
+        uint32_t k = 0;
+        // Pearson correlation with running means and co-moments (cal_abd_corr)
+        double sxx = 0., syy = 0., sxy = 0., mx = 0., my = 0.;
+        for (uint32_t i = 0; i < p.nabd; ++i) {
+            const double x = a1[i], y = a2[i];
+            // cal_abd_dist for sample i
+            if (x > p.min_cv || y > p.min_cv) {
+                double d = 0.;
+                const double m1 = x < 1e-6 ? 1e-6 : x, m2 = y < 1e-6 ? 1e-6 : y;
+                if (m1 != m2) {
+                    const double u1 = w1[i], u2 = w2[i];
+                    const double v1 = u1 < 1 ? 1. : u1, v2 = u2 < 1 ? 1. : u2;
+                    d = abd_dist2(m1, sqrt(v1), m2, sqrt(v2));
+                }
+                d = d < 1e-6 ? 1e-6 : d;  // std::min(std::max(d, 1e-6), 1 - 1e-6), NaN kept
+                d = (1. - 1e-6) < d ? 1. - 1e-6 : d;
+                sum += 1. - d;
+                ++k;
+            }
+            if (i == 0) {
+                mx = x;
+                my = y;
+            } else {
+                const double ratio = i / (i + 1.0);
+                const double dx = x - mx, dy = y - my;
+                sxx += dx * dx * ratio;
+                syy += dy * dy * ratio;
+                sxy += dx * dy * ratio;
+                mx += dx / (i + 1.0);
+                my += dy / (i + 1.0);
+            }
+        }
+        if (k == 0) atomicAdd(p.bad, 1ull);
+        p.raw[e] = sum / (double)k;
+        p.nnz[e] = k;
+        if (p.corr) p.cor[e] = sxy / (sqrt(sxx) * sqrt(syy));
+    }
+}
+
+// Sorted position p starts its run of equal keys: p, else 0 (a max-scan then
+// gives every position the start of its run).
+__global__ void k_run_heads(const double* __restrict__ keys, uint64_t ne, uint32_t* __restrict__ head) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ne; q += (uint64_t)gridDim.x * blockDim.x)
+        head[q] = (q == 0 || keys[q] != keys[q - 1]) ? (uint32_t)q : 0u;
+}
+
+// Ranks from the run starts: ascending sort -> the run's first rank ("min");
+// descending sort -> the run's last rank in ascending order ("max").
+__global__ void k_run_ranks(const uint32_t* __restrict__ order, const uint32_t* __restrict__ start, uint64_t ne,
+                            bool descending, uint32_t* __restrict__ rank) {
+    for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < ne; q += (uint64_t)gridDim.x * blockDim.x)
+        rank[order[q]] = descending ? (uint32_t)(ne - start[q]) : start[q] + 1u;
+}
+
+__global__ void k_sscr(const double* __restrict__ raw, const uint32_t* __restrict__ nnz,
+                       const uint32_t* __restrict__ rt, const uint32_t* __restrict__ rc,
+                       const double* __restrict__ distr, uint64_t ne, bool corr, double* __restrict__ out) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < ne; e += (uint64_t)gridDim.x * blockDim.x) {
+        const double t = distr[rt[e] - 1];
+        const double w = 1. / (double)(1 + nnz[e]);
+        const double s = pow(raw[e], 1. - w) * pow(t, w);
+        out[e] = corr ? pow(s * distr[rc[e] - 1], 1. / 2.) : s;
+    }
+}
+
+struct MaxOp {
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
+};
+
+unsigned grid_for(mdet_ctx* ctx, uint64_t items, unsigned block) {
+    const uint64_t want = (items + block - 1) / block, cap = (uint64_t)ctx->num_sms * 16;
+    return (unsigned)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+// ranks of keys[0..ne) into rank (ascending "min" or, descending, "max")
+int rank_runs(mdet_ctx* ctx, const double* keys, const uint32_t* idx, uint64_t ne, bool descending, double* ks,
+              uint32_t* os, uint32_t* head, uint32_t* start, uint32_t* rank, void* tmp, size_t tmpb) {
+    cudaStream_t s = ctx->stream;
+    size_t tb = tmpb;
+    if (descending)
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairsDescending(tmp, tb, keys, ks, idx, os, (int)ne, 0, 64, s));
+    else
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, ks, idx, os, (int)ne, 0, 64, s));
+    k_run_heads<<<grid_for(ctx, ne, 256), 256, 0, s>>>(ks, ne, head);
+    MDET_LAUNCHED(ctx, "k_run_heads");
+    tb = tmpb;
+    MDET_CUDA(ctx, cub::DeviceScan::InclusiveScan(tmp, tb, head, start, MaxOp(), (int)ne, s));
+    k_run_ranks<<<grid_for(ctx, ne, 256), 256, 0, s>>>(os, start, ne, descending, rank);
+    MDET_LAUNCHED(ctx, "k_run_ranks");
+    return MDET_OK;
+}
+
+int sscr_core(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* stnf, uint64_t ne,
+              double min_cv, uint32_t min_sample, double* out) {
+    cudaStream_t s = ctx->stream;
+    if (ne == 0) return MDET_OK;
+    if (ctx->abd_nabd == 0) {  // no abundance: sSCR = sTNF
+        MDET_CUDA(ctx, cudaMemcpyAsync(out, stnf, ne * 8, cudaMemcpyDeviceToDevice, s));
+        return MDET_OK;
+    }
+    if (ne >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many edges (%llu)", (unsigned long long)ne);
+    const bool corr = ctx->abd_nabd >= min_sample;
+    double* raw = (double*)ctx_scratch(ctx, "abd.raw", ne * 8);
+    uint32_t* nnz = (uint32_t*)ctx_scratch(ctx, "abd.nnz", ne * 4);
+    double* cor = (double*)ctx_scratch(ctx, "abd.cor", ne * 8);
+    uint32_t* idx = (uint32_t*)ctx_scratch(ctx, "abd.idx", ne * 4);
+    double* ks = (double*)ctx_scratch(ctx, "abd.ks", ne * 8);
+    uint32_t* os = (uint32_t*)ctx_scratch(ctx, "abd.os", ne * 4);
+    uint32_t* head = (uint32_t*)ctx_scratch(ctx, "abd.head", ne * 4);
+    uint32_t* start = (uint32_t*)ctx_scratch(ctx, "abd.start", ne * 4);
+    uint32_t* rt = (uint32_t*)ctx_scratch(ctx, "abd.rt", ne * 4);
+    uint32_t* rc = (uint32_t*)ctx_scratch(ctx, "abd.rc", ne * 4);
+    double* distr = (double*)ctx_scratch(ctx, "abd.distr", ne * 8);
+    unsigned long long* bad = (unsigned long long*)ctx_scratch(ctx, "abd.bad", 8);
+    if (!raw || !nnz || !cor || !idx || !ks || !os || !head || !start || !rt || !rc || !distr || !bad)
+        return MDET_ERR_NOMEM;
+    size_t t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortKeys(nullptr, t1, raw, distr, (int)ne, 0, 64, s));
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(nullptr, t2, stnf, ks, idx, os, (int)ne, 0, 64, s));
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairsDescending(nullptr, t3, cor, ks, idx, os, (int)ne, 0, 64, s));
+    MDET_CUDA(ctx, cub::DeviceScan::InclusiveScan(nullptr, t4, head, start, MaxOp(), (int)ne, s));
+    const size_t tmpb = std::max(std::max(t1, t2), std::max(t3, t4));
+    void* tmp = ctx_scratch(ctx, "abd.cubtmp", tmpb);
+    if (!tmp) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(bad, 0, 8, s));
+
+    ScoreArgs p;
+    p.from = from;
+    p.to = to;
+    p.ne = ne;
+    p.n = ctx->abd_n;
+    p.abd = (const double*)ctx->bufs["abd.m"].p;
+    p.var = (const double*)ctx->bufs["abd.v"].p;
+    p.nabd = ctx->abd_nabd;
+    p.min_cv = min_cv;
+    p.corr = corr;
+    p.raw = raw;
+    p.nnz = nnz;
+    p.cor = cor;
+    p.idx = idx;
+    p.bad = bad;
+    ctx_timer_begin(ctx, "k_abd_score");
+    k_abd_score<<<grid_for(ctx, ne, 128), 128, 0, s>>>(p);
+    ctx_timer_end(ctx, "k_abd_score");
+    MDET_LAUNCHED(ctx, "k_abd_score");
+
+    // the abundance similarities in ascending order (partial_sort_copy)
+    size_t tb = tmpb;
+    MDET_CUDA(ctx, cub::DeviceRadixSort::SortKeys(tmp, tb, raw, distr, (int)ne, 0, 64, s));
+    MDET_TRY(rank_runs(ctx, stnf, idx, ne, false, ks, os, head, start, rt, tmp, tmpb));
+    if (corr) MDET_TRY(rank_runs(ctx, cor, idx, ne, true, ks, os, head, start, rc, tmp, tmpb));
+    k_sscr<<<grid_for(ctx, ne, 256), 256, 0, s>>>(raw, nnz, rt, rc, distr, ne, corr, out);
+    MDET_LAUNCHED(ctx, "k_sscr");
+
+    unsigned long long nbad = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&nbad, bad, 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    if (nbad)
+        return ctx_fail(ctx, MDET_ERR_INVALID,
+                        "%llu edges have a contig index out of range or no sample with depth above min_cv",
+                        (unsigned long long)nbad);
+    return MDET_OK;
+}
+
+}  // namespace
+
+int abd_gate(mdet_ctx* ctx, GraphPrep& g) {
+    g.low = nullptr;
+    if (ctx->abd_nabd == 0) return MDET_OK;
+    if (ctx->abd_n != g.n)
+        return ctx_fail(ctx, MDET_ERR_INVALID, "the abundance set on the context covers %llu contigs, the graph %llu",
+                        (unsigned long long)ctx->abd_n, (unsigned long long)g.n);
+    uint8_t* low_s = (uint8_t*)ctx_scratch(ctx, "abd.lows", g.n);
+    if (!low_s) return MDET_ERR_NOMEM;
+    k_low_sorted<<<grid_for(ctx, g.n, 256), 256, 0, ctx->stream>>>(g.perm, (const uint8_t*)ctx->bufs["abd.low"].p,
+                                                                    g.n, low_s);
+    MDET_LAUNCHED(ctx, "k_low_sorted");
+    g.low = low_s;
+    return MDET_OK;
+}
+
+extern "C" {
+
+int mdet_ctx_set_abundance(mdet_ctx* ctx, const double* abd, const double* abd_var, uint64_t n, uint32_t nabd) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (nabd == 0 || n == 0 || !abd) {
+        ctx->abd_n = 0;
+        ctx->abd_nabd = 0;
+        return MDET_OK;
+    }
+    if (!abd_var) return ctx_fail(ctx, MDET_ERR_INVALID, "null variance matrix");
+    if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
+    cudaStream_t s = ctx->stream;
+    double* dm = (double*)ctx_scratch(ctx, "abd.m", n * nabd * 8);
+    double* dv = (double*)ctx_scratch(ctx, "abd.v", n * nabd * 8);
+    uint8_t* low = (uint8_t*)ctx_scratch(ctx, "abd.low", n);
+    if (!dm || !dv || !low) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(dm, abd, n * nabd * 8, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(dv, abd_var, n * nabd * 8, cudaMemcpyHostToDevice, s));
+    k_abd_low<<<grid_for(ctx, n, 256), 256, 0, s>>>(dm, n, nabd, low);
+    MDET_LAUNCHED(ctx, "k_abd_low");
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->abd_n = n;
+    ctx->abd_nabd = nabd;
+    return MDET_OK;
+}
+
+int mdet_edges_sscr_dev(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const double* d_stnf,
+                        uint64_t n_edges, double min_cv, uint32_t min_sample, double* d_sscr) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    if (n_edges && (!d_from || !d_to || !d_stnf || !d_sscr)) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    return sscr_core(ctx, d_from, d_to, d_stnf, n_edges, min_cv, min_sample, d_sscr);
+}
+
+int mdet_edges_sscr(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* stnf, uint64_t n_edges,
+                    double min_cv, uint32_t min_sample, double* sscr) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    if (n_edges == 0) return MDET_OK;
+    if (!from || !to || !stnf || !sscr) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    cudaStream_t s = ctx->stream;
+    uint64_t* df = (uint64_t*)ctx_scratch(ctx, "io.efrom", n_edges * 8);
+    uint64_t* dt = (uint64_t*)ctx_scratch(ctx, "io.eto", n_edges * 8);
+    double* ds = (double*)ctx_scratch(ctx, "io.estnf", n_edges * 8);
+    double* dout = (double*)ctx_scratch(ctx, "io.esscr", n_edges * 8);
+    if (!df || !dt || !ds || !dout) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(df, from, n_edges * 8, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(dt, to, n_edges * 8, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(ds, stnf, n_edges * 8, cudaMemcpyHostToDevice, s));
+    MDET_TRY(sscr_core(ctx, df, dt, ds, n_edges, min_cv, min_sample, dout));
+    MDET_CUDA(ctx, cudaMemcpyAsync(sscr, dout, n_edges * 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDET_OK;
+}
+
+}  // extern "C"

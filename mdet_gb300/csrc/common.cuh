@@ -88,6 +88,11 @@ struct mdet_ctx {
     } prep_cache;
     // copy streams of the host-buffer entry points (created on first use)
     cudaStream_t io_in = nullptr, io_out = nullptr;
+    // abundance set by mdet_ctx_set_abundance: contigs and samples (the
+    // matrices and per-contig low flags live in scratch "abd.m", "abd.v",
+    // "abd.low"); nabd == 0: none
+    uint64_t abd_n = 0;
+    uint32_t abd_nabd = 0;
 };
 
 // Event pair around one launch of a named kernel when timing is enabled.

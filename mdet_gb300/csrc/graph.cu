@@ -328,6 +328,7 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
     PhaseTimer tm(ctx->stream);
     tm.mark();
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, mode != MDET_MODE_PLAIN, &g));
+    MDET_TRY(abd_gate(ctx, g));
     const double L = logit(cutoff);
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl));

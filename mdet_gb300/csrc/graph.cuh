@@ -110,7 +110,13 @@ struct GraphPrep {
     BlockMeta* meta;                 // per 128-row block (bf16 rounding)
     BlockMeta* meta32;               // per 128-row block (no rounding term)
     float* mu;                       // column means [136]
+    const uint8_t* low = nullptr;    // abundance gate: sorted position has no depth above 1 (null: no gate)
 };
+
+// Sets g.low from the abundance on the context (a pair of two low contigs is
+// not an edge); no abundance: g.low = null.  Fails when the abundance covers a
+// different number of contigs.
+int abd_gate(mdet_ctx* ctx, GraphPrep& g);
 
 // Prepares the contigs in ascending log-size order, or in `order` (original
 // index per position, device) when given.

@@ -29,6 +29,7 @@ struct ExactArgs {
     ff Lff;
     const BlkCut* blk_L;  // optional per-256-row-block cutoff
     const unsigned long long* ncand_dev;  // optional device candidate count (ncand is then its cap)
+    const uint8_t* low;   // optional abundance gate per sorted position (graph only)
     // graph outputs
     Edge* edges;
     unsigned long long* nedges;
@@ -119,7 +120,8 @@ __global__ void __launch_bounds__(256) k_exact_graph(ExactArgs p) {
         const ff d2 = warp_dist2(p.cand, p.ncand, base, nullptr, p.x32, lane, si, sj);
         bool edge = false;
         double sim = 0;
-        if (base + lane < p.ncand) {
+        // a pair of two contigs without a depth above 1 is never an edge (is_nz)
+        if (base + lane < p.ncand && !(p.low && p.low[si] && p.low[sj])) {
             ff Lc = p.Lff;
             bool m2 = model2;
             if (p.blk_L) {
@@ -654,6 +656,7 @@ int exact_graph(mdet_ctx* ctx, const GraphPrep& g, const uint2* cand, unsigned l
         p.Lff.lo = (float)(L - (double)p.Lff.hi);
         p.blk_L = blk_L;
         p.ncand_dev = ncand_dev;
+        p.low = g.low;
         p.edges = edges;
         p.nedges = cnt;
         p.deg = deg;

@@ -386,6 +386,7 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     if (!z || !order) return MDET_ERR_NOMEM;
     MDET_TRY(learned_order(ctx, net, d_tnf, d_ls, n, z, seg, order));
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, true, &g, order));
+    MDET_TRY(abd_gate(ctx, g));
     const double L = logit(cutoff);
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl, false));

@@ -76,3 +76,23 @@ def generate(seed: int, n: int, genomes: int, min_len=2500, max_len=500000, medi
     data = buf[:total]
     ls = np.log10(np.minimum(L, 500000).astype(np.float64))
     return SynthAssembly(data, so, sl, L, g, ls)
+
+
+def abundance(genome: np.ndarray, nabd: int, seed: int, low_frac: float = 0.03):
+    """Seeded coverage for an assembly, shaped like a depth table (mean and
+    variance per contig and sample): each genome gets a mean depth per sample
+    (log-normal around 10x), each contig that depth times log-normal noise
+    (sigma 0.15) as its mean and mean * U(0.5, 2) as its variance.  A fraction
+    low_frac of the contigs get depths in [0, 1) in every sample (no depth
+    above 1, so a pair of two of them is not an edge).  Returns (abd, var),
+    n x nabd float64."""
+    rng = np.random.default_rng(seed)
+    genome = np.asarray(genome)
+    n = genome.size
+    G = int(genome.max()) + 1 if n else 1
+    gd = rng.lognormal(np.log(10.0), 1.0, size=(G, nabd))
+    abd = gd[genome] * rng.lognormal(0.0, 0.15, size=(n, nabd))
+    low = rng.random(n) < low_frac
+    abd[low] = rng.uniform(0.0, 1.0, size=(int(low.sum()), nabd))
+    var = abd * rng.uniform(0.5, 2.0, size=(n, nabd))
+    return abd, var

@@ -154,6 +154,9 @@ SIGNATURES = [
     ("mdet_mlp_train", ctypes.c_int,
      [P, P, P, P, u64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)]),
     ("mdet_ctx_set_learned", ctypes.c_int, [P, P, ctypes.POINTER(LearnedReport)]),
+    ("mdet_ctx_set_abundance", ctypes.c_int, [P, P, P, u64, u32]),
+    ("mdet_edges_sscr", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
+    ("mdet_edges_sscr_dev", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
 ]
 
 _lib = None
@@ -340,6 +343,36 @@ class Context:
                                                 MODES[mode], P(d_from), P(d_to), P(d_stnf), capacity,
                                                 ctypes.byref(ne), ctypes.byref(stats)))
         return ne.value, stats.as_dict()
+
+    def set_abundance(self, abd, var):
+        """Coverage of the contigs (n x nabd mean depths and variances, the
+        reference's ABD / ABD_VAR); None clears it.  While set, tnf_graph /
+        tnf_graph_dev drop pairs of two contigs with no depth above 1."""
+        if abd is None:
+            self._check(self.lib.mdet_ctx_set_abundance(self.h, None, None, 0, 0))
+            return
+        abd = np.ascontiguousarray(abd, np.float64)
+        var = np.ascontiguousarray(var, np.float64)
+        if abd.ndim != 2 or var.shape != abd.shape:
+            raise ValueError("abd and var must be n x nabd matrices of the same shape")
+        self._check(self.lib.mdet_ctx_set_abundance(self.h, P(abd.ctypes.data), P(var.ctypes.data), abd.shape[0],
+                                                    abd.shape[1]))
+
+    def edges_sscr(self, from_, to, stnf, min_cv=1.0, min_sample=3):
+        """sTNF -> sSCR of edges (host arrays) with the context's abundance."""
+        f = np.ascontiguousarray(from_, np.uint64)
+        t = np.ascontiguousarray(to, np.uint64)
+        s = np.ascontiguousarray(stnf, np.float64)
+        if not (f.size == t.size == s.size):
+            raise ValueError("from, to and stnf must have the same length")
+        out = np.empty(s.size, np.float64)
+        self._check(self.lib.mdet_edges_sscr(self.h, P(f.ctypes.data), P(t.ctypes.data), P(s.ctypes.data), s.size,
+                                             float(min_cv), int(min_sample), P(out.ctypes.data)))
+        return out
+
+    def edges_sscr_dev(self, d_from, d_to, d_stnf, n_edges, d_sscr, min_cv=1.0, min_sample=3):
+        self._check(self.lib.mdet_edges_sscr_dev(self.h, P(d_from), P(d_to), P(d_stnf), n_edges, float(min_cv),
+                                                 int(min_sample), P(d_sscr)))
 
     def pair_scores_dev(self, d_tnf, d_ls, n, d_pairs, m, d_dist, d_prob):
         self._check(self.lib.mdet_tnf_pair_scores_dev(self.h, P(d_tnf), P(d_ls), n, P(d_pairs), m, P(d_dist),

@@ -11,7 +11,12 @@ them into this repository:
   (host form, cuda/Cuda2.cu:721-779).  Cuda2.cu as a whole needs Boost and a
   GPU, so this script cuts those two spans out of the file at build time into
   oracle/_ref/cuda2_prob.inc and compiles them on the host behind the shim
-  oracle/ref_prob_shim.cpp -> oracle/_ref/libref_prob.so.
+  oracle/ref_prob_shim.cpp -> oracle/_ref/libref_prob.so;
+* the abundance scoring of cuda/Cuda2.cu -- cal_abd_dist2, cal_abd_dist,
+  is_nz, cal_abd_corr and the sTNF -> sSCR block of main -- cut the same way
+  into oracle/_ref/cuda2_abd.inc and compiled with the reference's own
+  cuda/ranker.h behind oracle/ref_abd_shim.cpp (which stands in for Boost's
+  normal CDF) -> oracle/_ref/libref_abd.so.
 
 Only runs where the reference is mounted (MDET_REFERENCE or /root/reference).
 """
@@ -46,6 +51,35 @@ def extract_prob(src: str) -> str:
     return dev + "\n" + host + "\n"
 
 
+def cut_block(src: str, head: str) -> str:
+    """The function that starts with `head`, through its closing brace."""
+    i = src.index(head)
+    depth, j = 0, src.index("{", i)
+    while True:
+        if src[j] == "{":
+            depth += 1
+        elif src[j] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[i : j + 1]
+        j += 1
+
+
+def extract_abd(src: str) -> str:
+    """cal_abd_dist2, cal_abd_dist, is_nz, cal_abd_corr and the sTNF -> sSCR
+    block of main, the latter wrapped as sscr_block(Graph&, size_t)."""
+    funcs = [
+        cut_block(src, "Distance cal_abd_dist2(Normal& p1, Normal& p2) {"),
+        cut_block(src, "Distance cal_abd_dist(size_t r1, size_t r2, size_t i, bool& nz) {"),
+        cut_block(src, "bool is_nz(size_t r1, size_t r2) {"),
+        cut_block(src, "Distance cal_abd_corr(size_t r1, size_t r2, bool is_small = false) {"),
+    ]
+    a = src.index("// 3. convert sTNF to sSCR")
+    b = src.index("std::vector<double>().swap(g.sTNF);", a)
+    block = "static void sscr_block(Graph& g, size_t nEdges) {\n" + src[a:b] + "\n}\n"
+    return "\n\n".join(funcs) + "\n\n" + block
+
+
 def main() -> int:
     cuda2 = os.path.join(REF, "cuda", "Cuda2.cu")
     if not os.path.exists(cuda2):
@@ -62,6 +96,14 @@ def main() -> int:
         "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
         f"-I{OUT}", "-o", os.path.join(OUT, "libref_prob.so"),
         os.path.join(HERE, "ref_prob_shim.cpp"),
+    ])
+    inc = os.path.join(OUT, "cuda2_abd.inc")
+    with open(inc, "w") as f:
+        f.write(extract_abd(src))
+    subprocess.check_call([
+        "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+        f"-I{OUT}", f"-I{os.path.join(REF, 'cuda')}", "-o", os.path.join(OUT, "libref_abd.so"),
+        os.path.join(HERE, "ref_abd_shim.cpp"),
     ])
     return 0
 

@@ -56,6 +56,12 @@ def lib():
         L.orc_rand.restype = ctypes.c_int
         L.orc_ptnf_search.restype = D
         L.orc_ptnf_search.argtypes = [P, P, u64, D, ctypes.c_int]
+        L.orc_tnf_graph_nz.restype = u64
+        L.orc_tnf_graph_nz.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int, P]
+        L.orc_tnf_topk_rows_nz.restype = u64
+        L.orc_tnf_topk_rows_nz.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int, P]
+        L.orc_abd_low.argtypes = [P, u64, ctypes.c_uint32, P]
+        L.orc_sscr.argtypes = [P, P, P, u64, P, P, ctypes.c_uint32, D, ctypes.c_uint32, P, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -111,7 +117,17 @@ def pair_scores(tnf, ls, pairs, threads=0):
     return d, p
 
 
-def graph(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
+def _low_arg(low, n):
+    if low is None:
+        return None, None
+    low = np.ascontiguousarray(low, np.uint8)
+    assert low.size == n
+    return low, _p(low)
+
+
+def graph(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0, low=None):
+    """low (optional): per contig 1 when no depth exceeds 1 (the abundance
+    pair gate, see abd_low)."""
     tnf = np.ascontiguousarray(tnf, np.float32)
     ls = np.ascontiguousarray(ls, np.float64)
     n = tnf.shape[0]
@@ -120,11 +136,13 @@ def graph(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
     fr = np.zeros(cap, np.uint64)
     to = np.zeros(cap, np.uint64)
     st = np.zeros(cap, np.float64)
-    k = lib().orc_tnf_graph(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(fr), _p(to), _p(st), cap, threads)
+    low, lp = _low_arg(low, n)
+    k = lib().orc_tnf_graph_nz(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(fr), _p(to), _p(st), cap,
+                               threads, lp)
     return fr[:k], to[:k], st[:k]
 
 
-def topk_rows(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
+def topk_rows(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0, low=None):
     tnf = np.ascontiguousarray(tnf, np.float32)
     ls = np.ascontiguousarray(ls, np.float64)
     n = tnf.shape[0]
@@ -133,9 +151,30 @@ def topk_rows(tnf, ls, cutoff, max_edges=200, row0=0, row1=None, threads=0):
     rp = np.zeros(row1 - row0 + 1, np.uint64)
     cols = np.zeros(cap, np.uint64)
     sims = np.zeros(cap, np.float64)
-    lib().orc_tnf_topk_rows(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(rp), _p(cols), _p(sims), cap,
-                            threads)
+    low, lp = _low_arg(low, n)
+    lib().orc_tnf_topk_rows_nz(_p(tnf), _p(ls), n, cutoff, max_edges, row0, row1, _p(rp), _p(cols), _p(sims), cap,
+                               threads, lp)
     return rp, cols, sims
+
+
+def abd_low(abd):
+    """1 per contig none of whose depths exceeds 1 (is_nz's threshold)."""
+    abd = np.ascontiguousarray(abd, np.float64)
+    low = np.zeros(abd.shape[0], np.uint8)
+    lib().orc_abd_low(_p(abd), abd.shape[0], abd.shape[1], _p(low))
+    return low
+
+
+def sscr(from_, to, stnf, abd, var, min_cv=1.0, min_sample=3, threads=0):
+    """sTNF -> sSCR of edges (from_, to, stnf) with coverage abd / var (n x nabd)."""
+    f = np.ascontiguousarray(from_, np.uint64)
+    t = np.ascontiguousarray(to, np.uint64)
+    s = np.ascontiguousarray(stnf, np.float64)
+    abd = np.ascontiguousarray(abd, np.float64)
+    var = np.ascontiguousarray(var, np.float64)
+    out = np.zeros(s.size, np.float64)
+    lib().orc_sscr(_p(f), _p(t), _p(s), s.size, _p(abd), _p(var), abd.shape[1], min_cv, min_sample, _p(out), threads)
+    return out
 
 
 def max_prob(tnf, ls, contigs, m, threads=0):

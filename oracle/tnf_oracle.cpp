@@ -125,11 +125,15 @@ struct CompareEdge {
 };
 typedef std::priority_queue<std::pair<uint64_t, double>, std::vector<std::pair<uint64_t, double>>, CompareEdge> EdgeHeap;
 
+/* low (optional): per contig 1 when none of its depths exceeds 1; a pair of
+ * two such contigs is skipped before the heap (is_nz, cuda/Cuda2.cu:845-856,
+ * applied at 925). */
 void row_heap(const float* tnf, const double* logsize, uint64_t n, double floor_cut, uint32_t max_edges, uint64_t i,
-              EdgeHeap& heap) {
+              EdgeHeap& heap, const uint8_t* low) {
     const float* ti = tnf + i * 136;
     for (uint64_t j = 0; j < n; ++j) {
         if (i == j) continue;
+        if (low && low[i] && low[j]) continue;
         double pre = orc_pre_prob(logsize[i], logsize[j], ti, tnf + j * 136);
         double s = pre > floor_cut ? 1. - 1. / (1. + exp(pre)) : 0.;
         if (s != 0. && (heap.size() < max_edges || (heap.size() == max_edges && s > heap.top().second))) {
@@ -334,6 +338,12 @@ void orc_pair_scores(const float* tnf, const double* logsize, const uint64_t* pa
 uint64_t orc_tnf_graph(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
                        uint64_t row0, uint64_t row1, uint64_t* from, uint64_t* to, double* stnf, uint64_t cap,
                        int threads) {
+    return orc_tnf_graph_nz(tnf, logsize, n, cutoff, max_edges, row0, row1, from, to, stnf, cap, threads, nullptr);
+}
+
+uint64_t orc_tnf_graph_nz(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
+                          uint64_t row0, uint64_t row1, uint64_t* from, uint64_t* to, double* stnf, uint64_t cap,
+                          int threads, const uint8_t* low) {
     if (row1 > n) row1 = n;
     if (row0 >= row1) return 0;
     const double floor_cut = orc_logit_cutoff(cutoff);
@@ -345,7 +355,7 @@ uint64_t orc_tnf_graph(const float* tnf, const double* logsize, uint64_t n, doub
     for (int64_t r = 0; r < (int64_t)nr; ++r) {
         uint64_t i = row0 + (uint64_t)r;
         EdgeHeap heap;
-        row_heap(tnf, logsize, n, floor_cut, max_edges, i, heap);
+        row_heap(tnf, logsize, n, floor_cut, max_edges, i, heap, low);
         /* emission rule of cuda/Cuda2.cu:936-946: only i < j */
         while (!heap.empty()) {
             std::pair<uint64_t, double> e = heap.top();
@@ -370,6 +380,13 @@ uint64_t orc_tnf_graph(const float* tnf, const double* logsize, uint64_t n, doub
 uint64_t orc_tnf_topk_rows(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
                            uint64_t row0, uint64_t row1, uint64_t* row_ptr, uint64_t* cols, double* sims, uint64_t cap,
                            int threads) {
+    return orc_tnf_topk_rows_nz(tnf, logsize, n, cutoff, max_edges, row0, row1, row_ptr, cols, sims, cap, threads,
+                                nullptr);
+}
+
+uint64_t orc_tnf_topk_rows_nz(const float* tnf, const double* logsize, uint64_t n, double cutoff,
+                              uint32_t max_edges, uint64_t row0, uint64_t row1, uint64_t* row_ptr, uint64_t* cols,
+                              double* sims, uint64_t cap, int threads, const uint8_t* low) {
     if (row1 > n) row1 = n;
     if (row0 >= row1) {
         row_ptr[0] = 0;
@@ -383,7 +400,7 @@ uint64_t orc_tnf_topk_rows(const float* tnf, const double* logsize, uint64_t n, 
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
     for (int64_t r = 0; r < (int64_t)nr; ++r) {
         EdgeHeap heap;
-        row_heap(tnf, logsize, n, floor_cut, max_edges, row0 + (uint64_t)r, heap);
+        row_heap(tnf, logsize, n, floor_cut, max_edges, row0 + (uint64_t)r, heap, low);
         while (!heap.empty()) {
             per_row[r].push_back(heap.top());
             heap.pop();
@@ -489,6 +506,170 @@ double orc_ptnf_search(const float* tnf, const double* logsize, uint64_t n, doub
         if (i == 9) ptnf /= 10.;
     }
     return ptnf;
+}
+
+/* ----------------------------------------------------------- abundance --
+ * Coverage side of the edge score.  abd and var are n x nabd row-major
+ * matrices: mean depth and depth variance of contig r in sample i (the
+ * reference's ABD(r, i) and ABD_VAR(r, i)). */
+
+/* A contig is "low" when none of its depths exceeds 1; is_nz
+ * (cuda/Cuda2.cu:845-856, fixed threshold 1) rejects a pair of two low
+ * contigs. */
+void orc_abd_low(const double* abd, uint64_t n, uint32_t nabd, uint8_t* low) {
+    for (uint64_t r = 0; r < n; ++r) {
+        bool any = false;
+        for (uint32_t i = 0; i < nabd; ++i) any = any || abd[r * nabd + i] > 1.;
+        low[r] = (nabd > 0 && !any) ? 1 : 0;
+    }
+}
+
+}  // extern "C"
+
+namespace {
+
+/* The reference evaluates boost::math::cdf(normal_distribution(mean, sd), x)
+ * (Boost.Math, a dependency that is not part of the MdeT sources).  Its
+ * published definition: erfc(-(x - mean) / (sd * sqrt(2))) / 2. */
+double normal_cdf(double mean, double sd, double x) {
+    const double z = (x - mean) / (sd * 1.4142135623730951);
+    return erfc(-z) / 2;
+}
+
+/* cal_abd_dist2 (cuda/Cuda2.cu:667-700): the overlap of two normal densities,
+ * from the crossing points k1 <= k2 of the densities; the narrower
+ * distribution is evaluated first. */
+double abd_dist2(double m1, double s1, double m2, double s2) {
+    const double v1 = s1 * s1, v2 = s2 * s2;
+    double k1, k2;
+    if (fabs(v2 - v1) < 1e-4) {
+        k1 = k2 = (m1 + m2) / 2;
+    } else {
+        const double t = sqrt(v1 * v2 * ((m1 - m2) * (m1 - m2) - 2 * (v1 - v2) * log(sqrt(v2 / v1))));
+        k1 = (t - m1 * v2 + m2 * v1) / (v1 - v2);
+        k2 = (t + m1 * v2 - m2 * v1) / (v2 - v1);
+    }
+    if (k1 > k2) std::swap(k1, k2);
+    double ma = m1, sa = s1, mb = m2, sb = s2;
+    if (v1 > v2) {
+        std::swap(ma, mb);
+        std::swap(sa, sb);
+    }
+    if (k1 == k2) return fabs(normal_cdf(ma, sa, k1) - normal_cdf(mb, sb, k1));
+    return fabs(normal_cdf(ma, sa, k2) - normal_cdf(ma, sa, k1) + normal_cdf(mb, sb, k1) - normal_cdf(mb, sb, k2));
+}
+
+/* cal_abd_dist (cuda/Cuda2.cu:702-719) for sample i; *nz is set when either
+ * depth exceeds min_cv. */
+double abd_dist(const double* abd, const double* var, uint32_t nabd, uint64_t r1, uint64_t r2, uint32_t i,
+                double min_cv, bool* nz) {
+    double d = 0;
+    double m1 = abd[r1 * nabd + i], m2 = abd[r2 * nabd + i];
+    if (m1 > min_cv || m2 > min_cv) {
+        *nz = true;
+        m1 = std::max(m1, 1e-6);
+        m2 = std::max(m2, 1e-6);
+        if (m1 != m2) {
+            const double w1 = var[r1 * nabd + i], w2 = var[r2 * nabd + i];
+            const double v1 = w1 < 1 ? 1 : w1, v2 = w2 < 1 ? 1 : w2;
+            d = abd_dist2(m1, sqrt(v1), m2, sqrt(v2));
+        }
+    }
+    return std::min(std::max(d, 1e-6), 1. - 1e-6);
+}
+
+/* cal_abd_corr (cuda/Cuda2.cu:1219-1245): Pearson correlation of the two
+ * depth profiles with running (Welford) means and co-moments. */
+double abd_corr(const double* abd, uint32_t nabd, uint64_t r1, uint64_t r2) {
+    double sxx = 0, syy = 0, sxy = 0, mx = 0, my = 0;
+    for (uint32_t i = 0; i < nabd; ++i) {
+        const double x = abd[r1 * nabd + i], y = abd[r2 * nabd + i];
+        if (i == 0) {
+            mx = x;
+            my = y;
+            continue;
+        }
+        const double ratio = i / (i + 1.0);
+        const double dx = x - mx, dy = y - my;
+        sxx += dx * dx * ratio;
+        syy += dy * dy * ratio;
+        sxy += dx * dy * ratio;
+        mx += dx / (i + 1.0);
+        my += dy / (i + 1.0);
+    }
+    return sxy / (sqrt(sxx) * sqrt(syy));
+}
+
+/* rank(v, w, "min" | "max") (cuda/ranker.h:56-80): 1-based ranks in
+ * ascending order; a run of equal values gets its first ("min") or last
+ * ("max") rank. */
+void rank_ties(const double* v, uint64_t n, bool last, std::vector<double>& r) {
+    std::vector<uint64_t> ord(n);
+    std::iota(ord.begin(), ord.end(), (uint64_t)0);
+    std::sort(ord.begin(), ord.end(), [&](uint64_t a, uint64_t b) { return v[a] < v[b]; });
+    r.resize(n);
+    for (uint64_t c = 0; c < n;) {
+        uint64_t k = 1;
+        while (c + k < n && v[ord[c]] == v[ord[c + k]]) ++k;
+        for (uint64_t q = 0; q < k; ++q) r[ord[c + q]] = (double)(last ? c + k : c + 1);
+        c += k;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* sTNF -> sSCR (cuda/Cuda2.cu:1921-1971): per edge the mean abundance
+ * similarity over the samples where either contig is covered (nnz of them);
+ * sTNF, and with nabd >= min_sample the depth correlation, are mapped by
+ * rank onto the sorted abundance similarities; the score is their weighted
+ * geometric mean.  Edge e joins to[e] (r1) and from[e] (r2), in that order.
+ * nabd == 0: sSCR = sTNF. */
+void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint64_t ne, const double* abd,
+              const double* var, uint32_t nabd, double min_cv, uint32_t min_sample, double* sscr, int threads) {
+    if (nabd == 0) {
+        for (uint64_t e = 0; e < ne; ++e) sscr[e] = stnf[e];
+        return;
+    }
+    int nt = resolve_threads(threads);
+    (void)nt;
+    std::vector<double> raw(ne, 0.0);
+    std::vector<int> nnz(ne, 0);
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t e = 0; e < (int64_t)ne; ++e) {
+        for (uint32_t i = 0; i < nabd; ++i) {
+            bool nz = false;
+            const double a = 1. - abd_dist(abd, var, nabd, to[e], from[e], i, min_cv, &nz);
+            if (nz) {
+                raw[e] += a;
+                ++nnz[e];
+            }
+        }
+        raw[e] /= nnz[e];
+    }
+    std::vector<double> distr(raw);
+    std::sort(distr.begin(), distr.end());
+    std::vector<double> rt, rc;
+    rank_ties(stnf, ne, false, rt);
+    const bool corr = nabd >= min_sample;
+    if (corr) {
+        std::vector<double> c(ne);
+#pragma omp parallel for schedule(static) num_threads(nt)
+        for (int64_t e = 0; e < (int64_t)ne; ++e) c[e] = abd_corr(abd, nabd, to[e], from[e]);
+        rank_ties(c.data(), ne, true, rc);
+    }
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int64_t e = 0; e < (int64_t)ne; ++e) {
+        const double t = distr[(uint64_t)round(rt[e]) - 1];
+        const double w = 1. / (1 + nnz[e]);
+        if (corr) {
+            const double c = distr[(uint64_t)round(rc[e]) - 1];
+            sscr[e] = pow(pow(raw[e], 1. - w) * pow(t, w) * c, 1. / 2.);
+        } else {
+            sscr[e] = pow(raw[e], 1. - w) * pow(t, w);
+        }
+    }
 }
 
 }  // extern "C"

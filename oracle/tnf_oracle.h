@@ -77,6 +77,17 @@ uint64_t orc_tnf_topk_rows(const float* tnf, const double* logsize, uint64_t n, 
                            uint32_t max_edges, uint64_t row0, uint64_t row1, uint64_t* row_ptr,
                            uint64_t* cols, double* sims, uint64_t cap, int threads);
 
+/* orc_tnf_graph / orc_tnf_topk_rows with the abundance pair gate: low
+ * (optional, n entries) marks contigs none of whose depths exceeds 1, and a
+ * pair of two such contigs is skipped (is_nz, cuda/Cuda2.cu:845-856, 925). */
+uint64_t orc_tnf_graph_nz(const float* tnf, const double* logsize, uint64_t n, double cutoff,
+                          uint32_t max_edges, uint64_t row0, uint64_t row1, uint64_t* from,
+                          uint64_t* to, double* stnf, uint64_t cap, int threads, const uint8_t* low);
+uint64_t orc_tnf_topk_rows_nz(const float* tnf, const double* logsize, uint64_t n, double cutoff,
+                              uint32_t max_edges, uint64_t row0, uint64_t row1, uint64_t* row_ptr,
+                              uint64_t* cols, double* sims, uint64_t cap, int threads,
+                              const uint8_t* low);
+
 /* get_tnf_max_prob_sample (cuda/Cuda2.cu:281-314) for sampled positions
  * [0, m) of the permutation `contigs` (length n): for each sampled contig,
  * sigmoid of the max pre-probability over all other contigs, local max
@@ -95,6 +106,21 @@ int orc_rand(void);
  * reference's `pTNF` variable after the driver). */
 double orc_ptnf_search(const float* tnf, const double* logsize, uint64_t n, double coverage,
                        int threads);
+
+/* Abundance: abd, var are n x nabd row-major (mean depth and variance of
+ * contig r in sample i, the reference's ABD / ABD_VAR).
+ * orc_abd_low: low[r] = 1 when no depth of contig r exceeds 1 (is_nz,
+ * cuda/Cuda2.cu:845-856). */
+void orc_abd_low(const double* abd, uint64_t n, uint32_t nabd, uint8_t* low);
+
+/* sTNF -> sSCR of the edges (cuda/Cuda2.cu:1921-1971, with cal_abd_dist
+ * 667-719, cal_abd_corr 1219-1245 and rank, cuda/ranker.h:56-80).  Edge e
+ * joins to[e] and from[e]; min_cv is the reference's minCV, min_sample its
+ * minSample (the correlation term is used when nabd >= min_sample).
+ * nabd == 0 copies sTNF. */
+void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint64_t ne, const double* abd,
+              const double* var, uint32_t nabd, double min_cv, uint32_t min_sample, double* sscr,
+              int threads);
 
 #ifdef __cplusplus
 }

@@ -20,12 +20,13 @@ def exact_sim(tnf, ls, i, j):
     return 1.0 - 1.0 / (1.0 + np.exp(pre)), pre
 
 
-def compare_graph(gpu_from, gpu_to, gpu_sim, tnf, ls, cutoff, max_edges):
+def compare_graph(gpu_from, gpu_to, gpu_sim, tnf, ls, cutoff, max_edges, low=None):
     """Edge sets must match except pairs whose probability lies within BAND of
     the cutoff or of either row's top-k cutoff; common edges must agree on
-    sTNF.  Returns (n_common, n_band_exempt)."""
+    sTNF.  low: the abundance pair gate of the oracle (optional).  Returns
+    (n_common, n_band_exempt)."""
     n = tnf.shape[0]
-    rp, cols, sims = oracle.topk_rows(tnf, ls, cutoff, max_edges)
+    rp, cols, sims = oracle.topk_rows(tnf, ls, cutoff, max_edges, low=low)
     kth = np.full(n, -np.inf)
     for i in range(n):
         if rp[i + 1] - rp[i] == max_edges:

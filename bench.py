@@ -14,6 +14,9 @@ program: tetranucleotide counting of every contig, the pTNF search
          every copy inside the timed region; e2e.link_h2d_gbs is a plain copy
          of the same pinned buffer measured right after (the link's speed on
          that box, which moves e2e by tens of milliseconds between boxes)
+  abundance  outside the step: the sTNF -> sSCR scoring of the step's edges
+         with 10 samples of seeded coverage (mdet_edges_sscr_dev), with the
+         CPU oracle's rate on a sample of them
 
 Lower is better (seconds per step).  `--impl reference` times the
 reference's CPU arithmetic (the oracle restatement; the reference's own
@@ -185,6 +188,56 @@ def cpu_baseline(a, tnf_host, n, target_s=8.0):
 
 
 # --------------------------------------------------------------- our arm --
+
+ABD_SAMPLES = 10
+
+
+def abundance_leg(ctx, a, d_tnf, d_ls, n, cutoff, d_from, d_to, d_st, cap, mode, run_cpu):
+    """The abundance form after the step: seeded coverage of ABD_SAMPLES
+    samples (synth.abundance) set on the context, the TNF graph again at the
+    step's cutoff with the is_nz pair gate, then sTNF -> sSCR of its edges
+    (mdet_edges_sscr_dev): 1 untimed and 3 timed calls, each synchronous (it
+    reads its error count back).  The CPU oracle scores the first 200,000 of
+    those edges with every host thread."""
+    import torch
+
+    from mdet_gb300 import synth
+
+    abd, var = synth.abundance(a.genome, ABD_SAMPLES, 20240607)
+    ctx.set_abundance(abd, var)
+    ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, cutoff, MAX_EDGES, mode, d_from.data_ptr(),
+                               d_to.data_ptr(), d_st.data_ptr(), cap)
+    out = torch.empty(max(ne, 1), dtype=torch.float64, device=d_st.device)
+    ctx.edges_sscr_dev(d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), ne, out.data_ptr())
+    ctx.set_timing(True)
+    reps = 3
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(reps):
+        ctx.edges_sscr_dev(d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), ne, out.data_ptr())
+    torch.cuda.synchronize()
+    call_s = (time.perf_counter() - t) / reps
+    score_ms, score_n = ctx.kernel_ms("k_abd_score")
+    ctx.set_timing(False)
+    leg = {"metric": "sTNF -> sSCR edge scoring throughput", "value": ne / call_s, "unit": "edges/s",
+           "edges": int(ne), "samples": ABD_SAMPLES, "ms_per_call": call_s * 1e3,
+           "k_abd_score_ms": score_ms / max(score_n, 1), "bound": "fp64 (erfc/log/sqrt per edge and sample)",
+           "gated_graph_ms": st["ms_total"], "data": "synthetic coverage (synth.abundance, seed 20240607)"}
+    if run_cpu:
+        from oracle import oracle
+
+        k = min(ne, 200000)
+        f = d_from[:k].cpu().numpy().astype(np.uint64)
+        t_ = d_to[:k].cpu().numpy().astype(np.uint64)
+        s_ = d_st[:k].cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.sscr(f, t_, s_, abd, var, threads=0)
+        dt = time.perf_counter() - t0
+        leg["cpu_baseline"] = {"value": k / dt, "unit": "edges/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"first {k} edges of the gated graph, all host threads"}
+    ctx.set_abundance(None, None)
+    return leg
+
 
 def run_ours(args):
     import torch
@@ -370,6 +423,9 @@ def run_ours(args):
             "filter_tile": (f"{int(st['tile_m_n']) // 1000}x{int(st['tile_m_n']) % 1000} (autotuned)"
                             if args.mode == "bf16" else "128x128 SIMT"),
         }
+        if not args.no_abd:
+            result["abundance"] = abundance_leg(ctx, a, d_tnf, d_ls, n, info["ptnf"] / 1000.0, d_from, d_to, d_st,
+                                                cap, args.mode, not args.no_cpu and ws == 1)
         if not args.no_plain:
             torch.cuda.synchronize()
             ne_p, stp = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, info["ptnf"] / 1000.0, MAX_EDGES,
@@ -436,6 +492,7 @@ def main():
     ap.add_argument("--mode", default="bf16", choices=["bf16", "plain"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-abd", action="store_true", help="skip the sTNF -> sSCR leg")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

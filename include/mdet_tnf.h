@@ -199,8 +199,8 @@ uint64_t mdet_ctx_graph_replays(mdet_ctx* ctx);
 /* ---- abundance (coverage) side --------------------------------------------
  * The coverage matrices the reference reads from its abundance file into the
  * globals ABD (mean depth) and ABD_VAR (depth variance) (cuda/Cuda2.cu:
- * 1593-1700): n x nabd, row-major FP64, rows in the contig order of the TNF
- * rows.  mdet_ctx_set_abundance copies them (host buffers) into the context;
+ * 1593-1700; float matrices there, cuda/Cuda2.cu:124-125): n x nabd,
+ * row-major, widened to FP64, rows in the contig order of the TNF rows.  mdet_ctx_set_abundance copies them (host buffers) into the context;
  * abd == null or nabd == 0 clears them.  While they are set, mdet_tnf_graph
  * and mdet_tnf_graph_dev skip every pair of two contigs none of whose depths
  * exceeds 1 before the per-contig top-k (is_nz, cuda/Cuda2.cu:845-856, as

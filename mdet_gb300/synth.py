@@ -85,7 +85,7 @@ def abundance(genome: np.ndarray, nabd: int, seed: int, low_frac: float = 0.03):
     (sigma 0.15) as its mean and mean * U(0.5, 2) as its variance.  A fraction
     low_frac of the contigs get depths in [0, 1) in every sample (no depth
     above 1, so a pair of two of them is not an edge).  Returns (abd, var),
-    n x nabd float64."""
+    n x nabd float64 holding float32 values."""
     rng = np.random.default_rng(seed)
     genome = np.asarray(genome)
     n = genome.size
@@ -95,4 +95,5 @@ def abundance(genome: np.ndarray, nabd: int, seed: int, low_frac: float = 0.03):
     low = rng.random(n) < low_frac
     abd[low] = rng.uniform(0.0, 1.0, size=(int(low.sum()), nabd))
     var = abd * rng.uniform(0.5, 2.0, size=(n, nabd))
-    return abd, var
+    # the reference keeps depths in float matrices
+    return abd.astype(np.float32).astype(np.float64), var.astype(np.float32).astype(np.float64)

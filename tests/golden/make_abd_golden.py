@@ -64,6 +64,9 @@ def make_inputs(seed=2024):
     for e in range(5, ne, 41):
         k = e % nabd
         var[to[e], k] = var[fr[e], k]
+    # float-valued, as the reference's ABD / ABD_VAR matrices are
+    abd = abd.astype(np.float32).astype(np.float64)
+    var = var.astype(np.float32).astype(np.float64)
     # every edge needs a sample above min_cv in both cases (else the
     # reference divides 0 by 0)
     cov = lambda k: ((abd[to, :k] > 1.0) | (abd[fr, :k] > 1.0)).any(1)

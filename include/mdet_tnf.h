@@ -109,6 +109,39 @@ int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, cons
 int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, const uint64_t* d_off, const uint64_t* d_len,
                            uint64_t n, uint32_t* d_counts, float* d_tnf, void* stream);
 
+/* ---- FASTA ingest ------------------------------------------------------
+ * Replaces the reader of main (cuda/Cuda2.cu:1486-1553) for the file's bytes
+ * already in memory: the record split, the size classes and the log sizes,
+ * run on the GPU.  Record rules (the reference's loop, read sequentially): a
+ * '>' starts a record wherever it stands, except inside the name line of the
+ * record before it; the name is the rest of that line cut at its first space;
+ * the sequence view runs from after that line's newline to the next record's
+ * '>' (or the end of the buffer), inner newlines kept, one trailing newline
+ * dropped; size = the view's bytes before that drop minus its newlines.  A
+ * name line that reaches the end of the buffer without a newline is not a
+ * record (the reference would read past its buffer there).  Records with
+ * size >= min_contig are written in file order: sequence view (offset and
+ * length into the buffer, as mdet_tnf_count takes them), size, log size
+ * log10(min(size, 500000)) (cuda/Cuda2.cu:1535) and name (offset, length).
+ * n_small counts the records with 1000 <= size < min_contig (the reference's
+ * small contigs).  MDET_ERR_CAPACITY when more than `capacity` records
+ * qualify (n_large then holds the count).  size, log_size, name_off and
+ * name_len may be null.  The device form needs a 16-byte aligned buffer. */
+typedef struct {
+    uint64_t n_records;  /* records found */
+    uint64_t n_large;    /* records with size >= min_contig */
+    uint64_t n_small;    /* records with 1000 <= size < min_contig */
+    double ms_total;     /* device time of the call */
+} mdet_fasta_stats;
+
+int mdet_fasta_index(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint64_t min_contig,
+                     uint64_t capacity, uint64_t* seq_off, uint64_t* seq_len, uint64_t* size,
+                     double* log_size, uint64_t* name_off, uint32_t* name_len, mdet_fasta_stats* stats);
+int mdet_fasta_index_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, uint64_t min_contig,
+                         uint64_t capacity, uint64_t* d_seq_off, uint64_t* d_seq_len, uint64_t* d_size,
+                         double* d_log_size, uint64_t* d_name_off, uint32_t* d_name_len,
+                         mdet_fasta_stats* stats);
+
 /* ---- max-probability sample --------------------------------------------
  * Replaces launch_tnf_max_prob_sample_kernel_multi (cuda/Cuda2.cu:356-379)
  * with get_tnf_max_prob_sample (cuda/Cuda2.cu:281-314): for each sampled

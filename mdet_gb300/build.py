@@ -34,6 +34,7 @@ CU_UNITS = [
     "graph_learned",
     "graph_batch",
     "abundance",
+    "fasta_index",
 ]
 # per-unit flags: the abundance unit rounds every product and sum separately
 # (no FMA contraction), as the reference's host arithmetic does

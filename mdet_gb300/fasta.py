@@ -1,7 +1,9 @@
 """FASTA reading with the reference reader's semantics (cuda/Cuda2.cu:1487-1572).
 
-Every '>' starts a record.  The name runs to the end of its line and is cut
-at the first space.  The sequence view starts after the header's newline and
+A '>' starts a record wherever it stands, except inside the name line of the
+record before it (there it is part of the name): the record starts are the
+first '>' of each line.  The name runs to the end of its line and is cut at
+the first space.  The sequence view starts after the header's newline and
 runs to the next '>' (or end of file), keeping its inner newlines, with one
 trailing newline dropped.  The contig size is the view's length minus its
 newlines.  Records with size >= min_contig are the "large" contigs that get
@@ -32,6 +34,13 @@ def parse_fasta_bytes(data: np.ndarray, min_contig: int = 2500) -> Assembly:
     fsize = data.size
     names, offs, lens, sizes = [], [], [], []
     nl_pos = np.flatnonzero(data == ord("\n"))
+    # keep the first '>' of each line: the previous '>' lies before the line's start
+    if gt.size:
+        k = np.searchsorted(nl_pos, gt) - 1
+        line0 = np.where(k >= 0, nl_pos[np.maximum(k, 0)] if nl_pos.size else -1, -1)
+        first = np.ones(gt.size, bool)
+        first[1:] = gt[:-1] < line0[1:]
+        gt = gt[first]
     for k, g in enumerate(gt):
         h = np.searchsorted(nl_pos, g + 1)
         if h >= nl_pos.size:

@@ -31,6 +31,13 @@ P = ctypes.c_void_p
 D = ctypes.c_double
 
 
+class FastaStats(ctypes.Structure):
+    _fields_ = [("n_records", u64), ("n_large", u64), ("n_small", u64), ("ms_total", D)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class GraphStats(ctypes.Structure):
     _fields_ = [
         ("n_candidates", u64),
@@ -155,6 +162,8 @@ SIGNATURES = [
      [P, P, P, P, u64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)]),
     ("mdet_ctx_set_learned", ctypes.c_int, [P, P, ctypes.POINTER(LearnedReport)]),
     ("mdet_ctx_set_abundance", ctypes.c_int, [P, P, P, u64, u32]),
+    ("mdet_fasta_index", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
+    ("mdet_fasta_index_dev", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
     ("mdet_edges_sscr", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
     ("mdet_edges_sscr_dev", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
 ]
@@ -343,6 +352,39 @@ class Context:
                                                 MODES[mode], P(d_from), P(d_to), P(d_stnf), capacity,
                                                 ctypes.byref(ne), ctypes.byref(stats)))
         return ne.value, stats.as_dict()
+
+    def fasta_index(self, data, min_contig=2500, capacity=None):
+        """The reference reader's record split of a FASTA buffer, on the GPU.
+        Returns (seq_off, seq_len, sizes, log_sizes, names, stats) for the
+        records with size >= min_contig, in file order."""
+        data = np.ascontiguousarray(data, np.uint8)
+        cap = int(capacity) if capacity is not None else max(1, data.size // 1000 + 16)
+        while True:
+            off, ln, sz, no = (np.empty(cap, np.uint64) for _ in range(4))
+            ls = np.empty(cap, np.float64)
+            nl = np.empty(cap, np.uint32)
+            st = FastaStats()
+            rc = self.lib.mdet_fasta_index(self.h, P(data.ctypes.data), data.size, int(min_contig), cap,
+                                           P(off.ctypes.data), P(ln.ctypes.data), P(sz.ctypes.data),
+                                           P(ls.ctypes.data), P(no.ctypes.data), P(nl.ctypes.data),
+                                           ctypes.byref(st))
+            if rc == ERR_CAPACITY and capacity is None and st.n_large > cap:
+                cap = int(st.n_large)
+                continue
+            self._check(rc)
+            break
+        k = int(st.n_large)
+        raw = data.tobytes() if k else b""
+        names = [raw[int(o):int(o) + int(n)].decode(errors="replace") for o, n in zip(no[:k], nl[:k])]
+        return off[:k], ln[:k], sz[:k], ls[:k], names, st.as_dict()
+
+    def fasta_index_dev(self, d_bytes, nbytes, min_contig, capacity, d_seq_off, d_seq_len, d_size=None,
+                        d_log_size=None, d_name_off=None, d_name_len=None):
+        st = FastaStats()
+        self._check(self.lib.mdet_fasta_index_dev(self.h, P(d_bytes), nbytes, int(min_contig), capacity,
+                                                  P(d_seq_off), P(d_seq_len), P(d_size), P(d_log_size),
+                                                  P(d_name_off), P(d_name_len), ctypes.byref(st)))
+        return st.as_dict()
 
     def set_abundance(self, abd, var):
         """Coverage of the contigs (n x nabd mean depths and variances, the

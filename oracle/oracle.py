@@ -62,6 +62,8 @@ def lib():
         L.orc_tnf_topk_rows_nz.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int, P]
         L.orc_abd_low.argtypes = [P, u64, ctypes.c_uint32, P]
         L.orc_sscr.argtypes = [P, P, P, u64, P, P, ctypes.c_uint32, D, ctypes.c_uint32, P, ctypes.c_int]
+        L.orc_fasta_index.restype = u64
+        L.orc_fasta_index.argtypes = [P, u64, u64, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -195,3 +197,14 @@ def ptnf_search(tnf, ls, coverage=0.95, seed=1, threads=0):
 
 def srand(seed):
     lib().orc_srand(seed)
+
+
+def fasta_index(data):
+    """Every record of a FASTA buffer: (seq_off, seq_len, size, name_off, name_len)."""
+    data = np.ascontiguousarray(data, np.uint8)
+    n = lib().orc_fasta_index(_p(data), data.size, 0, None, None, None, None, None)
+    cap = max(1, n)
+    so, sl, sz, no = (np.zeros(cap, np.uint64) for _ in range(4))
+    nl = np.zeros(cap, np.uint32)
+    lib().orc_fasta_index(_p(data), data.size, cap, _p(so), _p(sl), _p(sz), _p(no), _p(nl))
+    return so[:n], sl[:n], sz[:n], no[:n], nl[:n]

@@ -673,3 +673,50 @@ void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint
 }
 
 }  // extern "C"
+
+extern "C" {
+
+/* The reference reader's record split (cuda/Cuda2.cu:1507-1544), read
+ * sequentially: a '>' starts a record wherever it stands (a '>' inside the
+ * record's own name line belongs to the name); the name is the rest of that
+ * line cut at its first space; the sequence view runs from after the name
+ * line's newline to the next record's '>' (or the end), inner newlines kept,
+ * and drops one trailing newline; size = the view's bytes before that drop
+ * minus its newlines.  A name line with no newline before the end of the
+ * buffer ends the scan (the reference would read past its buffer there).
+ * Every record is returned (no size classes); at most cap are written. */
+uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t* seq_off, uint64_t* seq_len,
+                         uint64_t* size, uint64_t* name_off, uint32_t* name_len) {
+    uint64_t nr = 0, i = 0;
+    while (i < nbytes) {
+        const char* gt = (const char*)memchr(b + i, '>', nbytes - i);
+        if (!gt) break;
+        const uint64_t p = (uint64_t)(gt - b);
+        const char* nl = (const char*)memchr(b + p + 1, '\n', nbytes - p - 1);
+        if (!nl) break;
+        const uint64_t h = (uint64_t)(nl - b);
+        uint64_t nlen = h - (p + 1);
+        const char* sp = (const char*)memchr(b + p + 1, ' ', nlen);
+        if (sp) nlen = (uint64_t)(sp - (b + p + 1));
+        const uint64_t s0 = h + 1;
+        const char* nx = (const char*)memchr(b + s0, '>', nbytes - s0);
+        const uint64_t s1 = nx ? (uint64_t)(nx - b) : nbytes;
+        uint64_t lines = 0;
+        for (uint64_t q = s0; q < s1; ++q) lines += b[q] == '\n';
+        uint64_t view = s1 - s0;
+        const uint64_t sz = view - lines;
+        if (view > 0 && b[s1 - 1] == '\n') --view;
+        if (nr < cap) {
+            seq_off[nr] = s0;
+            seq_len[nr] = view;
+            size[nr] = sz;
+            name_off[nr] = p + 1;
+            name_len[nr] = (uint32_t)nlen;
+        }
+        ++nr;
+        i = s1;
+    }
+    return nr;
+}
+
+}  // extern "C"

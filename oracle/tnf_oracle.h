@@ -122,6 +122,14 @@ void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint
               const double* var, uint32_t nabd, double min_cv, uint32_t min_sample, double* sscr,
               int threads);
 
+/* The reference reader's record split (cuda/Cuda2.cu:1507-1544), taken
+ * sequentially: every record (no size classes) with its sequence view
+ * (offset, length: inner newlines kept, one trailing newline dropped), its
+ * size (bases: view bytes before the drop minus newlines) and its name (after
+ * '>', cut at the first space).  Returns the record count; writes <= cap. */
+uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t* seq_off, uint64_t* seq_len,
+                         uint64_t* size, uint64_t* name_off, uint32_t* name_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,6 +6,9 @@
                                                           assembly, then the learned graph
   python -m mdet_gb300.profile_case batch --count 64      many assemblies, n ~ logU(nmin, nmax):
                                                           one call per assembly vs one batched call
+  python -m mdet_gb300.profile_case fasta --n 100000     FASTA record split of ~0.85 GB on the device
+  python -m mdet_gb300.profile_case abd --n 100000       gated graph, then sTNF -> sSCR of its edges
+                                                          with 10 samples of coverage
 
 The graph case frees the FASTA before the pairwise call so that only the
 stage's own buffers (~1-2 GB) are resident when it runs.
@@ -22,7 +25,8 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("stage", choices=["count", "graph", "learned", "batch"])
+    ap.add_argument("stage", choices=["count", "graph", "learned", "batch", "fasta", "abd"])
+    ap.add_argument("--samples", type=int, default=10)
     ap.add_argument("--count", type=int, default=64)
     ap.add_argument("--nmin", type=int, default=5000)
     ap.add_argument("--nmax", type=int, default=300000)
@@ -53,6 +57,15 @@ def main():
     d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
     d_cnt = torch.empty((args.n, 136), dtype=torch.int32, device=dev)
     d_tnf = torch.empty((args.n, 136), dtype=torch.float32, device=dev)
+    if args.stage == "fasta":
+        off = torch.empty(args.n, dtype=torch.int64, device=dev)
+        ln = torch.empty(args.n, dtype=torch.int64, device=dev)
+        for _ in range(args.repeat):
+            st = ctx.fasta_index_dev(d_bytes.data_ptr(), nb, 2500, args.n, off.data_ptr(), ln.data_ptr())
+        print(st)
+        torch.cuda.synchronize()
+        ctx.close()
+        return
     reps = args.repeat if args.stage == "count" else 1
     for _ in range(reps):
         ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), args.n, d_cnt.data_ptr(),
@@ -91,6 +104,20 @@ def main():
             extra = lr.as_dict() if mode == "learned" else {}
             print({"mode": mode, "edges": ne, **{k: round(v, 3) if isinstance(v, float) else v
                                                  for k, v in st.items()}, **extra})
+    if args.stage == "abd":
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        abd, var = synth.abundance(a.genome, args.samples, 7)
+        ctx.set_abundance(abd, var)
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, args.mode,
+                                   out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+        sscr = torch.empty(max(ne, 1), dtype=torch.float64, device=dev)
+        for _ in range(args.repeat):
+            ctx.edges_sscr_dev(out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), ne, sscr.data_ptr())
+        print({"edges": ne, "graph_ms": st["ms_total"]})
     if args.stage == "graph":
         del d_bytes, d_cnt
         torch.cuda.empty_cache()

@@ -268,6 +268,14 @@ def fasta_leg(ctx, d_bytes, nbytes, a, pinned, pk, run_cpu):
                         "frac": gbs / pk["hbm_gbs"],
                         "note": "file bytes read twice (record starts, then each record's newlines): frac 0.5 "
                                 "would be both passes at the copy rate"}}
+    # the reader's split and the TNF loop from host bytes in one call
+    # (mdet_tnf_count_fasta: one copy of the pinned file, split, count, rows back)
+    host = pinned.numpy()[:nbytes]
+    ctx.tnf_count_fasta(host, 2500, capacity=n)
+    t0 = time.perf_counter()
+    _, _, _, _, _, st2 = ctx.tnf_count_fasta(host, 2500, capacity=n)
+    leg["count_from_host_bytes_s"] = time.perf_counter() - t0
+    leg["count_from_host_bytes_contigs"] = int(st2["n_large"])
     if run_cpu:
         from oracle import oracle
 

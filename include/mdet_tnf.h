@@ -142,6 +142,16 @@ int mdet_fasta_index_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, ui
                          double* d_log_size, uint64_t* d_name_off, uint32_t* d_name_len,
                          mdet_fasta_stats* stats);
 
+/* The reader's record split and the TNF loop of main (cuda/Cuda2.cu:
+ * 1486-1553, 1825-1863) in one call from the file's bytes in host memory: one
+ * copy to the device, the split there, the count on the views it produced.
+ * Outputs for the contigs with size >= min_contig, in file order, up to
+ * `capacity` of them: views (seq_off, seq_len; may be null), log sizes (may
+ * be null), counts and TNF (n x 136 each).  stats as mdet_fasta_index. */
+int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint64_t min_contig,
+                         uint64_t capacity, uint64_t* seq_off, uint64_t* seq_len, double* log_size,
+                         uint32_t* counts, float* tnf, mdet_fasta_stats* stats);
+
 /* ---- max-probability sample --------------------------------------------
  * Replaces launch_tnf_max_prob_sample_kernel_multi (cuda/Cuda2.cu:356-379)
  * with get_tnf_max_prob_sample (cuda/Cuda2.cu:281-314): for each sampled

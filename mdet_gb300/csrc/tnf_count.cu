@@ -435,6 +435,46 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
     return check_flag(ctx);
 }
 
+// The reader's record split and the TNF loop in one call from host bytes:
+// one copy of the file to the device, the split there (mdet_fasta_index_dev),
+// the count on the views it produced, and the rows copied back.
+int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint64_t min_contig, uint64_t capacity,
+                         uint64_t* seq_off, uint64_t* seq_len, double* log_size, uint32_t* counts, float* tnf,
+                         mdet_fasta_stats* stats) {
+    if (!ctx || !stats) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    memset(stats, 0, sizeof(*stats));
+    if (nbytes == 0) return MDET_OK;
+    if (!bytes) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    if (capacity && (!counts || !tnf)) return ctx_fail(ctx, MDET_ERR_INVALID, "null output pointer");
+    cudaStream_t s = ctx->stream;
+    const uint64_t padded = (nbytes + 31) & ~(uint64_t)15, cap = capacity ? capacity : 1;
+    char* d_bytes = (char*)ctx_scratch(ctx, "io.bytes", padded);
+    uint64_t* d_off = (uint64_t*)ctx_scratch(ctx, "io.off", cap * 8);
+    uint64_t* d_len = (uint64_t*)ctx_scratch(ctx, "io.len", cap * 8);
+    double* d_ls = (double*)ctx_scratch(ctx, "io.fa_ls", cap * 8);
+    if (!d_bytes || !d_off || !d_len || !d_ls) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemcpyAsync(d_bytes, bytes, nbytes, cudaMemcpyHostToDevice, s));
+    MDET_TRY(mdet_fasta_index_dev(ctx, d_bytes, nbytes, min_contig, capacity, d_off, d_len, nullptr, d_ls, nullptr,
+                                  nullptr, stats));
+    const uint64_t n = stats->n_large;
+    if (n == 0) return MDET_OK;
+    uint32_t* d_counts = (uint32_t*)ctx_scratch(ctx, "io.counts", n * MDET_NTNF * 4);
+    float* d_tnf = (float*)ctx_scratch(ctx, "io.tnf", n * MDET_NTNF * 4);
+    if (!d_counts || !d_tnf) return MDET_ERR_NOMEM;
+    int rc = count_impl(ctx, d_bytes, nbytes, d_off, d_len, n, d_counts, d_tnf);
+    if (rc != MDET_OK) {
+        ctx->count_scratch_dirty = true;
+        return rc;
+    }
+    if (seq_off) MDET_CUDA(ctx, cudaMemcpyAsync(seq_off, d_off, n * 8, cudaMemcpyDeviceToHost, s));
+    if (seq_len) MDET_CUDA(ctx, cudaMemcpyAsync(seq_len, d_len, n * 8, cudaMemcpyDeviceToHost, s));
+    if (log_size) MDET_CUDA(ctx, cudaMemcpyAsync(log_size, d_ls, n * 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(tnf, d_tnf, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
+    return check_flag(ctx);
+}
+
 }  // extern "C"
 
 // ------------------------------------------------- allocation-free variant --

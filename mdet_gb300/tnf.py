@@ -164,6 +164,7 @@ SIGNATURES = [
     ("mdet_ctx_set_abundance", ctypes.c_int, [P, P, P, u64, u32]),
     ("mdet_fasta_index", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
     ("mdet_fasta_index_dev", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
+    ("mdet_tnf_count_fasta", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
     ("mdet_edges_sscr", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
     ("mdet_edges_sscr_dev", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
 ]
@@ -377,6 +378,29 @@ class Context:
         raw = data.tobytes() if k else b""
         names = [raw[int(o):int(o) + int(n)].decode(errors="replace") for o, n in zip(no[:k], nl[:k])]
         return off[:k], ln[:k], sz[:k], ls[:k], names, st.as_dict()
+
+    def tnf_count_fasta(self, data, min_contig=2500, capacity=None):
+        """Record split and TNF counting from FASTA bytes in one call.
+        Returns (seq_off, seq_len, log_sizes, counts, tnf, stats) for the
+        contigs with size >= min_contig, in file order."""
+        data = np.ascontiguousarray(data, np.uint8)
+        cap = int(capacity) if capacity is not None else max(1, data.size // 1000 + 16)
+        while True:
+            off, ln = np.empty(cap, np.uint64), np.empty(cap, np.uint64)
+            ls = np.empty(cap, np.float64)
+            counts = np.empty((cap, 136), np.uint32)
+            tnf = np.empty((cap, 136), np.float32)
+            st = FastaStats()
+            rc = self.lib.mdet_tnf_count_fasta(self.h, P(data.ctypes.data), data.size, int(min_contig), cap,
+                                               P(off.ctypes.data), P(ln.ctypes.data), P(ls.ctypes.data),
+                                               P(counts.ctypes.data), P(tnf.ctypes.data), ctypes.byref(st))
+            if rc == ERR_CAPACITY and capacity is None and st.n_large > cap:
+                cap = int(st.n_large)
+                continue
+            self._check(rc)
+            break
+        k = int(st.n_large)
+        return off[:k], ln[:k], ls[:k], counts[:k], tnf[:k], st.as_dict()
 
     def fasta_index_dev(self, d_bytes, nbytes, min_contig, capacity, d_seq_off, d_seq_len, d_size=None,
                         d_log_size=None, d_name_off=None, d_name_len=None):

@@ -106,3 +106,22 @@ def test_capacity_and_device_path(gpu_ctx):
     assert np.array_equal(d_cnt.cpu().numpy().view(np.uint32), oc)
     with pytest.raises(MdetError):  # unaligned device buffer
         gpu_ctx.fasta_index_dev(buf.data_ptr() + 1, data.size - 1, 0, n, d_off.data_ptr(), d_len.data_ptr())
+
+
+@pytest.mark.parametrize("name,min_contig", [("count_synth.fa.gz", 2500), ("count_edge.fa", 0)])
+def test_count_from_fasta_bytes(gpu_ctx, name, min_contig):
+    """Record split + counting in one call equals the oracle's count of the
+    reference reader's views."""
+    import gzip
+
+    p = os.path.join(G, name)
+    raw = gzip.open(p).read() if name.endswith(".gz") else open(p, "rb").read()
+    data = np.frombuffer(raw, np.uint8)
+    off, ln, ls, counts, tnf, st = gpu_ctx.tnf_count_fasta(data, min_contig)
+    a = parse_fasta_bytes(data, min_contig)
+    assert np.array_equal(off, a.seq_off) and np.array_equal(ln, a.seq_len)
+    assert np.allclose(ls, a.log_sizes, rtol=4e-16, atol=0)
+    oc, ot = oracle.tnf_count(data, a.seq_off, a.seq_len)
+    assert np.array_equal(counts, oc)
+    c2, t2 = gpu_ctx.tnf_count(data, a.seq_off, a.seq_len)
+    assert np.array_equal(tnf.view(np.uint32), t2.view(np.uint32))

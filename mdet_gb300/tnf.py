@@ -485,6 +485,7 @@ class Context:
     # ---- reference-named aliases ----------------------------------------
     calc_tnf = tnf_count
     gen_tnf_graph = tnf_graph
+    gen_tnf_graph_sample = ptnf_search
     max_prob_sample = max_prob
 
 

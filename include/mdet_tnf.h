@@ -78,6 +78,13 @@ int mdet_ctx_kernel_ms(mdet_ctx* ctx, const char* kernel, double* ms, uint32_t* 
 /* Kernels this context has launched since it was created. */
 uint64_t mdet_ctx_launch_count(const mdet_ctx* ctx);
 
+/* Page-locked host memory, as the reference allocates its file buffer and
+ * TNF rows (cudaMallocHost, cuda/Cuda2.cu:1462, 1826): copies between it and
+ * the device run at the link's full rate, copies from ordinary memory are
+ * staged.  mdet_host_free(null) does nothing. */
+int mdet_host_alloc(uint64_t bytes, void** out);
+int mdet_host_free(void* p);
+
 /* ---- TNF counting ------------------------------------------------------
  * Replaces the TNF loop of main (cuda/Cuda2.cu:1825-1863) and the copy of
  * TNF/logSizes to the devices (cuda/Cuda2.cu:1866-1874).  bytes[off[i] ..
@@ -146,11 +153,13 @@ int mdet_fasta_index_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, ui
  * 1486-1553, 1825-1863) in one call from the file's bytes in host memory: one
  * copy to the device, the split there, the count on the views it produced.
  * Outputs for the contigs with size >= min_contig, in file order, up to
- * `capacity` of them: views (seq_off, seq_len; may be null), log sizes (may
- * be null), counts and TNF (n x 136 each).  stats as mdet_fasta_index. */
+ * `capacity` of them: views (seq_off, seq_len), sizes, log sizes and names
+ * (name_off, name_len) as mdet_fasta_index writes them (each may be null),
+ * counts and TNF (n x 136 each).  stats as mdet_fasta_index. */
 int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint64_t min_contig,
-                         uint64_t capacity, uint64_t* seq_off, uint64_t* seq_len, double* log_size,
-                         uint32_t* counts, float* tnf, mdet_fasta_stats* stats);
+                         uint64_t capacity, uint64_t* seq_off, uint64_t* seq_len, uint64_t* size,
+                         double* log_size, uint64_t* name_off, uint32_t* name_len, uint32_t* counts,
+                         float* tnf, mdet_fasta_stats* stats);
 
 /* ---- max-probability sample --------------------------------------------
  * Replaces launch_tnf_max_prob_sample_kernel_multi (cuda/Cuda2.cu:356-379)

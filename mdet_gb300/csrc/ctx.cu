@@ -362,3 +362,26 @@ int mdet_ctx_kernel_ms(mdet_ctx* ctx, const char* kernel, double* ms, uint32_t* 
 uint64_t mdet_ctx_launch_count(const mdet_ctx* ctx) { return ctx ? ctx->total_launches : 0; }
 
 }  // extern "C"
+
+extern "C" {
+
+int mdet_host_alloc(uint64_t bytes, void** out) {
+    if (!out) return MDET_ERR_INVALID;
+    *out = nullptr;
+    if (cudaMallocHost(out, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return MDET_ERR_NOMEM;
+    }
+    return MDET_OK;
+}
+
+int mdet_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    return MDET_OK;
+}
+
+}  // extern "C"

@@ -7,6 +7,7 @@
 //   <out>.tnf_graph.tsv   name_i <TAB> name_j <TAB> sTNF   (i < j)
 //   <out>.TNF.bin         n x 136 float64 rows c/sqrt(sum c^2), the TNF.bin
 //                         layout of openmp/TNF.cpp
+#include <charconv>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -15,6 +16,7 @@
 #include <ctime>
 #include <fstream>
 #include <iostream>
+#include <memory>
 #include <string>
 #include <string_view>
 #include <unordered_map>
@@ -117,51 +119,26 @@ bool parse(int ac, char** av, Opts& o) {
 }
 
 struct Fasta {
-    std::vector<char> mem;
+    char* mem = nullptr;  // page-locked (mdet_host_alloc)
+    size_t size = 0;
     std::vector<std::string_view> names;
-    std::vector<uint64_t> off, len;
     std::vector<double> log_size;
+    ~Fasta() { mdet_host_free(mem); }
 };
 
-// The reference reader's record rules (cuda/Cuda2.cu:1507-1544), sequentially.
-bool read_fasta(const std::string& path, size_t min_contig, Fasta& f) {
+// The file's bytes (the reference maps the whole file into pinned memory,
+// cuda/Cuda2.cu:1459-1484); the record split runs on the GPU.
+bool read_file(const std::string& path, Fasta& f) {
     std::ifstream is(path, std::ios::binary | std::ios::ate);
     if (!is) return false;
-    size_t fsize = (size_t)is.tellg();
+    const size_t fsize = (size_t)is.tellg();
     is.seekg(0);
-    f.mem.resize(fsize + 32);
-    is.read(f.mem.data(), (std::streamsize)fsize);
-    const char* m = f.mem.data();
-    size_t i = 0;
-    while (i < fsize) {
-        const char* gt = (const char*)memchr(m + i, '>', fsize - i);
-        if (!gt) break;
-        i = (size_t)(gt - m) + 1;
-        size_t name0 = i;
-        const char* nl = (const char*)memchr(m + i, '\n', fsize - i);
-        if (!nl) break;
-        i = (size_t)(nl - m);
-        std::string_view name(m + name0, i - name0);
-        size_t sp = name.find_first_of(' ');
-        if (sp != std::string_view::npos) name = name.substr(0, sp);
-        ++i;
-        size_t s0 = i;
-        const char* next = (const char*)memchr(m + i, '>', fsize - i);
-        size_t s1 = next ? (size_t)(next - m) : fsize;
-        size_t lines = 0;
-        for (const char* p = m + s0; (p = (const char*)memchr(p, '\n', (size_t)(m + s1 - p))) != nullptr; ++p) ++lines;
-        size_t view = s1 - s0;
-        size_t size = view - lines;
-        if (view > 0 && m[s1 - 1] == '\n') --view;
-        if (size >= min_contig) {
-            f.names.push_back(name);
-            f.off.push_back(s0);
-            f.len.push_back(view);
-            f.log_size.push_back(std::log10((double)std::min(size, (size_t)500000)));
-        }
-        i = s1;
-    }
-    return true;
+    void* m = nullptr;
+    if (mdet_host_alloc(fsize + 32, &m) != MDET_OK) return false;
+    f.mem = (char*)m;
+    f.size = fsize;
+    is.read(f.mem, (std::streamsize)fsize);
+    return (bool)is || fsize == 0;
 }
 
 int check(mdet_ctx* ctx, int rc, const char* what) {
@@ -221,9 +198,50 @@ int main(int ac, char** av) {
 
     auto t_read = Clock::now();
     Fasta fa;
-    if (!read_fasta(o.in, o.min_contig, fa)) {
+    if (!read_file(o.in, fa)) {
         std::cerr << "[Error!] can't open the sequence fasta file " << o.in << std::endl;
         return 1;
+    }
+    timer_line("read", t_read);
+    auto t_abd = Clock::now();
+    timer_line("ABD", t_abd);
+
+    mdet_ctx* ctx = nullptr;
+    if (mdet_ctx_create(o.device, &ctx) != MDET_OK) {
+        std::cerr << "[Error!] no usable CUDA device " << o.device << std::endl;
+        return 1;
+    }
+    // record split (reader rules of cuda/Cuda2.cu:1507-1544) and TNF counting
+    // on the GPU, from one copy of the file
+    auto t_tnf = Clock::now();
+    uint64_t rcap = fa.size / 1000 + 16;
+    // outputs sized for the largest possible count and left uninitialised
+    // (only the first n rows are written, so only their pages are touched)
+    std::unique_ptr<uint64_t[]> size, name_off;
+    std::unique_ptr<uint32_t[]> name_len, counts_buf;
+    std::unique_ptr<float[]> tnf_buf;
+    mdet_fasta_stats fs;
+    while (true) {
+        size.reset(new uint64_t[rcap]);
+        name_off.reset(new uint64_t[rcap]);
+        name_len.reset(new uint32_t[rcap]);
+        counts_buf.reset(new uint32_t[rcap * 136]);
+        tnf_buf.reset(new float[rcap * 136]);
+        int rc = mdet_tnf_count_fasta(ctx, fa.mem, fa.size, o.min_contig, rcap, nullptr, nullptr, size.get(),
+                                      nullptr, name_off.get(), name_len.get(), counts_buf.get(), tnf_buf.get(),
+                                      &fs);
+        if (rc == MDET_ERR_CAPACITY && fs.n_large > rcap) {
+            rcap = fs.n_large;
+            continue;
+        }
+        check(ctx, rc, "TNF counting");
+        break;
+    }
+    const uint64_t n = fs.n_large;
+    for (uint64_t k = 0; k < n; ++k) {
+        fa.names.emplace_back(fa.mem + name_off[k], name_len[k]);
+        // log10(min(size, 500000)) on the host, as the reference computes it (cuda/Cuda2.cu:1535)
+        fa.log_size.push_back(std::log10((double)std::min(size[k], (uint64_t)500000)));
     }
     {
         std::unordered_map<std::string_view, size_t> seen;
@@ -234,29 +252,15 @@ int main(int ac, char** av) {
                 return 1;
             }
     }
-    const uint64_t n = fa.names.size();
     if (o.verbose) std::cout << "Number of large contigs >= " << o.min_contig << " are " << n << ". " << std::endl;
-    timer_line("read", t_read);
-    auto t_abd = Clock::now();
-    timer_line("ABD", t_abd);
-
-    mdet_ctx* ctx = nullptr;
-    if (mdet_ctx_create(o.device, &ctx) != MDET_OK) {
-        std::cerr << "[Error!] no usable CUDA device " << o.device << std::endl;
-        return 1;
-    }
-    auto t_tnf = Clock::now();
-    std::vector<uint32_t> counts(n * 136);
-    std::vector<float> tnf(n * 136);
-    check(ctx, mdet_tnf_count(ctx, fa.mem.data(), fa.mem.size() - 32, fa.off.data(), fa.len.data(), n, counts.data(),
-                              tnf.data()),
-          "TNF counting");
+    const uint32_t* counts = counts_buf.get();
+    const float* tnf = tnf_buf.get();
     timer_line("TNF_CAL", t_tnf);
 
     auto t_sample = Clock::now();
     double ptnf = o.pTNF;
     if (n >= 2 && ptnf < 1.)
-        check(ctx, mdet_tnf_ptnf_search(ctx, tnf.data(), fa.log_size.data(), n, coverage, mode, &ptnf), "pTNF search");
+        check(ctx, mdet_tnf_ptnf_search(ctx, tnf, fa.log_size.data(), n, coverage, mode, &ptnf), "pTNF search");
     else
         ptnf *= 10;
     if (o.verbose) printf("Finished Preparing TNF Graph Building [pTNF = %2.2f]\n", ptnf / 10.);
@@ -264,26 +268,47 @@ int main(int ac, char** av) {
 
     auto t_graph = Clock::now();
     uint64_t cap = n * o.max_edges + 1, ne = 0;
-    std::vector<uint64_t> from(cap), to(cap);
-    std::vector<double> stnf(cap);
+    // outputs left uninitialised: the call writes the first ne entries
+    std::unique_ptr<uint64_t[]> from(new uint64_t[cap]), to(new uint64_t[cap]);
+    std::unique_ptr<double[]> stnf(new double[cap]);
     mdet_graph_stats st;
     if (n >= 2)
-        check(ctx, mdet_tnf_graph(ctx, tnf.data(), fa.log_size.data(), n, ptnf / 1000., (uint32_t)o.max_edges, mode,
-                                  from.data(), to.data(), stnf.data(), cap, &ne, &st),
+        check(ctx, mdet_tnf_graph(ctx, tnf, fa.log_size.data(), n, ptnf / 1000., (uint32_t)o.max_edges, mode,
+                                  from.get(), to.get(), stnf.get(), cap, &ne, &st),
               "TNF graph");
     timer_line("TNF_GRAPH", t_graph);
     if (ne == 0) std::cout << "No edges were formed by TNF." << std::endl;
 
     {
-        std::ofstream g(o.out + ".tnf_graph.tsv");
+        FILE* g = fopen((o.out + ".tnf_graph.tsv").c_str(), "wb");
         if (!g) {
             std::cerr << "[Error!] can't open the output file: " << o.out << ".tnf_graph.tsv" << std::endl;
             return 1;
         }
-        char buf[64];
+        // shortest round-trip decimal of each sTNF (std::to_chars), written in
+        // large blocks
+        std::vector<char> blk(1 << 24);
+        size_t used = 0;
         for (uint64_t e = 0; e < ne; ++e) {
-            snprintf(buf, sizeof(buf), "%.17g", stnf[e]);
-            g << fa.names[from[e]] << '\t' << fa.names[to[e]] << '\t' << buf << '\n';
+            const std::string_view a = fa.names[from[e]], b = fa.names[to[e]];
+            if (used + a.size() + b.size() + 40 > blk.size()) {
+                if (a.size() + b.size() + 40 > blk.size()) blk.resize(2 * (a.size() + b.size() + 40));
+                fwrite(blk.data(), 1, used, g);
+                used = 0;
+            }
+            memcpy(blk.data() + used, a.data(), a.size());
+            used += a.size();
+            blk[used++] = '\t';
+            memcpy(blk.data() + used, b.data(), b.size());
+            used += b.size();
+            blk[used++] = '\t';
+            used = (size_t)(std::to_chars(blk.data() + used, blk.data() + blk.size(), stnf[e]).ptr - blk.data());
+            blk[used++] = '\n';
+        }
+        fwrite(blk.data(), 1, used, g);
+        if (fclose(g) != 0) {
+            std::cerr << "[Error!] failed to write " << o.out << ".tnf_graph.tsv" << std::endl;
+            return 1;
         }
     }
     if (!o.no_tnf_bin) {

@@ -439,8 +439,8 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
 // one copy of the file to the device, the split there (mdet_fasta_index_dev),
 // the count on the views it produced, and the rows copied back.
 int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint64_t min_contig, uint64_t capacity,
-                         uint64_t* seq_off, uint64_t* seq_len, double* log_size, uint32_t* counts, float* tnf,
-                         mdet_fasta_stats* stats) {
+                         uint64_t* seq_off, uint64_t* seq_len, uint64_t* size, double* log_size, uint64_t* name_off,
+                         uint32_t* name_len, uint32_t* counts, float* tnf, mdet_fasta_stats* stats) {
     if (!ctx || !stats) return MDET_ERR_INVALID;
     MDET_CUDA(ctx, cudaSetDevice(ctx->device));
     memset(stats, 0, sizeof(*stats));
@@ -453,10 +453,13 @@ int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint
     uint64_t* d_off = (uint64_t*)ctx_scratch(ctx, "io.off", cap * 8);
     uint64_t* d_len = (uint64_t*)ctx_scratch(ctx, "io.len", cap * 8);
     double* d_ls = (double*)ctx_scratch(ctx, "io.fa_ls", cap * 8);
-    if (!d_bytes || !d_off || !d_len || !d_ls) return MDET_ERR_NOMEM;
+    uint64_t* d_size = (uint64_t*)ctx_scratch(ctx, "io.fa_size", cap * 8);
+    uint64_t* d_noff = (uint64_t*)ctx_scratch(ctx, "io.fa_noff", cap * 8);
+    uint32_t* d_nlen = (uint32_t*)ctx_scratch(ctx, "io.fa_nlen", cap * 4);
+    if (!d_bytes || !d_off || !d_len || !d_ls || !d_size || !d_noff || !d_nlen) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cudaMemcpyAsync(d_bytes, bytes, nbytes, cudaMemcpyHostToDevice, s));
-    MDET_TRY(mdet_fasta_index_dev(ctx, d_bytes, nbytes, min_contig, capacity, d_off, d_len, nullptr, d_ls, nullptr,
-                                  nullptr, stats));
+    MDET_TRY(mdet_fasta_index_dev(ctx, d_bytes, nbytes, min_contig, capacity, d_off, d_len, d_size, d_ls, d_noff,
+                                  d_nlen, stats));
     const uint64_t n = stats->n_large;
     if (n == 0) return MDET_OK;
     uint32_t* d_counts = (uint32_t*)ctx_scratch(ctx, "io.counts", n * MDET_NTNF * 4);
@@ -469,7 +472,10 @@ int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint
     }
     if (seq_off) MDET_CUDA(ctx, cudaMemcpyAsync(seq_off, d_off, n * 8, cudaMemcpyDeviceToHost, s));
     if (seq_len) MDET_CUDA(ctx, cudaMemcpyAsync(seq_len, d_len, n * 8, cudaMemcpyDeviceToHost, s));
+    if (size) MDET_CUDA(ctx, cudaMemcpyAsync(size, d_size, n * 8, cudaMemcpyDeviceToHost, s));
     if (log_size) MDET_CUDA(ctx, cudaMemcpyAsync(log_size, d_ls, n * 8, cudaMemcpyDeviceToHost, s));
+    if (name_off) MDET_CUDA(ctx, cudaMemcpyAsync(name_off, d_noff, n * 8, cudaMemcpyDeviceToHost, s));
+    if (name_len) MDET_CUDA(ctx, cudaMemcpyAsync(name_len, d_nlen, n * 4, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(tnf, d_tnf, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     return check_flag(ctx);

@@ -162,9 +162,11 @@ SIGNATURES = [
      [P, P, P, P, u64, ctypes.POINTER(TrainParams), ctypes.POINTER(TrainReport)]),
     ("mdet_ctx_set_learned", ctypes.c_int, [P, P, ctypes.POINTER(LearnedReport)]),
     ("mdet_ctx_set_abundance", ctypes.c_int, [P, P, P, u64, u32]),
+    ("mdet_host_alloc", ctypes.c_int, [u64, ctypes.POINTER(P)]),
+    ("mdet_host_free", ctypes.c_int, [P]),
     ("mdet_fasta_index", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
     ("mdet_fasta_index_dev", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
-    ("mdet_tnf_count_fasta", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
+    ("mdet_tnf_count_fasta", ctypes.c_int, [P, P, u64, u64, u64, P, P, P, P, P, P, P, P, ctypes.POINTER(FastaStats)]),
     ("mdet_edges_sscr", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
     ("mdet_edges_sscr_dev", ctypes.c_int, [P, P, P, P, u64, D, u32, P]),
 ]
@@ -392,8 +394,9 @@ class Context:
             tnf = np.empty((cap, 136), np.float32)
             st = FastaStats()
             rc = self.lib.mdet_tnf_count_fasta(self.h, P(data.ctypes.data), data.size, int(min_contig), cap,
-                                               P(off.ctypes.data), P(ln.ctypes.data), P(ls.ctypes.data),
-                                               P(counts.ctypes.data), P(tnf.ctypes.data), ctypes.byref(st))
+                                               P(off.ctypes.data), P(ln.ctypes.data), None, P(ls.ctypes.data),
+                                               None, None, P(counts.ctypes.data), P(tnf.ctypes.data),
+                                               ctypes.byref(st))
             if rc == ERR_CAPACITY and capacity is None and st.n_large > cap:
                 cap = int(st.n_large)
                 continue

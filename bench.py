@@ -102,7 +102,12 @@ def workload_config(n, genomes, mode, ws):
 class ClockSampler:
     def __init__(self, gpu_index):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # the raw samples (MDET_CLOCKS_DIR, default the temp directory); the
+        # JSON line carries their summary
+        import tempfile
+
+        self.path = os.path.join(os.environ.get("MDET_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"mdet_clocks_{os.getpid()}.csv")
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"

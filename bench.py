@@ -93,7 +93,7 @@ def workload_config(n, genomes, mode, ws):
         "max_edges": MAX_EDGES,
         "maxP": MAXP,
         "filter": mode,
-        "exact_stage": "fp32 compensated distance + fp64 logistic model",
+        "exact_stage": "fp32 terms, float-float (~48-bit) sum, root and logistic model",
         "cache": "inputs larger than L2 (FASTA bytes ~8.5 GB per assembly)",
         "parallelism": f"{ws} independent assemblies, one per GPU" if ws > 1 else "1 GPU",
     }
@@ -157,9 +157,18 @@ def peaks():
 
 # ------------------------------------------------------------ CPU baseline --
 
-def cpu_baseline(a, tnf_host, n, target_s=8.0):
+# The cutoff the pTNF search finds on the 1M-contig workload (seed 2) with
+# srand(12345): the reference arm scores its rows at this cutoff so that both
+# arms time the same graph (ours checks that its search still finds it).
+PTNF_1M_PERMILLE = 907.8
+
+
+def cpu_baseline(a, tnf_host, n, cutoff, target_s=8.0, keep_rows=False):
     """The oracle (the reference's arithmetic restated in C++/OpenMP) on a
-    bounded sample, extrapolated to the full step."""
+    bounded sample, extrapolated to the full step: the counting of the first
+    ~200 MB of sequence, and the per-row top-k (cuda/Cuda2.cu:921-934) of the
+    first R rows against all n columns at `cutoff`.  keep_rows: also return
+    those rows' oracle top-k (for the parity check of the GPU graph)."""
     from oracle import oracle
 
     cores = os.cpu_count() or 1
@@ -173,25 +182,28 @@ def cpu_baseline(a, tnf_host, n, target_s=8.0):
     # pairwise sample: rows [0, R) against all n columns, R sized to ~target_s
     r0 = max(cores, 16)
     t = time.perf_counter()
-    oracle.graph(tnf_host, a.log_sizes, 0.95, MAX_EDGES, 0, r0, threads=cores)
+    oracle.topk_rows(tnf_host, a.log_sizes, cutoff, MAX_EDGES, 0, r0, threads=cores)
     per_row = (time.perf_counter() - t) / r0
     R = int(max(r0, min(n, target_s / max(per_row, 1e-9))))
     t = time.perf_counter()
-    oracle.graph(tnf_host, a.log_sizes, 0.95, MAX_EDGES, 0, R, threads=cores)
+    rows = oracle.topk_rows(tnf_host, a.log_sizes, cutoff, MAX_EDGES, 0, R, threads=cores)
     per_row = (time.perf_counter() - t) / R
     graph_est = per_row * n
     sample_est = per_row * (10 * min(n, 2500) if n > 25000 else n)
     total = count_est + sample_est + graph_est
-    return {
+    res = {
         "value": total,
         "unit": "s",
         "cores": cores,
         "kind": "port",
         "sample": (f"oracle counting of {k} contigs ({a.seq_len[:k].sum() / 1e6:.0f} MB) scaled by bytes; oracle "
-                   f"pairwise probability + top-{MAX_EDGES} for {R} rows x {n} columns scaled to the graph's {n} "
-                   f"rows and the search's {10 * 2500 if n > 25000 else n} rows"),
+                   f"pairwise probability + top-{MAX_EDGES} at cutoff {cutoff:.4f} for {R} rows x {n} columns "
+                   f"scaled to the graph's {n} rows and the search's {10 * 2500 if n > 25000 else n} rows"),
         "parts_s": {"count": count_est, "ptnf_search": sample_est, "graph": graph_est},
     }
+    if keep_rows:
+        return res, (R, rows)
+    return res
 
 
 # --------------------------------------------------------------- our arm --
@@ -366,7 +378,6 @@ def run_ours(args):
     ms = reduce_max(ms, dev)
 
     # ---- e2e through the host-buffer C ABI (pinned buffers, copies timed) ----
-    cnt_h = torch.empty((n, 136), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     tnf_h = torch.empty((n, 136), dtype=torch.float32, pin_memory=True).numpy()
     from_h = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
     to_h = torch.empty(cap, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
@@ -379,7 +390,8 @@ def run_ours(args):
 
     def step_e2e():
         t0 = time.perf_counter()
-        ctx.tnf_count(data_h, off_h, len_h, out=(cnt_h, tnf_h))
+        # the reference pipeline reads only the TNF rows: no counts copied back
+        ctx.tnf_count(data_h, off_h, len_h, out=(None, tnf_h))
         t1 = time.perf_counter()
         libc.srand(12345)
         p = ctx.ptnf_search(tnf_h, ls_h, MAXP / 100.0, args.mode)
@@ -411,7 +423,7 @@ def run_ours(args):
     link_gbs = nbytes / (time.perf_counter() - t_link) / 1e9
     ne = e2e_info["edges"]
     h2d = nbytes + 2 * n * 8 + 2 * (n * 136 * 4 + n * 8)
-    d2h = n * 136 * 8 + ne * 24
+    d2h = n * 136 * 4 + ne * 24
 
     result = None
     if rank == 0:
@@ -477,27 +489,220 @@ def run_ours(args):
             "filter_tile": (f"{int(st['tile_m_n']) // 1000}x{int(st['tile_m_n']) % 1000} (autotuned)"
                             if args.mode == "bf16" else "128x128 SIMT"),
         }
+        ne = int(info["edges"])
+        cut = info["ptnf"] / 1000.0
+        parity_info = {"ptnf_equals_reference_arm_cutoff": abs(info["ptnf"] - PTNF_1M_PERMILLE) < 1e-9
+                       if (n == 1_000_000 and args.genomes == 2000) else None}
+        # the host-buffer (e2e) graph equals the device-resident one
+        parity_info["e2e_graph_equals_device_graph"] = bool(
+            e2e_info["edges"] == ne
+            and torch.equal(torch.from_numpy(from_h[:ne].view(np.int64)).to(dev), d_from[:ne])
+            and torch.equal(torch.from_numpy(to_h[:ne].view(np.int64)).to(dev), d_to[:ne])
+            and torch.equal(torch.from_numpy(st_h[:ne]).to(dev), d_st[:ne]))
+        # the legs below write their graphs into a second set of buffers, so
+        # the step's graph stays in d_from/d_to/d_st for the checks
+        o_from, o_to, o_st = (torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64,
+                                                                             torch.float64))
         if not args.no_fasta:
             result["fasta_ingest"] = fasta_leg(ctx, d_bytes, nbytes, a, pinned, pk, not args.no_cpu and ws == 1)
         if not args.no_abd:
-            result["abundance"] = abundance_leg(ctx, a, d_tnf, d_ls, n, info["ptnf"] / 1000.0, d_from, d_to, d_st,
+            result["abundance"] = abundance_leg(ctx, a, d_tnf, d_ls, n, cut, o_from, o_to, o_st,
                                                 cap, args.mode, not args.no_cpu and ws == 1)
         if not args.no_plain:
             torch.cuda.synchronize()
-            ne_p, stp = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, info["ptnf"] / 1000.0, MAX_EDGES,
-                                          "plain", d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), cap)
+            ne_p, stp = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), n, cut, MAX_EDGES,
+                                          "plain", o_from.data_ptr(), o_to.data_ptr(), o_st.data_ptr(), cap)
             result["plain_fp32_graph_s"] = stp["ms_total"] / 1e3
             result["graph_speedup_vs_plain"] = stp["ms_total"] / st["ms_total"]
-            result["plain_edges_equal_count"] = int(ne_p) == int(info["edges"])
+            # the whole edge arrays, compared on the device
+            parity_info[f"{args.mode}_graph_equals_plain"] = bool(
+                int(ne_p) == ne and torch.equal(o_from[:ne], d_from[:ne]) and torch.equal(o_to[:ne], d_to[:ne])
+                and torch.equal(o_st[:ne], d_st[:ne]))
         if not args.no_cpu and ws == 1:
             tnf_host = d_tnf.cpu().numpy()
-            result["cpu_baseline"] = cpu_baseline(a, tnf_host, n)
+            base, (R, rows) = cpu_baseline(a, tnf_host, n, cut, keep_rows=True)
+            result["cpu_baseline"] = base
+            # the oracle rows the baseline just scored, against the step's graph
+            from oracle import parity
+
+            k = int(torch.searchsorted(d_from[:ne], torch.tensor([R], device=dev)).item())
+            r = parity.compare_rows(d_from[:k].cpu().numpy(), d_to[:k].cpu().numpy(), d_st[:k].cpu().numpy(),
+                                    tnf_host, a.log_sizes, cut, MAX_EDGES, 0, R, ref=rows)
+            parity_info["oracle_rows"] = {key: r[key] for key in (
+                "rows", "ref_edges", "gpu_edges", "common", "missed", "extra", "band_exempt", "n_outside_band",
+                "max_sim_diff", "recall", "precision")}
+            parity_info["oracle_rows"]["band"] = parity.BAND
+        result["parity"] = parity_info
     ctx.close()
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
     if result is not None:
         print(json.dumps(result), flush=True)
+
+
+# ------------------------------------------------------ single-stage cases --
+# `--case STAGE`: one small invocation of a single stage, the workloads the
+# ncu summaries under profiles/ were captured on (not part of the step):
+#   --case count --n 100000     K1 on ~0.85 GB of FASTA
+#   --case graph --n 300000     pairwise stage (bf16, tf32 or plain)
+#   --case learned --n 500000   network trained on a second assembly, then the learned graph
+#   --case batch --count 64     many assemblies, n ~ logU(nmin, nmax): one call per
+#                               assembly vs one batched call
+#   --case fasta --n 100000     FASTA record split of ~0.85 GB on the device
+#   --case abd --n 100000       gated graph, then sTNF -> sSCR of its edges with 10 samples
+# The graph case frees the FASTA before the pairwise call so that only the
+# stage's own buffers (~1-2 GB) are resident when it runs.
+
+def run_case(args):
+    import torch
+
+    import mdet_gb300 as m
+    from mdet_gb300 import synth
+
+    ctx = m.Context(0)
+    dev = torch.device("cuda:0")
+    if args.case == "batch":
+        return batch_case(args, m, synth, ctx, dev, torch)
+    G = args.genomes or max(10, args.n // 500)
+    a = synth.generate(3, args.n, G)
+    nb = a.data.size
+    d_bytes = torch.zeros(nb + 64, dtype=torch.uint8, device=dev)
+    d_bytes[:nb].copy_(torch.from_numpy(a.data))
+    d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+    d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+    d_cnt = torch.empty((args.n, 136), dtype=torch.int32, device=dev)
+    d_tnf = torch.empty((args.n, 136), dtype=torch.float32, device=dev)
+    if args.case == "fasta":
+        off = torch.empty(args.n, dtype=torch.int64, device=dev)
+        ln = torch.empty(args.n, dtype=torch.int64, device=dev)
+        for _ in range(args.repeat):
+            st = ctx.fasta_index_dev(d_bytes.data_ptr(), nb, 2500, args.n, off.data_ptr(), ln.data_ptr())
+        print(st)
+        torch.cuda.synchronize()
+        ctx.close()
+        return
+    reps = args.repeat if args.case == "count" else 1
+    for _ in range(reps):
+        ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), args.n, d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+    torch.cuda.synchronize()
+    if args.case == "learned":
+        import time
+
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        # training assembly: other genomes (another seed)
+        b = synth.generate(4, args.train_n, max(10, args.train_n // 500))
+        tb = torch.zeros(b.data.size + 64, dtype=torch.uint8, device=dev)
+        tb[:b.data.size].copy_(torch.from_numpy(b.data))
+        t_off = torch.from_numpy(b.seq_off.astype(np.int64)).to(dev)
+        t_len = torch.from_numpy(b.seq_len.astype(np.int64)).to(dev)
+        t_cnt = torch.empty((args.train_n, 136), dtype=torch.int32, device=dev)
+        t_tnf = torch.empty((args.train_n, 136), dtype=torch.float32, device=dev)
+        ctx.tnf_count_dev(tb.data_ptr(), b.data.size, t_off.data_ptr(), t_len.data_ptr(), args.train_n,
+                          t_cnt.data_ptr(), t_tnf.data_ptr())
+        t_ls = torch.from_numpy(b.log_sizes).to(dev)
+        torch.cuda.synchronize()
+        del tb, t_cnt
+        net = m.Network(ctx, seed=5)
+        t0 = time.time()
+        rep = net.train_dev(t_tnf.data_ptr(), t_ls.data_ptr(), args.train_n, steps=args.train_steps)
+        print({"train_s": round(time.time() - t0, 2), **rep})
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        runs = [("bf16", 0)] + [("learned", int(x)) for x in args.segs.split(",") for _ in range(2)] + [("bf16", 0)]
+        for mode, seg in runs:
+            lr = ctx.set_learned(net, segment=seg)
+            ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, mode,
+                                       out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+            extra = lr.as_dict() if mode == "learned" else {}
+            print({"mode": mode, "edges": ne, **{k: round(v, 3) if isinstance(v, float) else v
+                                                 for k, v in st.items()}, **extra})
+    if args.case == "abd":
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        abd, var = synth.abundance(a.genome, args.samples, 7)
+        ctx.set_abundance(abd, var)
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, args.mode,
+                                   out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+        sscr = torch.empty(max(ne, 1), dtype=torch.float64, device=dev)
+        for _ in range(args.repeat):
+            ctx.edges_sscr_dev(out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), ne, sscr.data_ptr())
+        print({"edges": ne, "graph_ms": st["ms_total"]})
+    if args.case == "graph":
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        for _ in range(args.repeat):
+            ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, args.mode,
+                                       out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+        print({"edges": ne, **{k: st[k] for k in ("n_candidates", "ms_filter", "ms_total")}})
+    torch.cuda.synchronize()
+    ctx.close()
+
+
+def batch_case(args, m, synth, ctx, dev, torch):
+    """Assemblies of n ~ logU(nmin, nmax) contigs, 20-800 genomes each (each
+    one's TNF counted on the GPU, its FASTA freed), then the graphs: one call
+    per assembly, and the batched call (sized run + recording, then replays)."""
+    import time
+
+    rng = np.random.default_rng(44)
+    sizes = np.exp(rng.uniform(np.log(args.nmin), np.log(args.nmax), args.count)).astype(np.int64)
+    genomes = np.clip((sizes / 400).astype(np.int64), 20, 800)
+    tnfs, lss = [], []
+    t0 = time.time()
+    for k, (n, G) in enumerate(zip(sizes, genomes)):
+        a = synth.generate(1000 + k, int(n), int(G))
+        nb = a.data.size
+        d_bytes = torch.zeros(nb + 64, dtype=torch.uint8, device=dev)
+        d_bytes[:nb].copy_(torch.from_numpy(a.data))
+        d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+        d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+        d_cnt = torch.empty((int(n), 136), dtype=torch.int32, device=dev)
+        d_tnf = torch.empty((int(n), 136), dtype=torch.float32, device=dev)
+        ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), int(n), d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+        tnfs.append(d_tnf)
+        lss.append(torch.from_numpy(a.log_sizes).to(dev))
+        del d_bytes, d_cnt
+    torch.cuda.synchronize()
+    print({"assemblies": args.count, "contigs": int(sizes.sum()), "sum_n2": float((sizes.astype(np.float64) ** 2).sum()),
+           "prep_s": round(time.time() - t0, 1)})
+    K, cut = 200, 0.9
+    outs = [[torch.empty(int(n) * K, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+            for n in sizes]
+    items = [dict(d_tnf=t.data_ptr(), d_ls=l.data_ptr(), n=int(n), cutoff=cut, max_edges=K, d_from=o[0].data_ptr(),
+                  d_to=o[1].data_ptr(), d_stnf=o[2].data_ptr(), capacity=int(n) * K)
+             for t, l, n, o in zip(tnfs, lss, sizes, outs)]
+    for rep in range(2):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        tot = cands = 0
+        for t, l, n, o in zip(tnfs, lss, sizes, outs):
+            ne, st = ctx.tnf_graph_dev(t.data_ptr(), l.data_ptr(), int(n), cut, K, "bf16", o[0].data_ptr(),
+                                       o[1].data_ptr(), o[2].data_ptr(), int(n) * K)
+            tot += ne
+            cands += st["n_candidates"]
+        torch.cuda.synchronize()
+        print({"per_assembly_calls_s": round(time.time() - t0, 4), "edges": tot, "candidates": cands})
+    for rep in range(5):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        res, st = ctx.tnf_graph_batched(items, mode="bf16")
+        torch.cuda.synchronize()
+        print({"batched_call_s": round(time.time() - t0, 4), "edges": sum(r[1] for r in res),
+               "replays": ctx.graph_replays(), "gpu_launches": st["gpu_launches"], "tile": st["tile_m_n"],
+               "candidates": st["n_candidates"]})
+    ctx.close()
+
 
 
 # --------------------------------------------------------- reference arm --
@@ -517,7 +722,7 @@ def run_reference(args):
     base = None
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
-        b = cpu_baseline(a, tnf, n, target_s=5.0)
+        b = cpu_baseline(a, tnf, n, PTNF_1M_PERMILLE / 1000.0, target_s=5.0)
         if i >= args.warmup:
             times.append(b["value"])
             base = b
@@ -544,13 +749,31 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
-    ap.add_argument("--genomes", type=int, default=2000)
+    ap.add_argument("--genomes", type=int, default=None)
     ap.add_argument("--mode", default="bf16", choices=["bf16", "plain"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-abd", action="store_true", help="skip the sTNF -> sSCR leg")
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
+    ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
+                    help="run one single-stage case instead of the benchmark (profiler workloads)")
+    ap.add_argument("--samples", type=int, default=10)
+    ap.add_argument("--count", type=int, default=64)
+    ap.add_argument("--nmin", type=int, default=5000)
+    ap.add_argument("--nmax", type=int, default=300000)
+    ap.add_argument("--train-n", type=int, default=200000)
+    ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--segs", default="1024", help="comma-separated size-sorted run lengths to try (learned case)")
+    ap.add_argument("--cutoff", type=float, default=0.95)
+    ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()
+    if args.case:
+        if args.n == 1_000_000 and "--n" not in sys.argv:
+            args.n = 100000
+        run_case(args)
+        return
+    if args.genomes is None:
+        args.genomes = 2000
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -92,7 +92,10 @@ int mdet_host_free(void* p);
  * reader builds it (newlines included, cuda/Cuda2.cu:1521-1530).  Outputs
  * counts (n*136 uint32, canonical tetranucleotide columns in TNF.bin order)
  * and tnf (n*136 float, c / sqrt(sum float(c*c))).  A contig with no valid
- * tetranucleotide gets zero counts and NaN TNF (0/0), as in the reference. */
+ * tetranucleotide gets zero counts and NaN TNF (0/0), as in the reference.
+ * mdet_tnf_count takes counts == null when the caller needs only the TNF
+ * rows (the reference pipeline reads TNF alone); the integer counts are then
+ * not copied back. */
 int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint64_t* off,
                    const uint64_t* len, uint64_t n, uint32_t* counts, float* tnf);
 int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const uint64_t* d_off,
@@ -107,12 +110,14 @@ int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, cons
  * `stream` (a cudaStream_t, 0 for the default stream) with its scratch in a
  * static device array of about 4.9 MB that every GPU loading the library
  * holds until exit.  Limits: n <= 8192 contigs and at most 65536 64-KB pieces
- * of sequence (about 4 GB); larger inputs return MDET_ERR_CAPACITY.  The
- * first call on a device resolves the array's device address there (make it
- * before any stream capture).  All calls share the one array, so calls whose
- * work overlaps on the GPU race; serialise them.  The call returns after its
- * work has finished.  Errors are status codes only (there is no context for
- * mdet_last_error). */
+ * of sequence (about 4 GB); larger inputs return MDET_ERR_CAPACITY, and a
+ * contig view outside [0, nbytes) returns MDET_ERR_INVALID, both checked
+ * on the device before any sequence byte is read.  The first call on a
+ * device resolves the array's device address there; make that first call
+ * before any stream capture begins.  All calls share the one array, so calls
+ * whose work overlaps on the GPU race; serialise them.  Every call,
+ * successful or not, synchronises `stream` before it returns.  Errors are
+ * status codes only (there is no context for mdet_last_error). */
 int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, const uint64_t* d_off, const uint64_t* d_len,
                            uint64_t n, uint32_t* d_counts, float* d_tnf, void* stream);
 

@@ -2,9 +2,10 @@
 //
 // Every pair that passed a distance filter is scored again from the FP32
 // TNF rows: the reference's terms float((a_k - b_k)^2) (cuda/Cuda2.cu:194-196)
-// summed with compensated FP32 arithmetic, sqrt in FP64, then the
-// MetaBAT2 logistic model in FP64 (cuda/Cuda2.cu:199-240) from per-contig
-// parts F(x), G(y) and the pair term H(x*y).  A pair is an edge when its
+// summed with compensated FP32 arithmetic, the square root and the MetaBAT2
+// logistic model (cuda/Cuda2.cu:199-240) in float-float arithmetic (ff.cuh,
+// about 48 significant bits) from per-contig parts F(x), G(y) and the pair
+// term H(x*y).  A pair is an edge when its
 // pre-probability beats logit(cutoff) (cuda/Cuda2.cu:257-260); its score is
 // sigmoid(pre).  Edges are then grouped per contig (both directions), each
 // contig keeps its best max_edges by (score desc, original column asc), and

@@ -35,11 +35,35 @@ struct FoldTables {
     uint8_t rc[MDET_NTNF];
 };
 
-__global__ void k_piece_counts(const uint64_t* __restrict__ len, uint64_t n, uint32_t* __restrict__ npieces) {
+// Pieces per contig, checked before anything is sized from them: a view
+// outside [0, nbytes) counts in status[1] (and gets one piece, so nothing
+// downstream grows from garbage lengths), and status[0] receives the 64-bit
+// piece total, which the host compares with its limits before the uint32 scan
+// of npieces is used.  status must be zero on entry.
+__global__ void k_piece_counts(const uint64_t* __restrict__ off, const uint64_t* __restrict__ len, uint64_t n,
+                               uint64_t nbytes, uint32_t* __restrict__ npieces,
+                               unsigned long long* __restrict__ status) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint64_t L = len[i];
-    npieces[i] = L == 0 ? 1u : (uint32_t)((L + kPiece - 1) / kPiece);
+    uint64_t np = 0, bad = 0;
+    if (i < n) {
+        const uint64_t L = len[i], o = off[i];
+        if (o > nbytes || L > nbytes - o) {
+            bad = 1;
+            np = 1;
+        } else {
+            np = L == 0 ? 1 : L / kPiece + (L % kPiece != 0);  // <= 2^48: no overflow
+        }
+        npieces[i] = (uint32_t)min(np, (uint64_t)0xFFFFFFFFu);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        np += __shfl_xor_sync(0xffffffffu, np, o);
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0 && np) {
+        atomicAdd(&status[0], (unsigned long long)np);
+        if (bad) atomicAdd(&status[1], (unsigned long long)bad);
+    }
 }
 
 __global__ void k_piece_map(const uint32_t* __restrict__ npieces, const uint32_t* __restrict__ start, uint64_t n,
@@ -251,11 +275,10 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
     ctx->prep_cache.valid = false;  // new TNF rows: no preparation carries over past a count
     if (((uintptr_t)d_bytes & 15) != 0)
         return ctx_fail(ctx, MDET_ERR_INVALID, "sequence buffer must be 16-byte aligned");
-    (void)nbytes;
     cudaStream_t s = ctx->stream;
     uint32_t* npieces = (uint32_t*)ctx_scratch(ctx, "cnt.np", n * 4);
     uint32_t* start = (uint32_t*)ctx_scratch(ctx, "cnt.start", n * 4);
-    uint32_t* work = (uint32_t*)ctx_scratch(ctx, "cnt.work", 16);
+    uint32_t* work = (uint32_t*)ctx_scratch(ctx, "cnt.work", 32);  // counter + piece total/bad views (u64 at +8)
     // per-contig accumulators for multi-piece contigs: zero when grown, and
     // every finishing warp clears its row again, so they stay zero between calls
     if (ctx->count_scratch_dirty) {
@@ -266,20 +289,25 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
     uint32_t* acc = (uint32_t*)ctx_scratch(ctx, "cnt.acc", n * MDET_NTNF * 4, true);
     uint32_t* done = (uint32_t*)ctx_scratch(ctx, "cnt.done", n * 4, true);
     if (!npieces || !start || !work || !acc || !done) return MDET_ERR_NOMEM;
+    unsigned long long* status = (unsigned long long*)(work + 2);
+    MDET_CUDA(ctx, cudaMemsetAsync(status, 0, 16, s));
     unsigned blocks = (unsigned)((n + 255) / 256);
-    k_piece_counts<<<blocks, 256, 0, s>>>(d_len, n, npieces);
+    k_piece_counts<<<blocks, 256, 0, s>>>(d_off, d_len, n, nbytes, npieces, status);
     MDET_LAUNCHED(ctx, "k_piece_counts");
     size_t tmp_bytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s);
     void* tmp = ctx_scratch(ctx, "cnt.cubtmp", tmp_bytes);
     if (!tmp) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, npieces, start, (int)n, s));
-    // exact piece total (contig views may overlap, so it is not bounded by nbytes)
-    uint32_t tail[2] = {0, 0};
-    MDET_CUDA(ctx, cudaMemcpyAsync(&tail[0], start + n - 1, 4, cudaMemcpyDeviceToHost, s));
-    MDET_CUDA(ctx, cudaMemcpyAsync(&tail[1], npieces + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    // exact piece total in 64 bits (contig views may overlap, so it is not
+    // bounded by nbytes) and the number of views outside the buffer
+    unsigned long long st[2] = {0, 0};
+    MDET_CUDA(ctx, cudaMemcpyAsync(st, status, 16, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    uint64_t max_pieces = (uint64_t)tail[0] + tail[1];
+    if (st[1]) return ctx_fail(ctx, MDET_ERR_INVALID, "%llu contig view(s) lie outside the byte buffer", st[1]);
+    if (st[0] > 0xFFFFFFFFull)
+        return ctx_fail(ctx, MDET_ERR_CAPACITY, "%llu 64-KB pieces of sequence (views overlap too much)", st[0]);
+    uint64_t max_pieces = st[0];
     uint32_t* pmap = (uint32_t*)ctx_scratch(ctx, "cnt.pmap", max_pieces * 4);
     if (!pmap) return MDET_ERR_NOMEM;
     k_piece_map<<<blocks, 256, 0, s>>>(npieces, start, n, pmap);
@@ -372,7 +400,7 @@ static int count_chunked(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, cons
                             d_tnf + c0 * MDET_NTNF);
         if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaEventRecord(counted[k], s), "cudaEventRecord");
         if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaStreamWaitEvent(ctx->io_out, counted[k], 0), "cudaStreamWaitEvent");
-        if (rc == MDET_OK && nk)
+        if (rc == MDET_OK && nk && counts)
             rc = ctx_cuda(ctx,
                           cudaMemcpyAsync(counts + c0 * MDET_NTNF, d_counts + c0 * MDET_NTNF, nk * MDET_NTNF * 4,
                                           cudaMemcpyDeviceToHost, ctx->io_out),
@@ -398,7 +426,7 @@ static int count_chunked(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, cons
 int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint64_t* off, const uint64_t* len,
                    uint64_t n, uint32_t* counts, float* tnf) {
     if (!ctx) return MDET_ERR_INVALID;
-    if (n && (!bytes || !off || !len || !counts || !tnf)) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    if (n && (!bytes || !off || !len || !tnf)) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
     MDET_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->launches = 0;
     if (n == 0) return MDET_OK;
@@ -430,7 +458,7 @@ int mdet_tnf_count(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, const uint
         ctx->count_scratch_dirty = true;
         return rc;
     }
-    MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
+    if (counts) MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(tnf, d_tnf, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     return check_flag(ctx);
 }
@@ -446,7 +474,7 @@ int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint
     memset(stats, 0, sizeof(*stats));
     if (nbytes == 0) return MDET_OK;
     if (!bytes) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
-    if (capacity && (!counts || !tnf)) return ctx_fail(ctx, MDET_ERR_INVALID, "null output pointer");
+    if (capacity && !tnf) return ctx_fail(ctx, MDET_ERR_INVALID, "null output pointer");
     cudaStream_t s = ctx->stream;
     const uint64_t padded = (nbytes + 31) & ~(uint64_t)15, cap = capacity ? capacity : 1;
     char* d_bytes = (char*)ctx_scratch(ctx, "io.bytes", padded);
@@ -476,7 +504,7 @@ int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint
     if (log_size) MDET_CUDA(ctx, cudaMemcpyAsync(log_size, d_ls, n * 8, cudaMemcpyDeviceToHost, s));
     if (name_off) MDET_CUDA(ctx, cudaMemcpyAsync(name_off, d_noff, n * 8, cudaMemcpyDeviceToHost, s));
     if (name_len) MDET_CUDA(ctx, cudaMemcpyAsync(name_len, d_nlen, n * 4, cudaMemcpyDeviceToHost, s));
-    MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
+    if (counts) MDET_CUDA(ctx, cudaMemcpyAsync(counts, d_counts, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(tnf, d_tnf, n * MDET_NTNF * 4, cudaMemcpyDeviceToHost, s));
     return check_flag(ctx);
 }
@@ -559,33 +587,43 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
     uint32_t* acc = sc + kNaAcc;
     uint32_t* work = sc + kNaWork;
     int* flag = (int*)(sc + kNaWork + 1);
+    unsigned long long* status = (unsigned long long*)(sc + kNaWork + 2);  // piece total, views outside
     void* cub_tmp = sc + kNaCub;
+    size_t tmp_bytes = 0;
+    if (cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess) {
+        cudaGetLastError();
+        return MDET_ERR_CUDA;
+    }
+    if (tmp_bytes > MDET_NOALLOC_CUB_BYTES) return MDET_ERR_CAPACITY;
+    // From the first enqueued operation on, every error return first waits
+    // for the stream, so no work of a failed call still writes the shared
+    // array (or the caller's buffers) after it returns.
+    auto fail = [&](int code) {
+        cudaGetLastError();
+        cudaStreamSynchronize(s);
+        cudaGetLastError();
+        return code;
+    };
     // the array keeps the previous call's contents: clear what must start at zero
     if (cudaMemsetAsync(done, 0, (size_t)n * 4, s) != cudaSuccess ||
         cudaMemsetAsync(acc, 0, (size_t)n * MDET_NTNF * 4, s) != cudaSuccess ||
-        cudaMemsetAsync(work, 0, 64 * 4, s) != cudaSuccess) {
-        cudaGetLastError();
-        return MDET_ERR_CUDA;
-    }
+        cudaMemsetAsync(work, 0, 64 * 4, s) != cudaSuccess)
+        return fail(MDET_ERR_CUDA);
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    k_piece_counts<<<blocks, 256, 0, s>>>(d_len, n, npieces);
-    size_t tmp_bytes = 0;
-    if (cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess ||
-        tmp_bytes > MDET_NOALLOC_CUB_BYTES)
-        return MDET_ERR_CUDA;
-    if (cub::DeviceScan::ExclusiveSum(cub_tmp, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess) {
-        cudaGetLastError();
-        return MDET_ERR_CUDA;
-    }
-    uint32_t tail[2] = {0, 0};
-    if (cudaMemcpyAsync(&tail[0], start + n - 1, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(&tail[1], npieces + n - 1, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
-        return MDET_ERR_CUDA;
-    }
-    if ((uint64_t)tail[0] + tail[1] > MDET_NOALLOC_MAX_PIECES) return MDET_ERR_CAPACITY;
+    k_piece_counts<<<blocks, 256, 0, s>>>(d_off, d_len, n, nbytes, npieces, status);
+    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
+    if (cub::DeviceScan::ExclusiveSum(cub_tmp, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess)
+        return fail(MDET_ERR_CUDA);
+    // the 64-bit piece total and the count of views outside [0, nbytes),
+    // checked before k_piece_map writes piece entries into the array
+    unsigned long long st[2] = {0, 0};
+    if (cudaMemcpyAsync(st, status, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(MDET_ERR_CUDA);
+    if (st[1]) return MDET_ERR_INVALID;
+    if (st[0] > MDET_NOALLOC_MAX_PIECES) return MDET_ERR_CAPACITY;
     k_piece_map<<<blocks, 256, 0, s>>>(npieces, start, n, pmap);
+    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
     FoldTables tabs;
     const TnTables& t = tn_tables();
     memcpy(tabs.fw, t.col_fw, MDET_NTNF);
@@ -593,12 +631,10 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
     k_count<<<d.num_sms * d.per_sm, kWarps * 32, 0, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
                                                            npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
                                                            flag);
-    if (cudaGetLastError() != cudaSuccess) return MDET_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
     int h_flag = 0;
     if (cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        cudaGetLastError();
-        return MDET_ERR_CUDA;
-    }
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return fail(MDET_ERR_CUDA);
     return h_flag ? MDET_ERR_TIMEOUT : MDET_OK;
 }

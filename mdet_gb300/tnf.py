@@ -270,7 +270,8 @@ class Context:
     # ---- TNF counting -------------------------------------------------
     def tnf_count(self, data: np.ndarray, seq_off: np.ndarray, seq_len: np.ndarray, out=None):
         """Counts (n x 136 uint32) and TNF (n x 136 float32); `out` may give
-        preallocated (e.g. pinned) output arrays."""
+        preallocated (e.g. pinned) output arrays.  out=(None, tnf): the TNF
+        rows only (the counts are not copied back; counts is returned as None)."""
         data = np.ascontiguousarray(data, dtype=np.uint8)
         off = np.ascontiguousarray(seq_off, dtype=np.uint64)
         ln = np.ascontiguousarray(seq_len, dtype=np.uint64)
@@ -280,10 +281,11 @@ class Context:
             tnf = np.zeros((n, 136), np.float32)
         else:
             counts, tnf = out
-            assert counts.dtype == np.uint32 and tnf.dtype == np.float32 and counts.size >= n * 136
-            assert tnf.size >= n * 136 and counts.flags.c_contiguous and tnf.flags.c_contiguous
-        self._check(self.lib.mdet_tnf_count(self.h, _ptr(data), data.size, _ptr(off), _ptr(ln), n, _ptr(counts),
-                                            _ptr(tnf)))
+            assert counts is None or (counts.dtype == np.uint32 and counts.size >= n * 136
+                                      and counts.flags.c_contiguous)
+            assert tnf.dtype == np.float32 and tnf.size >= n * 136 and tnf.flags.c_contiguous
+        self._check(self.lib.mdet_tnf_count(self.h, _ptr(data), data.size, _ptr(off), _ptr(ln), n,
+                                            None if counts is None else _ptr(counts), _ptr(tnf)))
         return counts, tnf
 
     def tnf_count_dev(self, d_bytes: int, nbytes: int, d_off: int, d_len: int, n: int, d_counts: int, d_tnf: int):

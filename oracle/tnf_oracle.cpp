@@ -10,9 +10,12 @@
  * Pinning: the counting half is pinned against TNF.bin files written by the
  * unmodified openmp/TNF.cpp (tests/golden/), the canonical-index table against
  * the reference's TNmap_d/BN tables (tests/golden/ref_tables.json).  The
- * probability half has no reference golden vectors (the reference ships no
- * tests); it is a line-by-line restatement of cuda/Cuda2.cu:192-241 and
- * 721-779, cross-checked against each other in tests/test_oracle.py.
+ * probability half is a line-by-line restatement of cuda/Cuda2.cu:192-241 and
+ * 721-779; it is pinned bit for bit to those two reference functions, cut out
+ * of the reference sources and compiled on the host by oracle/build_ref.py,
+ * on the fixture tests/golden/prob_golden.npz (tests/test_oracle.py).  The
+ * selection rules (per-row heap, strict '>', i<j emission) are a restatement
+ * only: the reference's gen_tnf_graph needs Boost and a GPU.
  */
 #include "tnf_oracle.h"
 

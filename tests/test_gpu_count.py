@@ -111,6 +111,13 @@ def test_host_path_chunked_equals_device(gpu_ctx):
     torch.cuda.synchronize()
     assert np.array_equal(counts, d_cnt.cpu().numpy().view(np.uint32))
     assert np.array_equal(tnf.view(np.uint32), d_tnf.cpu().numpy().view(np.uint32))
+    # TNF rows only (no counts copied back), chunked path and single-copy path
+    t_only = np.zeros_like(tnf)
+    c_none, _ = gpu_ctx.tnf_count(a.data, a.seq_off, a.seq_len, out=(None, t_only))
+    assert c_none is None and np.array_equal(t_only.view(np.uint32), tnf.view(np.uint32))
+    t_small = np.zeros((1000, 136), np.float32)
+    gpu_ctx.tnf_count(a.data, a.seq_off[:1000], a.seq_len[:1000], out=(None, t_small))
+    assert np.array_equal(t_small.view(np.uint32), tnf[:1000].view(np.uint32))
 
 
 def test_short_and_empty_contigs(gpu_ctx):
@@ -142,3 +149,34 @@ def test_device_api_alignment_check(gpu_ctx):
     with pytest.raises(MdetError):
         gpu_ctx.tnf_count_dev(buf.data_ptr() + 3, a.data.size, off.data_ptr(), ln.data_ptr(), n, cnt.data_ptr(),
                               tnf.data_ptr())
+
+
+def test_device_api_rejects_views_outside_buffer(gpu_ctx):
+    """mdet_tnf_count_dev checks every view against nbytes on the device (from
+    a 64-bit piece total) before it sizes anything from the lengths; garbage
+    lengths are an error, and the context counts correctly afterwards."""
+    torch = pytest.importorskip("torch")
+    from mdet_gb300 import MdetError
+    from mdet_gb300 import tnf as T
+
+    a = read_fasta(os.path.join(G, "count_edge.fa"))
+    n = a.seq_off.size
+    buf = torch.zeros(a.data.size + 64, dtype=torch.uint8, device="cuda")
+    buf[:a.data.size] = torch.from_numpy(a.data.copy()).cuda()
+    cnt = torch.zeros((n, 136), dtype=torch.int32, device="cuda")
+    tnf = torch.zeros((n, 136), dtype=torch.float32, device="cuda")
+    for bad_len in (a.data.size + 1, 1 << 40, -3):
+        ln_h = a.seq_len.astype(np.int64)
+        ln_h[n // 2] = bad_len
+        off = torch.from_numpy(a.seq_off.astype(np.int64)).cuda()
+        ln = torch.from_numpy(ln_h).cuda()
+        with pytest.raises(MdetError) as e:
+            gpu_ctx.tnf_count_dev(buf.data_ptr(), a.data.size, off.data_ptr(), ln.data_ptr(), n, cnt.data_ptr(),
+                                  tnf.data_ptr())
+        assert e.value.code == T.ERR_INVALID
+    off = torch.from_numpy(a.seq_off.astype(np.int64)).cuda()
+    ln = torch.from_numpy(a.seq_len.astype(np.int64)).cuda()
+    gpu_ctx.tnf_count_dev(buf.data_ptr(), a.data.size, off.data_ptr(), ln.data_ptr(), n, cnt.data_ptr(),
+                          tnf.data_ptr())
+    oc, _ = oracle.tnf_count(a.data, a.seq_off, a.seq_len)
+    assert np.array_equal(cnt.cpu().numpy().view(np.uint32), oc)

@@ -74,3 +74,51 @@ def test_noalloc_rejects_oversized_input():
     rc = lib.mdet_tnf_count_noalloc(x.data_ptr() + 1, 16, x.data_ptr(), x.data_ptr(), 1, x.data_ptr(), x.data_ptr(),
                                     None)
     assert rc == T.ERR_INVALID
+
+
+def test_noalloc_rejects_bad_views_and_piece_overflow():
+    """Views outside the byte buffer (a garbage or huge length included) and
+    a piece total above the array's limit are rejected from the device-side
+    64-bit check, before any piece entry is written into the shared array;
+    a valid call afterwards still matches the regular entry point."""
+    torch = pytest.importorskip("torch")
+    import mdet_gb300 as m
+    from mdet_gb300 import synth
+    from mdet_gb300 import tnf as T
+
+    lib = T.load_library()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream().cuda_stream
+    nb = 1 << 20
+    buf = torch.full((nb + 64,), ord("A"), dtype=torch.uint8, device=dev)
+    out_c = torch.zeros((8192, 136), dtype=torch.int32, device=dev)
+    out_t = torch.zeros((8192, 136), dtype=torch.float32, device=dev)
+
+    def call(off, ln, nbytes=nb):
+        o = torch.tensor(off, dtype=torch.int64, device=dev)
+        ln_ = torch.tensor(ln, dtype=torch.int64, device=dev)
+        return lib.mdet_tnf_count_noalloc(buf.data_ptr(), nbytes, o.data_ptr(), ln_.data_ptr(), len(off),
+                                          out_c.data_ptr(), out_t.data_ptr(), stream)
+
+    # 8192 views of the whole 1 MB buffer: 16 pieces each, 131,072 > 65,536
+    assert call([0] * 8192, [nb] * 8192) == T.ERR_CAPACITY
+    # a view that runs past the buffer, one with a huge length, one starting past it
+    assert call([0, 10], [100, nb]) == T.ERR_INVALID
+    assert call([0], [1 << 40]) == T.ERR_INVALID
+    assert call([nb + 1], [0]) == T.ERR_INVALID
+    # lengths that would wrap a 32-bit piece count
+    assert call([0, 0, 0], [nb, -3, 2]) == T.ERR_INVALID  # -3: 2^64 - 3 as uint64
+    # the shared array is still usable
+    a = synth.generate(seed=73, n=500, genomes=5, max_len=200000, threads=8)
+    n = a.seq_off.size
+    b2, off, ln = _device_inputs(torch, a)
+    c0 = torch.zeros((n, 136), dtype=torch.int32, device=dev)
+    t0 = torch.zeros((n, 136), dtype=torch.float32, device=dev)
+    with m.Context(0) as ctx:
+        ctx.tnf_count_dev(b2.data_ptr(), a.data.size, off.data_ptr(), ln.data_ptr(), n, c0.data_ptr(), t0.data_ptr())
+    rc = lib.mdet_tnf_count_noalloc(b2.data_ptr(), a.data.size, off.data_ptr(), ln.data_ptr(), n, out_c.data_ptr(),
+                                    out_t.data_ptr(), stream)
+    assert rc == T.OK
+    torch.cuda.synchronize()
+    assert torch.equal(c0, out_c[:n])
+    assert torch.equal(t0.view(torch.int32), out_t[:n].view(torch.int32))

@@ -12,11 +12,16 @@
 // one contig; each warp takes pieces from a global counter, and each lane
 // walks a contiguous 1/32 of the piece with its own rolling state
 // (16-byte loads, the next one in flight), warmed up on the bytes just
-// before its run, so no lane depends on another while it counts.  Windows go
+// before its run, so no lane depends on another while it counts.  The
+// 16-byte chunks at the two ends of a lane's run are clipped by turning the
+// bytes outside the run into newlines (no state change, nothing counted), so
+// every chunk goes through the same branch-free 16-byte step.  Windows go
 // into the warp's 256-bin shared histogram of raw 8-bit codes, folded onto
 // the 136 canonical columns per piece.  A contig cut into several pieces
 // accumulates into a per-contig scratch row and the last piece to finish
-// normalises it (and clears the scratch row).
+// normalises it (and clears the scratch row).  Normalisation runs in FP32
+// (float-float square root and reciprocal of the exact integer square sum):
+// no FP64 on the counting path.
 #include <cub/cub.cuh>
 
 #include <mutex>
@@ -80,7 +85,26 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
     return v;
 }
 
-// Writes one finished contig row from per-lane canonical counts.
+// 1/sqrt(s) of an exact integer s < 2^53 as a float-float pair ih + il
+// (about 46 significant bits) from FP32 arithmetic alone: one Newton step on
+// the square root from sqrtf of its leading float, then one on the
+// reciprocal, with the residuals formed exactly by FMA.
+__device__ __forceinline__ void inv_sqrt_ff(uint64_t s, float& ih, float& il) {
+    const float sh = __ull2float_rn(s);
+    const float sl = (float)(long long)(s - (unsigned long long)sh);  // s - sh, exact to ~2^-24 of itself
+    const float r0 = __fsqrt_rn(sh);
+    const float ph = __fmul_rn(r0, r0), pl = __fmaf_rn(r0, r0, -ph);
+    const float res = __fadd_rn(__fadd_rn(__fsub_rn(sh, ph), -pl), sl);  // s - r0^2
+    const float r1 = __fdiv_rn(res, __fmul_rn(2.0f, r0));              // r = r0 + r1
+    const float q0 = __fdiv_rn(1.0f, r0);
+    const float e = __fsub_rn(__fmaf_rn(-r0, q0, 1.0f), __fmul_rn(r1, q0));  // 1 - r q0
+    ih = q0;
+    il = __fmul_rn(q0, e);
+}
+
+// Writes one finished contig row from per-lane canonical counts: counts, then
+// float(c / sqrt(sum float(c*c))).  The square sum is exact (integers
+// < 2^53); c * (ih + il) is formed in float-float and rounded once to float.
 __device__ __forceinline__ void finish_row(uint32_t lane, const uint32_t (&v)[5], uint64_t c,
                                            uint32_t* __restrict__ counts, float* __restrict__ tnf) {
     uint64_t s = 0;
@@ -94,14 +118,17 @@ __device__ __forceinline__ void finish_row(uint32_t lane, const uint32_t (&v)[5]
         }
     }
     s = warp_sum_u64(s);
-    double rsum = sqrt((double)s);
-    double inv = 1.0 / rsum;
+    float ih = 0.f, il = 0.f;
+    if (s) inv_sqrt_ff(s, ih, il);
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
         uint32_t col = lane + 32 * j;
         if (col < MDET_NTNF) {
+            const float f = (float)v[j];
+            const float p = __fmul_rn(f, ih);
+            const float e = __fmaf_rn(f, il, __fmaf_rn(f, ih, -p));
             counts[c * MDET_NTNF + col] = v[j];
-            tnf[c * MDET_NTNF + col] = s ? (float)((double)v[j] * inv) : __int_as_float(0x7fffffff);
+            tnf[c * MDET_NTNF + col] = s ? __fadd_rn(p, e) : __int_as_float(0x7fffffff);
         }
     }
 }
@@ -122,16 +149,33 @@ __device__ __forceinline__ uint32_t byte_of(const uint4& v, int b) {
     return __byte_perm(w, 0u, 0x4440u | (uint32_t)(b & 3));
 }
 
+// Bytes of the 16-byte chunk at q that lie outside [a, b) become '\n': a
+// newline leaves the rolling state alone and counts nowhere, so a run starts
+// from its warm-up state at a and stops counting at b.
+__device__ __forceinline__ void clip_chunk(uint4& v, uint64_t q, uint64_t a, uint64_t b) {
+    const uint32_t lo = q < a ? (uint32_t)(a - q) : 0u;
+    const uint32_t hi = q >= b ? 0u : (q + 16 <= b ? 16u : (uint32_t)(b - q));
+    const uint32_t keep = hi > lo ? (((1u << hi) - 1u) & ~((1u << lo) - 1u)) : 0u;
+    uint32_t* w = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t bits = (keep >> (4 * j)) & 0xFu;
+        const uint32_t bm = ((bits * 0x00204081u) & 0x01010101u) * 0xFFu;  // 4 bits -> 4 byte masks
+        w[j] = (w[j] & bm) | (0x0A0A0A0Au & ~bm);
+    }
+}
+
 // Warp per piece (<= 64 KB of one contig, taken from a global counter);
-// lane l walks its 1/32 of the piece in order with its own rolling state, warmed up on the bytes just before its run, and counts
-// each window that ends in its run into the warp's shared histogram of raw
-// 8-bit codes.  No lane waits on another until the piece is folded.
+// lane l walks its 1/32 of the piece in order with its own rolling state,
+// warmed up on the bytes just before its run, and counts each window that
+// ends in its run into the warp's shared histogram of raw 8-bit codes.  No
+// lane waits on another until the piece is folded.
 __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __restrict__ bytes,
                                                       const uint64_t* __restrict__ off,
                                                       const uint64_t* __restrict__ len, uint64_t n,
                                                       const uint32_t* __restrict__ piece_start,
                                                       const uint32_t* __restrict__ npieces,
-                                                      const uint32_t* __restrict__ piece_contig,
+                                                      const uint32_t* __restrict__ piece_contig, uint32_t total,
                                                       uint32_t* __restrict__ work, uint32_t* __restrict__ acc,
                                                       uint32_t* __restrict__ done, uint32_t* __restrict__ counts,
                                                       float* __restrict__ tnf, FoldTables tabs, int* flag) {
@@ -146,7 +190,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
         lut[c] = (uint16_t)(c == '\n' ? 0x8000u : (((c >> 1) & 3u) | (valid ? 0u : 0x300u)));
     }
     __syncthreads();
-    const uint32_t total = piece_start[n - 1] + npieces[n - 1];
 
     while (true) {
         // the next piece (lane 0) and the abort flag (lane 1) load side by side
@@ -198,28 +241,21 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
                 }
                 for (uint64_t q = ws; q < seg0; ++q) x = roll(x, lut[bytes[q]], t);
             }
-            // counting pass over aligned 16-byte chunks, the next one in flight
+            // counting pass over aligned 16-byte chunks, the next one in
+            // flight; chunks at the ends of the run are clipped to it
             const uint64_t a0 = seg0 & ~(uint64_t)15;
-            uint4 nxt = __ldg(reinterpret_cast<const uint4*>(bytes + a0));
-            for (uint64_t a = a0; a < seg1; a += 16) {
-                const uint4 v = nxt;
-                if (a + 16 < seg1) nxt = __ldg(reinterpret_cast<const uint4*>(bytes + a + 16));
-                if (a >= seg0 && a + 16 <= seg1) {
+            const uint32_t nch = (uint32_t)((seg1 - a0 + 15) >> 4);
+            const unsigned char* ptr = bytes + a0;
+            uint4 nxt = __ldg(reinterpret_cast<const uint4*>(ptr));
+            for (uint32_t i = 0; i < nch; ++i) {
+                uint4 v = nxt;
+                if (i + 1 < nch) nxt = __ldg(reinterpret_cast<const uint4*>(ptr + 16 * (i + 1)));
+                const uint64_t q = a0 + 16ull * i;
+                if (q < seg0 || q + 16 > seg1) clip_chunk(v, q, seg0, seg1);
 #pragma unroll
-                    for (int b = 0; b < 16; ++b) {
-                        x = roll(x, lut[byte_of(v, b)], t);
-                        atomicAdd(&hist[min(t, 256u)], 1u);  // bin 256 takes the windows not counted
-                    }
-                } else {
-                    const uint32_t lo = a < seg0 ? (uint32_t)(seg0 - a) : 0u;
-                    const uint32_t hi = seg1 - a < 16 ? (uint32_t)(seg1 - a) : 16u;
-#pragma unroll
-                    for (int b = 0; b < 16; ++b) {
-                        if ((uint32_t)b >= lo && (uint32_t)b < hi) {
-                            x = roll(x, lut[byte_of(v, b)], t);
-                            if (t < 256u) atomicAdd(&hist[t], 1u);
-                        }
-                    }
+                for (int b = 0; b < 16; ++b) {
+                    x = roll(x, lut[byte_of(v, b)], t);
+                    atomicAdd(&hist[min(t, 256u)], 1u);  // bin 256 takes the windows not counted
                 }
             }
         }
@@ -268,6 +304,57 @@ __global__ void __launch_bounds__(kWarps * 32) k_count(const unsigned char* __re
 
 }  // namespace
 
+// Device scratch of one count.
+struct CountScratch {
+    uint32_t *npieces, *start, *pmap, *work, *acc, *done;
+    unsigned long long* status;  // [0] piece total, [1] views outside the buffer
+    void* cub_tmp;
+    size_t cub_bytes;
+};
+
+static size_t count_cub_bytes(uint64_t n, cudaStream_t s) {
+    size_t a = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, a, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, s);
+    return a;
+}
+
+// Phase 1 of a count: pieces per contig and the view check (status), piece
+// starts; the caller reads status back and checks it before phase 2.
+static cudaError_t count_phase1(const CountScratch& S, const uint64_t* d_off, const uint64_t* d_len, uint64_t n,
+                                uint64_t nbytes, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(S.status, 0, 16, s);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_piece_counts<<<blocks, 256, 0, s>>>(d_off, d_len, n, nbytes, S.npieces, S.status);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    size_t tb = S.cub_bytes;
+    return cub::DeviceScan::ExclusiveSum(S.cub_tmp, tb, S.npieces, S.start, (int)n, s);
+}
+
+// Phase 2: piece map and the counting kernel.
+static cudaError_t count_phase2(const CountScratch& S, const unsigned char* d_bytes, const uint64_t* d_off,
+                                const uint64_t* d_len, uint64_t n, uint32_t total, uint32_t* d_counts, float* d_tnf,
+                                int* flag, int grid, cudaStream_t s) {
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_piece_map<<<blocks, 256, 0, s>>>(S.npieces, S.start, n, S.pmap);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(S.work, 0, 4, s)) != cudaSuccess) return e;
+    FoldTables tabs;
+    const TnTables& t = tn_tables();
+    memcpy(tabs.fw, t.col_fw, MDET_NTNF);
+    memcpy(tabs.rc, t.col_rc, MDET_NTNF);
+    k_count<<<grid, kWarps * 32, 0, s>>>(d_bytes, d_off, d_len, n, S.start, S.npieces, S.pmap, total, S.work, S.acc,
+                                         S.done, d_counts, d_tnf, tabs, flag);
+    return cudaGetLastError();
+}
+
+static int k_count_grid(int num_sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_count, kWarps * 32, 0);
+    return num_sms * (per_sm < 1 ? 1 : per_sm);
+}
+
 static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const uint64_t* d_off,
                       const uint64_t* d_len, uint64_t n, uint32_t* d_counts, float* d_tnf) {
     if (n == 0) return MDET_OK;
@@ -276,9 +363,10 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
     if (((uintptr_t)d_bytes & 15) != 0)
         return ctx_fail(ctx, MDET_ERR_INVALID, "sequence buffer must be 16-byte aligned");
     cudaStream_t s = ctx->stream;
-    uint32_t* npieces = (uint32_t*)ctx_scratch(ctx, "cnt.np", n * 4);
-    uint32_t* start = (uint32_t*)ctx_scratch(ctx, "cnt.start", n * 4);
-    uint32_t* work = (uint32_t*)ctx_scratch(ctx, "cnt.work", 32);  // counter + piece total/bad views (u64 at +8)
+    CountScratch S{};
+    S.npieces = (uint32_t*)ctx_scratch(ctx, "cnt.np", n * 4);
+    S.start = (uint32_t*)ctx_scratch(ctx, "cnt.start", n * 4);
+    S.work = (uint32_t*)ctx_scratch(ctx, "cnt.work", 32);  // piece counter; status (2 x u64) at +8
     // per-contig accumulators for multi-piece contigs: zero when grown, and
     // every finishing warp clears its row again, so they stay zero between calls
     if (ctx->count_scratch_dirty) {
@@ -286,44 +374,28 @@ static int count_impl(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, const
         ctx->bufs.erase("cnt.done");
         ctx->count_scratch_dirty = false;
     }
-    uint32_t* acc = (uint32_t*)ctx_scratch(ctx, "cnt.acc", n * MDET_NTNF * 4, true);
-    uint32_t* done = (uint32_t*)ctx_scratch(ctx, "cnt.done", n * 4, true);
-    if (!npieces || !start || !work || !acc || !done) return MDET_ERR_NOMEM;
-    unsigned long long* status = (unsigned long long*)(work + 2);
-    MDET_CUDA(ctx, cudaMemsetAsync(status, 0, 16, s));
-    unsigned blocks = (unsigned)((n + 255) / 256);
-    k_piece_counts<<<blocks, 256, 0, s>>>(d_off, d_len, n, nbytes, npieces, status);
+    S.acc = (uint32_t*)ctx_scratch(ctx, "cnt.acc", n * MDET_NTNF * 4, true);
+    S.done = (uint32_t*)ctx_scratch(ctx, "cnt.done", n * 4, true);
+    if (!S.npieces || !S.start || !S.work || !S.acc || !S.done) return MDET_ERR_NOMEM;
+    S.status = (unsigned long long*)(S.work + 2);
+    S.cub_bytes = count_cub_bytes(n, s);
+    S.cub_tmp = ctx_scratch(ctx, "cnt.cubtmp", S.cub_bytes);
+    if (!S.cub_tmp) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, count_phase1(S, d_off, d_len, n, nbytes, s));
     MDET_LAUNCHED(ctx, "k_piece_counts");
-    size_t tmp_bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s);
-    void* tmp = ctx_scratch(ctx, "cnt.cubtmp", tmp_bytes);
-    if (!tmp) return MDET_ERR_NOMEM;
-    MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, npieces, start, (int)n, s));
     // exact piece total in 64 bits (contig views may overlap, so it is not
     // bounded by nbytes) and the number of views outside the buffer
     unsigned long long st[2] = {0, 0};
-    MDET_CUDA(ctx, cudaMemcpyAsync(st, status, 16, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(st, S.status, 16, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
     if (st[1]) return ctx_fail(ctx, MDET_ERR_INVALID, "%llu contig view(s) lie outside the byte buffer", st[1]);
     if (st[0] > 0xFFFFFFFFull)
         return ctx_fail(ctx, MDET_ERR_CAPACITY, "%llu 64-KB pieces of sequence (views overlap too much)", st[0]);
-    uint64_t max_pieces = st[0];
-    uint32_t* pmap = (uint32_t*)ctx_scratch(ctx, "cnt.pmap", max_pieces * 4);
-    if (!pmap) return MDET_ERR_NOMEM;
-    k_piece_map<<<blocks, 256, 0, s>>>(npieces, start, n, pmap);
-    MDET_LAUNCHED(ctx, "k_piece_map");
-    MDET_CUDA(ctx, cudaMemsetAsync(work, 0, 4, s));
-    FoldTables tabs;
-    const TnTables& t = tn_tables();
-    memcpy(tabs.fw, t.col_fw, MDET_NTNF);
-    memcpy(tabs.rc, t.col_rc, MDET_NTNF);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_count, kWarps * 32, 0);
-    if (per_sm < 1) per_sm = 1;
+    S.pmap = (uint32_t*)ctx_scratch(ctx, "cnt.pmap", (size_t)st[0] * 4);
+    if (!S.pmap) return MDET_ERR_NOMEM;
     ctx_timer_begin(ctx, "k_count");
-    k_count<<<ctx->num_sms * per_sm, kWarps * 32, 0, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
-                                                            npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
-                                                            ctx->d_flag);
+    MDET_CUDA(ctx, count_phase2(S, (const unsigned char*)d_bytes, d_off, d_len, n, (uint32_t)st[0], d_counts, d_tnf,
+                                ctx->d_flag, k_count_grid(ctx->num_sms), s));
     ctx_timer_end(ctx, "k_count");
     MDET_LAUNCHED(ctx, "k_count");
     return MDET_OK;
@@ -521,7 +593,7 @@ int mdet_tnf_count_fasta(mdet_ctx* ctx, const char* bytes, uint64_t nbytes, uint
 // loaded with the library and held by every GPU that loads it until exit.
 
 #define MDET_NOALLOC_MAX_CONTIGS 8192u
-#define MDET_NOALLOC_MAX_PIECES 65536u
+#define MDET_NOALLOC_MAX_PIECES 65536u  // 64-KB pieces: about 4 GB of sequence
 #define MDET_NOALLOC_CUB_BYTES (64u * 1024u)
 
 namespace {
@@ -531,7 +603,7 @@ constexpr uint32_t kNaStart = kNaNp + MDET_NOALLOC_MAX_CONTIGS;         // piece
 constexpr uint32_t kNaDone = kNaStart + MDET_NOALLOC_MAX_CONTIGS;       // finished pieces per contig
 constexpr uint32_t kNaMap = kNaDone + MDET_NOALLOC_MAX_CONTIGS;         // piece -> contig
 constexpr uint32_t kNaAcc = kNaMap + MDET_NOALLOC_MAX_PIECES;           // multi-piece accumulators
-constexpr uint32_t kNaWork = kNaAcc + MDET_NOALLOC_MAX_CONTIGS * MDET_NTNF;  // work counter + flag (64 words)
+constexpr uint32_t kNaWork = kNaAcc + MDET_NOALLOC_MAX_CONTIGS * MDET_NTNF;  // counter, flag, status (64 words)
 constexpr uint32_t kNaCub = kNaWork + 64;                               // CUB scan temp storage
 constexpr uint32_t kNaWords = kNaCub + MDET_NOALLOC_CUB_BYTES / 4;      // ~4.9 MB in total
 }  // namespace
@@ -541,8 +613,7 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
 namespace {
 struct NoallocDevice {
     uint32_t* scratch = nullptr;  // device address of g_noalloc_scratch
-    int num_sms = 0;
-    int per_sm = 0;
+    int grid = 0;                 // k_count grid on this device
 };
 NoallocDevice g_na_dev[64];
 std::mutex g_na_mutex;
@@ -569,32 +640,29 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
                 cudaGetLastError();
                 return MDET_ERR_CUDA;
             }
-            if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.per_sm, k_count, kWarps * 32, 0) != cudaSuccess) {
+            int num_sms = 0;
+            if (cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
                 cudaGetLastError();
                 return MDET_ERR_CUDA;
             }
-            if (d.per_sm < 1) d.per_sm = 1;
+            d.grid = k_count_grid(num_sms);
             d.scratch = (uint32_t*)p;
         }
     }
     const NoallocDevice& d = g_na_dev[dev];
     uint32_t* sc = d.scratch;
-    uint32_t* npieces = sc + kNaNp;
-    uint32_t* start = sc + kNaStart;
-    uint32_t* done = sc + kNaDone;
-    uint32_t* pmap = sc + kNaMap;
-    uint32_t* acc = sc + kNaAcc;
-    uint32_t* work = sc + kNaWork;
+    CountScratch S{};
+    S.npieces = sc + kNaNp;
+    S.start = sc + kNaStart;
+    S.done = sc + kNaDone;
+    S.pmap = sc + kNaMap;
+    S.acc = sc + kNaAcc;
+    S.work = sc + kNaWork;
     int* flag = (int*)(sc + kNaWork + 1);
-    unsigned long long* status = (unsigned long long*)(sc + kNaWork + 2);  // piece total, views outside
-    void* cub_tmp = sc + kNaCub;
-    size_t tmp_bytes = 0;
-    if (cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess) {
-        cudaGetLastError();
-        return MDET_ERR_CUDA;
-    }
-    if (tmp_bytes > MDET_NOALLOC_CUB_BYTES) return MDET_ERR_CAPACITY;
+    S.status = (unsigned long long*)(sc + kNaWork + 2);
+    S.cub_tmp = sc + kNaCub;
+    S.cub_bytes = count_cub_bytes(n, s);
+    if (S.cub_bytes > MDET_NOALLOC_CUB_BYTES) return MDET_ERR_CAPACITY;
     // From the first enqueued operation on, every error return first waits
     // for the stream, so no work of a failed call still writes the shared
     // array (or the caller's buffers) after it returns.
@@ -605,33 +673,22 @@ extern "C" int mdet_tnf_count_noalloc(const char* d_bytes, uint64_t nbytes, cons
         return code;
     };
     // the array keeps the previous call's contents: clear what must start at zero
-    if (cudaMemsetAsync(done, 0, (size_t)n * 4, s) != cudaSuccess ||
-        cudaMemsetAsync(acc, 0, (size_t)n * MDET_NTNF * 4, s) != cudaSuccess ||
-        cudaMemsetAsync(work, 0, 64 * 4, s) != cudaSuccess)
+    if (cudaMemsetAsync(S.done, 0, (size_t)n * 4, s) != cudaSuccess ||
+        cudaMemsetAsync(S.acc, 0, (size_t)n * MDET_NTNF * 4, s) != cudaSuccess ||
+        cudaMemsetAsync(S.work, 0, 64 * 4, s) != cudaSuccess)
         return fail(MDET_ERR_CUDA);
-    const unsigned blocks = (unsigned)((n + 255) / 256);
-    k_piece_counts<<<blocks, 256, 0, s>>>(d_off, d_len, n, nbytes, npieces, status);
-    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
-    if (cub::DeviceScan::ExclusiveSum(cub_tmp, tmp_bytes, npieces, start, (int)n, s) != cudaSuccess)
-        return fail(MDET_ERR_CUDA);
+    if (count_phase1(S, d_off, d_len, n, nbytes, s) != cudaSuccess) return fail(MDET_ERR_CUDA);
     // the 64-bit piece total and the count of views outside [0, nbytes),
     // checked before k_piece_map writes piece entries into the array
     unsigned long long st[2] = {0, 0};
-    if (cudaMemcpyAsync(st, status, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    if (cudaMemcpyAsync(st, S.status, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return fail(MDET_ERR_CUDA);
     if (st[1]) return MDET_ERR_INVALID;
     if (st[0] > MDET_NOALLOC_MAX_PIECES) return MDET_ERR_CAPACITY;
-    k_piece_map<<<blocks, 256, 0, s>>>(npieces, start, n, pmap);
-    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
-    FoldTables tabs;
-    const TnTables& t = tn_tables();
-    memcpy(tabs.fw, t.col_fw, MDET_NTNF);
-    memcpy(tabs.rc, t.col_rc, MDET_NTNF);
-    k_count<<<d.num_sms * d.per_sm, kWarps * 32, 0, s>>>((const unsigned char*)d_bytes, d_off, d_len, n, start,
-                                                           npieces, pmap, work, acc, done, d_counts, d_tnf, tabs,
-                                                           flag);
-    if (cudaGetLastError() != cudaSuccess) return fail(MDET_ERR_CUDA);
+    if (count_phase2(S, (const unsigned char*)d_bytes, d_off, d_len, n, (uint32_t)st[0], d_counts, d_tnf, flag,
+                     d.grid, s) != cudaSuccess)
+        return fail(MDET_ERR_CUDA);
     int h_flag = 0;
     if (cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

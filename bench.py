@@ -258,6 +258,41 @@ def abundance_leg(ctx, a, d_tnf, d_ls, n, cutoff, d_from, d_to, d_st, cap, mode,
     return leg
 
 
+def tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st_bf16, pk, pk_kind):
+    """The graph of the step's cutoff with the TF32 tcgen05 filter (128 x 128
+    tiles, 18 MMAs of K = 8 per tile): 1 untimed and 2 timed calls, the
+    filter timed with CUDA events on the context's stream, the edge arrays
+    compared with the BF16 graph's on the device.  The roofline peak is half
+    the measured sustained BF16 rate (tcgen05 runs TF32 at half the BF16 rate;
+    the pool measures no TF32 figure)."""
+    import torch
+
+    args = (d_tnf.data_ptr(), d_ls.data_ptr(), n, cut, MAX_EDGES, "tf32", o_from.data_ptr(), o_to.data_ptr(),
+            o_st.data_ptr(), cap)
+    ctx.tnf_graph_dev(*args)
+    ctx.set_timing(True)
+    ms = []
+    for _ in range(2):
+        ne_t, st = ctx.tnf_graph_dev(*args)
+        ms.append(st["ms_total"])
+    fms, fl = ctx.kernel_ms("k_filter_tc")
+    ctx.set_timing(False)
+    flops = 2 * 136 * n * (n - 1) / 2
+    achieved = flops / (fms / fl / 1e3) / 1e12
+    peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops")) / 2
+    same = bool(int(ne_t) == ne and torch.equal(o_from[:ne], d_from[:ne]) and torch.equal(o_to[:ne], d_to[:ne])
+                and torch.equal(o_st[:ne], d_st[:ne]))
+    return {"metric": "TNF graph time, TF32 tcgen05 filter", "value": float(np.median(ms)) / 1e3, "unit": "s",
+            "graph_equals_bf16": same, "edges": int(ne_t), "candidates": int(st["n_candidates"]),
+            "candidates_per_above_cutoff": st["n_candidates"] / max(1, st["n_above_cutoff"]),
+            "bf16_candidates_per_above_cutoff": st_bf16["n_candidates"] / max(1, st_bf16["n_above_cutoff"]),
+            "phases_ms": {"filter": st["ms_filter"], "exact": st["ms_exact"], "select": st["ms_select"]},
+            "roofline": {"kernel": "k_filter_tc<128,128,2,4>", "bound": "tensor", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": f"half the bf16 sustained rate ({pk_kind})"},
+            "exact_stage": "shared with the BF16 and plain forms: same error statement (tests/test_gpu_error.py)"}
+
+
 def fasta_leg(ctx, d_bytes, nbytes, a, pinned, pk, run_cpu):
     """FASTA ingest on the device (mdet_fasta_index_dev) over the step's file
     bytes in HBM (8.6 GB, far larger than L2): 1 untimed and 3 timed calls;
@@ -518,6 +553,9 @@ def run_ours(args):
             parity_info[f"{args.mode}_graph_equals_plain"] = bool(
                 int(ne_p) == ne and torch.equal(o_from[:ne], d_from[:ne]) and torch.equal(o_to[:ne], d_to[:ne])
                 and torch.equal(o_st[:ne], d_st[:ne]))
+        if not args.no_tf32 and args.mode == "bf16":
+            result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,
+                                      pk, pk_kind)
         if not args.no_cpu and ws == 1:
             tnf_host = d_tnf.cpu().numpy()
             base, (R, rows) = cpu_baseline(a, tnf_host, n, cut, keep_rows=True)
@@ -750,11 +788,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000)
     ap.add_argument("--genomes", type=int, default=None)
-    ap.add_argument("--mode", default="bf16", choices=["bf16", "plain"])
+    ap.add_argument("--mode", default="bf16", choices=["bf16", "plain", "tf32"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-abd", action="store_true", help="skip the sTNF -> sSCR leg")
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
+    ap.add_argument("--no-tf32", action="store_true", help="skip the TF32 graph leg")
     ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
                     help="run one single-stage case instead of the benchmark (profiler workloads)")
     ap.add_argument("--samples", type=int, default=10)

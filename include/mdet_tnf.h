@@ -34,7 +34,8 @@ extern "C" {
 /* distance-filter forms of the pairwise stage */
 #define MDET_MODE_PLAIN 0   /* FP32 SIMT all-pairs distance in the reference's element order */
 #define MDET_MODE_BF16 1    /* tcgen05 BF16 tile GEMM, FP32 accumulation in TMEM */
-#define MDET_MODE_TF32 2    /* tcgen05 TF32 tile GEMM, FP32 accumulation in TMEM */
+#define MDET_MODE_TF32 2    /* tcgen05 TF32 tile GEMM (128 x 128 tiles), FP32 accumulation in TMEM; the
+                             * max-probability sample passes use the BF16 filter (same maxima) */
 #define MDET_MODE_LEARNED 3 /* learned embedding proposal + BF16 tiles (see mdet_tnf_learned_*) */
 
 typedef struct mdet_ctx mdet_ctx;

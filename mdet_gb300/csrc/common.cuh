@@ -80,10 +80,11 @@ struct mdet_ctx {
         const void* tnf = nullptr;
         const void* ls = nullptr;
         uint64_t n = 0;
-        bool bf16 = false;
+        int tck = 0;  // reduced-precision rows made (0 none, 1 BF16, 2 TF32)
         unsigned long long hash = 0;
         const void* x32 = nullptr;
         const void* xa = nullptr;
+        const void* ta = nullptr;
         uint64_t gen = 0;  // scratch_gen when it was made (no buffer moved since)
     } prep_cache;
     // copy streams of the host-buffer entry points (created on first use)

@@ -200,6 +200,9 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
     cudaStream_t s = ctx->stream;
     if (bside && (mode == MDET_MODE_PLAIN || fixed_cap || tiles))
         return ctx_fail(ctx, MDET_ERR_INVALID, "a B-role subset needs a tensor-core form without a tile list");
+    const bool tf32 = mode == MDET_MODE_TF32;
+    if (tf32 && (rect || bside || g.tck != kTcTf32))
+        return ctx_fail(ctx, MDET_ERR_INVALID, "the TF32 filter runs over a TF32 preparation, all pairs");
     unsigned long long* cnt = (unsigned long long*)ctx_scratch(ctx, "flt.cnt", 8);
     if (!cnt) return MDET_ERR_NOMEM;
     if (fixed_cap) {
@@ -212,6 +215,9 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
         if (mode == MDET_MODE_PLAIN) {
             MDET_TRY(filter_simt(ctx, rect ? a32 : g.x32, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n,
                                  g.meta32, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride));
+        } else if (tf32) {
+            MDET_TRY(filter_tc(ctx, g.ta, g.nsq, g.n, g.meta, g.tb, g.n, g.meta, true, tbl, out, tiles, nlist, row_tbl,
+                               tbl_stride, kShapeTf32, rowoff));
         } else {
             MDET_TRY(filter_tc(ctx, rect ? ab : g.xa, rect ? ansq : g.nsq, rect ? na : g.n, rect ? ameta : g.meta, g.xb,
                                g.n, g.meta, !rect, tbl, out, tiles, nlist, row_tbl, tbl_stride, bn ? bn : 256, rowoff));
@@ -237,6 +243,10 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
                 MDET_TRY(filter_simt(ctx, A, rect ? na : g.n, rect ? ameta32 : g.meta32, g.x32, g.n, g.meta32, !rect,
                                      tbl, out, tiles, nlist, row_tbl, tbl_stride));
                 ctx->last_tile_n = 128128;
+            } else if (tf32) {
+                MDET_TRY(filter_tc(ctx, g.ta, g.nsq, g.n, g.meta, g.tb, g.n, g.meta, true, tbl, out, tiles, nlist,
+                                   row_tbl, tbl_stride, kShapeTf32, rowoff));
+                ctx->last_tile_n = 128128;
             } else if (bside) {  // all rows (A role) against a B-role subset
                 MDET_TRY(filter_tc(ctx, g.xa, g.nsq, g.n, g.meta, bside->xb, bside->nb, bside->meta, false, tbl, out,
                                    nullptr, 0, nullptr, 0, w, nullptr));
@@ -249,7 +259,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
             }
             return MDET_OK;
         };
-        if (mode == MDET_MODE_PLAIN || bn != 0 || tiles)
+        if (mode == MDET_MODE_PLAIN || tf32 || bn != 0 || tiles)
             MDET_TRY(run(bn ? bn : 256));
         else
             MDET_TRY(tc_autotune(ctx, bside ? tc_shape_key(true, false, g.n, bside->nb)
@@ -270,7 +280,7 @@ int run_filter(mdet_ctx* ctx, int mode, const GraphPrep& g, bool rect, const flo
 
 int check_mode(mdet_ctx* ctx, int mode) {
     if (mode == MDET_MODE_PLAIN) return MDET_OK;
-    if (mode == MDET_MODE_BF16) {
+    if (mode == MDET_MODE_BF16 || mode == MDET_MODE_TF32) {
         if (ctx->cc_major != 10 || ctx->cc_minor != 3)
             return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "tensor-core forms need an sm_103 device (have sm_%d%d)",
                             ctx->cc_major, ctx->cc_minor);
@@ -327,7 +337,7 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
     if (mode == MDET_MODE_LEARNED) return graph_learned(ctx, d_tnf, d_ls, n, cutoff, max_edges, st, g, total);
     PhaseTimer tm(ctx->stream);
     tm.mark();
-    MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, mode != MDET_MODE_PLAIN, &g));
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, tc_kind(mode), &g));
     MDET_TRY(abd_gate(ctx, g));
     const double L = logit(cutoff);
     DstarTable tbl;
@@ -555,6 +565,11 @@ int mdet_tnf_max_prob_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log
     if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
     if (m == 0) return MDET_OK;
     if (!d_tnf || !d_log_size || !d_contigs || !d_out) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    // Each sampled row's maximum comes from the exact stage over the
+    // filter's candidates, so every filter form gives the same maxima; the
+    // sample passes (sampled rows in the B role) use the BF16 filter when
+    // TF32 is asked for.
+    if (mode == MDET_MODE_TF32) mode = MDET_MODE_BF16;
     GraphPrep g;
     MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, mode != MDET_MODE_PLAIN, &g));
     MDET_TRY(maxprob_core(ctx, g, d_contigs, m, mode, floor_prob, d_out));
@@ -595,6 +610,9 @@ int mdet_tnf_ptnf_search_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_
     if (n < 2) return ctx_fail(ctx, MDET_ERR_INVALID, "need at least two contigs");
     if (n >= (1ull << 31)) return ctx_fail(ctx, MDET_ERR_INVALID, "too many contigs");
     cudaStream_t s = ctx->stream;
+    // the sample passes use the BF16 filter when TF32 is asked for (the
+    // maxima are exact whatever the filter form; see mdet_tnf_max_prob_dev)
+    if (mode == MDET_MODE_TF32) mode = MDET_MODE_BF16;
     GraphPrep g;
     MDET_TRY(prep_sorted(ctx, d_tnf, d_log_size, n, mode != MDET_MODE_PLAIN, &g));
     std::vector<uint64_t> idx(n);

@@ -8,6 +8,7 @@
 
 #define MDET_KPAD 144     // BF16 row length: 136 features + 8 zeros (9 x 16)
 constexpr int kShapeTall = 1256;  // filter_tc shape code of 256 x 128 tiles
+constexpr int kShapeTf32 = 2128;  // filter_tc shape code of 128 x 128 TF32 tiles
 #define MDET_TBL 256      // threshold table cells per axis
 #define MDET_TBL_LEVELS 9 // sparse-table levels (2^8 = 256)
 #define MDET_BLK 128      // rows per metadata block
@@ -106,8 +107,11 @@ struct GraphPrep {
     PartsFF* parts;                  // sorted model parts and log sizes (float-float)
     uint16_t* xa;                    // A role: sorted centred BF16 rows [x~, 1, 1, 0..] [npad][144]
     uint16_t* xb;                    // B role: [x~, -hi(||x~||^2/2), -lo(||x~||^2/2), 0..]; padding -inf
+    float* ta;                       // the same two roles with TF32-rounded rows (FP32 containers)
+    float* tb;
+    int tck;                         // reduced-precision rows held: kTcNone, kTcBf16 or kTcTf32
     float* nsq;                      // ||x~||^2 per sorted row (inf for padding rows)
-    BlockMeta* meta;                 // per 128-row block (bf16 rounding)
+    BlockMeta* meta;                 // per 128-row block (rounding of the rows held)
     BlockMeta* meta32;               // per 128-row block (no rounding term)
     float* mu;                       // column means [136]
     const uint8_t* low = nullptr;    // abundance gate: sorted position has no depth above 1 (null: no gate)
@@ -118,15 +122,22 @@ struct GraphPrep {
 // different number of contigs.
 int abd_gate(mdet_ctx* ctx, GraphPrep& g);
 
+// Reduced-precision rows a preparation holds for the tensor-core filter.
+constexpr int kTcNone = 0, kTcBf16 = 1, kTcTf32 = 2;
+inline int tc_kind(int mode) {
+    return mode == MDET_MODE_PLAIN ? kTcNone : (mode == MDET_MODE_TF32 ? kTcTf32 : kTcBf16);
+}
+
 // Prepares the contigs in ascending log-size order, or in `order` (original
-// index per position, device) when given.
-int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* out,
+// index per position, device) when given.  tck: the reduced-precision rows
+// to make (kTcNone, kTcBf16, kTcTf32; a bool true means kTcBf16).
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, int tck, GraphPrep* out,
                 const uint32_t* order = nullptr);
 // Arrays of a prepared set of `rows` positions (a multiple of 256) in
 // scratch named after tag; prep_into fills positions [base, base + npad) of
 // them with one contig set (perm/inv values are base + local indices).
-int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, GraphPrep* g);
-int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, const GraphPrep& g,
+int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, int tck, GraphPrep* g);
+int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, int tck, const GraphPrep& g,
               uint64_t base, const uint32_t* order = nullptr);
 // sorted: d_ls_sorted is ascending (else its range is found by a scan).
 // range: optional host copy of the log-size range {min, max}; when given with
@@ -164,17 +175,18 @@ int filter_simt(mdet_ctx* ctx, const float* a, uint32_t na, const BlockMeta* ame
                 const BlockMeta* bmeta, bool triangular, const DstarTable& tbl, CandBuf out,
                 const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
                 uint64_t tbl_stride = 0);
-// Tensor-core filter over centred BF16 rows: a (A role, na rows) against b
-// (B role, nb rows), both padded to 256 rows; a_nsq = ||a~||^2 (+inf on
-// padding rows).
+// Tensor-core filter over centred reduced-precision rows: a (A role, na
+// rows) against b (B role, nb rows), both padded to 256 rows; a_nsq =
+// ||a~||^2 (+inf on padding rows).  BF16 rows (uint16) by default; with
+// bn == kShapeTf32 TF32 rows (FP32 containers, 128 x 128 tiles).
 // tiles/nlist: optional row-major list (I * tiles_b + J) of the tile pairs
 // to evaluate (column tiles of bn); null evaluates the whole schedule.
 // rowoff (with a list): entries of row tile I are [rowoff[I], rowoff[I+1]),
 // and row tiles are taken in the waves of the full schedule.
 // bn: tile shape: 256 = 128 x 256 tiles (one CTA per SM), 128 = 128 x 128
 // (two per SM), kShapeTall = 256 x 128 with four B stages (no tile lists).
-int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
-              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+int filter_tc(mdet_ctx* ctx, const void* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+              const void* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles = nullptr, uint64_t nlist = 0, const uint8_t* row_tbl = nullptr,
               uint64_t tbl_stride = 0, int bn = 256, const unsigned long long* rowoff = nullptr);
 // Cutoff of one 256-row block of a batch: logit(cutoff) in float-float and

@@ -1,13 +1,14 @@
 // graph_filter_tc.cu -- tensor-core distance filter (tcgen05, sm_103a).
 //
 // The pairwise stage restructured as ||a||^2 + ||b||^2 - 2 a.b over centred
-// BF16 rows: a.b - ||b||^2/2 is a 128 x 256 x 144 tile GEMM per (row tile,
-// column tile) -- the column term rides in two spare K columns --
-// issued by one thread with tcgen05.mma (kind::f16, BF16 x BF16 -> FP32),
-// operands staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
-// swizzle for K 0..127, 32-byte swizzle for K 128..143), accumulators in TMEM
-// (two 256-column buffers, so the epilogue of one tile overlaps the MMA of
-// the next).  The epilogue reads TMEM with tcgen05.ld and keeps pairs with
+// reduced-precision rows: a.b - ||b||^2/2 is a 128 x 256 x 144 tile GEMM per
+// (row tile, column tile) -- the column term rides in two spare K columns --
+// issued by one thread with tcgen05.mma (kind::f16, BF16 x BF16 -> FP32; or
+// kind::tf32 on TF32 rows in FP32 containers, 128 x 128 tiles), operands
+// staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte swizzle for
+// K 0..127, 32-byte (BF16) or 64-byte (TF32) swizzle for K 128..143),
+// accumulators in TMEM (two buffers, so the epilogue of one tile overlaps
+// the MMA of the next).  The epilogue reads TMEM with tcgen05.ld and keeps pairs with
 //     a~.b~ - ||b~||^2/2 > (||a~||^2 - R^2)/2,
 // R = d*_tile + e_a + e_b + slack, where d*_tile bounds the model's distance
 // threshold over the tile's sizes and e_a, e_b bound the BF16 rounding of the
@@ -28,38 +29,56 @@
 namespace {
 
 constexpr int kBM = 128;
-constexpr uint32_t kAChunk = kBM * 128;           // 16 KB, 64 bf16 per row
-constexpr uint32_t kATail = kBM * 32;             // 4 KB, 16 bf16 per row
-constexpr uint32_t kABytes = 2 * kAChunk + kATail;  // 36 KB
 constexpr int kMaxEpiWarps = 16;
 
+// Row layout in shared memory for EB-byte elements (2: BF16, 4: TF32): EB
+// chunks of 128 bytes per row (K 0..127, 128-byte swizzle) and a tail of
+// 16 elements (K 128..143; 32-byte swizzle for BF16, 64-byte for TF32).
+// Every MMA consumes 32 bytes of K per row: four per chunk, EB/2 in the tail.
+template <int EB>
+struct Elem {
+    static constexpr int kChunks = EB;                    // 128-byte K chunks
+    static constexpr uint32_t kChunkEl = 128 / EB;         // elements per chunk
+    static constexpr uint32_t kTailBytes = 16 * EB;        // bytes per row of the tail
+    static constexpr uint32_t kTailLayout = EB == 2 ? 6u : 4u;  // SW32 or SW64 descriptor layout
+    static constexpr int kTailSteps = EB / 2;
+    static constexpr int kSteps = 4 * kChunks + kTailSteps;      // 9 or 18 MMAs per tile
+    static constexpr uint32_t kFormat = EB == 2 ? 1u : 2u;     // instruction-descriptor A/B format: BF16, TF32
+};
+
 // Tile shapes: BM rows (one or two M = 128 MMAs) x BN columns, with NST
-// stages of B tiles in shared memory.  128 x 256 x 2 and 256 x 128 x 4 run one
-// CTA per SM; 128 x 128 x 2 runs two.  A 256-row tile reads each B tile for
-// twice the rows, halving the B traffic per output.
-template <int BM, int BN, int NST>
+// stages of B tiles in shared memory.  BF16: 128 x 256 x 2 and 256 x 128 x 4
+// run one CTA per SM, 128 x 128 x 2 runs two; a 256-row tile reads each B
+// tile for twice the rows, halving the B traffic per output.  TF32 rows are
+// twice as wide: 128 x 128 x 2 (216 KB of operands) runs one CTA per SM.
+template <int BM, int BN, int NST, int EB = 2>
 struct Shape {
+    using E = Elem<EB>;
     static constexpr int MH = BM / 128;                         // M halves
+    static constexpr uint32_t kAChunk = kBM * 128;              // one 128-byte K chunk of an A half
+    static constexpr uint32_t kABytes = E::kChunks * kAChunk + kBM * E::kTailBytes;
     static constexpr uint32_t kABytesAll = MH * kABytes;
-    static constexpr uint32_t kBChunk = BN * 128;               // K 0..63 or 64..127
-    static constexpr uint32_t kBBytes = 2 * kBChunk + BN * 32;  // + K 128..143
+    static constexpr uint32_t kBChunk = BN * 128;               // one 128-byte K chunk of B
+    static constexpr uint32_t kBBytes = E::kChunks * kBChunk + BN * E::kTailBytes;
     static constexpr uint32_t kAccCols = MH * BN;               // one accumulator
     static constexpr uint32_t kTmemCols = 2 * kAccCols;         // double buffered
     static constexpr uint32_t kSmemBytes = kABytesAll + NST * kBBytes + 1024;  // + alignment slack
-    static constexpr int kCtasPerSm = (BM == 128 && BN == 128) ? 2 : 1;
-    // epilogue warps: 4 TMEM lane quarters x kEpi/4 groups; the groups of an
-    // M half split its columns.  One-CTA shapes take 16 so that the TMEM
-    // reads of a tile are spread over more warps in flight.
-    static constexpr int kEpi = kCtasPerSm == 2 ? 8 : 16;
+    static constexpr int kCtasPerSm = (BM == 128 && BN == 128 && EB == 2) ? 2 : 1;
+    // epilogue warps: 4 TMEM lane quarters x one group per 64 columns of each
+    // M half (16 for the 128 x 256 and 256 x 128 shapes, 8 for 128 x 128), so
+    // each warp reads one 64-column chunk of its quarter per tile.
+    static constexpr int kEpi = 4 * (BN / 64) * MH;
     static constexpr int kThreads = (2 + kEpi) * 32;
     static constexpr int kGroupsPerHalf = kEpi / 4 / MH;
     static constexpr uint32_t kWarpCols = BN / kGroupsPerHalf;
     // candidate queue per epilogue warp, within the shared memory left
     static constexpr int kQueue = kCtasPerSm == 2 ? 32 : (kSmemBytes + kEpi * 256 * 8 <= 227 * 1024 ? 256 : 64);
     static_assert(kWarpCols == 64, "each epilogue warp reads one 64-column chunk per tile");
-    // BF16 x BF16 -> FP32, M = 128, N = BN, A and B K-major.
-    static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                                       ((uint32_t)(128 >> 4) << 24);
+    static_assert(kSmemBytes + kEpi * kQueue * 8 + 512 <= 227 * 1024, "shared memory of one CTA");
+    // BF16 x BF16 or TF32 x TF32 -> FP32 (D format bits 4-5), A/B formats
+    // (bits 7-9, 10-12), M = 128, N = BN, A and B K-major.
+    static constexpr uint32_t kIdesc = (1u << 4) | (E::kFormat << 7) | (E::kFormat << 10) |
+                                       ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
     static_assert(kTmemCols <= 512, "TMEM holds 512 columns");
     static_assert(NST <= 4, "at most four B stages");
 };
@@ -115,15 +134,24 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t layout, u
     d |= (uint64_t)layout << 61;
     return d;
 }
-constexpr uint32_t kLayoutSW128 = 2, kLayoutSW32 = 6;
+constexpr uint32_t kLayoutSW128 = 2;
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+template <int EB>
+__device__ __forceinline__ void mma_rows(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
+    if constexpr (EB == 2) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    }
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -336,11 +364,13 @@ __device__ __forceinline__ void advance(const TcArgs& p, Cursor& k, uint32_t c, 
 
 // -------------------------------------------------------------- kernel --
 
-template <int BM, int BN, int NST>
-__global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NST>::kCtasPerSm)
+// tmA32/tmB32: the K 128..143 tail (32-byte swizzle for BF16, 64-byte for TF32)
+template <int BM, int BN, int NST, int EB>
+__global__ void __launch_bounds__(Shape<BM, BN, NST, EB>::kThreads, Shape<BM, BN, NST, EB>::kCtasPerSm)
     k_filter_tc(const __grid_constant__ CUtensorMap tmA128, const __grid_constant__ CUtensorMap tmA32,
                 const __grid_constant__ CUtensorMap tmB128, const __grid_constant__ CUtensorMap tmB32, TcArgs p) {
-    using S = Shape<BM, BN, NST>;
+    using S = Shape<BM, BN, NST, EB>;
+    using E = typename S::E;
     extern __shared__ unsigned char smem_raw[];
     __shared__ Ctl ctl;
     constexpr int kQueue = S::kQueue;
@@ -401,10 +431,11 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
 #pragma unroll
                         for (int h = 0; h < S::MH; ++h) {
                             const int y = (int)(c.I * BM + h * 128);
-                            unsigned char* dA = sA + h * kABytes;
-                            tma_load_2d(dA, &tmA128, 0, y, &ctl.a_full);
-                            tma_load_2d(dA + kAChunk, &tmA128, 64, y, &ctl.a_full);
-                            tma_load_2d(dA + 2 * kAChunk, &tmA32, 128, y, &ctl.a_full);
+                            unsigned char* dA = sA + h * S::kABytes;
+#pragma unroll
+                            for (int ch = 0; ch < E::kChunks; ++ch)
+                                tma_load_2d(dA + ch * S::kAChunk, &tmA128, ch * (int)E::kChunkEl, y, &ctl.a_full);
+                            tma_load_2d(dA + E::kChunks * S::kAChunk, &tmA32, 128, y, &ctl.a_full);
                         }
                         curI = c.I;
                     }
@@ -414,9 +445,10 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
                     unsigned char* dst = sB + bs * S::kBBytes;
                     mbar_arrive_tx(&ctl.b_full[bs], S::kBBytes);
                     const int y = (int)(c.J * BN);
-                    tma_load_2d(dst, &tmB128, 0, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + S::kBChunk, &tmB128, 64, y, &ctl.b_full[bs]);
-                    tma_load_2d(dst + 2 * S::kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
+#pragma unroll
+                    for (int ch = 0; ch < E::kChunks; ++ch)
+                        tma_load_2d(dst + ch * S::kBChunk, &tmB128, ch * (int)E::kChunkEl, y, &ctl.b_full[bs]);
+                    tma_load_2d(dst + E::kChunks * S::kBChunk, &tmB32, 128, y, &ctl.b_full[bs]);
                 }
             }
         } else if (warp == 1) {
@@ -455,19 +487,21 @@ __global__ void __launch_bounds__(Shape<BM, BN, NST>::kThreads, Shape<BM, BN, NS
 #pragma unroll
                     for (int h = 0; h < S::MH; ++h) {
                         const uint32_t d = tmem + s * S::kAccCols + h * BN;
-                        const uint32_t ab = a_base + h * kABytes;
+                        const uint32_t ab = a_base + h * S::kABytes;
 #pragma unroll
-                        for (int k = 0; k < 9; ++k) {
+                        for (int k = 0; k < E::kSteps; ++k) {
                             uint64_t ad, bd;
-                            if (k < 8) {
+                            if (k < 4 * E::kChunks) {
                                 const uint32_t ch = k >> 2, ko = (k & 3) * 32;
-                                ad = smem_desc(ab + ch * kAChunk + ko, kLayoutSW128, 1024);
+                                ad = smem_desc(ab + ch * S::kAChunk + ko, kLayoutSW128, 1024);
                                 bd = smem_desc(bb + ch * S::kBChunk + ko, kLayoutSW128, 1024);
                             } else {
-                                ad = smem_desc(ab + 2 * kAChunk, kLayoutSW32, 256);
-                                bd = smem_desc(bb + 2 * S::kBChunk, kLayoutSW32, 256);
+                                // tail: 8-row core groups E::kTailBytes * 8 apart, 32 bytes of K per step
+                                const uint32_t ko = (k - 4 * E::kChunks) * 32;
+                                ad = smem_desc(ab + E::kChunks * S::kAChunk + ko, E::kTailLayout, 8 * E::kTailBytes);
+                                bd = smem_desc(bb + E::kChunks * S::kBChunk + ko, E::kTailLayout, 8 * E::kTailBytes);
                             }
-                            mma_bf16(d, ad, bd, S::kIdesc, k > 0 ? 1u : 0u);
+                            mma_rows<EB>(d, ad, bd, S::kIdesc, k > 0 ? 1u : 0u);
                         }
                     }
                     mma_commit(&ctl.b_empty[bs]);
@@ -613,33 +647,38 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode(mdet_ctx* ctx) {
     return (PFN_cuTensorMapEncodeTiled_v12000)ctx->encode_tiled;
 }
 
-int make_map(mdet_ctx* ctx, CUtensorMap* map, const uint16_t* base, uint64_t rows, uint32_t box_k, uint32_t box_rows,
-             CUtensorMapSwizzle sw) {
+// Tensor map over [rows][144] elements of eb bytes (2: BF16, 4: FP32 holding
+// TF32 values), box {box_k elements, box_rows rows}.
+int make_map(mdet_ctx* ctx, CUtensorMap* map, const void* base, uint64_t rows, uint32_t box_k, uint32_t box_rows,
+             CUtensorMapSwizzle sw, int eb) {
     auto enc = get_encode(ctx);
     if (!enc) return ctx_fail(ctx, MDET_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {MDET_KPAD, rows};
-    cuuint64_t strides[1] = {MDET_KPAD * 2};
+    cuuint64_t strides[1] = {(cuuint64_t)MDET_KPAD * eb};
     cuuint32_t box[2] = {box_k, box_rows};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, es,
+    CUresult r = enc(map, eb == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                     (void*)base, dims, strides, box, es,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return ctx_fail(ctx, MDET_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return MDET_OK;
 }
 
-template <int BM, int BN, int NST>
-int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
-              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+template <int BM, int BN, int NST, int EB>
+int launch_tc(mdet_ctx* ctx, const void* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+              const void* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride,
               const unsigned long long* rowoff) {
-    using S = Shape<BM, BN, NST>;
+    using S = Shape<BM, BN, NST, EB>;
+    using E = typename S::E;
     const uint64_t na_pad = (na + 255) / 256 * 256, nb_pad = (nb + 255) / 256 * 256;
+    const CUtensorMapSwizzle tail_sw = EB == 2 ? CU_TENSOR_MAP_SWIZZLE_32B : CU_TENSOR_MAP_SWIZZLE_64B;
     CUtensorMap mA128, mA32, mB128, mB32;
-    MDET_TRY(make_map(ctx, &mA128, a, na_pad, 64, kBM, CU_TENSOR_MAP_SWIZZLE_128B));
-    MDET_TRY(make_map(ctx, &mA32, a, na_pad, 16, kBM, CU_TENSOR_MAP_SWIZZLE_32B));
-    MDET_TRY(make_map(ctx, &mB128, b, nb_pad, 64, BN, CU_TENSOR_MAP_SWIZZLE_128B));
-    MDET_TRY(make_map(ctx, &mB32, b, nb_pad, 16, BN, CU_TENSOR_MAP_SWIZZLE_32B));
+    MDET_TRY(make_map(ctx, &mA128, a, na_pad, E::kChunkEl, kBM, CU_TENSOR_MAP_SWIZZLE_128B, EB));
+    MDET_TRY(make_map(ctx, &mA32, a, na_pad, 16, kBM, tail_sw, EB));
+    MDET_TRY(make_map(ctx, &mB128, b, nb_pad, E::kChunkEl, BN, CU_TENSOR_MAP_SWIZZLE_128B, EB));
+    MDET_TRY(make_map(ctx, &mB32, b, nb_pad, 16, BN, tail_sw, EB));
     TcArgs p;
     p.na = na;
     p.nb = nb;
@@ -657,7 +696,7 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     p.ntiles = 0;
     static bool attr[64] = {false};
     if (!attr[ctx->device & 63]) {
-        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc<BM, BN, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        MDET_CUDA(ctx, cudaFuncSetAttribute(k_filter_tc<BM, BN, NST, EB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)S::kSmemBytes));
         attr[ctx->device & 63] = true;
     }
@@ -675,7 +714,7 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
     if (p.rowoff) grid = (unsigned)std::min<unsigned long long>(grid, p.ta);  // one row tile per CTA and wave
     if (grid == 0) return MDET_OK;
     ctx_timer_begin(ctx, "k_filter_tc");
-    k_filter_tc<BM, BN, NST><<<grid, S::kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
+    k_filter_tc<BM, BN, NST, EB><<<grid, S::kThreads, S::kSmemBytes, ctx->stream>>>(mA128, mA32, mB128, mB32, p);
     ctx_timer_end(ctx, "k_filter_tc");
     MDET_LAUNCHED(ctx, "k_filter_tc");
     return MDET_OK;
@@ -683,19 +722,22 @@ int launch_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na,
 
 }  // namespace
 
-int filter_tc(mdet_ctx* ctx, const uint16_t* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
-              const uint16_t* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
+int filter_tc(mdet_ctx* ctx, const void* a, const float* a_nsq, uint32_t na, const BlockMeta* ameta,
+              const void* b, uint32_t nb, const BlockMeta* bmeta, bool triangular, const DstarTable& tbl,
               CandBuf out, const uint32_t* tiles, uint64_t nlist, const uint8_t* row_tbl, uint64_t tbl_stride,
               int bn, const unsigned long long* rowoff) {
     if (na == 0 || nb == 0) return MDET_OK;
+    if (bn == kShapeTf32)
+        return launch_tc<128, 128, 2, 4>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                         row_tbl, tbl_stride, rowoff);
     if (bn == 128)
-        return launch_tc<128, 128, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                      row_tbl, tbl_stride, rowoff);
+        return launch_tc<128, 128, 2, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                         row_tbl, tbl_stride, rowoff);
     if (bn == kShapeTall) {
         if (tiles) return ctx_fail(ctx, MDET_ERR_INVALID, "tile lists use 128-row tiles");
-        return launch_tc<256, 128, 4>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                      row_tbl, tbl_stride, rowoff);
+        return launch_tc<256, 128, 4, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                         row_tbl, tbl_stride, rowoff);
     }
-    return launch_tc<128, 256, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
-                                  row_tbl, tbl_stride, rowoff);
+    return launch_tc<128, 256, 2, 2>(ctx, a, a_nsq, na, ameta, b, nb, bmeta, triangular, tbl, out, tiles, nlist,
+                                     row_tbl, tbl_stride, rowoff);
 }

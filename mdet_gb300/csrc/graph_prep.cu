@@ -175,6 +175,70 @@ __global__ void k_bf16(const float* __restrict__ x32, const float* __restrict__ 
     }
 }
 
+// TF32 form of k_bf16: the same rows rounded to TF32 (round to nearest,
+// ties away; low 13 bits zero, so the tensor cores read them unchanged) in
+// FP32 containers.  hv^2 is exact in FP32 (11-bit significands); the column
+// term -||x~||^2/2 rides in columns 136/137 as a two-term TF32 split.
+__device__ __forceinline__ float to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__global__ void k_tf32(const float* __restrict__ x32, const float* __restrict__ mu, uint64_t n, uint64_t npad,
+                       float* __restrict__ ta, float* __restrict__ tb, float* __restrict__ nsq,
+                       float* __restrict__ err, float* __restrict__ nrm) {
+    uint64_t s = blockIdx.x * (uint64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    uint32_t lane = threadIdx.x & 31;
+    if (s >= npad) return;
+    float* rowa = ta + s * MDET_KPAD;
+    float* rowb = tb + s * MDET_KPAD;
+    if (s >= n) {
+        for (int k = lane; k < MDET_KPAD; k += 32) {
+            rowa[k] = (k == MDET_NTNF || k == MDET_NTNF + 1) ? 1.f : 0.f;
+            rowb[k] = (k == MDET_NTNF) ? __int_as_float(0xff800000) : 0.f;
+        }
+        if (lane == 0) {
+            nsq[s] = __int_as_float(0x7f800000);
+            err[s] = 0.f;
+            nrm[s] = 0.f;
+        }
+        return;
+    }
+    float e2 = 0.f;
+    ff q = ff_make(0.f, 0.f);
+    for (int k = lane; k < MDET_NTNF; k += 32) {
+        const float a = x32[s * MDET_NTNF + k];
+        const ff v = two_sum(a, -mu[k]);  // v.hi + v.lo == a - mu exactly
+        const float hv = to_tf32(v.hi);
+        const float d = __fadd_rn(__fsub_rn(v.hi, hv), v.lo);
+        e2 = __fmaf_rn(d, d, e2);
+        q = ff_add_f(q, __fmul_rn(hv, hv));
+        rowa[k] = hv;
+        rowb[k] = hv;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        ff t;
+        t.hi = __shfl_xor_sync(0xffffffffu, q.hi, o);
+        t.lo = __shfl_xor_sync(0xffffffffu, q.lo, o);
+        q = ff_add(q, t);
+    }
+    const float half = 0.5f * q.hi;
+    const float hi = to_tf32(half);
+    const float lo = to_tf32(__fsub_rn(half, hi));
+    for (int k = MDET_NTNF + lane; k < MDET_KPAD; k += 32) {
+        rowa[k] = (k < MDET_NTNF + 2) ? 1.f : 0.f;
+        rowb[k] = k == MDET_NTNF ? -hi : (k == MDET_NTNF + 1 ? -lo : 0.f);
+    }
+    if (lane == 0) {
+        nsq[s] = q.hi;
+        err[s] = __fsqrt_ru(__fmul_ru(e2, 1.001f));
+        nrm[s] = __fsqrt_ru(__fadd_ru(q.hi, q.lo));
+    }
+}
+
 __global__ void k_meta(const double* __restrict__ ls_s, const float* __restrict__ err, const float* __restrict__ nrm,
                        uint64_t n, uint64_t nblk, BlockMeta* __restrict__ meta, BlockMeta* __restrict__ meta32) {
     uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -359,7 +423,7 @@ ModelH model_h() {
     return h;
 }
 
-int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, GraphPrep* g) {
+int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, int tck, GraphPrep* g) {
     const std::string t(tag);
     const uint64_t nblk = rows / MDET_BLK;
     g->perm = (uint32_t*)ctx_scratch(ctx, (t + ".perm").c_str(), rows * 4);
@@ -370,20 +434,29 @@ int prep_alloc(mdet_ctx* ctx, const char* tag, uint64_t rows, bool need_bf16, Gr
     g->meta32 = (BlockMeta*)ctx_scratch(ctx, (t + ".meta32").c_str(), nblk * sizeof(BlockMeta));
     g->mu = (float*)ctx_scratch(ctx, (t + ".mu").c_str(), MDET_NTNF * 4);
     g->xa = g->xb = nullptr;
+    g->ta = g->tb = nullptr;
+    g->tck = tck;
     g->nsq = nullptr;
     g->meta = nullptr;
-    if (need_bf16) {
+    if (tck == kTcBf16) {
         g->xa = (uint16_t*)ctx_scratch(ctx, (t + ".xa").c_str(), rows * MDET_KPAD * 2);
         g->xb = (uint16_t*)ctx_scratch(ctx, (t + ".xb").c_str(), rows * MDET_KPAD * 2);
+        if (!g->xa || !g->xb) return MDET_ERR_NOMEM;
+    } else if (tck == kTcTf32) {
+        g->ta = (float*)ctx_scratch(ctx, (t + ".ta").c_str(), rows * MDET_KPAD * 4);
+        g->tb = (float*)ctx_scratch(ctx, (t + ".tb").c_str(), rows * MDET_KPAD * 4);
+        if (!g->ta || !g->tb) return MDET_ERR_NOMEM;
+    }
+    if (tck != kTcNone) {
         g->nsq = (float*)ctx_scratch(ctx, (t + ".nsq").c_str(), rows * 4);
         g->meta = (BlockMeta*)ctx_scratch(ctx, (t + ".meta").c_str(), nblk * sizeof(BlockMeta));
-        if (!g->xa || !g->xb || !g->nsq || !g->meta) return MDET_ERR_NOMEM;
+        if (!g->nsq || !g->meta) return MDET_ERR_NOMEM;
     }
     if (!g->perm || !g->inv || !g->x32 || !g->ls || !g->parts || !g->meta32 || !g->mu) return MDET_ERR_NOMEM;
     return MDET_OK;
 }
 
-int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, const GraphPrep& g,
+int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, int tck, const GraphPrep& g,
               uint64_t base, const uint32_t* order) {
     cudaStream_t s = ctx->stream;
     const uint64_t npad = (n + 255) / 256 * 256;
@@ -415,7 +488,7 @@ int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n,
     MDET_LAUNCHED(ctx, "k_gather");
     float* err = nullptr;
     float* nrm = nullptr;
-    if (need_bf16) {
+    if (tck != kTcNone) {
         err = (float*)ctx_scratch(ctx, "pre.err", npad * 4);
         nrm = (float*)ctx_scratch(ctx, "pre.nrm", npad * 4);
         if (!err || !nrm) return MDET_ERR_NOMEM;
@@ -424,12 +497,18 @@ int prep_into(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n,
         MDET_LAUNCHED(ctx, "k_colsum");
         k_mean<<<1, MDET_NTNF, 0, s>>>(sums, n, g.mu);
         MDET_LAUNCHED(ctx, "k_mean");
-        k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(x32, g.mu, n, npad, g.xa + base * MDET_KPAD,
-                                                         g.xb + base * MDET_KPAD, g.nsq + base, err, nrm);
-        MDET_LAUNCHED(ctx, "k_bf16");
+        if (tck == kTcTf32) {
+            k_tf32<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(x32, g.mu, n, npad, g.ta + base * MDET_KPAD,
+                                                             g.tb + base * MDET_KPAD, g.nsq + base, err, nrm);
+            MDET_LAUNCHED(ctx, "k_tf32");
+        } else {
+            k_bf16<<<(unsigned)((npad + 7) / 8), 256, 0, s>>>(x32, g.mu, n, npad, g.xa + base * MDET_KPAD,
+                                                             g.xb + base * MDET_KPAD, g.nsq + base, err, nrm);
+            MDET_LAUNCHED(ctx, "k_bf16");
+        }
     }
     k_meta<<<(unsigned)((nblk + 127) / 128), 128, 0, s>>>(ls, err, nrm, n, nblk,
-                                                         need_bf16 ? g.meta + base / MDET_BLK : nullptr,
+                                                         tck != kTcNone ? g.meta + base / MDET_BLK : nullptr,
                                                          g.meta32 + base / MDET_BLK);
     MDET_LAUNCHED(ctx, "k_meta");
     return MDET_OK;
@@ -455,15 +534,15 @@ __global__ void k_content_hash(const uint32_t* __restrict__ a, uint64_t na, cons
 // Rows sorted by size (or in the caller's order).  A preparation of the very
 // same inputs that is still in place (same pointers and contents, no count
 // since) is used as it is: the search and the graph of one assembly share it.
-int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, bool need_bf16, GraphPrep* g,
+int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, int tck, GraphPrep* g,
                 const uint32_t* order) {
     g->n = (uint32_t)n;
     g->npad = (uint32_t)((n + 255) / 256 * 256);
-    MDET_TRY(prep_alloc(ctx, "pre", g->npad, need_bf16, g));
+    MDET_TRY(prep_alloc(ctx, "pre", g->npad, tck, g));
     auto& c = ctx->prep_cache;
     if (order) {
         c.valid = false;
-        return prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, order);
+        return prep_into(ctx, d_tnf, d_ls, n, tck, *g, 0, order);
     }
     unsigned long long* dh = (unsigned long long*)ctx_scratch(ctx, "pre.hash", 8);
     if (!dh) return MDET_ERR_NOMEM;
@@ -475,19 +554,23 @@ int prep_sorted(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t 
     MDET_LAUNCHED(ctx, "k_content_hash");
     MDET_CUDA(ctx, cudaMemcpyAsync(&h, dh, 8, cudaMemcpyDeviceToHost, s));
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    if (c.valid && c.tnf == d_tnf && c.ls == d_ls && c.n == n && (c.bf16 || !need_bf16) && c.hash == h &&
-        c.x32 == g->x32 && (!need_bf16 || c.xa == g->xa) && c.gen == ctx->scratch_gen)
+    // a preparation with other reduced-precision rows (or none) is remade:
+    // nsq and the block metadata describe the rows last made
+    if (c.valid && c.tnf == d_tnf && c.ls == d_ls && c.n == n && (c.tck == tck || tck == kTcNone) &&
+        c.hash == h && c.x32 == g->x32 && (tck == kTcNone || (c.xa == g->xa && c.ta == g->ta)) &&
+        c.gen == ctx->scratch_gen)
         return MDET_OK;
     c.valid = false;
-    MDET_TRY(prep_into(ctx, d_tnf, d_ls, n, need_bf16, *g, 0, nullptr));
+    MDET_TRY(prep_into(ctx, d_tnf, d_ls, n, tck, *g, 0, nullptr));
     c.valid = true;
     c.tnf = d_tnf;
     c.ls = d_ls;
     c.n = n;
-    c.bf16 = need_bf16;
+    c.tck = tck;
     c.hash = h;
     c.x32 = g->x32;
     c.xa = g->xa;
+    c.ta = g->ta;
     c.gen = ctx->scratch_gen;
     return MDET_OK;
 }

@@ -34,7 +34,7 @@ def test_config0_counts(gpu_ctx, config0):
     assert np.allclose(t, tnf, rtol=1e-6, atol=0)
 
 
-@pytest.mark.parametrize("mode", ["bf16", "plain"])
+@pytest.mark.parametrize("mode", ["bf16", "tf32", "plain"])
 def test_config0_graph_pinned_cutoff(gpu_ctx, config0, mode):
     a, _, tnf = config0
     g = gpu_ctx.tnf_graph(tnf, a.log_sizes, 0.95, K, mode=mode)

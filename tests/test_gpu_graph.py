@@ -39,6 +39,35 @@ def test_bf16_equals_plain(gpu_ctx, set_a, cutoff, k):
     assert t.stats["n_candidates"] >= t.stats["n_above_cutoff"]
 
 
+@pytest.mark.parametrize("cutoff,k", [(0.95, 200), (0.9, 10), (0.8, 40)])
+def test_tf32_equals_plain(gpu_ctx, set_a, cutoff, k):
+    """The TF32 tcgen05 filter is conservative like the BF16 one (its rows'
+    rounding errors enter the bound), so the graph equals the plain form's bit
+    for bit; its tighter rounding keeps fewer candidates than BF16."""
+    a, _, tnf = set_a
+    p = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="plain")
+    t = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="tf32")
+    b = gpu_ctx.tnf_graph(tnf, a.log_sizes, cutoff, k, mode="bf16")
+    assert np.array_equal(p.from_, t.from_) and np.array_equal(p.to, t.to) and np.array_equal(p.sTNF, t.sTNF)
+    assert t.stats["n_above_cutoff"] <= t.stats["n_candidates"] <= b.stats["n_candidates"]
+    assert t.stats["tile_m_n"] == 128128
+
+
+def test_tf32_sample_passes(gpu_ctx, set_a):
+    """Max-probability and pTNF requests in the TF32 form give the BF16/plain
+    results (the sample passes run the BF16 filter; the maxima are exact)."""
+    a, _, tnf = set_a
+    idx = np.arange(0, tnf.shape[0], 5)
+    assert np.array_equal(gpu_ctx.max_prob(tnf, a.log_sizes, idx, mode="tf32"),
+                          gpu_ctx.max_prob(tnf, a.log_sizes, idx, mode="plain"))
+    from oracle import oracle as _o
+    _o.srand(77)
+    p1 = gpu_ctx.ptnf_search(tnf, a.log_sizes, 0.95, mode="tf32")
+    _o.srand(77)
+    p2 = gpu_ctx.ptnf_search(tnf, a.log_sizes, 0.95, mode="bf16")
+    assert p1 == p2
+
+
 @pytest.mark.parametrize("shape", [128256, 128128, 256128])
 def test_every_tile_shape_equals_plain(gpu_ctx, set_a, shape):
     a, _, tnf = set_a

@@ -78,6 +78,15 @@ int mdet_ctx_set_timing(mdet_ctx* ctx, int enable);
 int mdet_ctx_kernel_ms(mdet_ctx* ctx, const char* kernel, double* ms, uint32_t* launches);
 /* Kernels this context has launched since it was created. */
 uint64_t mdet_ctx_launch_count(const mdet_ctx* ctx);
+/* Failure detection check (no counterpart in the reference, which has no
+ * device-side waits): one thread of a one-block kernel waits, through the
+ * same bounded mbarrier wait the tensor-core filter uses, on a barrier that
+ * nothing arrives on, with a budget of budget_cycles SM cycles (at most the
+ * library's own ~2 s budget).  The wait runs out, the kernel raises the
+ * context's error flag and returns, and the call returns MDET_ERR_TIMEOUT
+ * with the context still usable -- what every other entry point does when
+ * one of its waits runs out. */
+int mdet_ctx_check_wait(mdet_ctx* ctx, uint64_t budget_cycles);
 
 /* Page-locked host memory, as the reference allocates its file buffer and
  * TNF rows (cudaMallocHost, cuda/Cuda2.cu:1462, 1826): copies between it and

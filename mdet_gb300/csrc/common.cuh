@@ -203,13 +203,14 @@ static __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint
 }
 
 // Bounded wait: returns false (and raises the device flag) when the budget
-// runs out, so no wait in this library can spin forever.
-static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* flag) {
+// (SM clock cycles) runs out, so no wait in this library can spin forever.
+static __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* flag,
+                                                 unsigned long long budget = MDET_SPIN_CYCLES) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     while (true) {
         if (mbar_try_wait_suspend(bar, parity)) return true;
-        if ((unsigned long long)(clock64() - t0) > MDET_SPIN_CYCLES) {
+        if ((unsigned long long)(clock64() - t0) > budget) {
             if (flag) atomicOr(flag, MDET_FLAG_TIMEOUT);
             return false;
         }

@@ -328,6 +328,36 @@ int mdet_ctx_set_autotune(mdet_ctx* ctx, int mode) {
     return MDET_OK;
 }
 
+}  // extern "C"
+
+int check_flag(mdet_ctx* ctx);  // graph.cu: reads and clears the device error flag
+
+namespace {
+// One thread waits, with the library's bounded wait, on an mbarrier that no
+// thread ever arrives on; the wait runs out after `budget` cycles, raises the
+// context's error flag and the kernel returns.  Nothing else is in flight.
+__global__ void k_wait_probe(int* flag, unsigned long long budget) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+        mbar_wait(&bar, 0, flag, budget);
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int mdet_ctx_check_wait(mdet_ctx* ctx, uint64_t budget_cycles) {
+    if (!ctx) return MDET_ERR_INVALID;
+    if (budget_cycles > MDET_SPIN_CYCLES) return ctx_fail(ctx, MDET_ERR_INVALID, "budget above the library's");
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->launches = 0;
+    k_wait_probe<<<1, 32, 0, ctx->stream>>>(ctx->d_flag, budget_cycles);
+    MDET_LAUNCHED(ctx, "k_wait_probe");
+    return check_flag(ctx);
+}
+
 int mdet_ctx_set_timing(mdet_ctx* ctx, int enable) {
     if (!ctx) return MDET_ERR_INVALID;
     cudaSetDevice(ctx->device);

@@ -137,6 +137,7 @@ SIGNATURES = [
     ("mdet_tnf_count", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_dev", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_noalloc", ctypes.c_int, [P, u64, P, P, u64, P, P, P]),
+    ("mdet_ctx_check_wait", ctypes.c_int, [P, u64]),
     ("mdet_tnf_max_prob", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_max_prob_dev", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_ptnf_search", ctypes.c_int, [P, P, P, u64, D, ctypes.c_int, ctypes.POINTER(D)]),

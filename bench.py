@@ -293,6 +293,59 @@ def tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to
             "exact_stage": "shared with the BF16 and plain forms: same error statement (tests/test_gpu_error.py)"}
 
 
+def recruit_leg(ctx, a, run_cpu):
+    """Dissolving small bins and recruiting leftover and small contigs
+    (mdet_recruit) after binning the step's assembly: labels are the contigs'
+    genomes with 1 % of the contigs split off into singleton bins (dissolved
+    into leftovers at minClsSize 200 kb), 20,000 small contigs (1-2.5 kb) drawn
+    from the same genomes, 10 samples of seeded depths.  1 untimed and 3
+    timed calls through the host-buffer entry point.  The CPU oracle (one
+    thread, the reference's loops) runs the same workload scaled down to
+    every tenth contig and 2,000 small contigs; the GPU is timed on that too."""
+    from mdet_gb300 import synth
+
+    rng = np.random.default_rng(99)
+    n = a.genome.size
+    ns = 20000
+    sg = rng.integers(0, int(a.genome.max()) + 1, ns).astype(np.uint32)
+    both, _ = synth.abundance(np.concatenate([a.genome, sg]), 10, 20240611)
+    abd = both[:n].astype(np.float32)
+    sabd = both[n:].astype(np.float32)
+    label = a.genome.astype(np.int64)
+    tiny = rng.random(n) < 0.01
+    label[tiny] = 1 << 40 | np.arange(int(tiny.sum()))
+    sizes = a.sizes.astype(np.uint64)
+    ssz = rng.integers(1000, 2500, ns).astype(np.uint64)
+    tot = int(ssz.sum())
+    ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        out, sout, st = ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
+        ts.append(time.perf_counter() - t0)
+    leg = {"metric": "dissolve + recruit time (host buffers)", "value": float(np.median(ts)), "unit": "s",
+           "contigs": int(n), "small_contigs": ns, "samples": 10, **{k: int(v) for k, v in st.items()},
+           "data": "synthetic depths (synth.abundance, seed 20240611), genome labels, 1 % singleton bins"}
+    sub = np.arange(0, n, 10)
+    s_abd, s_lab, s_sz = abd[sub], label[sub], sizes[sub]
+    s_sabd, s_ssz = sabd[:2000], ssz[:2000]
+    ctx.recruit(s_abd, s_sabd, s_lab, s_sz, s_ssz, 200000, int(s_ssz.sum()))
+    t0 = time.perf_counter()
+    g_out, g_sout, _ = ctx.recruit(s_abd, s_sabd, s_lab, s_sz, s_ssz, 200000, int(s_ssz.sum()))
+    leg["scaled_gpu_s"] = time.perf_counter() - t0
+    if run_cpu:
+        from oracle import oracle
+
+        t0 = time.perf_counter()
+        o_out, o_sout, _ = oracle.recruit(s_abd, s_sabd, s_lab, s_sz, s_ssz, 200000, int(s_ssz.sum()))
+        dt = time.perf_counter() - t0
+        leg["cpu_baseline"] = {"value": dt, "unit": "s", "cores": 1, "kind": "port",
+                               "sample": f"every tenth contig ({sub.size}) and 2,000 small contigs, the oracle's "
+                                         f"loops on one thread (the reference's are OpenMP tasks)"}
+        leg["scaled_equal_oracle"] = bool(np.array_equal(g_out, o_out) and np.array_equal(g_sout, o_sout))
+    return leg
+
+
 def fasta_leg(ctx, d_bytes, nbytes, a, pinned, pk, run_cpu):
     """FASTA ingest on the device (mdet_fasta_index_dev) over the step's file
     bytes in HBM (8.6 GB, far larger than L2): 1 untimed and 3 timed calls;
@@ -553,6 +606,8 @@ def run_ours(args):
             parity_info[f"{args.mode}_graph_equals_plain"] = bool(
                 int(ne_p) == ne and torch.equal(o_from[:ne], d_from[:ne]) and torch.equal(o_to[:ne], d_to[:ne])
                 and torch.equal(o_st[:ne], d_st[:ne]))
+        if not args.no_recruit:
+            result["recruit"] = recruit_leg(ctx, a, not args.no_cpu and ws == 1)
         if not args.no_tf32 and args.mode == "bf16":
             result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,
                                       pk, pk_kind)
@@ -794,6 +849,7 @@ def main():
     ap.add_argument("--no-abd", action="store_true", help="skip the sTNF -> sSCR leg")
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
     ap.add_argument("--no-tf32", action="store_true", help="skip the TF32 graph leg")
+    ap.add_argument("--no-recruit", action="store_true", help="skip the dissolve / recruit leg")
     ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
                     help="run one single-stage case instead of the benchmark (profiler workloads)")
     ap.add_argument("--samples", type=int, default=10)

@@ -352,6 +352,39 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* mlp, const float* d_tnf, const doubl
  * report may be null; the context keeps both pointers. */
 int mdet_ctx_set_learned(mdet_ctx* ctx, const mdet_mlp* mlp, mdet_learned_report* report);
 
+/* ---- dissolving small bins, recruiting leftover and small contigs -------
+ * Replaces the block of main after label propagation (cuda/Cuda2.cu:
+ * 2064-2283): the large contigs are grouped into bins by label[i] (members in
+ * ascending index); a bin whose sizes sum below min_cls_size is dissolved and
+ * its members become leftovers.  Depth rows are replaced by their average
+ * ranks (Spearman), every bin with at least 10 members gets the mean pairwise
+ * depth correlation of its members, and a leftover (a small contig, against
+ * the small contigs' own depths) joins a bin when its mean correlation with
+ * the bin's first 10 members, and then with all of them, reaches the bin's
+ * mean -- and only when exactly one bin accepts it.  Leftover recruits are
+ * kept when their bases are under 10 % of the binned bases, small-contig
+ * recruits when theirs are under 15 % of small_total (pass the reference's
+ * totalSize1: it sums the small contigs' sizes only with --verbose, and 0
+ * rejects every small recruit).  abd (n x nabd) and small_abd (n_small x
+ * nabd) are the reference's ABD and small_ABD (float, row-major; 1 <= nabd
+ * <= 256); they are not modified.  out[i]: the bin label of large contig i
+ * afterwards, -1 if it has none; small_out[s] likewise.  The caller applies
+ * the reference's own condition for running this block (!noAdd, nABD >=
+ * minSample). */
+typedef struct {
+    uint64_t n_bins;              /* bins kept (sizes sum to >= min_cls_size) */
+    uint64_t n_bins_scored;       /* kept bins with >= 10 members: the ones that recruit */
+    uint64_t n_leftovers;         /* large contigs of dissolved bins */
+    uint64_t n_leftovers_matched; /* leftovers exactly one bin accepts */
+    uint64_t n_small_matched;     /* small contigs exactly one bin accepts */
+    uint64_t binned_bases, leftover_bases, small_bases;
+    int leftovers_accepted, small_accepted; /* the 10 % and 15 % gates */
+} mdet_recruit_stats;
+int mdet_recruit(mdet_ctx* ctx, const float* abd, const float* small_abd, uint64_t n, uint64_t n_small,
+                 uint32_t nabd, const int64_t* label, const uint64_t* sizes, const uint64_t* small_sizes,
+                 uint64_t min_cls_size, uint64_t small_total, int64_t* out, int64_t* small_out,
+                 mdet_recruit_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

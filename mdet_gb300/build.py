@@ -35,10 +35,11 @@ CU_UNITS = [
     "graph_batch",
     "abundance",
     "fasta_index",
+    "recruit",
 ]
 # per-unit flags: the abundance unit rounds every product and sum separately
 # (no FMA contraction), as the reference's host arithmetic does
-UNIT_FLAGS = {"abundance": ["-fmad=false"]}
+UNIT_FLAGS = {"abundance": ["-fmad=false"], "recruit": ["-fmad=false"]}
 
 
 def _headers():

@@ -31,6 +31,15 @@ P = ctypes.c_void_p
 D = ctypes.c_double
 
 
+class RecruitStats(ctypes.Structure):
+    _fields_ = [("n_bins", u64), ("n_bins_scored", u64), ("n_leftovers", u64), ("n_leftovers_matched", u64),
+                ("n_small_matched", u64), ("binned_bases", u64), ("leftover_bases", u64), ("small_bases", u64),
+                ("leftovers_accepted", ctypes.c_int), ("small_accepted", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class FastaStats(ctypes.Structure):
     _fields_ = [("n_records", u64), ("n_large", u64), ("n_small", u64), ("ms_total", D)]
 
@@ -138,6 +147,7 @@ SIGNATURES = [
     ("mdet_tnf_count_dev", ctypes.c_int, [P, P, u64, P, P, u64, P, P]),
     ("mdet_tnf_count_noalloc", ctypes.c_int, [P, u64, P, P, u64, P, P, P]),
     ("mdet_ctx_check_wait", ctypes.c_int, [P, u64]),
+    ("mdet_recruit", ctypes.c_int, [P, P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, u64, P, P, P]),
     ("mdet_tnf_max_prob", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_max_prob_dev", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_ptnf_search", ctypes.c_int, [P, P, P, u64, D, ctypes.c_int, ctypes.POINTER(D)]),
@@ -429,6 +439,26 @@ class Context:
             raise ValueError("abd and var must be n x nabd matrices of the same shape")
         self._check(self.lib.mdet_ctx_set_abundance(self.h, P(abd.ctypes.data), P(var.ctypes.data), abd.shape[0],
                                                     abd.shape[1]))
+
+    def recruit(self, abd, small_abd, label, sizes, small_sizes, min_cls_size=200000, small_total=0):
+        """Dissolve small bins and recruit leftover and small contigs
+        (mdet_recruit).  abd: n x nabd, small_abd: n_small x nabd depths
+        (float); label: bin label of each large contig.  Returns (bin of
+        each large contig, bin of each small contig, stats); -1 = no bin."""
+        abd = np.ascontiguousarray(abd, np.float32)
+        n, nabd = abd.shape
+        small = np.ascontiguousarray(small_abd, np.float32).reshape(-1, nabd)
+        n1 = small.shape[0]
+        lab = np.ascontiguousarray(label, np.int64)
+        sz = np.ascontiguousarray(sizes, np.uint64)
+        ssz = np.ascontiguousarray(small_sizes, np.uint64)
+        out = np.zeros(n, np.int64)
+        sout = np.zeros(max(n1, 1), np.int64)
+        st = RecruitStats()
+        self._check(self.lib.mdet_recruit(self.h, _ptr(abd), _ptr(small), n, n1, nabd, _ptr(lab), _ptr(sz), _ptr(ssz),
+                                          int(min_cls_size), int(small_total), _ptr(out), _ptr(sout),
+                                          ctypes.byref(st)))
+        return out, sout[:n1], st.as_dict()
 
     def edges_sscr(self, from_, to, stnf, min_cv=1.0, min_sample=3):
         """sTNF -> sSCR of edges (host arrays) with the context's abundance."""

@@ -16,7 +16,11 @@ them into this repository:
   is_nz, cal_abd_corr and the sTNF -> sSCR block of main -- cut the same way
   into oracle/_ref/cuda2_abd.inc and compiled with the reference's own
   cuda/ranker.h behind oracle/ref_abd_shim.cpp (which stands in for Boost's
-  normal CDF) -> oracle/_ref/libref_abd.so.
+  normal CDF) -> oracle/_ref/libref_abd.so;
+* the dissolving of small bins and the recruiting of leftover and small
+  contigs (cuda/Cuda2.cu:2064-2283) with cal_abd_corr, cut the same way into
+  oracle/_ref/cuda2_recruit.inc and compiled with cuda/ranker.h behind
+  oracle/ref_recruit_shim.cpp -> oracle/_ref/libref_recruit.so.
 
 Only runs where the reference is mounted (MDET_REFERENCE or /root/reference).
 """
@@ -80,6 +84,17 @@ def extract_abd(src: str) -> str:
     return "\n\n".join(funcs) + "\n\n" + block
 
 
+def extract_recruit(src: str) -> str:
+    """cal_abd_corr and the block of main that groups the contigs into bins
+    after label propagation, dissolves the small bins and recruits leftover
+    and small contigs, wrapped as recruit_block(ClassMap&, mems)."""
+    corr = cut_block(src, "Distance cal_abd_corr(size_t r1, size_t r2, bool is_small = false) {")
+    a = src.index("        for (size_t i = 0; i < nobs; ++i) {\n            cls[mems[i]].push_back(i);")
+    b = src.index("        ABD.clear();", a)
+    block = ("static void recruit_block(ClassMap& cls, std::vector<size_t>& mems) {\n" + src[a:b] + "\n}\n")
+    return corr + "\n\n" + block
+
+
 def main() -> int:
     cuda2 = os.path.join(REF, "cuda", "Cuda2.cu")
     if not os.path.exists(cuda2):
@@ -104,6 +119,14 @@ def main() -> int:
         "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
         f"-I{OUT}", f"-I{os.path.join(REF, 'cuda')}", "-o", os.path.join(OUT, "libref_abd.so"),
         os.path.join(HERE, "ref_abd_shim.cpp"),
+    ])
+    inc = os.path.join(OUT, "cuda2_recruit.inc")
+    with open(inc, "w") as f:
+        f.write(extract_recruit(src))
+    subprocess.check_call([
+        "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp",
+        f"-I{OUT}", f"-I{os.path.join(REF, 'cuda')}", "-o", os.path.join(OUT, "libref_recruit.so"),
+        os.path.join(HERE, "ref_recruit_shim.cpp"),
     ])
     return 0
 

@@ -62,6 +62,7 @@ def lib():
         L.orc_tnf_topk_rows_nz.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int, P]
         L.orc_abd_low.argtypes = [P, u64, ctypes.c_uint32, P]
         L.orc_sscr.argtypes = [P, P, P, u64, P, P, ctypes.c_uint32, D, ctypes.c_uint32, P, ctypes.c_int]
+        L.orc_recruit.argtypes = [P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, u64, P, P, P]
         L.orc_fasta_index.restype = u64
         L.orc_fasta_index.argtypes = [P, u64, u64, P, P, P, P, P]
         _lib = L
@@ -208,3 +209,45 @@ def fasta_index(data):
     nl = np.zeros(cap, np.uint32)
     lib().orc_fasta_index(_p(data), data.size, cap, _p(so), _p(sl), _p(sz), _p(no), _p(nl))
     return so[:n], sl[:n], sz[:n], no[:n], nl[:n]
+
+
+REF_RECRUIT = os.path.join(HERE, "_ref", "libref_recruit.so")
+
+
+def _recruit_args(abd, small_abd, label, sizes, small_sizes):
+    abd = np.array(abd, np.float32, order="C", copy=True)  # ranked in place, as in the reference
+    n, nabd = abd.shape
+    small = np.array(small_abd, np.float32, order="C", copy=True).reshape(-1, nabd)
+    lab = np.ascontiguousarray(label, np.int64)
+    sz = np.ascontiguousarray(sizes, np.uint64)
+    ssz = np.ascontiguousarray(small_sizes, np.uint64)
+    assert lab.size == n and sz.size == n and ssz.size == small.shape[0]
+    return abd, small, lab, sz, ssz, n, small.shape[0], nabd
+
+
+def recruit(abd, small_abd, label, sizes, small_sizes, min_cls_size=200000, small_total=0):
+    """Dissolving small bins and recruiting leftover / small contigs
+    (orc_recruit).  Returns (bin of each large contig, bin of each small
+    contig, stats dict); -1 = no bin."""
+    abd, small, lab, sz, ssz, n, n1, nabd = _recruit_args(abd, small_abd, label, sizes, small_sizes)
+    out = np.zeros(n, np.int64)
+    sout = np.zeros(max(n1, 1), np.int64)
+    st = np.zeros(7, np.uint64)
+    lib().orc_recruit(_p(abd), _p(small), n, n1, nabd, _p(lab), _p(sz), _p(ssz), min_cls_size, small_total, _p(out),
+                      _p(sout), _p(st))
+    keys = ["bins", "bins_scored", "leftovers", "leftovers_matched", "small_matched", "leftovers_accepted",
+            "small_accepted"]
+    return out, sout[:n1], dict(zip(keys, (int(x) for x in st)))
+
+
+def ref_recruit(abd, small_abd, label, sizes, small_sizes, min_cls_size=200000, verbose=False):
+    """The reference's own block (oracle/_ref/libref_recruit.so, built where
+    the reference is mounted)."""
+    abd, small, lab, sz, ssz, n, n1, nabd = _recruit_args(abd, small_abd, label, sizes, small_sizes)
+    L = ctypes.CDLL(REF_RECRUIT)
+    L.ref_recruit.argtypes = [P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, ctypes.c_int, P, P]
+    out = np.zeros(n, np.int64)
+    sout = np.zeros(max(n1, 1), np.int64)
+    L.ref_recruit(_p(abd), _p(small), n, n1, nabd, _p(lab), _p(sz), _p(ssz), min_cls_size, 1 if verbose else 0,
+                  _p(out), _p(sout))
+    return out, sout[:n1]

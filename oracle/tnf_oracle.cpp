@@ -20,6 +20,7 @@
 #include "tnf_oracle.h"
 
 #include <algorithm>
+#include <map>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
@@ -672,6 +673,164 @@ void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint
         } else {
             sscr[e] = pow(raw[e], 1. - w) * pow(t, w);
         }
+    }
+}
+
+}  // extern "C"
+
+// ------------------------------------------------ leftover recruiting ----
+
+namespace {
+
+/* rank(rowMat, rowMat) on a float row (cuda/ranker.h:56-68, method
+ * "average"): 1-based ranks in ascending order; a run of equal values gets
+ * the mean of its ranks, formed in float as the reference's S = float. */
+void rank_average_f(float* v, uint32_t n) {
+    std::vector<uint32_t> ord(n);
+    std::iota(ord.begin(), ord.end(), 0u);
+    std::sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return v[a] < v[b]; });
+    std::vector<float> w(n);
+    for (uint32_t c = 0; c < n;) {
+        uint32_t k = 1;
+        while (c + k < n && v[ord[c]] == v[ord[c + k]]) ++k;
+        for (uint32_t q = 0; q < k; ++q) w[ord[c + q]] = (float)(2 * c + k - 1) / 2 + 1;
+        c += k;
+    }
+    std::copy(w.begin(), w.end(), v);
+}
+
+/* cal_abd_corr (cuda/Cuda2.cu:1219-1245) between row r1 of a and row r2 of b
+ * (float matrices, values read as double). */
+double corr_f(const float* a, const float* b, uint32_t nabd, uint64_t r1, uint64_t r2) {
+    double sxx = 0, syy = 0, sxy = 0, mx = 0, my = 0;
+    for (uint32_t i = 0; i < nabd; ++i) {
+        const double x = a[r1 * nabd + i], y = b[r2 * nabd + i];
+        if (i == 0) {
+            mx = x;
+            my = y;
+            continue;
+        }
+        const double ratio = i / (i + 1.0);
+        const double dx = x - mx, dy = y - my;
+        sxx += dx * dx * ratio;
+        syy += dy * dy * ratio;
+        sxy += dx * dy * ratio;
+        mx += dx / (i + 1.0);
+        my += dy / (i + 1.0);
+    }
+    return sxy / (sqrt(sxx) * sqrt(syy));
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Dissolving small bins and recruiting leftover and small contigs
+ * (cuda/Cuda2.cu:2064-2283, after label propagation).  Bins are the label
+ * groups of the large contigs, members in ascending index; a bin whose
+ * sizes sum below min_cls_size is dissolved and its members become
+ * leftovers.  The depth rows are replaced by their average ranks (Spearman).
+ * Bins with at least 10 members get the mean pairwise correlation of their
+ * members (cls_corr).  A leftover (a small contig) joins bin k when its mean
+ * correlation with the first 10 members, and then with all members, is at
+ * least cls_corr[k] -- and only when exactly one bin qualifies (the
+ * reference stops at a second one and keeps none).  The leftovers are added
+ * when their bases are under 10 % of the binned bases, the small contigs when
+ * theirs are under 15 % of small_total (the reference's totalSize1, which it
+ * only sums in verbose runs; 0 rejects every small recruit).  Out: the bin
+ * label of every large contig (-1: dissolved and not recruited) and of every
+ * small contig (-1: none).  stats: [0] kept bins, [1] scored bins,
+ * [2] leftovers, [3] leftovers matched, [4] smalls matched, [5] leftovers
+ * accepted, [6] smalls accepted.  abd and small_abd are overwritten by their
+ * ranks, as in the reference. */
+void orc_recruit(float* abd, float* small_abd, uint64_t n, uint64_t n1, uint32_t nabd, const int64_t* label,
+                 const uint64_t* sizes, const uint64_t* small_sizes, uint64_t min_cls_size, uint64_t small_total,
+                 int64_t* out, int64_t* small_out, uint64_t* stats) {
+    std::map<int64_t, std::vector<uint64_t>> cls;
+    for (uint64_t i = 0; i < n; ++i) cls[label[i]].push_back(i);
+    std::vector<uint64_t> leftovers;
+    for (auto it = cls.begin(); it != cls.end();) {
+        uint64_t s = 0;
+        for (uint64_t m : it->second) s += sizes[m];
+        if (s < min_cls_size) {
+            leftovers.insert(leftovers.end(), it->second.begin(), it->second.end());
+            it = cls.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    for (uint64_t i = 0; i < n; ++i) out[i] = -1;
+    for (uint64_t i = 0; i < n1; ++i) small_out[i] = -1;
+    for (auto& kv : cls)
+        for (uint64_t m : kv.second) out[m] = kv.first;
+    for (int k = 0; k < 7; ++k) stats[k] = 0;
+    stats[0] = cls.size();
+    stats[2] = leftovers.size();
+    if (leftovers.empty() && n1 == 0) return;
+    const size_t minCS = 10;
+    for (uint64_t r = 0; r < n; ++r) rank_average_f(abd + r * nabd, nabd);
+    uint64_t binned = 0;
+    for (auto& kv : cls)
+        for (uint64_t m : kv.second) binned += sizes[m];
+    std::map<int64_t, double> cls_corr;
+    for (auto& kv : cls) {
+        const auto& c = kv.second;
+        const size_t cs = c.size();
+        if (cs < minCS) continue;
+        double corr = 0;
+        for (size_t i = 0; i < cs; ++i)
+            for (size_t j = i + 1; j < cs; ++j) corr += corr_f(abd, abd, nabd, c[i], c[j]);
+        cls_corr[kv.first] = corr / (cs * (cs - 1) / 2);
+        ++stats[1];
+    }
+    // the bin a contig joins: the single qualifying bin, or -1
+    auto assign = [&](const float* other, uint64_t r) -> int64_t {
+        int64_t best = -1;
+        for (auto& kv : cls) {
+            const auto& c = kv.second;
+            const size_t cs = c.size();
+            if (cs < minCS) continue;
+            const double th = cls_corr[kv.first];
+            double corr = 0;
+            size_t i = 0;
+            for (; i < minCS; ++i) corr += corr_f(abd, other, nabd, c[i], r);
+            if (corr / minCS < th) continue;
+            for (; i < cs; ++i) corr += corr_f(abd, other, nabd, c[i], r);
+            corr /= cs;
+            if (corr >= th) {
+                if (best > -1) return -1;
+                best = kv.first;
+            }
+        }
+        return best;
+    };
+    std::vector<int64_t> lb(leftovers.size());
+    for (size_t l = 0; l < leftovers.size(); ++l) lb[l] = assign(abd, leftovers[l]);
+    std::vector<int64_t> sb(n1, -1);
+    if (n1 > 0) {
+        for (uint64_t r = 0; r < n1; ++r) rank_average_f(small_abd + r * nabd, nabd);
+        for (uint64_t s = 0; s < n1; ++s) sb[s] = assign(small_abd, s);
+    }
+    unsigned long long added = 0;
+    for (size_t l = 0; l < leftovers.size(); ++l)
+        if (lb[l] > -1) {
+            added += sizes[leftovers[l]];
+            ++stats[3];
+        }
+    if (added > 0 && (double)added / binned < .10) {
+        stats[5] = 1;
+        for (size_t l = 0; l < leftovers.size(); ++l)
+            if (lb[l] > -1) out[leftovers[l]] = lb[l];
+    }
+    added = 0;
+    for (uint64_t s = 0; s < n1; ++s)
+        if (sb[s] > -1) {
+            added += small_sizes[s];
+            ++stats[4];
+        }
+    if (added > 0 && (double)added / small_total < .15) {
+        stats[6] = 1;
+        for (uint64_t s = 0; s < n1; ++s) small_out[s] = sb[s];
     }
 }
 

@@ -319,12 +319,16 @@ def recruit_leg(ctx, a, run_cpu):
     tot = int(ssz.sum())
     ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
     ts = []
+    ctx.set_timing(True)
     for _ in range(3):
         t0 = time.perf_counter()
         out, sout, st = ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
         ts.append(time.perf_counter() - t0)
+    kms = {k: ctx.kernel_ms(k)[0] / 3 for k in ("k_rank_rows", "k_bin_corr", "k_recruit")}
+    ctx.set_timing(False)
     leg = {"metric": "dissolve + recruit time (host buffers)", "value": float(np.median(ts)), "unit": "s",
            "contigs": int(n), "small_contigs": ns, "samples": 10, **{k: int(v) for k, v in st.items()},
+           "kernels_ms": kms, "bound": "fp64 (the correlations and their sums in the reference's order)",
            "data": "synthetic depths (synth.abundance, seed 20240611), genome labels, 1 % singleton bins"}
     sub = np.arange(0, n, 10)
     s_abd, s_lab, s_sz = abd[sub], label[sub], sizes[sub]

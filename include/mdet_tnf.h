@@ -217,6 +217,21 @@ int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint
 int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,
                        double cutoff, uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to,
                        double* d_stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
+/* Row shard `shard` of `nshards` (0 <= shard < nshards) of the same graph,
+ * for one GPU each: the contigs in ascending log size are cut into nshards
+ * contiguous blocks on 256-row boundaries, and a shard emits the edges (i, j),
+ * i < j, of the rows i in its block, scored against all n contigs.  The
+ * shards' edge lists together are exactly the mdet_tnf_graph edge list (as
+ * when cuda/Cuda2.cu:888-891 deals row tiles to devices), so the only exchange
+ * is their concatenation.  TNF and log sizes are passed whole to every shard.
+ * PLAIN or BF16 form; max_edges <= 512. */
+int mdet_tnf_graph_shard(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                         uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* from,
+                         uint64_t* to, double* stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats);
+int mdet_tnf_graph_shard_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
+                             uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* d_from,
+                             uint64_t* d_to, double* d_stnf, uint64_t capacity, uint64_t* n_edges,
+                             mdet_graph_stats* stats);
 
 /* Exact-stage distance and probability of m given pairs (no counterpart in
  * the reference as an entry point): the arithmetic of cal_tnf_pre_dist_d

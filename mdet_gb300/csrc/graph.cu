@@ -370,6 +370,88 @@ int graph_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n
     return MDET_OK;
 }
 
+// Candidates of a rectangular pass (A row a = sorted position s0 + a, B
+// column c) compacted into pairs of sorted positions: the pair with itself
+// goes, and a pair of two rows of the shard is kept once (r < c); so every
+// unordered pair that touches the shard is scored exactly once.
+__global__ void k_shard_pairs(const uint2* __restrict__ in, unsigned long long nin, uint32_t s0, uint32_t s1,
+                              uint2* __restrict__ out, unsigned long long* __restrict__ nout) {
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < nin;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 p = in[i];
+        const uint32_t r = s0 + p.x, c = p.y;
+        if (c == r || (c >= s0 && c < s1 && c < r)) continue;
+        out[atomicAdd(nout, 1ull)] = make_uint2(r, c);
+    }
+}
+
+// Row shard `shard` of `nshards` (PLAIN or BF16): the contiguous block
+// [s0, s1) of the size-sorted rows (256-row boundaries) against all rows;
+// the edges emitted are those of the block's rows, so the shards' outputs
+// together are the whole graph (cuda/Cuda2.cu:888-891 splits row tiles over
+// devices the same way).
+int graph_shard_core(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff,
+                     uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, mdet_graph_stats* st,
+                     GraphPrep& g, uint64_t* total) {
+    if (mode != MDET_MODE_PLAIN && mode != MDET_MODE_BF16)
+        return ctx_fail(ctx, MDET_ERR_UNSUPPORTED, "row shards run the plain or BF16 form");
+    if (nshards == 0 || shard >= nshards) return ctx_fail(ctx, MDET_ERR_INVALID, "shard %u of %u", shard, nshards);
+    if (max_edges > 512) return ctx_fail(ctx, MDET_ERR_INVALID, "row shards need max_edges <= 512");
+    PhaseTimer tm(ctx->stream);
+    tm.mark();
+    MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, tc_kind(mode), &g));
+    MDET_TRY(abd_gate(ctx, g));
+    const uint64_t blocks = (n + 255) / 256;
+    const uint32_t s0 = (uint32_t)std::min<uint64_t>(n, blocks * shard / nshards * 256);
+    const uint32_t s1 = (uint32_t)std::min<uint64_t>(n, blocks * (shard + 1) / nshards * 256);
+    const double L = logit(cutoff);
+    DstarTable tbl;
+    MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl));
+    tm.mark();
+    uint2* cand = nullptr;
+    unsigned long long ncand = 0;
+    const uint32_t na = s1 - s0;
+    if (na) {
+        uint2* raw = nullptr;
+        unsigned long long nraw = 0;
+        MDET_TRY(run_filter(ctx, mode, g, true, g.x32 + (uint64_t)s0 * MDET_NTNF,
+                            mode == MDET_MODE_BF16 ? g.xa + (uint64_t)s0 * MDET_KPAD : nullptr,
+                            mode == MDET_MODE_BF16 ? g.nsq + s0 : nullptr, na,
+                            mode == MDET_MODE_BF16 ? g.meta + s0 / MDET_BLK : nullptr, g.meta32 + s0 / MDET_BLK, tbl,
+                            "sh", &raw, &nraw));
+        cand = (uint2*)ctx_scratch(ctx, "sh.pairs", (nraw ? nraw : 1) * sizeof(uint2));
+        unsigned long long* dn = (unsigned long long*)ctx_scratch(ctx, "sh.np", 8);
+        if (!cand || !dn) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cudaMemsetAsync(dn, 0, 8, ctx->stream));
+        if (nraw) {
+            const unsigned gb = (unsigned)std::min<unsigned long long>((nraw + 255) / 256, ctx->num_sms * 16ull);
+            k_shard_pairs<<<gb, 256, 0, ctx->stream>>>(raw, nraw, s0, s1, cand, dn);
+            MDET_LAUNCHED(ctx, "k_shard_pairs");
+        }
+        MDET_CUDA(ctx, cudaMemcpyAsync(&ncand, dn, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        MDET_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    tm.mark();
+    Edge* edges = nullptr;
+    unsigned long long ne = 0;
+    uint32_t* deg = nullptr;
+    MDET_TRY(exact_graph(ctx, g, cand, ncand, L, &edges, &ne, &deg));
+    tm.mark();
+    MDET_TRY(select_topk(ctx, g, edges, ne, deg, max_edges, total, nullptr, nullptr, s0, s1));
+    tm.mark();
+    if (st) {
+        st->n_candidates = ncand;
+        st->n_above_cutoff = ne;
+        st->tiles_total = st->tiles_computed = ((uint64_t)na + 127) / 128 * ((n + 255) / 256);
+        st->ms_prep = tm.ms(0, 1);
+        st->ms_filter = tm.ms(1, 2);
+        st->ms_exact = tm.ms(2, 3);
+        st->ms_select = tm.ms(3, 4);
+        st->tile_m_n = (uint32_t)ctx->last_tile_n;
+    }
+    return MDET_OK;
+}
+
 int validate_graph_args(mdet_ctx* ctx, uint64_t n, double cutoff, uint32_t max_edges, int mode) {
     if (!(cutoff > 0.0 && cutoff < 1.0)) return ctx_fail(ctx, MDET_ERR_INVALID, "cutoff must lie in (0, 1)");
     if (max_edges == 0 || max_edges > 4096) return ctx_fail(ctx, MDET_ERR_INVALID, "max_edges must be in [1, 4096]");
@@ -435,9 +517,18 @@ int maxprob_core(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* d_contigs, u
 
 extern "C" {
 
-int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
-                       uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to, double* d_stnf,
-                       uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats) {
+// The graph, or with nshards > 0 row shard `shard` of it (graph_shard_core).
+static int graph_select(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff,
+                        uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, mdet_graph_stats* st,
+                        GraphPrep& g, uint64_t* total) {
+    if (nshards) return graph_shard_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, mode, shard, nshards, st, g, total);
+    return graph_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, mode, st, g, total);
+}
+
+static int graph_dev_impl(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
+                          uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* d_from,
+                          uint64_t* d_to, double* d_stnf, uint64_t capacity, uint64_t* n_edges,
+                          mdet_graph_stats* stats) {
     if (!ctx || !n_edges) return MDET_ERR_INVALID;
     MDET_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->launches = 0;
@@ -452,7 +543,7 @@ int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_si
     cudaEventRecord(e0, ctx->stream);
     GraphPrep g;
     uint64_t total = 0;
-    int rc = graph_core(ctx, d_tnf, d_log_size, n, cutoff, max_edges, mode, stats, g, &total);
+    int rc = graph_select(ctx, d_tnf, d_log_size, n, cutoff, max_edges, mode, shard, nshards, stats, g, &total);
     if (rc == MDET_OK) {
         *n_edges = total;
         if (total > capacity)
@@ -478,9 +569,27 @@ int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_si
     return rc;
 }
 
-int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
-                   uint32_t max_edges, int mode, uint64_t* from, uint64_t* to, double* stnf, uint64_t capacity,
-                   uint64_t* n_edges, mdet_graph_stats* stats) {
+int mdet_tnf_graph_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
+                       uint32_t max_edges, int mode, uint64_t* d_from, uint64_t* d_to, double* d_stnf,
+                       uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats) {
+    return graph_dev_impl(ctx, d_tnf, d_log_size, n, cutoff, max_edges, mode, 0, 0, d_from, d_to, d_stnf, capacity,
+                          n_edges, stats);
+}
+
+int mdet_tnf_graph_shard_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n, double cutoff,
+                             uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* d_from,
+                             uint64_t* d_to, double* d_stnf, uint64_t capacity, uint64_t* n_edges,
+                             mdet_graph_stats* stats) {
+    if (!ctx) return MDET_ERR_INVALID;
+    if (nshards == 0) return ctx_fail(ctx, MDET_ERR_INVALID, "nshards must be at least 1");
+    return graph_dev_impl(ctx, d_tnf, d_log_size, n, cutoff, max_edges, mode, shard, nshards, d_from, d_to, d_stnf,
+                          capacity, n_edges, stats);
+}
+
+static int graph_host_impl(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                           uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* from,
+                           uint64_t* to, double* stnf, uint64_t capacity, uint64_t* n_edges,
+                           mdet_graph_stats* stats) {
     if (!ctx || !n_edges) return MDET_ERR_INVALID;
     MDET_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->launches = 0;
@@ -501,7 +610,7 @@ int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
-    int rc = graph_core(ctx, d_tnf, d_ls, n, cutoff, max_edges, mode, stats, g, &total);
+    int rc = graph_select(ctx, d_tnf, d_ls, n, cutoff, max_edges, mode, shard, nshards, stats, g, &total);
     if (rc == MDET_OK) {
         *n_edges = total;
         if (total > capacity) {
@@ -538,6 +647,22 @@ int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
+}
+
+int mdet_tnf_graph(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                   uint32_t max_edges, int mode, uint64_t* from, uint64_t* to, double* stnf, uint64_t capacity,
+                   uint64_t* n_edges, mdet_graph_stats* stats) {
+    return graph_host_impl(ctx, tnf, log_size, n, cutoff, max_edges, mode, 0, 0, from, to, stnf, capacity, n_edges,
+                           stats);
+}
+
+int mdet_tnf_graph_shard(mdet_ctx* ctx, const float* tnf, const double* log_size, uint64_t n, double cutoff,
+                         uint32_t max_edges, int mode, uint32_t shard, uint32_t nshards, uint64_t* from,
+                         uint64_t* to, double* stnf, uint64_t capacity, uint64_t* n_edges, mdet_graph_stats* stats) {
+    if (!ctx) return MDET_ERR_INVALID;
+    if (nshards == 0) return ctx_fail(ctx, MDET_ERR_INVALID, "nshards must be at least 1");
+    return graph_host_impl(ctx, tnf, log_size, n, cutoff, max_edges, mode, shard, nshards, from, to, stnf, capacity,
+                           n_edges, stats);
 }
 
 int mdet_tnf_pair_scores_dev(mdet_ctx* ctx, const float* d_tnf, const double* d_log_size, uint64_t n,

@@ -211,9 +211,11 @@ int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64
 // blk_K: optional per-256-row-block max_edges (each <= max_edges <= 512).
 // ne_dev: the edge count on the device (ne is then its cap); the total is
 // then left in the device outptr[n] and *n_out is 0.
+// keep0/keep1: only rows whose sorted position lies in [keep0, keep1) are
+// emitted (row shards; needs max_edges <= 512).
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
                 uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K = nullptr,
-                const unsigned long long* ne_dev = nullptr);
+                const unsigned long long* ne_dev = nullptr, uint32_t keep0 = 0, uint32_t keep1 = 0xFFFFFFFFu);
 int emit_topk(mdet_ctx* ctx, const GraphPrep& g, uint32_t max_edges, uint64_t* d_from, uint64_t* d_to,
               double* d_stnf, uint64_t total);
 

@@ -578,6 +578,15 @@ __global__ void __launch_bounds__(kSelWarps * 32) k_topk_sel(const unsigned long
 
 // Warp per original row: write its kept edges with ocol > row, in order.
 // compacted: the row starts with exactly those edges (selection top-k).
+// Rows (original index o) outside the sorted-position range [k0, k1) emit nothing.
+__global__ void k_keep_rows(const uint32_t* __restrict__ inv, uint32_t n, uint32_t k0, uint32_t k1,
+                            uint32_t* __restrict__ out_cnt) {
+    const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const uint32_t s = inv[o];
+    if (s < k0 || s >= k1) out_cnt[o] = 0;
+}
+
 __global__ void k_emit(const uint32_t* __restrict__ inv, const unsigned long long* __restrict__ rowptr,
                        const uint32_t* __restrict__ deg, const Ent* __restrict__ list,
                        const unsigned long long* __restrict__ outptr, uint32_t n, uint32_t max_edges, int compacted,
@@ -741,7 +750,8 @@ int pair_scores(mdet_ctx* ctx, const GraphPrep& g, const uint64_t* pairs, uint64
 }
 
 int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned long long ne, uint32_t* deg,
-                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K, const unsigned long long* ne_dev) {
+                uint32_t max_edges, uint64_t* n_out, const uint32_t* blk_K, const unsigned long long* ne_dev,
+                uint32_t keep0, uint32_t keep1) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = g.n;
     unsigned long long* rowptr = (unsigned long long*)ctx_scratch(ctx, "tk.rowptr", ((uint64_t)n + 1) * 8);
@@ -802,6 +812,11 @@ int select_topk(mdet_ctx* ctx, const GraphPrep& g, const Edge* edges, unsigned l
         k_topk_big<<<ctx->num_sms, 1024, kBigCap * sizeof(Ent), s>>>(big, nbig, rowptr, deg, g.perm, max_edges, list,
                                                                     out_cnt);
         MDET_LAUNCHED(ctx, "k_topk_big");
+    }
+    if (keep0 > 0 || keep1 < n) {
+        if (max_edges > 512) return ctx_fail(ctx, MDET_ERR_INVALID, "row shards need max_edges <= 512");
+        k_keep_rows<<<wblocks, 256, 0, s>>>(g.inv, n, keep0, keep1, out_cnt);
+        MDET_LAUNCHED(ctx, "k_keep_rows");
     }
     k_widen<<<wblocks, 256, 0, s>>>(out_cnt, n, w64);
     MDET_LAUNCHED(ctx, "k_widen");

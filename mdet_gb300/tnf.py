@@ -157,6 +157,10 @@ SIGNATURES = [
     ("mdet_tnf_graph_dev", ctypes.c_int,
      [P, P, P, u64, D, u32, ctypes.c_int, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
     ("mdet_tnf_pair_scores_dev", ctypes.c_int, [P, P, P, u64, P, u64, P, P]),
+    ("mdet_tnf_graph_shard", ctypes.c_int,
+     [P, P, P, u64, D, u32, ctypes.c_int, u32, u32, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
+    ("mdet_tnf_graph_shard_dev", ctypes.c_int,
+     [P, P, P, u64, D, u32, ctypes.c_int, u32, u32, P, P, P, u64, ctypes.POINTER(u64), ctypes.POINTER(GraphStats)]),
     ("mdet_tnf_graph_batched", ctypes.c_int, [P, ctypes.POINTER(Assembly), u32, ctypes.c_int,
                                               ctypes.POINTER(GraphStats)]),
     ("mdet_ctx_set_graph_capture", ctypes.c_int, [P, ctypes.c_int]),
@@ -360,6 +364,31 @@ class Context:
         if out is not None:
             return Graph(n, fr[:k], to[:k], st[:k], stats.as_dict())
         return Graph(n, fr[:k].copy(), to[:k].copy(), st[:k].copy(), stats.as_dict())
+
+    def tnf_graph_shard(self, tnf, log_size, cutoff, max_edges, mode, shard, nshards) -> Graph:
+        """Row shard `shard` of `nshards` of the graph (mdet_tnf_graph_shard):
+        the edges of the shard's block of size-sorted rows."""
+        tnf = np.ascontiguousarray(tnf, dtype=np.float32)
+        ls = np.ascontiguousarray(log_size, dtype=np.float64)
+        n = tnf.shape[0]
+        cap = max(1, ((n + nshards - 1) // nshards + 256) * max_edges)
+        fr, to, st = np.empty(cap, np.uint64), np.empty(cap, np.uint64), np.empty(cap, np.float64)
+        ne = u64(0)
+        stats = GraphStats()
+        self._check(self.lib.mdet_tnf_graph_shard(self.h, _ptr(tnf), _ptr(ls), n, float(cutoff), max_edges,
+                                                  MODES[mode], shard, nshards, _ptr(fr), _ptr(to), _ptr(st), cap,
+                                                  ctypes.byref(ne), ctypes.byref(stats)))
+        k = ne.value
+        return Graph(n, fr[:k].copy(), to[:k].copy(), st[:k].copy(), stats.as_dict())
+
+    def tnf_graph_shard_dev(self, d_tnf, d_ls, n, cutoff, max_edges, mode, shard, nshards, d_from, d_to, d_stnf,
+                            capacity):
+        ne = u64(0)
+        stats = GraphStats()
+        self._check(self.lib.mdet_tnf_graph_shard_dev(self.h, P(d_tnf), P(d_ls), n, float(cutoff), max_edges,
+                                                      MODES[mode], shard, nshards, P(d_from), P(d_to), P(d_stnf),
+                                                      capacity, ctypes.byref(ne), ctypes.byref(stats)))
+        return ne.value, stats.as_dict()
 
     def tnf_graph_dev(self, d_tnf, d_ls, n, cutoff, max_edges, mode, d_from, d_to, d_stnf, capacity):
         ne = u64(0)

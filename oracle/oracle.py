@@ -62,6 +62,8 @@ def lib():
         L.orc_tnf_topk_rows_nz.argtypes = [P, P, u64, D, ctypes.c_uint32, u64, u64, P, P, P, u64, ctypes.c_int, P]
         L.orc_abd_low.argtypes = [P, u64, ctypes.c_uint32, P]
         L.orc_sscr.argtypes = [P, P, P, u64, P, P, ctypes.c_uint32, D, ctypes.c_uint32, P, ctypes.c_int]
+        L.orc_tnf_graph_rows.restype = u64
+        L.orc_tnf_graph_rows.argtypes = [P, P, u64, D, ctypes.c_uint32, P, u64, P, P, P, u64, ctypes.c_int]
         L.orc_recruit.argtypes = [P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, u64, P, P, P]
         L.orc_fasta_index.restype = u64
         L.orc_fasta_index.argtypes = [P, u64, u64, P, P, P, P, P]
@@ -251,3 +253,15 @@ def ref_recruit(abd, small_abd, label, sizes, small_sizes, min_cls_size=200000, 
     L.ref_recruit(_p(abd), _p(small), n, n1, nabd, _p(lab), _p(sz), _p(ssz), min_cls_size, 1 if verbose else 0,
                   _p(out), _p(sout))
     return out, sout[:n1]
+
+
+def graph_rows(tnf, ls, cutoff, max_edges, rows, threads=0):
+    """The reference's graph edges (i < j) of the listed rows only."""
+    tnf = np.ascontiguousarray(tnf, np.float32)
+    ls = np.ascontiguousarray(ls, np.float64)
+    rows = np.ascontiguousarray(rows, np.uint64)
+    cap = max(1, rows.size * max_edges)
+    fr, to, st = np.zeros(cap, np.uint64), np.zeros(cap, np.uint64), np.zeros(cap, np.float64)
+    k = lib().orc_tnf_graph_rows(_p(tnf), _p(ls), tnf.shape[0], cutoff, max_edges, _p(rows), rows.size, _p(fr), _p(to),
+                                 _p(st), cap, threads)
+    return fr[:k], to[:k], st[:k]

@@ -381,6 +381,40 @@ uint64_t orc_tnf_graph_nz(const float* tnf, const double* logsize, uint64_t n, d
     return total;
 }
 
+/* gen_tnf_graph (cuda/Cuda2.cu:861-946) for a given list of rows only, in
+ * the order given: each row's heap over all n columns, then its i < j edges.
+ * A device's share of the reference's row tiles (888-891) is such a list. */
+uint64_t orc_tnf_graph_rows(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
+                            const uint64_t* rows, uint64_t nr, uint64_t* from, uint64_t* to, double* stnf,
+                            uint64_t cap, int threads) {
+    const double floor_cut = orc_logit_cutoff(cutoff);
+    std::vector<std::vector<std::pair<uint64_t, double>>> per_row(nr);
+    int nt = resolve_threads(threads);
+    (void)nt;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t r = 0; r < (int64_t)nr; ++r) {
+        const uint64_t i = rows[r];
+        EdgeHeap heap;
+        row_heap(tnf, logsize, n, floor_cut, max_edges, i, heap, nullptr);
+        while (!heap.empty()) {
+            std::pair<uint64_t, double> e = heap.top();
+            if (i < e.first) per_row[r].push_back(e);
+            heap.pop();
+        }
+    }
+    uint64_t total = 0;
+    for (uint64_t r = 0; r < nr; ++r)
+        for (auto& e : per_row[r]) {
+            if (total < cap) {
+                from[total] = rows[r];
+                to[total] = e.first;
+                stnf[total] = e.second;
+            }
+            ++total;
+        }
+    return total;
+}
+
 uint64_t orc_tnf_topk_rows(const float* tnf, const double* logsize, uint64_t n, double cutoff, uint32_t max_edges,
                            uint64_t row0, uint64_t row1, uint64_t* row_ptr, uint64_t* cols, double* sims, uint64_t cap,
                            int threads) {

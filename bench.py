@@ -297,6 +297,90 @@ def tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to
             "exact_stage": "shared with the BF16 and plain forms: same error statement (tests/test_gpu_error.py)"}
 
 
+def batch_leg(ctx, dev, count, nmin, nmax, seed):
+    """Many independent assemblies in one batched pass (mdet_tnf_graph_batched)
+    against one mdet_tnf_graph_dev call per assembly.  `count` assemblies with
+    n ~ logU(nmin, nmax) contigs and their own pools of clip(n/400, 20, 800)
+    Markov genomes (the workload generator, one seed per assembly), each
+    counted on the GPU from its FASTA (freed afterwards); cutoff 0.9,
+    maxEdges 200.  Per-assembly calls: 2 timed rounds; batched: the first call
+    (sizing, autotuning, CUDA-graph recording) untimed, then 3 timed replays.
+    Every assembly's batched edges are compared with its own call's on the
+    device."""
+    import torch
+
+    from mdet_gb300 import synth
+
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(nmin), np.log(nmax), count)).astype(np.int64)
+    genomes = np.clip(sizes // 400, 20, 800)
+    tnfs, lss = [], []
+    t0 = time.perf_counter()
+    for k, (n, G) in enumerate(zip(sizes, genomes)):
+        a = synth.generate(seed * 1000 + k, int(n), int(G))
+        nb = a.data.size
+        d_bytes = torch.empty(nb + 64, dtype=torch.uint8, device=dev)
+        d_bytes[:nb].copy_(torch.from_numpy(a.data))
+        d_off = torch.from_numpy(a.seq_off.astype(np.int64)).to(dev)
+        d_len = torch.from_numpy(a.seq_len.astype(np.int64)).to(dev)
+        d_cnt = torch.empty((int(n), 136), dtype=torch.int32, device=dev)
+        d_tnf = torch.empty((int(n), 136), dtype=torch.float32, device=dev)
+        ctx.tnf_count_dev(d_bytes.data_ptr(), nb, d_off.data_ptr(), d_len.data_ptr(), int(n), d_cnt.data_ptr(),
+                          d_tnf.data_ptr())
+        tnfs.append(d_tnf)
+        lss.append(torch.from_numpy(a.log_sizes).to(dev))
+        del d_bytes, d_cnt, d_off, d_len
+    torch.cuda.synchronize()
+    prep_s = time.perf_counter() - t0
+    K, cut = MAX_EDGES, 0.9
+    single = [[torch.empty(int(n) * K, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+              for n in sizes]
+    batch = [[torch.empty(int(n) * K, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+             for n in sizes]
+    ne_single = []
+    per_call = []
+    for rep in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ne_single = []
+        for t, l, n, o in zip(tnfs, lss, sizes, single):
+            ne, _ = ctx.tnf_graph_dev(t.data_ptr(), l.data_ptr(), int(n), cut, K, "bf16", o[0].data_ptr(),
+                                      o[1].data_ptr(), o[2].data_ptr(), int(n) * K)
+            ne_single.append(ne)
+        torch.cuda.synchronize()
+        if rep:  # the first round tunes the shape classes
+            per_call.append(time.perf_counter() - t0)
+    items = [dict(d_tnf=t.data_ptr(), d_ls=l.data_ptr(), n=int(n), cutoff=cut, max_edges=K, d_from=o[0].data_ptr(),
+                  d_to=o[1].data_ptr(), d_stnf=o[2].data_ptr(), capacity=int(n) * K)
+             for t, l, n, o in zip(tnfs, lss, sizes, batch)]
+    r0 = ctx.graph_replays()
+    t0 = time.perf_counter()
+    res, st = ctx.tnf_graph_batched(items, mode="bf16")
+    torch.cuda.synchronize()
+    first_s = time.perf_counter() - t0
+    reps = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, st = ctx.tnf_graph_batched(items, mode="bf16")
+        torch.cuda.synchronize()
+        reps.append(time.perf_counter() - t0)
+    equal = all(s == 0 and ne == ns and torch.equal(b[0][:ne], o[0][:ne]) and torch.equal(b[1][:ne], o[1][:ne])
+                and torch.equal(b[2][:ne], o[2][:ne])
+                for (s, ne), ns, b, o in zip(res, ne_single, batch, single))
+    per_assembly_s = float(np.median(per_call))
+    batched_s = float(np.median(reps))
+    out = {"assemblies": int(count), "contigs": int(sizes.sum()), "n_range": [int(nmin), int(nmax)],
+           "sum_n2": float((sizes.astype(np.float64) ** 2).sum()), "edges": int(sum(ne_single)),
+           "per_assembly_calls_s": per_assembly_s, "batched_replay_s": batched_s, "batched_first_call_s": first_s,
+           "gain": per_assembly_s / batched_s, "replays": int(ctx.graph_replays() - r0),
+           "gpu_launches_per_replay": int(st["gpu_launches"]), "edges_equal_single_calls": bool(equal),
+           "prep_s": prep_s}
+    del tnfs, lss, single, batch
+    torch.cuda.empty_cache()
+    return out
+
+
 def recruit_leg(ctx, a, run_cpu):
     """Dissolving small bins and recruiting leftover and small contigs
     (mdet_recruit) after binning the step's assembly: labels are the contigs'
@@ -621,6 +705,7 @@ def run_ours(args):
             parity_info["shard_edges"] = info["shard_edges"]
             del full_f, full_t, full_s
             args.no_fasta = args.no_abd = args.no_plain = args.no_recruit = args.no_tf32 = args.no_cpu = True
+            args.no_batch = True
         else:
             # the host-buffer (e2e) graph equals the device-resident one
             parity_info["e2e_graph_equals_device_graph"] = bool(
@@ -649,6 +734,11 @@ def run_ours(args):
                 and torch.equal(o_st[:ne], d_st[:ne]))
         if not args.no_recruit:
             result["recruit"] = recruit_leg(ctx, a, not args.no_cpu and ws == 1)
+        if not args.no_batch:
+            # SURVEY config 4 (64 assemblies of 5k-300k contigs) and the case the
+            # batch is for: many small assemblies, where per-call overhead rules
+            result["batched"] = {"config4": batch_leg(ctx, dev, 64, 5000, 300000, 41),
+                                 "small_assemblies": batch_leg(ctx, dev, 256, 1000, 20000, 42)}
         if not args.no_tf32 and args.mode == "bf16":
             result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,
                                       pk, pk_kind)
@@ -891,6 +981,7 @@ def main():
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
     ap.add_argument("--no-tf32", action="store_true", help="skip the TF32 graph leg")
     ap.add_argument("--no-recruit", action="store_true", help="skip the dissolve / recruit leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-assemblies legs")
     ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
                     help="run one single-stage case instead of the benchmark (profiler workloads)")
     ap.add_argument("--samples", type=int, default=10)

@@ -89,6 +89,9 @@ struct mdet_ctx {
     } prep_cache;
     // copy streams of the host-buffer entry points (created on first use)
     cudaStream_t io_in = nullptr, io_out = nullptr;
+    // stream CUDA-graph recordings are captured on (the caller's stream may be
+    // the legacy default stream, which cannot be captured)
+    cudaStream_t cap_stream = nullptr;
     // abundance set by mdet_ctx_set_abundance: contigs and samples (the
     // matrices and per-contig low flags live in scratch "abd.m", "abd.v",
     // "abd.low"); nabd == 0: none

@@ -298,6 +298,7 @@ int mdet_ctx_destroy(mdet_ctx* ctx) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     if (ctx->io_in) cudaStreamDestroy(ctx->io_in);
     if (ctx->io_out) cudaStreamDestroy(ctx->io_out);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     delete ctx;
     return MDET_OK;
 }

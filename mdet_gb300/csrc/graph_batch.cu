@@ -319,14 +319,22 @@ BatchPlan* record(mdet_ctx* ctx, const mdet_assembly* as, const Layout& L, int m
     int rc = device_pass(ctx, as, L, mode, d, nlist, shape, np->cand_cap);
     if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaStreamSynchronize(s), "sizing pass");
     cudaGraph_t graph = nullptr;
+    // the recording is captured on the context's own capture stream: the
+    // caller's stream may be the legacy default stream, which cannot be
+    // captured; the graph is launched on the caller's stream later
+    if (rc == MDET_OK && !ctx->cap_stream)
+        rc = ctx_cuda(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking), "capture stream");
     if (rc == MDET_OK) {
         const uint32_t l0 = ctx->launches;
-        rc = ctx_cuda(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+        const cudaStream_t cs = ctx->cap_stream;
+        rc = ctx_cuda(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
         if (rc == MDET_OK) {
             ctx->capturing = true;
+            ctx->stream = cs;
             const int crc = device_pass(ctx, as, L, mode, d, nlist, shape, np->cand_cap);
+            ctx->stream = s;
             ctx->capturing = false;
-            const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
             if (crc == MDET_OK && ce == cudaSuccess && graph) {
                 rc = ctx_cuda(ctx, cudaGraphInstantiate(&np->exec, graph, 0), "graph instantiate");
                 np->launches = ctx->launches - l0;

@@ -118,6 +118,33 @@ def test_recorded_batch_replays_with_new_data(gpu_ctx, batch_inputs):
         torch.cuda.synchronize()
 
 
+def test_replays_on_the_legacy_default_stream(batch_inputs):
+    """A context whose stream is the legacy default stream (what a caller
+    handing over torch's default stream gives it) still records the batch --
+    on its own capture stream -- and replays it on the caller's stream."""
+    import torch
+
+    import mdet_gb300 as m
+
+    with m.Context(0) as ctx:
+        ctx.set_stream(0)
+        outs, items = [], []
+        for x in batch_inputs:
+            o = _outputs(torch, x["n"], x["max_edges"])
+            outs.append(o)
+            items.append(dict(d_tnf=x["d_tnf"].data_ptr(), d_ls=x["d_ls"].data_ptr(), n=x["n"], cutoff=x["cutoff"],
+                              max_edges=x["max_edges"], d_from=o[0].data_ptr(), d_to=o[1].data_ptr(),
+                              d_stnf=o[2].data_ptr(), capacity=o[3]))
+        singles = [_single(ctx, torch, x, "bf16") for x in batch_inputs]
+        r0 = ctx.graph_replays()
+        for call in range(3):
+            res, _ = ctx.tnf_graph_batched(items, mode="bf16")
+            for (status, ne), o, (f, t, st) in zip(res, outs, singles):
+                assert status == 0 and ne == f.size
+                assert np.array_equal(o[0][:ne].cpu().numpy(), f) and np.array_equal(o[2][:ne].cpu().numpy(), st)
+        assert ctx.graph_replays() == r0 + 2
+
+
 def test_batch_capacity_shortfall(gpu_ctx, batch_inputs):
     import torch
 

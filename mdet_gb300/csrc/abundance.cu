@@ -7,8 +7,10 @@
 // Layout: the context keeps the reference's ABD (mean depth) and ABD_VAR
 // (variance) as n x nabd row-major FP64 matrices in the original contig order,
 // plus one byte per contig that says whether none of its depths exceeds 1.
-// sSCR runs one thread per edge over its nabd samples (FP64: the normal CDFs
-// need erfc/log at double precision), then three radix sorts (the abundance
+// sSCR runs one thread per edge over its nabd samples -- the crossing points
+// of the two normal densities in FP64 as the reference forms them, the four
+// normal CDFs per sample in float-float from this project's erfc table --
+// then three radix sorts (the abundance
 // similarities, sTNF and the depth correlations) turn values into ranks and
 // the ranks into quantiles of the similarity distribution.
 //
@@ -17,9 +19,47 @@
 // pick quantiles -- come out bit-identical to a host evaluation.
 #include <cub/cub.cuh>
 
+#include "erfc_table.cuh"
 #include "graph.cuh"
 
 namespace {
+
+// erfc in float-float from this project's own table (erfc_table.cuh,
+// generated by gen_erfc_table.py): degree-13 interpolants on 26 pieces of
+// [0, 6.5], absolute error ~5e-16 before the float-float evaluation; 0
+// beyond 6.5 (erfc < 4e-20 there); erfc(-z) = 2 - erfc(z).  The FP32 pipes
+// run this far faster than the FP64 pipe runs the double erfc.
+__device__ __forceinline__ ff erfc_ff(ff z) {
+    const bool neg = z.hi < 0.f;
+    if (neg) z = ff_neg(z);
+    ff r;
+    if (!(z.hi < 6.5f)) {
+        r = ff_make(0.f, 0.f);  // NaN arguments land here too
+        if (z.hi != z.hi) return z;
+    } else {
+        const int p = min((int)(z.hi * 4.f), MDET_ERFC_PIECES - 1);
+        // u = (z - centre) * 8, exact scaling of an exact difference
+        ff u = ff_add_f(z, -((float)p + 0.5f) * 0.25f);
+        u.hi *= 8.f;
+        u.lo *= 8.f;
+        const float(*c)[2] = kErfcTable[p];
+        r = ff_make(__ldg(&c[MDET_ERFC_DEG][0]), __ldg(&c[MDET_ERFC_DEG][1]));
+#pragma unroll
+        for (int j = MDET_ERFC_DEG - 1; j >= 0; --j)
+            r = ff_add(ff_mul(r, u), ff_make(__ldg(&c[j][0]), __ldg(&c[j][1])));
+    }
+    return neg ? ff_add_f(ff_neg(r), 2.f) : r;
+}
+
+// Boost's normal CDF, erfc(-(x - mean) / (sd * sqrt(2))) / 2 (the function
+// the reference calls), with x - mean formed in FP64 as the reference forms
+// it and the rest in float-float; returned in double.
+__device__ __forceinline__ double normal_cdf_ff(double mean, double sd, double x) {
+    const ff diff = ff_from_double(x - mean);
+    const ff den = ff_mul(ff_from_double(sd), ff_make(0x1.6a09e6p+0f, 0x1.9fcef4p-26f));  // sqrt(2)
+    const ff z = ff_mul(diff, ff_recip(den));
+    return ff_to_double(erfc_ff(ff_neg(z))) * 0.5;
+}
 
 __global__ void k_abd_low(const double* __restrict__ abd, uint64_t n, uint32_t nabd, uint8_t* __restrict__ low) {
     for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
@@ -35,16 +75,12 @@ __global__ void k_low_sorted(const uint32_t* __restrict__ perm, const uint8_t* _
         out[s] = low[perm[s]];
 }
 
-// CDF of the normal distribution N(mean, sd^2) as Boost.Math defines it for
-// normal_distribution (the function the reference calls):
-// erfc(-(x - mean) / (sd * sqrt(2))) / 2.
-__device__ double normal_cdf(double mean, double sd, double x) {
-    const double z = (x - mean) / (sd * 1.4142135623730951);
-    return erfc(-z) / 2;
-}
 
 // Overlap of two normal densities from their crossing points k1 <= k2, the
-// narrower distribution evaluated first (cal_abd_dist2).
+// narrower distribution evaluated first (cal_abd_dist2).  The crossing
+// points come from a numerator that cancels when the variances are close, so
+// they are formed in FP64 in the reference's order (bit-identical); the four
+// CDF values, the bulk of the work, run in float-float.
 __device__ double abd_dist2(double m1, double s1, double m2, double s2) {
     const double v1 = s1 * s1, v2 = s2 * s2;
     double k1, k2;
@@ -67,8 +103,8 @@ __device__ double abd_dist2(double m1, double s1, double m2, double s2) {
         mb = m1;
         sb = s1;
     }
-    if (k1 == k2) return fabs(normal_cdf(ma, sa, k1) - normal_cdf(mb, sb, k1));
-    return fabs(normal_cdf(ma, sa, k2) - normal_cdf(ma, sa, k1) + normal_cdf(mb, sb, k1) - normal_cdf(mb, sb, k2));
+    if (k1 == k2) return fabs(normal_cdf_ff(ma, sa, k1) - normal_cdf_ff(mb, sb, k1));
+    return fabs(normal_cdf_ff(ma, sa, k2) - normal_cdf_ff(ma, sa, k1) + normal_cdf_ff(mb, sb, k1) - normal_cdf_ff(mb, sb, k2));
 }
 
 struct ScoreArgs {

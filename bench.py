@@ -297,6 +297,71 @@ def tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to
             "exact_stage": "shared with the BF16 and plain forms: same error statement (tests/test_gpu_error.py)"}
 
 
+def learned_leg(ctx, dev, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, st_bf16):
+    """The learned proposal on the step's assembly: the 136-256-128-64 network
+    trained on a second, separately generated assembly (200,000 contigs from
+    400 genomes, seed 4) with 50M pairs labelled by the exact kernel, then 1
+    untimed and 2 timed learned graphs of the step's cutoff (embedding-major
+    order, runs of 1,024), their edges compared as sets with the BF16 graph
+    (recall, precision) and their time with the BF16 graph's."""
+    import torch
+
+    import mdet_gb300 as m
+    from mdet_gb300 import synth
+
+    tn, tg = 200_000, 400
+    b = synth.generate(4, tn, tg)
+    tb = torch.zeros(b.data.size + 64, dtype=torch.uint8, device=dev)
+    tb[:b.data.size].copy_(torch.from_numpy(b.data))
+    t_off = torch.from_numpy(b.seq_off.astype(np.int64)).to(dev)
+    t_len = torch.from_numpy(b.seq_len.astype(np.int64)).to(dev)
+    t_tnf = torch.empty((tn, 136), dtype=torch.float32, device=dev)
+    t_cnt = torch.empty((tn, 136), dtype=torch.int32, device=dev)
+    ctx.tnf_count_dev(tb.data_ptr(), b.data.size, t_off.data_ptr(), t_len.data_ptr(), tn, t_cnt.data_ptr(),
+                      t_tnf.data_ptr())
+    t_ls = torch.from_numpy(b.log_sizes).to(dev)
+    torch.cuda.synchronize()
+    del tb, t_cnt
+    net = m.Network(ctx, seed=5)
+    t0 = time.perf_counter()
+    rep = net.train_dev(t_tnf.data_ptr(), t_ls.data_ptr(), tn, steps=3000, pairs=50_000_000)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del t_tnf, t_ls
+    lr = ctx.set_learned(net, segment=1024, order=0)
+    args = (d_tnf.data_ptr(), d_ls.data_ptr(), n, cut, MAX_EDGES, "learned", o_from.data_ptr(), o_to.data_ptr(),
+            o_st.data_ptr(), cap)
+    ctx.tnf_graph_dev(*args)
+    ms, sts = [], []
+    for _ in range(2):
+        ne_l, st = ctx.tnf_graph_dev(*args)
+        ms.append(st["ms_total"])
+        sts.append(dict(lr.as_dict()))
+    ctx.set_learned(None)
+    net.close()
+    ref = d_from[:ne] * n + d_to[:ne]
+    got = o_from[:ne_l] * n + o_to[:ne_l]
+    common = int(torch.isin(got, ref).sum())
+    # edges present in both carry the same score (one exact stage scores both)
+    same_scores = bool(common == ne == ne_l and torch.equal(torch.sort(got)[0], torch.sort(ref)[0]))
+    lrep = sts[-1]
+    value = float(np.median(ms)) / 1e3
+    return {"metric": "1M-contig TNF graph time, learned proposal", "value": value, "unit": "s",
+            "bf16_graph_s": st_bf16["ms_total"] / 1e3, "speedup_vs_bf16": st_bf16["ms_total"] / 1e3 / value,
+            "recall": common / max(1, ne), "precision": common / max(1, ne_l), "edge_set_equals_bf16": same_scores,
+            "estimated_recall": lrep["recall"], "fell_back": bool(lrep["fell_back"]),
+            "tiles_total": int(st["tiles_total"]), "tiles_skipped": int(lrep["tiles_skipped"]),
+            "tiles_skipped_frac": lrep["tiles_skipped"] / max(1, st["tiles_total"]),
+            "candidates": int(st["n_candidates"]), "bf16_candidates": int(st_bf16["n_candidates"]),
+            "phases_ms": {"embed": lrep["ms_embed"], "order_and_prep": lrep["ms_order"],
+                          "calibration_and_tile_flags": lrep["ms_sample"], "filter": st["ms_filter"],
+                          "exact": st["ms_exact"], "select": st["ms_select"]},
+            "tau": lrep["tau"],
+            "training": {"assembly": f"{tn} contigs, {tg} genomes, seed 4", "train_s": train_s,
+                         **{k: rep[k] for k in ("steps", "pairs", "candidate_pairs", "held_pos", "held_neg",
+                                                "final_loss", "tau", "pos_median", "neg_median", "neg_below_tau")}}}
+
+
 def batch_leg(ctx, dev, count, nmin, nmax, seed):
     """Many independent assemblies in one batched pass (mdet_tnf_graph_batched)
     against one mdet_tnf_graph_dev call per assembly.  `count` assemblies with
@@ -705,6 +770,7 @@ def run_ours(args):
             parity_info["shard_edges"] = info["shard_edges"]
             del full_f, full_t, full_s
             args.no_fasta = args.no_abd = args.no_plain = args.no_recruit = args.no_tf32 = args.no_cpu = True
+            args.no_learned = True
             args.no_batch = True
         else:
             # the host-buffer (e2e) graph equals the device-resident one
@@ -742,6 +808,9 @@ def run_ours(args):
         if not args.no_tf32 and args.mode == "bf16":
             result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,
                                       pk, pk_kind)
+        if not args.no_learned and args.mode == "bf16":
+            result["learned"] = learned_leg(ctx, dev, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from,
+                                            d_to, st)
         if not args.no_cpu and ws == 1:
             tnf_host = d_tnf.cpu().numpy()
             base, (R, rows) = cpu_baseline(a, tnf_host, n, cut, keep_rows=True)
@@ -832,18 +901,29 @@ def run_case(args):
         del tb, t_cnt
         net = m.Network(ctx, seed=5)
         t0 = time.time()
-        rep = net.train_dev(t_tnf.data_ptr(), t_ls.data_ptr(), args.train_n, steps=args.train_steps)
+        rep = net.train_dev(t_tnf.data_ptr(), t_ls.data_ptr(), args.train_n, steps=args.train_steps,
+                            pairs=args.train_pairs)
         print({"train_s": round(time.time() - t0, 2), **rep})
         cap = args.n * 200
         out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
-        runs = [("bf16", 0)] + [("learned", int(x)) for x in args.segs.split(",") for _ in range(2)] + [("bf16", 0)]
-        for mode, seg in runs:
-            lr = ctx.set_learned(net, segment=seg)
+        # --segs entries "ORDER:SEG" (order 0 embedding-major, 1 size-major)
+        variants = [tuple(int(v) for v in x.split(":")) if ":" in x else (0, int(x)) for x in args.segs.split(",")]
+        runs = [("bf16", 0, 0)] + [("learned", o, sg) for o, sg in variants for _ in range(2)] + [("bf16", 0, 0)]
+        ref = None
+        for mode, order, seg in runs:
+            lr = ctx.set_learned(net, segment=seg, order=order)
             ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, mode,
                                        out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+            keys = torch.sort(out[0][:ne] * args.n + out[1][:ne])[0]
             extra = lr.as_dict() if mode == "learned" else {}
+            if ref is None:
+                ref = keys.clone()
+            else:
+                common = int(torch.isin(keys, ref).sum())
+                extra.update(recall=common / max(1, ref.numel()), precision=common / max(1, ne))
             print({"mode": mode, "edges": ne, **{k: round(v, 3) if isinstance(v, float) else v
-                                                 for k, v in st.items()}, **extra})
+                                                 for k, v in st.items()},
+                   **{k: round(v, 4) if isinstance(v, float) else v for k, v in extra.items()}}, flush=True)
     if args.case == "abd":
         del d_bytes, d_cnt
         torch.cuda.empty_cache()
@@ -980,6 +1060,7 @@ def main():
     ap.add_argument("--no-abd", action="store_true", help="skip the sTNF -> sSCR leg")
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
     ap.add_argument("--no-tf32", action="store_true", help="skip the TF32 graph leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal graph leg")
     ap.add_argument("--no-recruit", action="store_true", help="skip the dissolve / recruit leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-assemblies legs")
     ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
@@ -990,7 +1071,10 @@ def main():
     ap.add_argument("--nmax", type=int, default=300000)
     ap.add_argument("--train-n", type=int, default=200000)
     ap.add_argument("--train-steps", type=int, default=3000)
-    ap.add_argument("--segs", default="1024", help="comma-separated size-sorted run lengths to try (learned case)")
+    ap.add_argument("--train-pairs", type=int, default=50_000_000)
+    ap.add_argument("--segs", default="0:1024,1:16384",
+                    help="comma-separated ORDER:SEG contig orders to try (learned case): order 0 embedding-major "
+                         "with size-sorted runs of SEG, order 1 size bands of SEG")
     ap.add_argument("--cutoff", type=float, default=0.95)
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()

@@ -342,12 +342,16 @@ typedef struct {
 typedef struct {
     double recall_target;      /* fall back to all pairs below this estimated recall (0: 0.999) */
     uint32_t recall_rows;      /* rows sampled to calibrate tau and estimate recall (0: 2048) */
-    uint32_t segment;          /* contigs per size-sorted run of the embedding order (0: 1024; 1: none) */
+    uint32_t segment;          /* order 0: contigs per size-sorted run of the embedding order (0: 1024;
+                                  1: none); order 1: contigs per size band (0: 16384) */
     double recall;             /* out: estimated edge recall of the learned graph */
     uint32_t fell_back;        /* out: 1 when the all-pairs graph was returned */
-    uint32_t reserved;
+    uint32_t order;            /* 0: embedding-major Morton order (7 principal axes + log size);
+                                  1: size-major (size bands, 8 principal axes within a band) */
     uint64_t tiles_skipped;    /* out: 128 x 256 tiles skipped */
     double tau;                /* out: embedded-distance margin used */
+    double ms_embed, ms_order, ms_sample; /* out: network pass; order + row preparation; sampled-row
+                                  calibration, tile flags and recall estimate (device time) */
 } mdet_learned_report;
 
 int mdet_mlp_create(mdet_ctx* ctx, uint64_t seed, mdet_mlp** out);

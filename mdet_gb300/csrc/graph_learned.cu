@@ -1,7 +1,9 @@
 // graph_learned.cu -- MDET_MODE_LEARNED: the TNF graph with the learned
 // proposal.  The network embeds every contig (64 dims); contigs are ordered
-// along a Morton curve over the leading principal axes of the embedding and
-// their log size, so that 128-row blocks gather similar contigs; each tile
+// along a Morton curve over the leading principal axes of the embedding --
+// either embedding-major (7 axes and the log size, then runs re-sorted by
+// size) or size-major (size-sorted bands, 8 axes within a band) -- so that
+// 128-row blocks gather similar contigs; each tile
 // pair (128-row block I, 256-row block J) is kept when the triangle bound
 // ||c_I - c_J|| - r_I - r_J on embedded distances is within the trained
 // margin tau.  The kept tiles go through the same tensor-core filter and
@@ -24,31 +26,55 @@ using namespace mdet_exact;
 
 namespace {
 
-constexpr int kPcs = 7;           // principal axes in the Morton key (+ log size)
+constexpr int kPcs = 8;           // principal axes projected (the Morton key's dimensions)
 constexpr int kFlagGroup = 8;     // row tiles per thread in the tile-flag kernel
+constexpr uint32_t kBandRows = 16384;  // default band of the size-major order
 
-// Morton key of one contig: 8 bits each of kPcs principal coordinates and of
-// the log size, interleaved most significant bit first; the log size takes
-// the lowest position of each bit level.
+// Morton key of one contig: 8 bits each of 8 coordinates, interleaved most
+// significant bit first.  with_size: the 7 leading principal coordinates and
+// the log size (which takes the lowest position of each bit level); else the
+// 8 leading principal coordinates.
 __global__ void k_morton(const float* __restrict__ proj, const double* __restrict__ ls, uint64_t n,
                          const float* __restrict__ off, const float* __restrict__ inv_span, float ls0, float ls_inv,
-                         unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
+                         int with_size, unsigned long long* __restrict__ keys, uint32_t* __restrict__ vals) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    uint32_t q[kPcs + 1];
+    uint32_t q[kPcs];
 #pragma unroll
     for (int d = 0; d < kPcs; ++d) {
         const float u = (proj[i * kPcs + d] - off[d]) * inv_span[d];
         q[d] = (uint32_t)fminf(fmaxf(u * 256.f, 0.f), 255.f);
     }
-    q[kPcs] = (uint32_t)fminf(fmaxf(((float)ls[i] - ls0) * ls_inv * 256.f, 0.f), 255.f);
+    if (with_size) q[kPcs - 1] = (uint32_t)fminf(fmaxf(((float)ls[i] - ls0) * ls_inv * 256.f, 0.f), 255.f);
     unsigned long long key = 0;
 #pragma unroll
     for (int b = 7; b >= 0; --b)
 #pragma unroll
-        for (int d = 0; d <= kPcs; ++d) key = (key << 1) | ((q[d] >> b) & 1u);
+        for (int d = 0; d < kPcs; ++d) key = (key << 1) | ((q[d] >> b) & 1u);
     keys[i] = key;
     vals[i] = (uint32_t)i;
+}
+
+// size sort key: the log size's float bits (non-negative floats order as
+// their bit patterns)
+__global__ void k_size_keys(const double* __restrict__ ls, uint64_t n, unsigned long long* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = __float_as_uint(fmaxf((float)ls[i], 0.f));
+    vals[i] = (uint32_t)i;
+}
+
+// size-major key: band of the size order (16 bits) above the top 48 bits of
+// the embedding's Morton key
+__global__ void k_band_keys(const uint32_t* __restrict__ by_size, const unsigned long long* __restrict__ morton,
+                            uint64_t n, uint32_t band, unsigned long long* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+    const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t o = by_size[p];
+    keys[p] = ((unsigned long long)(p / band) << 48) | (morton[o] >> 16);
+    vals[p] = o;
 }
 
 // Centroid and radius (in embedding space) of each block of `rows` prepared
@@ -279,12 +305,14 @@ struct PhaseClock {
     }
 };
 
-// Embeds the contigs and returns the Morton order (original index per
-// position) in `order`.
-int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const double* d_ls, uint64_t n, float* z,
-                  uint32_t seg, uint32_t* order) {
+// The order of the embedded contigs z (original index per position) in
+// `order`: size_major 0 -- Morton over 7 principal axes and the log size,
+// then runs of `seg` positions re-sorted by size (seg <= 1: none);
+// size_major 1 -- size-sorted bands of `seg` contigs, Morton over 8 principal
+// axes within each band.
+int learned_order(mdet_ctx* ctx, const double* d_ls, uint64_t n, const float* z, int size_major, uint32_t seg,
+                  uint32_t* order) {
     cudaStream_t s = ctx->stream;
-    MDET_TRY(mlp_embed(ctx, net->params, d_tnf, n, z));
     // principal axes of the embedding: C = Z^T Z / n - mu mu^T
     float* G = (float*)ctx_scratch(ctx, "lrn.gram", MLP_OUT * MLP_OUT * 4);
     float* colsum = (float*)ctx_scratch(ctx, "lrn.colsum", MLP_OUT * 4);
@@ -293,8 +321,9 @@ int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const 
     float* proj = (float*)ctx_scratch(ctx, "lrn.proj", n * kPcs * 4);
     unsigned long long* keys = (unsigned long long*)ctx_scratch(ctx, "lrn.keys", n * 8);
     unsigned long long* keys2 = (unsigned long long*)ctx_scratch(ctx, "lrn.keys2", n * 8);
+    unsigned long long* keys3 = (unsigned long long*)ctx_scratch(ctx, "lrn.keys3", n * 8);
     uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "lrn.vals", n * 4);
-    if (!G || !colsum || !V || !off || !proj || !keys || !keys2 || !vals) return MDET_ERR_NOMEM;
+    if (!G || !colsum || !V || !off || !proj || !keys || !keys2 || !keys3 || !vals) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cudaMemsetAsync(G, 0, MLP_OUT * MLP_OUT * 4, s));
     MDET_CUDA(ctx, cudaMemsetAsync(colsum, 0, MLP_OUT * 4, s));
     MDET_TRY(mlp_gram(ctx, z, n, G));
@@ -328,12 +357,24 @@ int learned_order(mdet_ctx* ctx, const mdet_mlp* net, const float* d_tnf, const 
     MDET_CUDA(ctx, cudaMemcpyAsync(off, hoff.data(), hoff.size() * 4, cudaMemcpyHostToDevice, s));
     MDET_TRY(mlp_project(ctx, z, n, V, kPcs, proj));
     // log10 size over 3..7 (1 kb .. 10 Mb)
-    k_morton<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(proj, d_ls, n, off, off + kPcs, 3.f, 0.25f, keys, vals);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    k_morton<<<grid, 256, 0, s>>>(proj, d_ls, n, off, off + kPcs, 3.f, 0.25f, size_major ? 0 : 1, keys, vals);
     MDET_LAUNCHED(ctx, "k_morton");
     size_t tb = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys2, vals, order, (int)n, 0, 64, s);
     void* tmp = ctx_scratch(ctx, "lrn.sorttmp", tb);
     if (!tmp) return MDET_ERR_NOMEM;
+    if (size_major) {
+        // the band index must fit 16 bits
+        const uint32_t band = (uint32_t)std::max<uint64_t>(seg, n / 65535 + 1);
+        k_size_keys<<<grid, 256, 0, s>>>(d_ls, n, keys3, vals);
+        MDET_LAUNCHED(ctx, "k_size_keys");
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys3, keys2, vals, order, (int)n, 0, 32, s));
+        k_band_keys<<<grid, 256, 0, s>>>(order, keys, n, band, keys3, vals);
+        MDET_LAUNCHED(ctx, "k_band_keys");
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys3, keys2, vals, order, (int)n, 0, 64, s));
+        return MDET_OK;
+    }
     MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, keys, keys2, vals, order, (int)n, 0, 64, s));
     if (seg > 1) {
         k_seg_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(order, d_ls, n, seg, keys, vals);
@@ -352,12 +393,14 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     mdet_learned_report* rep = ctx->learned_report;
     const double target = rep && rep->recall_target > 0 ? rep->recall_target : 0.999;
     const uint32_t want_rows = rep && rep->recall_rows ? rep->recall_rows : 2048;
-    const uint32_t seg = rep && rep->segment ? rep->segment : 1024;
+    const int size_major = rep && rep->order == 1 ? 1 : 0;
+    const uint32_t seg = rep && rep->segment ? rep->segment : (size_major ? kBandRows : 1024);
     if (rep) {
         rep->recall = 0;
         rep->fell_back = 0;
         rep->tiles_skipped = 0;
         rep->tau = 0;
+        rep->ms_embed = rep->ms_order = rep->ms_sample = 0;
     }
     float tau_net = INFINITY;
     MDET_CUDA(ctx, cudaMemcpyAsync(&tau_net, net->params + MLP_TAU, 4, cudaMemcpyDeviceToHost, s));
@@ -384,12 +427,15 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     float* z = (float*)ctx_scratch(ctx, "lrn.z", n * MLP_OUT * 4);
     uint32_t* order = (uint32_t*)ctx_scratch(ctx, "lrn.order", n * 4);
     if (!z || !order) return MDET_ERR_NOMEM;
-    MDET_TRY(learned_order(ctx, net, d_tnf, d_ls, n, z, seg, order));
+    MDET_TRY(mlp_embed(ctx, net->params, d_tnf, n, z));
+    tm.mark();
+    MDET_TRY(learned_order(ctx, d_ls, n, z, size_major, seg, order));
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, true, &g, order));
     MDET_TRY(abd_gate(ctx, g));
     const double L = logit(cutoff);
     DstarTable tbl;
     MDET_TRY(build_dstar_table(ctx, g.ls, n, L, &tbl, false));
+    tm.mark();
 
     // block statistics in embedding space
     float* rcent = (float*)ctx_scratch(ctx, "lrn.rcent", (uint64_t)ta * MLP_OUT * 4);
@@ -514,16 +560,19 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
         st->n_above_cutoff = ne;
         st->tiles_total = full;
         st->tiles_computed = (uint64_t)hsel;
-        st->ms_prep = tm.ms(0, 1);
-        st->ms_filter = tm.ms(1, 2);
-        st->ms_exact = tm.ms(2, 3);
-        st->ms_select = tm.ms(3, 4);
+        st->ms_prep = tm.ms(0, 3);
+        st->ms_filter = tm.ms(3, 4);
+        st->ms_exact = tm.ms(4, 5);
+        st->ms_select = tm.ms(5, 6);
     }
     if (rep) {
         rep->recall = recall;
         rep->fell_back = 0;
         rep->tiles_skipped = full - (uint64_t)hsel;
         rep->tau = tau;
+        rep->ms_embed = tm.ms(0, 1);
+        rep->ms_order = tm.ms(1, 2);
+        rep->ms_sample = tm.ms(2, 3);
     }
     return MDET_OK;
 }

@@ -123,13 +123,16 @@ class LearnedReport(ctypes.Structure):
         ("segment", u32),
         ("recall", D),
         ("fell_back", u32),
-        ("reserved", u32),
+        ("order", u32),
         ("tiles_skipped", u64),
         ("tau", D),
+        ("ms_embed", D),
+        ("ms_order", D),
+        ("ms_sample", D),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 # (name, restype, argtypes) of every entry point in include/mdet_tnf.h
@@ -536,13 +539,15 @@ class Context:
 
     # ---- learned proposal -----------------------------------------------
     def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 2048,
-                    segment: int = 0):
+                    segment: int = 0, order: int = 0):
         """Network used by mode="learned" graph calls; returns the report that
-        those calls fill (recall estimate, fallback, tiles skipped, tau)."""
+        those calls fill (recall estimate, fallback, tiles skipped, tau, phase
+        times).  order 0: embedding-major contig order, order 1: size-major."""
         rep = LearnedReport()
         rep.recall_target = recall_target
         rep.recall_rows = recall_rows
         rep.segment = segment
+        rep.order = order
         self._learned = (net, rep)  # the context keeps both pointers
         self._check(self.lib.mdet_ctx_set_learned(self.h, net.h if net else None, ctypes.byref(rep)))
         return rep

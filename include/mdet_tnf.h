@@ -30,6 +30,7 @@ extern "C" {
 #define MDET_ERR_CAPACITY 4    /* caller's output buffer too small; *n_out holds the size needed */
 #define MDET_ERR_TIMEOUT 5     /* a bounded device-side wait ran out; the context stays usable */
 #define MDET_ERR_UNSUPPORTED 6 /* mode not available (e.g. tensor-core path on a non-sm_103 device) */
+#define MDET_ERR_INTERNAL 7    /* an internal consistency check of the device work failed */
 
 /* distance-filter forms of the pairwise stage */
 #define MDET_MODE_PLAIN 0   /* FP32 SIMT all-pairs distance in the reference's element order */
@@ -403,6 +404,45 @@ int mdet_recruit(mdet_ctx* ctx, const float* abd, const float* small_abd, uint64
                  uint32_t nabd, const int64_t* label, const uint64_t* sizes, const uint64_t* small_sizes,
                  uint64_t min_cls_size, uint64_t small_total, int64_t* out, int64_t* small_out,
                  mdet_recruit_stats* stats);
+
+/* ---- binning by label propagation --------------------------------------
+ * Replaces the traversal of the scored edges in main (cuda/Cuda2.cu:
+ * 1980-2061) and label_propagation (cuda/Cuda2.cu:569-656).  Edge e joins
+ * to[e] and from[e] (contigs < n) with score sscr[e] in [0, 1] (the
+ * reference's g.to, g.from, g.sSCR).  Edges are taken in decreasing score --
+ * equal scores in edge order, where the reference's std::sort leaves their
+ * order open.  An edge whose contigs are in different bins connects them and,
+ * when its score is above min_s, joins the traversal graph; the first such
+ * edge at or below min_s ends the traversal.  Label propagation runs each
+ * time the connected share of the contigs reaches max_p/10 * (1..10) and at
+ * the last edge (at most 10 runs): Gauss-Seidel sweeps in first-seen order,
+ * each contig taking the neighbour label with the largest chi-squared CDF of
+ * -2 * sum log(1 - score) (2 x count degrees of freedom), exact ties going to
+ * the label first in the reference's std::unordered_map iteration order
+ * (GNU libstdc++); a contig that returns to a label it held in the same run
+ * is frozen; a run stops when no contig moved to a new label, or after 10
+ * sweeps without a new low.  max_p and min_s are fractions (the reference's
+ * --maxP and --minS divided by 100).  The CDF and log(1 - score) are this
+ * project's (bit-identical host and device functions; the reference calls
+ * Boost's CDF and the C library's log).  mem[i] receives contig i's bin (a
+ * contig index).  n < 2^31, n_edges < 2^30. */
+typedef struct {
+    uint64_t calls;       /* label propagation runs */
+    uint64_t sweeps;      /* Gauss-Seidel sweeps, summed over runs */
+    uint64_t graph_edges; /* edges in the traversal graph */
+    uint64_t connected;   /* contigs in the first-seen order */
+    uint64_t frozen;      /* contigs frozen, summed over runs */
+    uint64_t ties;        /* contig updates decided among exactly tied labels */
+    uint64_t levels_max;  /* most dependency levels of a sweep */
+    uint64_t degree_max;  /* most traversal-graph edges of a contig */
+    double ms_total;      /* device time of the call */
+} mdet_lp_stats;
+int mdet_label_propagation(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* sscr,
+                           uint64_t n_edges, uint64_t n, double max_p, double min_s, uint64_t* mem,
+                           mdet_lp_stats* stats);
+int mdet_label_propagation_dev(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const double* d_sscr,
+                               uint64_t n_edges, uint64_t n, double max_p, double min_s, uint64_t* d_mem,
+                               mdet_lp_stats* stats);
 
 #ifdef __cplusplus
 }

@@ -36,10 +36,12 @@ CU_UNITS = [
     "abundance",
     "fasta_index",
     "recruit",
+    "labelprop",
 ]
-# per-unit flags: the abundance unit rounds every product and sum separately
-# (no FMA contraction), as the reference's host arithmetic does
-UNIT_FLAGS = {"abundance": ["-fmad=false"], "recruit": ["-fmad=false"]}
+# per-unit flags: the abundance, recruiting and label propagation units round
+# every product and sum separately (no FMA contraction), as the reference's
+# host arithmetic and the host checkers do
+UNIT_FLAGS = {"abundance": ["-fmad=false"], "recruit": ["-fmad=false"], "labelprop": ["-fmad=false"]}
 
 
 def _headers():

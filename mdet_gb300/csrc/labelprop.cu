@@ -1,0 +1,793 @@
+// labelprop.cu -- binning by label propagation over the scored edge graph:
+// the traversal of main (cuda/Cuda2.cu:1980-2061) and label_propagation
+// (cuda/Cuda2.cu:569-656), on the device.
+//
+// The traversal takes the edges in decreasing score.  An edge whose two
+// contigs are in different bins connects them (first-seen order) and, above
+// min_s, joins the traversal graph; the first such edge at or below min_s
+// ends the traversal.  Propagation runs when the connected share of the
+// contigs reaches max_p/10 * (1..10), and at the last edge.  Between two
+// runs the bins do not change, so each stretch of edges up to the next run
+// is one data-parallel step: the differing-bin test, the early stop, the
+// first appearance of each contig (an atomic minimum of the edge position)
+// and the run position follow from one pass and a sort.
+//
+// Label propagation is Gauss-Seidel: each contig, in first-seen order, takes
+// the neighbour label with the largest Fisher-combined chi-squared CDF,
+// reading the labels its predecessors in that order have just written.
+// Contigs that share no edge do not read each other, so the sweep runs level
+// by level over the order's dependency graph (level = 1 + the deepest level
+// among the contig's neighbours earlier in the order, found by Kahn peeling):
+// one block per contig of a level, the levels in turn -- the same result as
+// the sequential sweep.  A block sorts its contig's (neighbour label, edge
+// position) keys (bitonic sort in shared memory, or in a global slice for
+// contigs with more than 2,048 edges), folds each label's log(1 - score) in
+// edge order (the reference's summation order), evaluates the CDF
+// (lp_math.h, bit-identical to the host checker) and breaks exact ties by the
+// reference map's iteration order (lp_umap.h).  The visited (contig, label)
+// pairs of a call live in an open-addressing table; a call that overfills it
+// is re-run from its starting labels with a larger table.
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "lp_math.h"
+#include "lp_umap.h"
+
+int check_flag(mdet_ctx* ctx);
+
+namespace {
+
+constexpr uint32_t kSmallCap = 2048;  // incident edges a block sorts in shared memory
+constexpr int kThreads = 256;
+constexpr uint32_t kProbeLimit = 1u << 16;
+
+// flags
+constexpr unsigned long long kErrTable = 1;     // visited table too full
+constexpr unsigned long long kErrSlots = 2;     // global sort slice missing
+constexpr unsigned long long kErrScore = 4;     // a score outside [0, 1]
+
+__host__ __device__ inline uint32_t pow2_at_least(uint32_t d) {
+    uint32_t n = 2;
+    while (n < d) n <<= 1;
+    return n;
+}
+
+// bytes of one contig's work area for a sort of n keys (n a power of two)
+__host__ __device__ inline size_t ws_bytes(uint32_t n) {
+    return (size_t)n * (8 + 8 + 8 + 4 + 4 + 4) + (size_t)lpu::buckets_for(n) * 4;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+struct LpArgs {
+    const uint32_t* inc_off;  // [n + 1]
+    const uint32_t* inc;      // traversal-graph edge ids per contig, increasing
+    const uint32_t* ea;       // the edge's first contig (the reference's to)
+    const uint32_t* eb;       // the edge's second contig (from)
+    const double* lw;         // log(1 - score)
+    uint32_t* mem;
+    uint8_t* stuck;
+    unsigned long long* vt;   // visited (contig, label) table, 0 = empty
+    unsigned long long vt_mask;
+    const double* logfact;
+    unsigned long long* counters;  // [0] moved, [1] table entries, [2] error flags, [3] tied picks
+    unsigned char* big_ws;
+    size_t big_stride;
+    uint32_t big_slots;
+    const uint32_t* slot_of;
+};
+
+// true when (v, lab) was not in the table
+__device__ bool visit(const LpArgs& P, uint32_t v, uint32_t lab) {
+    const unsigned long long key = (((unsigned long long)v << 32) | lab) + 1ull;
+    unsigned long long h = mix64(key) & P.vt_mask;
+    for (uint32_t it = 0; it < kProbeLimit; ++it) {
+        const unsigned long long old = atomicCAS(P.vt + h, 0ull, key);
+        if (old == 0ull) {
+            const unsigned long long cnt = atomicAdd(P.counters + 1, 1ull) + 1;
+            if (cnt * 4 > (P.vt_mask + 1) * 3) atomicOr(P.counters + 2, kErrTable);
+            return true;
+        }
+        if (old == key) return false;
+        h = (h + 1) & P.vt_mask;
+    }
+    atomicOr(P.counters + 2, kErrTable);
+    return false;
+}
+
+// One sweep step for the contigs of one level: block per contig.
+__global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t* __restrict__ nodes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red_v[kThreads / 32];
+    __shared__ uint32_t red_c[kThreads / 32];
+    __shared__ double s_vmax;
+    __shared__ uint32_t s_ties, s_best;
+    const uint32_t v = nodes[blockIdx.x];
+    const uint32_t s = P.inc_off[v];
+    const uint32_t d = P.inc_off[v + 1] - s;
+    if (d == 0) return;
+    const uint32_t N = pow2_at_least(d);
+    unsigned char* base = smem;
+    if (N > kSmallCap) {
+        const uint32_t slot = P.slot_of[v];
+        if (slot >= P.big_slots) {
+            if (threadIdx.x == 0) atomicOr(P.counters + 2, kErrSlots);
+            return;
+        }
+        base = P.big_ws + (size_t)slot * P.big_stride;
+    }
+    unsigned long long* sk = reinterpret_cast<unsigned long long*>(base);
+    double* w = reinterpret_cast<double*>(base + (size_t)N * 8);
+    double* val = reinterpret_cast<double*>(base + (size_t)N * 16);
+    int32_t* fidx = reinterpret_cast<int32_t*>(base + (size_t)N * 24);
+    uint32_t* ins = reinterpret_cast<uint32_t*>(base + (size_t)N * 28);
+    int32_t* nxt = reinterpret_cast<int32_t*>(base + (size_t)N * 32);
+    int32_t* bb = reinterpret_cast<int32_t*>(base + (size_t)N * 36);
+    const uint32_t t = threadIdx.x;
+
+    // (neighbour label, edge position) keys and the edges' log(1 - score)
+    for (uint32_t j = t; j < N; j += kThreads) {
+        if (j < d) {
+            const uint32_t e = P.inc[s + j];
+            const uint32_t o = P.ea[e] == v ? P.eb[e] : P.ea[e];
+            sk[j] = ((unsigned long long)P.mem[o] << 32) | j;
+            w[j] = P.lw[e];
+        } else {
+            sk[j] = ~0ull;
+        }
+        fidx[j] = -1;
+    }
+    __syncthreads();
+    // bitonic sort, ascending
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        for (uint32_t jj = k >> 1; jj > 0; jj >>= 1) {
+            for (uint32_t i = t; i < N; i += kThreads) {
+                const uint32_t l = i ^ jj;
+                if (l > i) {
+                    const unsigned long long a = sk[i], b = sk[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        sk[i] = b;
+                        sk[l] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // each label's run: the Fisher-combined CDF of its edges, folded in edge
+    // order (positions are sorted within a label)
+    double vmax = -1.0;
+    for (uint32_t p = t; p < d; p += kThreads) {
+        const uint32_t lab = (uint32_t)(sk[p] >> 32);
+        double vp = -1.0;
+        if (p == 0 || (uint32_t)(sk[p - 1] >> 32) != lab) {
+            double sum = 0.0;
+            uint32_t q = p;
+            do {
+                sum = sum + w[(uint32_t)sk[q]];
+                ++q;
+            } while (q < d && (uint32_t)(sk[q] >> 32) == lab);
+            vp = lpm::chi2_cdf(2.0 * (double)(q - p), -2.0 * sum, P.logfact);
+            fidx[(uint32_t)sk[p]] = (int32_t)p;
+        }
+        val[p] = vp;
+        vmax = fmax(vmax, vp);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((t & 31) == 0) red_v[t >> 5] = vmax;
+    __syncthreads();
+    if (t == 0) {
+        double m = red_v[0];
+        for (int i = 1; i < kThreads / 32; ++i) m = fmax(m, red_v[i]);
+        s_vmax = m;
+    }
+    __syncthreads();
+    const double top = s_vmax;
+    uint32_t ties = 0;
+    for (uint32_t p = t; p < d; p += kThreads) ties += val[p] == top;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ties += __shfl_xor_sync(0xffffffffu, ties, o);
+    if ((t & 31) == 0) red_c[t >> 5] = ties;
+    __syncthreads();
+    if (t == 0) {
+        uint32_t nt = 0;
+        for (int i = 0; i < kThreads / 32; ++i) nt += red_c[i];
+        s_ties = nt;
+    }
+    __syncthreads();
+    if (s_ties == 1) {
+        for (uint32_t p = t; p < d; p += kThreads)
+            if (val[p] == top) s_best = (uint32_t)(sk[p] >> 32);
+    }
+    __syncthreads();
+    if (t != 0) return;
+    if (s_ties > 1) {
+        atomicAdd(P.counters + 3, 1ull);
+        // the first tied label in the map's iteration order: labels in
+        // first-seen order (edge position of their first edge), then the map
+        uint32_t K = 0;
+        for (uint32_t j = 0; j < d; ++j) {
+            const int32_t p = fidx[j];
+            if (p >= 0) {
+                fidx[K] = p;  // K <= j: fidx[j] is read before any later write reaches it
+                ins[K] = (uint32_t)(sk[p] >> 32);
+                ++K;
+            }
+        }
+        int32_t q = lpu::order(ins, K, nxt, bb);
+        while (q >= 0 && val[fidx[q]] != top) q = nxt[q];
+        s_best = ins[q >= 0 ? q : 0];
+    }
+    const uint32_t b = s_best;
+    if (P.mem[v] != b && !P.stuck[v]) {
+        P.mem[v] = b;
+        if (visit(P, v, b))
+            atomicAdd(P.counters, 1ull);
+        else
+            P.stuck[v] = 1;
+    }
+}
+
+// ---- dependency levels of the order --------------------------------------
+
+__global__ void k_lp_pos(const uint32_t* __restrict__ order, uint32_t norder, uint32_t* __restrict__ pos_of) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < norder) pos_of[order[i]] = i;
+}
+
+struct LevelInfo {
+    unsigned int count, maxdeg, nbig, pad;
+};
+
+__device__ __forceinline__ void lp_enqueue(uint32_t w, uint32_t deg, uint32_t* next, LevelInfo* info,
+                                           uint32_t* slot_of) {
+    next[atomicAdd(&info->count, 1u)] = w;
+    atomicMax(&info->maxdeg, deg);
+    if (pow2_at_least(deg) > kSmallCap) slot_of[w] = atomicAdd(&info->nbig, 1u);
+}
+
+// earlier neighbours of each contig of the order (warp per contig); those
+// with none form level 0
+__global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ order, uint32_t norder,
+                                                 const uint32_t* __restrict__ pos_of,
+                                                 const uint32_t* __restrict__ inc_off,
+                                                 const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
+                                                 const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
+                                                 uint32_t* __restrict__ level0, LevelInfo* info,
+                                                 uint32_t* __restrict__ slot_of) {
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= norder) return;
+    const uint32_t u = order[wid], pu = wid;
+    const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
+    uint32_t c = 0;
+    for (uint32_t j = lane; j < d; j += 32) {
+        const uint32_t e = inc[s + j];
+        const uint32_t o = ea[e] == u ? eb[e] : ea[e];
+        c += pos_of[o] < pu;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) {
+        pred[u] = c;
+        if (c == 0) lp_enqueue(u, d, level0, info, slot_of);
+    }
+}
+
+// one Kahn step: contigs whose last earlier neighbour is in this level join
+// the next one
+__global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cur, uint32_t ncur,
+                                                 const uint32_t* __restrict__ pos_of,
+                                                 const uint32_t* __restrict__ inc_off,
+                                                 const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
+                                                 const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
+                                                 uint32_t* __restrict__ next, LevelInfo* info,
+                                                 uint32_t* __restrict__ slot_of) {
+    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (wid >= ncur) return;
+    const uint32_t u = cur[wid];
+    const uint32_t pu = pos_of[u];
+    const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
+    for (uint32_t j = lane; j < d; j += 32) {
+        const uint32_t e = inc[s + j];
+        const uint32_t o = ea[e] == u ? eb[e] : ea[e];
+        if (pos_of[o] > pu && atomicSub(pred + o, 1u) == 1u)
+            lp_enqueue(o, inc_off[o + 1] - inc_off[o], next, info, slot_of);
+    }
+}
+
+// ---- the traversal ----------------------------------------------------------
+
+__global__ void k_lp_gather(const uint64_t* __restrict__ from, const uint64_t* __restrict__ to,
+                            const double* __restrict__ sscr, const uint32_t* __restrict__ ord, uint64_t ne, uint64_t n,
+                            uint32_t* __restrict__ sa, uint32_t* __restrict__ sb, double* __restrict__ ss,
+                            unsigned long long* __restrict__ flags) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ne; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = ord[i];
+        const double s = sscr[e];
+        const uint64_t a = to[e], b = from[e];
+        if (!(s >= 0.0 && s <= 1.0) || a >= n || b >= n) atomicOr(flags, kErrScore);
+        sa[i] = (uint32_t)min(a, n - 1);
+        sb[i] = (uint32_t)min(b, n - 1);
+        ss[i] = s;
+    }
+}
+
+// from position pos: the first differing-bin edge at or below min_s (the
+// early stop) and the first one above it
+__global__ void k_lp_seg(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
+                         const double* __restrict__ ss, uint64_t pos, uint64_t ne, const uint32_t* __restrict__ mem,
+                         double min_s, unsigned long long* __restrict__ out) {
+    for (uint64_t i = pos + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ne;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (mem[sa[i]] == mem[sb[i]]) continue;
+        if (ss[i] > min_s)
+            atomicMin(out + 1, (unsigned long long)i);
+        else
+            atomicMin(out, (unsigned long long)i);
+    }
+}
+
+// first appearance (2 * position, + 1 for the second contig) of the contigs
+// not yet connected, over the differing-bin edges of [pos, last]
+__global__ void k_lp_first(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb, uint64_t pos,
+                           uint64_t last, const uint32_t* __restrict__ mem, const uint8_t* __restrict__ seen,
+                           unsigned long long* __restrict__ first) {
+    for (uint64_t i = pos + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= last;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = sa[i], b = sb[i];
+        if (mem[a] == mem[b]) continue;
+        if (!seen[a]) atomicMin(first + a, 2ull * i);
+        if (!seen[b]) atomicMin(first + b, 2ull * i + 1);
+    }
+}
+
+__global__ void k_lp_iota(uint32_t* __restrict__ v, uint64_t n) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (uint32_t)i;
+}
+
+__global__ void k_lp_count_le(const unsigned long long* __restrict__ keys, uint64_t n, unsigned long long bound,
+                              unsigned long long* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n && keys[i] <= bound) atomicAdd(out, 1ull);
+}
+
+__global__ void k_lp_mark(const uint32_t* __restrict__ nodes, uint64_t k, uint8_t* __restrict__ seen) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < k) seen[nodes[i]] = 1;
+}
+
+// the edges of [pos, end] that join the traversal graph, appended in order
+__global__ void k_lp_edge_flags(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
+                                const double* __restrict__ ss, uint64_t pos, uint64_t cnt,
+                                const uint32_t* __restrict__ mem, double min_s, uint8_t* __restrict__ flag) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const uint64_t p = pos + i;
+    flag[i] = mem[sa[p]] != mem[sb[p]] && ss[p] > min_s;
+}
+
+__global__ void k_lp_append(const uint32_t* __restrict__ sel, uint64_t k, uint64_t pos,
+                            const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
+                            const double* __restrict__ ss, uint32_t* __restrict__ ea, uint32_t* __restrict__ eb,
+                            double* __restrict__ lw) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    const uint64_t p = pos + sel[i];
+    ea[i] = sa[p];
+    eb[i] = sb[p];
+    lw[i] = lpm::log(1. - ss[p]);
+}
+
+// incidence entries: (contig, edge) for both ends, edges in order
+__global__ void k_lp_inc_keys(const uint32_t* __restrict__ ea, const uint32_t* __restrict__ eb, uint64_t m,
+                              uint32_t* __restrict__ key, uint32_t* __restrict__ val,
+                              unsigned int* __restrict__ deg) {
+    const uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    key[2 * e] = ea[e];
+    val[2 * e] = (uint32_t)e;
+    key[2 * e + 1] = eb[e];
+    val[2 * e + 1] = (uint32_t)e;
+    atomicAdd(deg + ea[e], 1u);
+    atomicAdd(deg + eb[e], 1u);
+}
+
+__global__ void k_lp_logfact(double* out, uint32_t count) { lpm::log_factorials(out, count); }
+
+__global__ void k_lp_count_stuck(const uint8_t* __restrict__ stuck, uint64_t n, unsigned long long* __restrict__ out) {
+    unsigned long long c = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        c += stuck[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+__global__ void k_lp_widen(const uint32_t* __restrict__ mem, uint64_t n, uint64_t* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = mem[i];
+}
+
+inline unsigned grid_for(uint64_t n, unsigned b = 256) { return (unsigned)std::max<uint64_t>(1, (n + b - 1) / b); }
+
+struct LpState {
+    uint64_t n = 0, ne = 0;
+    uint32_t *sa = nullptr, *sb = nullptr, *mem = nullptr, *mem0 = nullptr, *order = nullptr;
+    double* ss = nullptr;
+    uint8_t *seen = nullptr, *stuck = nullptr, *eflag = nullptr;
+    unsigned long long *first = nullptr, *cnt = nullptr;
+    uint32_t *ea = nullptr, *eb = nullptr;
+    double* lw = nullptr;
+    uint64_t m2 = 0, norder = 0;
+};
+
+// One propagation call over the traversal graph (m2 edges) and order.
+int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
+    cudaStream_t s = ctx->stream;
+    const uint64_t n = S.n, m = S.m2, no = S.norder;
+    // incidence lists
+    uint32_t* ikey = (uint32_t*)ctx_scratch(ctx, "lp.ikey", 2 * m * 4 + 8);
+    uint32_t* ival = (uint32_t*)ctx_scratch(ctx, "lp.ival", 2 * m * 4 + 8);
+    uint32_t* ikey2 = (uint32_t*)ctx_scratch(ctx, "lp.ikey2", 2 * m * 4 + 8);
+    uint32_t* inc = (uint32_t*)ctx_scratch(ctx, "lp.inc", 2 * m * 4 + 8);
+    unsigned int* deg = (unsigned int*)ctx_scratch(ctx, "lp.deg", (n + 1) * 4);
+    uint32_t* inc_off = (uint32_t*)ctx_scratch(ctx, "lp.incoff", (n + 1) * 4);
+    uint32_t* pos_of = (uint32_t*)ctx_scratch(ctx, "lp.pos", n * 4);
+    uint32_t* pred = (uint32_t*)ctx_scratch(ctx, "lp.pred", n * 4);
+    uint32_t* lvl = (uint32_t*)ctx_scratch(ctx, "lp.lvl", (no + 1) * 4);
+    uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "lp.slot", n * 4);
+    LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", 16);
+    if (!ikey || !ival || !ikey2 || !inc || !deg || !inc_off || !pos_of || !pred || !lvl || !slot_of || !info)
+        return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (n + 1) * 4, s));
+    k_lp_inc_keys<<<grid_for(m), 256, 0, s>>>(S.ea, S.eb, m, ikey, ival, deg);
+    MDET_LAUNCHED(ctx, "k_lp_inc_keys");
+    {
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, tb, ikey, ikey2, ival, inc, (int)(2 * m), 0, 32, s);
+        void* tmp = ctx_scratch(ctx, "lp.sorttmp", tb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, ikey, ikey2, ival, inc, (int)(2 * m), 0, 32, s));
+        tb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, tb, deg, inc_off, (int)(n + 1), s);
+        tmp = ctx_scratch(ctx, "lp.scantmp", tb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, deg, inc_off, (int)(n + 1), s));
+    }
+    // dependency levels
+    MDET_CUDA(ctx, cudaMemsetAsync(pos_of, 0xFF, n * 4, s));
+    k_lp_pos<<<grid_for(no), 256, 0, s>>>(S.order, (uint32_t)no, pos_of);
+    MDET_LAUNCHED(ctx, "k_lp_pos");
+    MDET_CUDA(ctx, cudaMemsetAsync(info, 0, 16, s));
+    k_lp_pred<<<grid_for(no * 32), 256, 0, s>>>(S.order, (uint32_t)no, pos_of, inc_off, inc, S.ea, S.eb, pred, lvl,
+                                                 info, slot_of);
+    MDET_LAUNCHED(ctx, "k_lp_pred");
+    std::vector<uint64_t> loff{0};
+    std::vector<LevelInfo> linfo;
+    uint64_t done = 0;
+    uint32_t maxdeg = 0, maxbig = 0;
+    while (true) {
+        LevelInfo h;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&h, info, 16, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        if (h.count == 0) break;
+        linfo.push_back(h);
+        maxdeg = std::max(maxdeg, h.maxdeg);
+        maxbig = std::max(maxbig, h.nbig);
+        const uint64_t cur = loff.back();
+        done = cur + h.count;
+        loff.push_back(done);
+        if (done >= no) break;
+        MDET_CUDA(ctx, cudaMemsetAsync(info, 0, 16, s));
+        k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, inc, S.ea,
+                                                                    S.eb, pred, lvl + done, info, slot_of);
+        MDET_LAUNCHED(ctx, "k_lp_kahn");
+    }
+    if (done != no) return ctx_fail(ctx, MDET_ERR_INTERNAL, "label propagation: %llu of %llu contigs levelled",
+                                    (unsigned long long)done, (unsigned long long)no);
+    st->levels_max = std::max<uint64_t>(st->levels_max, linfo.size());
+    st->degree_max = std::max<uint64_t>(st->degree_max, maxdeg);
+    // the CDF's log-factorials up to the largest label count
+    double* logfact = (double*)ctx_scratch(ctx, "lp.logfact", ((uint64_t)maxdeg + 2) * 8);
+    if (!logfact) return MDET_ERR_NOMEM;
+    k_lp_logfact<<<1, 1, 0, s>>>(logfact, maxdeg + 2);
+    MDET_LAUNCHED(ctx, "k_lp_logfact");
+    // global sort slices for the contigs with more than kSmallCap edges
+    const size_t big_stride = maxdeg > kSmallCap ? (ws_bytes(pow2_at_least(maxdeg)) + 255) / 256 * 256 : 0;
+    unsigned char* big_ws = nullptr;
+    if (maxbig) {
+        big_ws = (unsigned char*)ctx_scratch(ctx, "lp.bigws", big_stride * maxbig);
+        if (!big_ws) return MDET_ERR_NOMEM;
+    }
+    const size_t small_max = ws_bytes(kSmallCap);
+    MDET_CUDA(ctx, cudaFuncSetAttribute(k_lp_level, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)small_max));
+    // visited table: sized for the order, doubled (and the call re-run from
+    // its starting labels) when a call overfills it
+    uint64_t vt_cap = 1u << 20;
+    while (vt_cap < 8 * no) vt_cap <<= 1;
+    MDET_CUDA(ctx, cudaMemcpyAsync(S.mem0, S.mem, n * 4, cudaMemcpyDeviceToDevice, s));
+    for (int attempt_table = 0;; ++attempt_table) {
+        unsigned long long* vt = (unsigned long long*)ctx_scratch(ctx, "lp.vt", vt_cap * 8);
+        if (!vt) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cudaMemsetAsync(vt, 0, vt_cap * 8, s));
+        MDET_CUDA(ctx, cudaMemsetAsync(S.stuck, 0, n, s));
+        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 4 * 8, s));
+        LpArgs P{inc_off, inc, S.ea, S.eb, S.lw, S.mem, S.stuck, vt, vt_cap - 1, logfact, S.cnt, big_ws, big_stride,
+                 maxbig, slot_of};
+        uint64_t low = INT_MAX, attempt = 0, sweeps = 0;
+        unsigned long long hc[4] = {0, 0, 0, 0};
+        bool overfull = false;
+        while (true) {
+            MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 8, s));
+            for (size_t L = 0; L < linfo.size(); ++L) {
+                const uint32_t cap = std::min<uint32_t>(pow2_at_least(linfo[L].maxdeg), kSmallCap);
+                k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), s>>>(P, lvl + loff[L]);
+                MDET_LAUNCHED(ctx, "k_lp_level");
+            }
+            MDET_CUDA(ctx, cudaMemcpyAsync(hc, S.cnt, 32, cudaMemcpyDeviceToHost, s));
+            MDET_CUDA(ctx, cudaStreamSynchronize(s));
+            ++sweeps;
+            if (hc[2] & (kErrSlots | kErrScore))
+                return ctx_fail(ctx, MDET_ERR_INTERNAL, "label propagation: flags %llu", hc[2]);
+            if (hc[2] & kErrTable) {
+                overfull = true;
+                break;
+            }
+            const uint64_t moved = hc[0];
+            if (moved < low) {
+                low = moved;
+                attempt = 0;
+            } else if (++attempt >= 10) {
+                break;
+            }
+            if (moved == 0) break;
+        }
+        if (!overfull) {
+            st->sweeps += sweeps;
+            st->ties += hc[3];
+            break;
+        }
+        if (attempt_table >= 6) return ctx_fail(ctx, MDET_ERR_CAPACITY, "label propagation: visited table");
+        vt_cap <<= 1;
+        MDET_CUDA(ctx, cudaMemcpyAsync(S.mem, S.mem0, n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
+    k_lp_count_stuck<<<std::min<unsigned>(grid_for(n), 1024), 256, 0, s>>>(S.stuck, n, S.cnt + 2);
+    MDET_LAUNCHED(ctx, "k_lp_count_stuck");
+    unsigned long long fz = 0;
+    MDET_CUDA(ctx, cudaMemcpyAsync(&fz, S.cnt + 2, 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    st->frozen += fz;
+    return MDET_OK;
+}
+
+int lp_impl(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const double* d_sscr, uint64_t ne,
+            uint64_t n, double max_p, double min_s, uint64_t* d_out, mdet_lp_stats* st) {
+    cudaStream_t s = ctx->stream;
+    LpState S;
+    S.n = n;
+    S.ne = ne;
+    const uint64_t ne1 = std::max<uint64_t>(ne, 1);
+    uint32_t* ord0 = (uint32_t*)ctx_scratch(ctx, "lp.ord0", ne1 * 4);
+    uint32_t* ord = (uint32_t*)ctx_scratch(ctx, "lp.ord", ne1 * 4);
+    double* key2 = (double*)ctx_scratch(ctx, "lp.skey", ne1 * 8);
+    S.sa = (uint32_t*)ctx_scratch(ctx, "lp.sa", ne1 * 4);
+    S.sb = (uint32_t*)ctx_scratch(ctx, "lp.sb", ne1 * 4);
+    S.ss = (double*)ctx_scratch(ctx, "lp.ss", ne1 * 8);
+    S.mem = (uint32_t*)ctx_scratch(ctx, "lp.mem", n * 4);
+    S.mem0 = (uint32_t*)ctx_scratch(ctx, "lp.mem0", n * 4);
+    S.order = (uint32_t*)ctx_scratch(ctx, "lp.order", n * 4);
+    S.seen = (uint8_t*)ctx_scratch(ctx, "lp.seen", n);
+    S.stuck = (uint8_t*)ctx_scratch(ctx, "lp.stuck", n);
+    S.eflag = (uint8_t*)ctx_scratch(ctx, "lp.eflag", ne1);
+    S.first = (unsigned long long*)ctx_scratch(ctx, "lp.first", n * 8);
+    S.cnt = (unsigned long long*)ctx_scratch(ctx, "lp.cnt", 64);
+    S.ea = (uint32_t*)ctx_scratch(ctx, "lp.ea", ne1 * 4);
+    S.eb = (uint32_t*)ctx_scratch(ctx, "lp.eb", ne1 * 4);
+    S.lw = (double*)ctx_scratch(ctx, "lp.lw", ne1 * 8);
+    unsigned long long* fkeys = (unsigned long long*)ctx_scratch(ctx, "lp.fkeys", n * 8);
+    uint32_t* nodes0 = (uint32_t*)ctx_scratch(ctx, "lp.nodes0", n * 4);
+    uint32_t* nodes = (uint32_t*)ctx_scratch(ctx, "lp.nodes", n * 4);
+    uint32_t* sel = (uint32_t*)ctx_scratch(ctx, "lp.sel", ne1 * 4);
+    if (!ord0 || !ord || !key2 || !S.sa || !S.sb || !S.ss || !S.mem || !S.mem0 || !S.order || !S.seen || !S.stuck ||
+        !S.eflag || !S.first || !S.cnt || !S.ea || !S.eb || !S.lw || !fkeys || !nodes0 || !nodes || !sel)
+        return MDET_ERR_NOMEM;
+    k_lp_iota<<<grid_for(n), 256, 0, s>>>(S.mem, n);
+    MDET_LAUNCHED(ctx, "k_lp_iota");
+    MDET_CUDA(ctx, cudaMemsetAsync(S.seen, 0, n, s));
+    if (ne) {
+        // edges by decreasing score; equal scores keep edge order (stable)
+        k_lp_iota<<<grid_for(ne), 256, 0, s>>>(ord0, ne);
+        MDET_LAUNCHED(ctx, "k_lp_iota");
+        size_t tb = 0;
+        cub::DeviceRadixSort::SortPairsDescending(nullptr, tb, d_sscr, key2, ord0, ord, (int)ne, 0, 64, s);
+        void* tmp = ctx_scratch(ctx, "lp.esort", tb);
+        if (!tmp) return MDET_ERR_NOMEM;
+        MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairsDescending(tmp, tb, d_sscr, key2, ord0, ord, (int)ne, 0, 64, s));
+        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 64, s));
+        k_lp_gather<<<std::min<unsigned>(grid_for(ne), 8 * ctx->num_sms), 256, 0, s>>>(d_from, d_to, d_sscr, ord, ne,
+                                                                                       n, S.sa, S.sb, S.ss, S.cnt);
+        MDET_LAUNCHED(ctx, "k_lp_gather");
+        unsigned long long bad = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&bad, S.cnt, 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        if (bad) return ctx_fail(ctx, MDET_ERR_INVALID, "label propagation: a score outside [0, 1] or a contig >= n");
+    }
+    std::vector<double> sched;
+    for (int i = 1; i <= 10; ++i) sched.push_back(max_p / 10 * i);
+    size_t which = 0;
+    uint64_t pos = 0;
+    while (ne && pos < ne) {
+        // the stretch from pos: early stop and first joining edge
+        unsigned long long h2[2] = {~0ull, ~0ull};
+        MDET_CUDA(ctx, cudaMemcpyAsync(S.cnt, h2, 16, cudaMemcpyHostToDevice, s));
+        k_lp_seg<<<std::min<unsigned>(grid_for(ne - pos), 8 * ctx->num_sms), 256, 0, s>>>(S.sa, S.sb, S.ss, pos, ne,
+                                                                                          S.mem, min_s, S.cnt);
+        MDET_LAUNCHED(ctx, "k_lp_seg");
+        MDET_CUDA(ctx, cudaMemcpyAsync(h2, S.cnt, 16, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint64_t stop = h2[0] < ne ? h2[0] : ne;
+        const uint64_t last = stop < ne ? stop : ne - 1;
+        const uint64_t first_add = h2[1];
+        // first appearances of new contigs over [pos, last], in order
+        MDET_CUDA(ctx, cudaMemsetAsync(S.first, 0xFF, n * 8, s));
+        k_lp_first<<<std::min<unsigned>(grid_for(last - pos + 1), 8 * ctx->num_sms), 256, 0, s>>>(
+            S.sa, S.sb, pos, last, S.mem, S.seen, S.first);
+        MDET_LAUNCHED(ctx, "k_lp_first");
+        k_lp_iota<<<grid_for(n), 256, 0, s>>>(nodes0, n);
+        MDET_LAUNCHED(ctx, "k_lp_iota");
+        {
+            size_t tb = 0;
+            cub::DeviceRadixSort::SortPairs(nullptr, tb, S.first, fkeys, nodes0, nodes, (int)n, 0, 64, s);
+            void* tmp = ctx_scratch(ctx, "lp.nsort", tb);
+            if (!tmp) return MDET_ERR_NOMEM;
+            MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, S.first, fkeys, nodes0, nodes, (int)n, 0, 64, s));
+        }
+        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
+        k_lp_count_le<<<grid_for(n), 256, 0, s>>>(fkeys, n, ~0ull - 1, S.cnt + 2);
+        MDET_LAUNCHED(ctx, "k_lp_count_le");
+        unsigned long long nn = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&nn, S.cnt + 2, 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        // the run position: the first edge where the graph has an edge and
+        // the connected count reaches the schedule, or the last edge
+        const double thr = sched[which];
+        uint64_t c_need = (uint64_t)std::ceil(thr * (double)n);
+        while (c_need > 0 && (double)(c_need - 1) / (double)n >= thr) --c_need;
+        while ((double)c_need / (double)n < thr) ++c_need;
+        const bool have_edge = S.m2 > 0 || first_add <= last;
+        if (!have_edge) break;  // no edge joins: the traversal ends without a run
+        const uint64_t i_e = S.m2 > 0 ? pos : first_add;
+        uint64_t i_run = last;
+        if (c_need <= S.norder) {
+            i_run = std::max(pos, i_e);
+        } else if (c_need <= S.norder + nn) {
+            unsigned long long key = 0;
+            MDET_CUDA(ctx, cudaMemcpyAsync(&key, fkeys + (c_need - S.norder - 1), 8, cudaMemcpyDeviceToHost, s));
+            MDET_CUDA(ctx, cudaStreamSynchronize(s));
+            i_run = std::max<uint64_t>(key >> 1, i_e);
+        }
+        if (i_run > last) i_run = last;
+        // commit [pos, i_run]: new contigs in first-seen order, joining edges
+        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
+        k_lp_count_le<<<grid_for(nn), 256, 0, s>>>(fkeys, nn, 2ull * i_run + 1, S.cnt + 2);
+        MDET_LAUNCHED(ctx, "k_lp_count_le");
+        unsigned long long kc = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&kc, S.cnt + 2, 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        if (kc) {
+            MDET_CUDA(ctx, cudaMemcpyAsync(S.order + S.norder, nodes, kc * 4, cudaMemcpyDeviceToDevice, s));
+            k_lp_mark<<<grid_for(kc), 256, 0, s>>>(nodes, kc, S.seen);
+            MDET_LAUNCHED(ctx, "k_lp_mark");
+            S.norder += kc;
+        }
+        const uint64_t span = i_run - pos + 1;
+        k_lp_edge_flags<<<grid_for(span), 256, 0, s>>>(S.sa, S.sb, S.ss, pos, span, S.mem, min_s, S.eflag);
+        MDET_LAUNCHED(ctx, "k_lp_edge_flags");
+        {
+            thrust::counting_iterator<uint32_t> it(0);
+            size_t tb = 0;
+            cub::DeviceSelect::Flagged(nullptr, tb, it, S.eflag, sel, S.cnt + 3, (int)span, s);
+            void* tmp = ctx_scratch(ctx, "lp.seltmp", tb);
+            if (!tmp) return MDET_ERR_NOMEM;
+            MDET_CUDA(ctx, cub::DeviceSelect::Flagged(tmp, tb, it, S.eflag, sel, S.cnt + 3, (int)span, s));
+        }
+        unsigned long long ka = 0;
+        MDET_CUDA(ctx, cudaMemcpyAsync(&ka, S.cnt + 3, 8, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaStreamSynchronize(s));
+        if (ka) {
+            k_lp_append<<<grid_for(ka), 256, 0, s>>>(sel, ka, pos, S.sa, S.sb, S.ss, S.ea + S.m2, S.eb + S.m2,
+                                                    S.lw + S.m2);
+            MDET_LAUNCHED(ctx, "k_lp_append");
+            S.m2 += ka;
+        }
+        ++st->calls;
+        MDET_TRY(lp_call(ctx, S, st));
+        if (++which == sched.size() || i_run == last) break;
+        pos = i_run + 1;
+    }
+    st->graph_edges = S.m2;
+    st->connected = S.norder;
+    k_lp_widen<<<grid_for(n), 256, 0, s>>>(S.mem, n, d_out);
+    MDET_LAUNCHED(ctx, "k_lp_widen");
+    return MDET_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdet_label_propagation_dev(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const double* d_sscr,
+                               uint64_t n_edges, uint64_t n, double max_p, double min_s, uint64_t* d_mem,
+                               mdet_lp_stats* stats) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    mdet_lp_stats st{};
+    if (stats) *stats = st;
+    if (n == 0) return MDET_OK;
+    if (!d_mem || (n_edges && (!d_from || !d_to || !d_sscr))) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    if (n >= 0x7FFFFFFFull || n_edges >= 0x3FFFFFFFull)
+        return ctx_fail(ctx, MDET_ERR_INVALID, "label propagation: 2^31 contigs or 2^30 edges or more");
+    if (!(max_p > 0 && max_p <= 1) || !(min_s >= 0 && min_s < 1))
+        return ctx_fail(ctx, MDET_ERR_INVALID, "label propagation: max_p in (0, 1], min_s in [0, 1)");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, ctx->stream);
+    int rc = lp_impl(ctx, d_from, d_to, d_sscr, n_edges, n, max_p, min_s, d_mem, &st);
+    cudaEventRecord(e1, ctx->stream);
+    if (rc == MDET_OK) {
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        st.ms_total = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == MDET_OK) rc = check_flag(ctx);
+    if (stats) *stats = st;
+    return rc;
+}
+
+int mdet_label_propagation(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* sscr,
+                           uint64_t n_edges, uint64_t n, double max_p, double min_s, uint64_t* mem,
+                           mdet_lp_stats* stats) {
+    if (!ctx) return MDET_ERR_INVALID;
+    MDET_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (n == 0) {
+        if (stats) *stats = mdet_lp_stats{};
+        return MDET_OK;
+    }
+    if (!mem || (n_edges && (!from || !to || !sscr))) return ctx_fail(ctx, MDET_ERR_INVALID, "null pointer");
+    cudaStream_t s = ctx->stream;
+    const uint64_t ne1 = std::max<uint64_t>(n_edges, 1);
+    uint64_t* d_from = (uint64_t*)ctx_scratch(ctx, "lpio.from", ne1 * 8);
+    uint64_t* d_to = (uint64_t*)ctx_scratch(ctx, "lpio.to", ne1 * 8);
+    double* d_s = (double*)ctx_scratch(ctx, "lpio.sscr", ne1 * 8);
+    uint64_t* d_mem = (uint64_t*)ctx_scratch(ctx, "lpio.mem", n * 8);
+    if (!d_from || !d_to || !d_s || !d_mem) return MDET_ERR_NOMEM;
+    if (n_edges) {
+        MDET_CUDA(ctx, cudaMemcpyAsync(d_from, from, n_edges * 8, cudaMemcpyHostToDevice, s));
+        MDET_CUDA(ctx, cudaMemcpyAsync(d_to, to, n_edges * 8, cudaMemcpyHostToDevice, s));
+        MDET_CUDA(ctx, cudaMemcpyAsync(d_s, sscr, n_edges * 8, cudaMemcpyHostToDevice, s));
+    }
+    MDET_TRY(mdet_label_propagation_dev(ctx, d_from, d_to, d_s, n_edges, n, max_p, min_s, d_mem, stats));
+    MDET_CUDA(ctx, cudaMemcpyAsync(mem, d_mem, n * 8, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    return MDET_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// lp_math.h -- the double-precision exp, log and chi-squared CDF of label
+// propagation, written with IEEE-754 basic operations only (+ - * /, and
+// frexp/ldexp, which are exact), so that a host build without contraction of
+// a*b+c (-ffp-contract=off) and a device build without it (-fmad=false) give
+// bit-identical results.  Label propagation picks, per contig, the label
+// with the largest chi-squared CDF and breaks exact ties by a fixed order, so
+// the device and the host checkers must agree to the last bit.
+//
+// Methods (all standard, written here from the mathematics):
+//  * exp: Cody-Waite reduction z = k ln2 + r with ln2 split into a 32-bit
+//    head (k * head exact) and a tail; e^r by the Taylor series to degree 13
+//    (|r| <= ln2/2, truncation below 4e-18); scaling by 2^k with ldexp.
+//  * log: x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
+//    s = (m-1)/(m+1), by the odd series of atanh to s^23 (|s| <= 0.172).
+//  * the chi-squared CDF with 2c degrees of freedom at x is the regularised
+//    lower incomplete gamma P(c, y), y = x/2, for integer c:
+//      y <  c:  P = pois(c; y) * sum_k y^k / ((c+1)...(c+k))
+//      y >= c:  P = 1 - pois(c-1; y) * sum_{i<c} (c-1)!/i! y^(i-c+1)
+//    with pois(j; y) = exp(-y + j log y - log j!) and log j! summed in order.
+//    This replaces boost::math::cdf(chi_squared(2c), x), which the reference
+//    calls (cuda/Cuda2.cu:611-616); Boost is not part of this build.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define LP_HD __host__ __device__ __forceinline__
+#else
+#define LP_HD inline
+#endif
+
+namespace lpm {
+
+constexpr double kLn2Hi = 0x1.62e42fee00000p-1;  // ln 2 to 32 fraction bits
+constexpr double kLn2Lo = 0x1.a39ef35793c76p-33; // ln 2 - kLn2Hi
+constexpr double kInvLn2 = 0x1.71547652b82fep+0;
+constexpr double kSqrtHalf = 0x1.6a09e667f3bcdp-1;
+
+LP_HD double exp(double z) {
+    if (z != z) return z;
+    if (z > 709.0) return INFINITY;
+    if (z < -745.5) return 0.0;
+    const double kd = floor(z * kInvLn2 + 0.5);
+    const double r = (z - kd * kLn2Hi) - kd * kLn2Lo;
+    double p = 1.0 / 6227020800.0;  // 1/13!
+    p = p * r + 1.0 / 479001600.0;
+    p = p * r + 1.0 / 39916800.0;
+    p = p * r + 1.0 / 3628800.0;
+    p = p * r + 1.0 / 362880.0;
+    p = p * r + 1.0 / 40320.0;
+    p = p * r + 1.0 / 5040.0;
+    p = p * r + 1.0 / 720.0;
+    p = p * r + 1.0 / 120.0;
+    p = p * r + 1.0 / 24.0;
+    p = p * r + 1.0 / 6.0;
+    p = p * r + 0.5;
+    p = p * r + 1.0;
+    p = p * r + 1.0;
+    const int k = (int)kd;
+    // two steps keep the intermediate normal when 2^k alone is subnormal
+    if (k < -1000) return ldexp(ldexp(p, k + 64), -64);
+    return ldexp(p, k);
+}
+
+LP_HD double log(double x) {
+    if (x != x || x < 0) return NAN;
+    if (x == 0) return -INFINITY;
+    if (x == INFINITY) return x;
+    int e = 0;
+    double m = frexp(x, &e);  // [0.5, 1)
+    if (m < kSqrtHalf) {
+        m = m * 2.0;
+        e -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double q = 1.0 / 23.0;
+    q = q * s2 + 1.0 / 21.0;
+    q = q * s2 + 1.0 / 19.0;
+    q = q * s2 + 1.0 / 17.0;
+    q = q * s2 + 1.0 / 15.0;
+    q = q * s2 + 1.0 / 13.0;
+    q = q * s2 + 1.0 / 11.0;
+    q = q * s2 + 1.0 / 9.0;
+    q = q * s2 + 1.0 / 7.0;
+    q = q * s2 + 1.0 / 5.0;
+    q = q * s2 + 1.0 / 3.0;
+    const double t = s + (s * s2) * q;
+    const double de = (double)e;
+    return de * kLn2Hi + (de * kLn2Lo + 2.0 * t);
+}
+
+// log(j!) for j = 0..count-1 into out, summed in increasing j
+LP_HD void log_factorials(double* out, uint32_t count) {
+    double acc = 0.0;
+    for (uint32_t j = 0; j < count; ++j) {
+        if (j >= 2) acc = acc + lpm::log((double)j);
+        out[j] = acc;
+    }
+}
+
+// chi-squared CDF with dof = 2c degrees of freedom at x (c >= 1 an
+// integer); logfact[j] = log(j!) for j <= c.
+LP_HD double chi2_cdf(double dof, double x, const double* logfact) {
+    const uint32_t c = (uint32_t)(dof * 0.5);
+    const double y = x * 0.5;
+    if (!(y > 0)) return 0.0;
+    if (y == INFINITY) return 1.0;
+    const double ly = lpm::log(y);
+    if (y < (double)c) {
+        const double lp = (-y + (double)c * ly) - logfact[c];
+        double t = 1.0, v = 1.0;
+        for (uint32_t k = 1; k < 1000000u; ++k) {
+            t = (t * y) / ((double)c + (double)k);
+            v = v + t;
+            if (t < v * 1e-17) break;
+        }
+        return lpm::exp(lp) * v;
+    }
+    const double lq = (-y + (double)(c - 1) * ly) - logfact[c - 1];
+    double u = 1.0, w = 1.0;
+    for (uint32_t i = c - 1; i >= 1; --i) {
+        u = (u * (double)i) / y;
+        w = w + u;
+        if (u < w * 1e-17) break;
+    }
+    return 1.0 - lpm::exp(lq) * w;
+}
+
+}  // namespace lpm

@@ -40,6 +40,14 @@ class RecruitStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class LpStats(ctypes.Structure):
+    _fields_ = [("calls", u64), ("sweeps", u64), ("graph_edges", u64), ("connected", u64), ("frozen", u64),
+                ("ties", u64), ("levels_max", u64), ("degree_max", u64), ("ms_total", D)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class FastaStats(ctypes.Structure):
     _fields_ = [("n_records", u64), ("n_large", u64), ("n_small", u64), ("ms_total", D)]
 
@@ -151,6 +159,8 @@ SIGNATURES = [
     ("mdet_tnf_count_noalloc", ctypes.c_int, [P, u64, P, P, u64, P, P, P]),
     ("mdet_ctx_check_wait", ctypes.c_int, [P, u64]),
     ("mdet_recruit", ctypes.c_int, [P, P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, u64, P, P, P]),
+    ("mdet_label_propagation", ctypes.c_int, [P, P, P, P, u64, u64, D, D, P, ctypes.POINTER(LpStats)]),
+    ("mdet_label_propagation_dev", ctypes.c_int, [P, P, P, P, u64, u64, D, D, P, ctypes.POINTER(LpStats)]),
     ("mdet_tnf_max_prob", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_max_prob_dev", ctypes.c_int, [P, P, P, u64, P, u64, ctypes.c_int, D, P]),
     ("mdet_tnf_ptnf_search", ctypes.c_int, [P, P, P, u64, D, ctypes.c_int, ctypes.POINTER(D)]),
@@ -491,6 +501,29 @@ class Context:
                                           int(min_cls_size), int(small_total), _ptr(out), _ptr(sout),
                                           ctypes.byref(st)))
         return out, sout[:n1], st.as_dict()
+
+    def label_propagation(self, from_, to, sscr, n, max_p=0.95, min_s=0.60):
+        """Bins by label propagation over the scored edges (host arrays;
+        mdet_label_propagation): edge e joins to[e] and from[e].  max_p and
+        min_s are fractions.  Returns (bin of every contig, stats)."""
+        f = np.ascontiguousarray(from_, np.uint64)
+        t = np.ascontiguousarray(to, np.uint64)
+        sc = np.ascontiguousarray(sscr, np.float64)
+        if not (f.size == t.size == sc.size):
+            raise ValueError("from, to and sscr must have the same length")
+        mem = np.zeros(max(n, 1), np.uint64)
+        st = LpStats()
+        self._check(self.lib.mdet_label_propagation(self.h, _ptr(f), _ptr(t), _ptr(sc), sc.size, n, max_p, min_s,
+                                                    _ptr(mem), ctypes.byref(st)))
+        return mem[:n], st.as_dict()
+
+    def label_propagation_dev(self, d_from: int, d_to: int, d_sscr: int, n_edges: int, n: int, d_mem: int,
+                              max_p=0.95, min_s=0.60) -> dict:
+        """Device-pointer form (uint64 from/to, float64 scores, uint64 bins)."""
+        st = LpStats()
+        self._check(self.lib.mdet_label_propagation_dev(self.h, P(d_from), P(d_to), P(d_sscr), n_edges, n, max_p,
+                                                        min_s, P(d_mem), ctypes.byref(st)))
+        return st.as_dict()
 
     def edges_sscr(self, from_, to, stnf, min_cv=1.0, min_sample=3):
         """sTNF -> sSCR of edges (host arrays) with the context's abundance."""

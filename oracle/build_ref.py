@@ -20,7 +20,12 @@ them into this repository:
 * the dissolving of small bins and the recruiting of leftover and small
   contigs (cuda/Cuda2.cu:2064-2283) with cal_abd_corr, cut the same way into
   oracle/_ref/cuda2_recruit.inc and compiled with cuda/ranker.h behind
-  oracle/ref_recruit_shim.cpp -> oracle/_ref/libref_recruit.so.
+  oracle/ref_recruit_shim.cpp -> oracle/_ref/libref_recruit.so;
+* label_propagation (cuda/Cuda2.cu:569-656) and the traversal of main that
+  calls it (cuda/Cuda2.cu:1980-2061), cut the same way into
+  oracle/_ref/cuda2_lp.inc and compiled with cuda/ranker.h behind
+  oracle/ref_lp_shim.cpp (which supplies the chi-squared CDF and LOG of
+  mdet_gb300/csrc/lp_math.h) -> oracle/_ref/libref_lp.so.
 
 Only runs where the reference is mounted (MDET_REFERENCE or /root/reference).
 """
@@ -95,6 +100,20 @@ def extract_recruit(src: str) -> str:
     return corr + "\n\n" + block
 
 
+def extract_lp(src: str) -> str:
+    """label_propagation and the block of main that traverses the scored
+    edges and calls it, the latter wrapped as lp_block(Graph&, nEdges, mems)."""
+    lp = cut_block(src, "int label_propagation(Graph& g, std::vector<size_t>& membership, "
+                        "std::vector<size_t>& node_order) {")
+    a = src.index("            // 4. build sequential graph covering")
+    b = src.index("if (++which_p == p_schedule2.size()) break;", a)
+    b = src.index("}", b)          # the propagation branch
+    b = src.index("}", b + 1)      # the loop over the edges
+    block = ("static int lp_block(Graph& g, size_t nEdges, std::vector<size_t>& mems) {\n" + src[a:b + 1]
+             + "\n    return 0;\n}\n")
+    return lp + "\n\n" + block
+
+
 def main() -> int:
     cuda2 = os.path.join(REF, "cuda", "Cuda2.cu")
     if not os.path.exists(cuda2):
@@ -127,6 +146,14 @@ def main() -> int:
         "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp",
         f"-I{OUT}", f"-I{os.path.join(REF, 'cuda')}", "-o", os.path.join(OUT, "libref_recruit.so"),
         os.path.join(HERE, "ref_recruit_shim.cpp"),
+    ])
+    inc = os.path.join(OUT, "cuda2_lp.inc")
+    with open(inc, "w") as f:
+        f.write(extract_lp(src))
+    subprocess.check_call([
+        "g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+        f"-I{OUT}", f"-I{os.path.join(REF, 'cuda')}", f"-I{os.path.join(HERE, '..', 'mdet_gb300', 'csrc')}",
+        "-o", os.path.join(OUT, "libref_lp.so"), os.path.join(HERE, "ref_lp_shim.cpp"),
     ])
     return 0
 

@@ -67,6 +67,14 @@ def lib():
         L.orc_recruit.argtypes = [P, P, u64, u64, ctypes.c_uint32, P, P, P, u64, u64, P, P, P]
         L.orc_fasta_index.restype = u64
         L.orc_fasta_index.argtypes = [P, u64, u64, P, P, P, P, P]
+        L.orc_label_prop.argtypes = [P, P, P, u64, u64, D, D, P, P]
+        L.orc_umap_order.argtypes = [P, u64, P]
+        L.orc_umap_emulated.argtypes = [P, u64, P]
+        for f in ("orc_lp_log", "orc_lp_exp"):
+            getattr(L, f).restype = D
+            getattr(L, f).argtypes = [D]
+        L.orc_lp_chi2_cdf.restype = D
+        L.orc_lp_chi2_cdf.argtypes = [u64, D]
         _lib = L
     return _lib
 
@@ -265,3 +273,55 @@ def graph_rows(tnf, ls, cutoff, max_edges, rows, threads=0):
     k = lib().orc_tnf_graph_rows(_p(tnf), _p(ls), tnf.shape[0], cutoff, max_edges, _p(rows), rows.size, _p(fr), _p(to),
                                  _p(st), cap, threads)
     return fr[:k], to[:k], st[:k]
+
+
+LP_STATS = ["calls", "sweeps", "graph_edges", "connected", "frozen", "ties"]
+REF_LP = os.path.join(HERE, "_ref", "libref_lp.so")
+
+
+def _lp_args(from_, to, sscr):
+    fr = np.ascontiguousarray(from_, np.uint64)
+    t = np.ascontiguousarray(to, np.uint64)
+    s = np.ascontiguousarray(sscr, np.float64)
+    assert fr.size == t.size == s.size
+    return fr, t, s
+
+
+def label_prop(from_, to, sscr, n, max_p=0.95, min_s=0.60):
+    """The binning traversal and its label propagation calls
+    (orc_label_prop).  Returns (bin of every contig, stats dict)."""
+    fr, t, s = _lp_args(from_, to, sscr)
+    mem = np.zeros(max(n, 1), np.uint64)
+    st = np.zeros(6, np.uint64)
+    lib().orc_label_prop(_p(fr), _p(t), _p(s), s.size, n, max_p, min_s, _p(mem), _p(st))
+    return mem[:n], dict(zip(LP_STATS, (int(x) for x in st)))
+
+
+def ref_label_prop(from_, to, sscr, n, max_p=0.95, min_s=0.60):
+    """The reference's own traversal and label_propagation
+    (oracle/_ref/libref_lp.so, built where the reference is mounted).
+    Returns (bin of every contig, number of propagation calls)."""
+    fr, t, s = _lp_args(from_, to, sscr)
+    L = ctypes.CDLL(REF_LP)
+    L.ref_label_prop.argtypes = [P, P, P, u64, u64, D, D, P]
+    L.ref_label_prop.restype = u64
+    mem = np.zeros(max(n, 1), np.uint64)
+    calls = L.ref_label_prop(_p(fr), _p(t), _p(s), s.size, n, max_p, min_s, _p(mem))
+    return mem[:n], int(calls)
+
+
+def umap_order(keys):
+    """Iteration order of this C++ library's unordered_map after inserting
+    the distinct keys in turn."""
+    k = np.ascontiguousarray(keys, np.uint64)
+    out = np.zeros(max(k.size, 1), np.uint64)
+    lib().orc_umap_order(_p(k), k.size, _p(out))
+    return out[:k.size]
+
+
+def umap_emulated(keys):
+    """The same order from the emulation the device form uses (lp_umap.h)."""
+    k = np.ascontiguousarray(keys, np.uint64)
+    out = np.zeros(max(k.size, 1), np.uint64)
+    lib().orc_umap_emulated(_p(k), k.size, _p(out))
+    return out[:k.size]

@@ -916,3 +916,200 @@ uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t*
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------------------------
+ * Label propagation over the scored edge graph (cuda/Cuda2.cu:1980-2061, the
+ * traversal of main, and label_propagation, cuda/Cuda2.cu:569-656),
+ * restated.  The chi-squared CDF, and the log of 1 - sSCR, are the
+ * project's own host/device functions of mdet_gb300/csrc/lp_math.h (the
+ * reference calls Boost's CDF and the C library's log; Boost is not part of
+ * this build), so that the device form can be held to the last bit.  The
+ * per-contig label tallies are std::unordered_map / unordered_set, as in the
+ * reference: the label picked among exact ties is the first in that map's
+ * iteration order.
+ * ---------------------------------------------------------------------- */
+#include <climits>
+#include <unordered_map>
+#include <unordered_set>
+
+#include "../mdet_gb300/csrc/lp_math.h"
+
+namespace {
+
+struct LpGraph {
+    std::vector<uint64_t> from, to;   // to: the edge's first contig (ii), from: the second (jj)
+    std::vector<double> lw;           // log(1 - sSCR)
+    std::vector<std::vector<uint64_t>> inc;
+};
+
+struct LpFact {
+    std::vector<double> t;
+    const double* at(uint64_t c) {
+        if (t.size() <= c) {
+            t.resize(std::max<uint64_t>(c + 1, 2 * t.size()));
+            lpm::log_factorials(t.data(), (uint32_t)t.size());
+        }
+        return t.data();
+    }
+};
+
+/* One call of label_propagation (cuda/Cuda2.cu:569-656): Gauss-Seidel sweeps
+ * over `order`; each contig takes the neighbour label with the largest
+ * Fisher-combined CDF; a contig that moves back to a label it held earlier
+ * in this call is frozen; the sweeps stop when no contig moved to a new
+ * label, or after 10 sweeps in a row without a new low of such moves. */
+void lp_call(LpGraph& g, std::vector<uint64_t>& mem, const std::vector<uint64_t>& order, LpFact& lf,
+             uint64_t* sweeps, uint64_t* frozen, uint64_t* ties) {
+    std::unordered_map<uint64_t, std::unordered_set<uint64_t>> held;
+    std::unordered_set<uint64_t> stuck;
+    uint64_t low = INT_MAX, attempt = 0;
+    bool again = true;
+    while (again) {
+        again = false;
+        uint64_t moved = 0;
+        ++*sweeps;
+        for (uint64_t v : order) {
+            std::unordered_map<uint64_t, double> score;
+            std::unordered_map<uint64_t, uint64_t> cnt;
+            for (uint64_t e : g.inc[v]) {
+                const uint64_t k = mem[g.from[e] == v ? g.to[e] : g.from[e]];
+                if (score.find(k) == score.end()) {
+                    score[k] = 0.;
+                    cnt[k] = 0;
+                }
+                score[k] += g.lw[e];
+                cnt[k]++;
+            }
+            if (score.empty()) continue;
+            for (auto& kv : score) {
+                const uint64_t c = cnt[kv.first];
+                kv.second = lpm::chi2_cdf(2.0 * (double)c, -2.0 * kv.second, lf.at(c));
+            }
+            auto best = score.begin();
+            for (auto it = score.begin(); it != score.end(); ++it)
+                if (best->second < it->second) best = it;
+            uint64_t at_top = 0;
+            for (auto& kv : score) at_top += kv.second == best->second;
+            *ties += at_top > 1;
+            if (mem[v] != best->first && stuck.find(v) == stuck.end()) {
+                mem[v] = best->first;
+                auto& h = held[v];
+                if (h.insert(best->first).second) {
+                    ++moved;
+                    again = true;
+                } else {
+                    stuck.insert(v);
+                }
+            }
+        }
+        if (moved < low) {
+            low = moved;
+            attempt = 0;
+        } else if (++attempt >= 10) {
+            break;
+        }
+    }
+    *frozen += stuck.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+/* The binning traversal (cuda/Cuda2.cu:1980-2061): edges in decreasing sSCR
+ * (equal scores in edge order; the reference's std::sort leaves their order
+ * open); every contig starts in its own bin; an edge whose two contigs are
+ * in different bins connects them (first-seen order: to before from) and,
+ * when its score is above min_s, joins the traversal graph -- the first such
+ * edge at or below min_s ends the traversal.  Label propagation runs each
+ * time the connected share of the n contigs reaches max_p/10 * (1..10), and
+ * at the last edge; at most 10 times.  mem_out: the bin of every contig.
+ * stats: [0] propagation calls, [1] sweeps, [2] traversal-graph edges,
+ * [3] connected contigs, [4] frozen contigs (summed over calls), [5] contig
+ * updates decided among exactly tied labels. */
+void orc_label_prop(const uint64_t* from, const uint64_t* to, const double* sscr, uint64_t ne, uint64_t n,
+                    double max_p, double min_s, uint64_t* mem_out, uint64_t* stats) {
+    for (int k = 0; k < 6; ++k) stats[k] = 0;
+    std::vector<uint64_t> ord(ne);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](uint64_t a, uint64_t b) { return sscr[a] > sscr[b]; });
+    std::vector<double> sched;
+    for (int i = 1; i <= 10; ++i) sched.push_back(max_p / 10 * i);
+    std::vector<uint64_t> mem(n);
+    std::iota(mem.begin(), mem.end(), 0);
+    std::vector<char> seen(n, 0);
+    std::vector<uint64_t> order;
+    LpGraph g;
+    g.inc.resize(n);
+    LpFact lf;
+    size_t which = 0;
+    for (uint64_t i = 0; i < ne; ++i) {
+        const uint64_t e = ord[i];
+        const uint64_t ii = to[e], jj = from[e];
+        if (mem[ii] != mem[jj]) {
+            if (!seen[ii]) {
+                seen[ii] = 1;
+                order.push_back(ii);
+            }
+            if (!seen[jj]) {
+                seen[jj] = 1;
+                order.push_back(jj);
+            }
+            const double s = sscr[e];
+            if (s > min_s) {
+                g.from.push_back(jj);
+                g.to.push_back(ii);
+                g.lw.push_back(lpm::log(1. - s));
+                g.inc[ii].push_back(g.from.size() - 1);
+                g.inc[jj].push_back(g.from.size() - 1);
+            } else {
+                i = ne - 1;
+            }
+        }
+        if (!g.from.empty() && ((double)order.size() / (double)n >= sched[which] || i == ne - 1)) {
+            ++stats[0];
+            lp_call(g, mem, order, lf, &stats[1], &stats[4], &stats[5]);
+            if (++which == sched.size()) break;
+        }
+    }
+    stats[2] = g.from.size();
+    stats[3] = order.size();
+    for (uint64_t i = 0; i < n; ++i) mem_out[i] = mem[i];
+}
+
+/* Iteration order of std::unordered_map<uint64_t, ...> after inserting the
+ * distinct keys keys[0..k) in turn (as this C++ library lays it out), for
+ * checking the device form's emulation of that order. */
+void orc_umap_order(const uint64_t* keys, uint64_t k, uint64_t* out) {
+    std::unordered_map<uint64_t, double> m;
+    for (uint64_t i = 0; i < k; ++i) m[keys[i]] = 0.;
+    uint64_t j = 0;
+    for (auto& kv : m) out[j++] = kv.first;
+}
+
+/* lp_math.h's functions, for checking them against independent references */
+double orc_lp_log(double x) { return lpm::log(x); }
+double orc_lp_exp(double x) { return lpm::exp(x); }
+double orc_lp_chi2_cdf(uint64_t count, double x) {
+    std::vector<double> lf(count + 1);
+    lpm::log_factorials(lf.data(), (uint32_t)lf.size());
+    return lpm::chi2_cdf(2.0 * (double)count, x, lf.data());
+}
+
+}  // extern "C"
+
+#include "../mdet_gb300/csrc/lp_umap.h"
+
+extern "C" {
+/* lp_umap.h's emulation of that order (the device form's tie rule), for
+ * checking it against orc_umap_order. */
+void orc_umap_emulated(const uint64_t* keys, uint64_t k, uint64_t* out) {
+    std::vector<int32_t> nxt(k + 1), bb(lpu::buckets_for((uint32_t)k));
+    int32_t p = lpu::order(keys, (uint32_t)k, nxt.data(), bb.data());
+    uint64_t j = 0;
+    while (p >= 0) {
+        out[j++] = keys[p];
+        p = nxt[p];
+    }
+}
+}  // extern "C"

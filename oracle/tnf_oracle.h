@@ -130,6 +130,15 @@ void orc_sscr(const uint64_t* from, const uint64_t* to, const double* stnf, uint
 uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t* seq_off, uint64_t* seq_len,
                          uint64_t* size, uint64_t* name_off, uint32_t* name_len);
 
+/* Label propagation: the binning traversal of the scored edges and its
+ * propagation calls (cuda/Cuda2.cu:569-656, 1980-2061); see tnf_oracle.cpp. */
+void orc_label_prop(const uint64_t* from, const uint64_t* to, const double* sscr, uint64_t ne, uint64_t n,
+                    double max_p, double min_s, uint64_t* mem_out, uint64_t* stats);
+void orc_umap_order(const uint64_t* keys, uint64_t k, uint64_t* out);
+double orc_lp_log(double x);
+double orc_lp_exp(double x);
+double orc_lp_chi2_cdf(uint64_t count, double x);
+
 #ifdef __cplusplus
 }
 #endif

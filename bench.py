@@ -362,6 +362,59 @@ def learned_leg(ctx, dev, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_fr
                                                 "final_loss", "tau", "pos_median", "neg_median", "neg_below_tau")}}}
 
 
+def labelprop_leg(ctx, dev, a, d_from, d_to, d_st, ne, n, run_cpu):
+    """Binning by label propagation (mdet_label_propagation) over the step's
+    graph with sSCR = sTNF (the reference's path without a depth file), at
+    the reference's defaults maxP 95, minS 60: 1 untimed and 2 timed calls on
+    the device-resident edges.  The CPU oracle (the reference's traversal and
+    label_propagation restated, std::unordered_map tallies, one thread) runs
+    on the sub-graph of the contigs of the first tenth of the genomes -- the
+    GPU is timed on it too (host buffers) and the bins are compared."""
+    import torch
+
+    mem = torch.empty(n, dtype=torch.int64, device=dev)
+    args = (d_from.data_ptr(), d_to.data_ptr(), d_st.data_ptr(), ne, n, mem.data_ptr())
+    ctx.label_propagation_dev(*args)
+    ctx.set_timing(True)
+    ms = []
+    for _ in range(2):
+        st = ctx.label_propagation_dev(*args)
+        ms.append(st["ms_total"])
+    kms = {k: ctx.kernel_ms(k)[0] / 2 for k in ("k_lp_level", "k_lp_kahn", "k_lp_pred", "k_lp_seg", "k_lp_first",
+                                                 "k_lp_gather", "k_lp_inc_keys")}
+    ctx.set_timing(False)
+    leg = {"metric": "label propagation time (1M-contig graph, sSCR = sTNF)", "value": float(np.median(ms)) / 1e3,
+           "unit": "s", "edges": int(ne), "bins": int(torch.unique(mem).numel()),
+           **{k: st[k] for k in ("calls", "sweeps", "graph_edges", "connected", "frozen", "ties", "levels_max",
+                                 "degree_max")},
+           "kernels_ms": kms, "max_p": 0.95, "min_s": 0.60}
+    # the sub-graph of the first tenth of the genomes, renumbered
+    gsel = a.genome < max(1, int(a.genome.max() + 1) // 10)
+    keep = torch.from_numpy(gsel).to(dev)
+    newid = torch.cumsum(keep.to(torch.int64), 0) - 1
+    m = keep[d_from[:ne]] & keep[d_to[:ne]]
+    fs = newid[d_from[:ne][m]].cpu().numpy().astype(np.uint64)
+    ts = newid[d_to[:ne][m]].cpu().numpy().astype(np.uint64)
+    ss = d_st[:ne][m].cpu().numpy()
+    ns = int(gsel.sum())
+    ctx.label_propagation(fs, ts, ss, ns)
+    t0 = time.perf_counter()
+    g_mem, _ = ctx.label_propagation(fs, ts, ss, ns)
+    leg["sample_gpu_s"] = time.perf_counter() - t0
+    leg["sample"] = f"{ns} contigs of the first tenth of the genomes, {ss.size} edges among them"
+    if run_cpu:
+        from oracle import oracle
+
+        t0 = time.perf_counter()
+        o_mem, _ = oracle.label_prop(fs, ts, ss, ns)
+        dt = time.perf_counter() - t0
+        leg["cpu_baseline"] = {"value": dt, "unit": "s", "cores": 1, "kind": "port",
+                               "sample": leg["sample"] + "; the oracle's restatement on one thread (the reference's "
+                                         "label propagation is single-threaded)"}
+        leg["sample_equal_oracle"] = bool(np.array_equal(g_mem, o_mem))
+    return leg
+
+
 def batch_leg(ctx, dev, count, nmin, nmax, seed):
     """Many independent assemblies in one batched pass (mdet_tnf_graph_batched)
     against one mdet_tnf_graph_dev call per assembly.  `count` assemblies with
@@ -770,7 +823,7 @@ def run_ours(args):
             parity_info["shard_edges"] = info["shard_edges"]
             del full_f, full_t, full_s
             args.no_fasta = args.no_abd = args.no_plain = args.no_recruit = args.no_tf32 = args.no_cpu = True
-            args.no_learned = True
+            args.no_learned = args.no_lp = True
             args.no_batch = True
         else:
             # the host-buffer (e2e) graph equals the device-resident one
@@ -808,6 +861,9 @@ def run_ours(args):
         if not args.no_tf32 and args.mode == "bf16":
             result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,
                                       pk, pk_kind)
+        if not args.no_lp:
+            result["label_propagation"] = labelprop_leg(ctx, dev, a, d_from, d_to, d_st, ne, n,
+                                                        not args.no_cpu and ws == 1)
         if not args.no_learned and args.mode == "bf16":
             result["learned"] = learned_leg(ctx, dev, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from,
                                             d_to, st)
@@ -844,6 +900,7 @@ def run_ours(args):
 #                               assembly vs one batched call
 #   --case fasta --n 100000     FASTA record split of ~0.85 GB on the device
 #   --case abd --n 100000       gated graph, then sTNF -> sSCR of its edges with 10 samples
+#   --case lp --n 1000000       graph, then label propagation over its edges (sSCR = sTNF)
 # The graph case frees the FASTA before the pairwise call so that only the
 # stage's own buffers (~1-2 GB) are resident when it runs.
 
@@ -924,6 +981,19 @@ def run_case(args):
             print({"mode": mode, "edges": ne, **{k: round(v, 3) if isinstance(v, float) else v
                                                  for k, v in st.items()},
                    **{k: round(v, 4) if isinstance(v, float) else v for k, v in extra.items()}}, flush=True)
+    if args.case == "lp":
+        del d_bytes, d_cnt
+        torch.cuda.empty_cache()
+        d_ls = torch.from_numpy(a.log_sizes).to(dev)
+        cap = args.n * 200
+        out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
+        ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, args.mode,
+                                   out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
+        mem = torch.empty(args.n, dtype=torch.int64, device=dev)
+        for _ in range(args.repeat):
+            lst = ctx.label_propagation_dev(out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), ne, args.n,
+                                            mem.data_ptr())
+            print({"edges": ne, "bins": int(torch.unique(mem).numel()), **lst}, flush=True)
     if args.case == "abd":
         del d_bytes, d_cnt
         torch.cuda.empty_cache()
@@ -1061,9 +1131,10 @@ def main():
     ap.add_argument("--no-fasta", action="store_true", help="skip the FASTA ingest leg")
     ap.add_argument("--no-tf32", action="store_true", help="skip the TF32 graph leg")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal graph leg")
+    ap.add_argument("--no-lp", action="store_true", help="skip the label propagation leg")
     ap.add_argument("--no-recruit", action="store_true", help="skip the dissolve / recruit leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-assemblies legs")
-    ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd"], default=None,
+    ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd", "lp"], default=None,
                     help="run one single-stage case instead of the benchmark (profiler workloads)")
     ap.add_argument("--samples", type=int, default=10)
     ap.add_argument("--count", type=int, default=64)

@@ -380,8 +380,9 @@ def labelprop_leg(ctx, dev, a, d_from, d_to, d_st, ne, n, run_cpu):
     for _ in range(2):
         st = ctx.label_propagation_dev(*args)
         ms.append(st["ms_total"])
-    kms = {k: ctx.kernel_ms(k)[0] / 2 for k in ("k_lp_level", "k_lp_kahn", "k_lp_pred", "k_lp_seg", "k_lp_first",
-                                                 "k_lp_gather", "k_lp_inc_keys")}
+    # device time of the sweeps, of building each run's levels, of the
+    # traversal's stretches (per call)
+    kms = {k: ctx.kernel_ms(k)[0] / 2 for k in ("lp_sweep", "lp_levels", "lp_traverse")}
     ctx.set_timing(False)
     leg = {"metric": "label propagation time (1M-contig graph, sSCR = sTNF)", "value": float(np.median(ms)) / 1e3,
            "unit": "s", "edges": int(ne), "bins": int(torch.unique(mem).numel()),
@@ -990,10 +991,13 @@ def run_case(args):
         ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, args.mode,
                                    out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
         mem = torch.empty(args.n, dtype=torch.int64, device=dev)
-        for _ in range(args.repeat):
+        for r in range(args.repeat):
+            ctx.set_timing(r == args.repeat - 1)
             lst = ctx.label_propagation_dev(out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), ne, args.n,
                                             mem.data_ptr())
             print({"edges": ne, "bins": int(torch.unique(mem).numel()), **lst}, flush=True)
+        print({k: ctx.kernel_ms(k) for k in ("lp_sweep", "lp_levels", "lp_traverse")})
+        ctx.set_timing(False)
     if args.case == "abd":
         del d_bytes, d_cnt
         torch.cuda.empty_cache()

@@ -432,7 +432,9 @@ typedef struct {
     uint64_t graph_edges; /* edges in the traversal graph */
     uint64_t connected;   /* contigs in the first-seen order */
     uint64_t frozen;      /* contigs frozen, summed over runs */
-    uint64_t ties;        /* contig updates decided among exactly tied labels */
+    uint64_t ties;        /* evaluations decided among exactly tied labels (a contig none of whose
+                             neighbours changed label since its last evaluation is not evaluated
+                             again: the same label would win) */
     uint64_t levels_max;  /* most dependency levels of a sweep */
     uint64_t degree_max;  /* most traversal-graph edges of a contig */
     double ms_total;      /* device time of the call */

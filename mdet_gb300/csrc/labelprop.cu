@@ -24,7 +24,12 @@
 // contigs with more than 2,048 edges), folds each label's log(1 - score) in
 // edge order (the reference's summation order), evaluates the CDF
 // (lp_math.h, bit-identical to the host checker) and breaks exact ties by the
-// reference map's iteration order (lp_umap.h).  The visited (contig, label)
+// reference map's iteration order (lp_umap.h); contigs with at most 32 edges
+// take a warp each, the keys sorted across its lanes.  A contig none of whose
+// neighbours changed label since its last evaluation is skipped: the same
+// label would win and its update would change nothing -- across runs too:
+// a run's first sweep evaluates the contigs with new edges, those frozen in
+// the previous run, and those whose neighbours changed since.  The visited (contig, label)
 // pairs of a call live in an open-addressing table; a call that overfills it
 // is re-run from its starting labels with a larger table.
 #include <cub/cub.cuh>
@@ -44,6 +49,7 @@ int check_flag(mdet_ctx* ctx);
 namespace {
 
 constexpr uint32_t kSmallCap = 2048;  // incident edges a block sorts in shared memory
+constexpr uint32_t kWarpCap = 32;     // incident edges a warp sorts in registers
 constexpr int kThreads = 256;
 constexpr uint32_t kProbeLimit = 1u << 16;
 
@@ -77,6 +83,7 @@ struct LpArgs {
     const double* lw;         // log(1 - score)
     uint32_t* mem;
     uint8_t* stuck;
+    uint8_t* dirty;           // a neighbour's label changed since the contig was last evaluated
     unsigned long long* vt;   // visited (contig, label) table, 0 = empty
     unsigned long long vt_mask;
     const double* logfact;
@@ -111,11 +118,13 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
     __shared__ double red_v[kThreads / 32];
     __shared__ uint32_t red_c[kThreads / 32];
     __shared__ double s_vmax;
-    __shared__ uint32_t s_ties, s_best;
+    __shared__ uint32_t s_ties, s_best, s_changed;
     const uint32_t v = nodes[blockIdx.x];
     const uint32_t s = P.inc_off[v];
     const uint32_t d = P.inc_off[v + 1] - s;
-    if (d == 0) return;
+    // no neighbour changed since the last evaluation: the same label wins
+    // and the update is a no-op
+    if (d == 0 || !P.dirty[v]) return;
     const uint32_t N = pow2_at_least(d);
     unsigned char* base = smem;
     if (N > kSmallCap) {
@@ -212,9 +221,10 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
             if (val[p] == top) s_best = (uint32_t)(sk[p] >> 32);
     }
     __syncthreads();
-    if (t != 0) return;
-    if (s_ties > 1) {
-        atomicAdd(P.counters + 3, 1ull);
+    if (t == 0) {
+        P.dirty[v] = 0;
+        if (s_ties > 1) {
+            atomicAdd(P.counters + 3, 1ull);
         // the first tied label in the map's iteration order: labels in
         // first-seen order (edge position of their first edge), then the map
         uint32_t K = 0;
@@ -229,15 +239,119 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
         int32_t q = lpu::order(ins, K, nxt, bb);
         while (q >= 0 && val[fidx[q]] != top) q = nxt[q];
         s_best = ins[q >= 0 ? q : 0];
+        }
+        const uint32_t b = s_best;
+        s_changed = 0;
+        if (P.mem[v] != b && !P.stuck[v]) {
+            P.mem[v] = b;
+            s_changed = 1;
+            if (visit(P, v, b))
+                atomicAdd(P.counters, 1ull);
+            else
+                P.stuck[v] = 1;
+        }
     }
-    const uint32_t b = s_best;
-    if (P.mem[v] != b && !P.stuck[v]) {
-        P.mem[v] = b;
-        if (visit(P, v, b))
-            atomicAdd(P.counters, 1ull);
-        else
-            P.stuck[v] = 1;
+    __syncthreads();
+    if (s_changed)
+        for (uint32_t j = t; j < d; j += kThreads) {
+            const uint32_t e = P.inc[s + j];
+            P.dirty[P.ea[e] == v ? P.eb[e] : P.ea[e]] = 1;
+        }
+}
+
+// The same step for contigs with at most 32 edges: a warp per contig, the
+// keys sorted in registers (bitonic over lanes), a lane per edge.
+constexpr int kWarpsPerBlock = kThreads / 32;
+struct WarpWs {
+    unsigned long long sk[32];
+    double w[32];
+    double val[32];
+    int32_t fidx[32];
+    uint32_t ins[32];
+    int32_t nxt[32];
+    int32_t bb[64];  // lpu::buckets_for(32) = 59
+};
+
+__global__ void __launch_bounds__(kThreads) k_lp_level_warp(LpArgs P, const uint32_t* __restrict__ nodes,
+                                                            uint32_t count) {
+    __shared__ WarpWs ws_all[kWarpsPerBlock];
+    const uint32_t wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t idx = blockIdx.x * kWarpsPerBlock + wid;
+    if (idx >= count) return;
+    WarpWs& W = ws_all[wid];
+    const uint32_t v = nodes[idx];
+    const uint32_t s = P.inc_off[v];
+    const uint32_t d = P.inc_off[v + 1] - s;
+    if (d == 0 || !P.dirty[v]) return;  // as in the block form
+    unsigned long long key = ~0ull;
+    uint32_t o = 0;
+    if (lane < d) {
+        const uint32_t e = P.inc[s + lane];
+        o = P.ea[e] == v ? P.eb[e] : P.ea[e];
+        key = ((unsigned long long)P.mem[o] << 32) | lane;
+        W.w[lane] = P.lw[e];
     }
+    W.fidx[lane] = -1;
+    // bitonic sort over the lanes, ascending
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, j);
+            const bool lower = (lane & j) == 0, up = (lane & k) == 0;
+            key = (lower == up) ? (o < key ? o : key) : (o > key ? o : key);
+        }
+    }
+    W.sk[lane] = key;
+    __syncwarp();
+    const uint32_t lab = (uint32_t)(key >> 32);
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, lab, 1);
+    double val = -1.0;
+    if (lane < d && (lane == 0 || prev != lab)) {
+        double sum = 0.0;
+        uint32_t q = lane;
+        do {
+            sum = sum + W.w[(uint32_t)W.sk[q]];
+            ++q;
+        } while (q < d && (uint32_t)(W.sk[q] >> 32) == lab);
+        val = lpm::chi2_cdf(2.0 * (double)(q - lane), -2.0 * sum, P.logfact);
+        W.fidx[(uint32_t)key] = (int32_t)lane;
+    }
+    W.val[lane] = val;
+    double top = val;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) top = fmax(top, __shfl_xor_sync(0xffffffffu, top, o));
+    const unsigned tied = __ballot_sync(0xffffffffu, lane < d && val == top);
+    __syncwarp();
+    uint32_t best = __shfl_sync(0xffffffffu, lab, __ffs(tied) - 1);
+    uint32_t changed = 0;
+    if (lane == 0) {
+        P.dirty[v] = 0;
+        if (__popc(tied) > 1) {
+            atomicAdd(P.counters + 3, 1ull);
+            uint32_t K = 0;
+            for (uint32_t j = 0; j < d; ++j) {
+                const int32_t p = W.fidx[j];
+                if (p >= 0) {
+                    W.fidx[K] = p;  // K <= j: fidx[j] is read before any later write reaches it
+                    W.ins[K] = (uint32_t)(W.sk[p] >> 32);
+                    ++K;
+                }
+            }
+            int32_t q = lpu::order(W.ins, K, W.nxt, W.bb);
+            while (q >= 0 && W.val[W.fidx[q]] != top) q = W.nxt[q];
+            best = W.ins[q >= 0 ? q : 0];
+        }
+        if (P.mem[v] != best && !P.stuck[v]) {
+            P.mem[v] = best;
+            changed = 1;
+            if (visit(P, v, best))
+                atomicAdd(P.counters, 1ull);
+            else
+                P.stuck[v] = 1;
+        }
+    }
+    if (__shfl_sync(0xffffffffu, changed, 0) && lane < d) P.dirty[o] = 1;
 }
 
 // ---- dependency levels of the order --------------------------------------
@@ -247,12 +361,19 @@ __global__ void k_lp_pos(const uint32_t* __restrict__ order, uint32_t norder, ui
     if (i < norder) pos_of[order[i]] = i;
 }
 
+// a level's contigs: those with at most kWarpCap edges (a warp each) and the
+// others (a block each; maxdeg and the global slices are theirs)
 struct LevelInfo {
-    unsigned int count, maxdeg, nbig, pad;
+    unsigned int count, maxdeg, nbig, nsmall, maxall, pad[3];
 };
 
-__device__ __forceinline__ void lp_enqueue(uint32_t w, uint32_t deg, uint32_t* next, LevelInfo* info,
-                                           uint32_t* slot_of) {
+__device__ __forceinline__ void lp_enqueue(uint32_t w, uint32_t deg, uint32_t* next, uint32_t* next_small,
+                                           LevelInfo* info, uint32_t* slot_of) {
+    atomicMax(&info->maxall, deg);
+    if (deg <= kWarpCap) {
+        next_small[atomicAdd(&info->nsmall, 1u)] = w;
+        return;
+    }
     next[atomicAdd(&info->count, 1u)] = w;
     atomicMax(&info->maxdeg, deg);
     if (pow2_at_least(deg) > kSmallCap) slot_of[w] = atomicAdd(&info->nbig, 1u);
@@ -265,8 +386,8 @@ __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ or
                                                  const uint32_t* __restrict__ inc_off,
                                                  const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
                                                  const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
-                                                 uint32_t* __restrict__ level0, LevelInfo* info,
-                                                 uint32_t* __restrict__ slot_of) {
+                                                 uint32_t* __restrict__ level0, uint32_t* __restrict__ level0_small,
+                                                 LevelInfo* info, uint32_t* __restrict__ slot_of) {
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (wid >= norder) return;
     const uint32_t u = order[wid], pu = wid;
@@ -281,7 +402,7 @@ __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ or
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (lane == 0) {
         pred[u] = c;
-        if (c == 0) lp_enqueue(u, d, level0, info, slot_of);
+        if (c == 0) lp_enqueue(u, d, level0, level0_small, info, slot_of);
     }
 }
 
@@ -292,8 +413,8 @@ __global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cu
                                                  const uint32_t* __restrict__ inc_off,
                                                  const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
                                                  const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
-                                                 uint32_t* __restrict__ next, LevelInfo* info,
-                                                 uint32_t* __restrict__ slot_of) {
+                                                 uint32_t* __restrict__ next, uint32_t* __restrict__ next_small,
+                                                 LevelInfo* info, uint32_t* __restrict__ slot_of) {
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (wid >= ncur) return;
     const uint32_t u = cur[wid];
@@ -303,7 +424,7 @@ __global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cu
         const uint32_t e = inc[s + j];
         const uint32_t o = ea[e] == u ? eb[e] : ea[e];
         if (pos_of[o] > pu && atomicSub(pred + o, 1u) == 1u)
-            lp_enqueue(o, inc_off[o + 1] - inc_off[o], next, info, slot_of);
+            lp_enqueue(o, inc_off[o + 1] - inc_off[o], next, next_small, info, slot_of);
     }
 }
 
@@ -324,27 +445,49 @@ __global__ void k_lp_gather(const uint64_t* __restrict__ from, const uint64_t* _
     }
 }
 
-// from position pos: the first differing-bin edge at or below min_s (the
-// early stop) and the first one above it
-__global__ void k_lp_seg(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
-                         const double* __restrict__ ss, uint64_t pos, uint64_t ne, const uint32_t* __restrict__ mem,
-                         double min_s, unsigned long long* __restrict__ out) {
-    for (uint64_t i = pos + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < ne;
+__device__ __forceinline__ unsigned long long block_min(unsigned long long v, unsigned long long* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u < v ? u : v;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (unsigned w = 1; w < blockDim.x / 32; ++w) v = red[w] < v ? red[w] : v;
+    return v;  // valid in thread 0
+}
+
+// over [p0, p1): the first differing-bin edge at or below min_s (the early
+// stop, out[0]) and the first one above it (out[1]); one atomic per block
+__global__ void __launch_bounds__(256) k_lp_seg(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb,
+                                                const double* __restrict__ ss, uint64_t p0, uint64_t p1,
+                                                const uint32_t* __restrict__ mem, double min_s,
+                                                unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long red[8];
+    unsigned long long lo = ~0ull, hi = ~0ull;
+    for (uint64_t i = p0 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p1;
          i += (uint64_t)gridDim.x * blockDim.x) {
         if (mem[sa[i]] == mem[sb[i]]) continue;
-        if (ss[i] > min_s)
-            atomicMin(out + 1, (unsigned long long)i);
-        else
-            atomicMin(out, (unsigned long long)i);
+        if (ss[i] > min_s) {
+            if (hi == ~0ull) hi = i;
+        } else if (lo == ~0ull) {
+            lo = i;
+        }
     }
+    lo = block_min(lo, red);
+    if (threadIdx.x == 0 && lo != ~0ull) atomicMin(out, lo);
+    __syncthreads();
+    hi = block_min(hi, red);
+    if (threadIdx.x == 0 && hi != ~0ull) atomicMin(out + 1, hi);
 }
 
 // first appearance (2 * position, + 1 for the second contig) of the contigs
-// not yet connected, over the differing-bin edges of [pos, last]
-__global__ void k_lp_first(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb, uint64_t pos,
-                           uint64_t last, const uint32_t* __restrict__ mem, const uint8_t* __restrict__ seen,
+// not yet connected, over the differing-bin edges of [p0, p1)
+__global__ void k_lp_first(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb, uint64_t p0,
+                           uint64_t p1, const uint32_t* __restrict__ mem, const uint8_t* __restrict__ seen,
                            unsigned long long* __restrict__ first) {
-    for (uint64_t i = pos + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= last;
+    for (uint64_t i = p0 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < p1;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t a = sa[i], b = sb[i];
         if (mem[a] == mem[b]) continue;
@@ -353,20 +496,36 @@ __global__ void k_lp_first(const uint32_t* __restrict__ sa, const uint32_t* __re
     }
 }
 
+// slot 2k (+1) of [p0, p1) is set when the edge at p0 + k is where its first
+// (second) contig is seen first: the first-seen order of the new contigs is
+// the order of the set slots
+__global__ void k_lp_slots(const uint32_t* __restrict__ sa, const uint32_t* __restrict__ sb, uint64_t p0,
+                           uint64_t cnt, const uint32_t* __restrict__ mem, const uint8_t* __restrict__ seen,
+                           const unsigned long long* __restrict__ first, uint8_t* __restrict__ slot) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= cnt) return;
+    const uint64_t i = p0 + k;
+    const uint32_t a = sa[i], b = sb[i];
+    const bool d = mem[a] != mem[b];
+    slot[2 * k] = d && !seen[a] && first[a] == 2ull * i;
+    slot[2 * k + 1] = d && !seen[b] && first[b] == 2ull * i + 1;
+}
+
+// the contigs of the selected slots, appended to the order and marked
+__global__ void k_lp_take(const uint32_t* __restrict__ sel, uint64_t k, uint64_t p0, const uint32_t* __restrict__ sa,
+                          const uint32_t* __restrict__ sb, uint32_t* __restrict__ order, uint8_t* __restrict__ seen) {
+    const uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (j >= k) return;
+    const uint32_t sl = sel[j];
+    const uint64_t i = p0 + (sl >> 1);
+    const uint32_t v = (sl & 1) ? sb[i] : sa[i];
+    order[j] = v;
+    seen[v] = 1;
+}
+
 __global__ void k_lp_iota(uint32_t* __restrict__ v, uint64_t n) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i < n) v[i] = (uint32_t)i;
-}
-
-__global__ void k_lp_count_le(const unsigned long long* __restrict__ keys, uint64_t n, unsigned long long bound,
-                              unsigned long long* __restrict__ out) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i < n && keys[i] <= bound) atomicAdd(out, 1ull);
-}
-
-__global__ void k_lp_mark(const uint32_t* __restrict__ nodes, uint64_t k, uint8_t* __restrict__ seen) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i < k) seen[nodes[i]] = 1;
 }
 
 // the edges of [pos, end] that join the traversal graph, appended in order
@@ -407,6 +566,22 @@ __global__ void k_lp_inc_keys(const uint32_t* __restrict__ ea, const uint32_t* _
 
 __global__ void k_lp_logfact(double* out, uint32_t count) { lpm::log_factorials(out, count); }
 
+// before a run: contigs with an edge added since the last run, and contigs
+// frozen in the last run (free again now), are evaluated in its first sweep;
+// the others keep their flag
+__global__ void k_lp_dirty_edges(const uint32_t* __restrict__ ea, const uint32_t* __restrict__ eb, uint64_t m0,
+                                 uint64_t m1, uint8_t* __restrict__ dirty) {
+    const uint64_t e = m0 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (e >= m1) return;
+    dirty[ea[e]] = 1;
+    dirty[eb[e]] = 1;
+}
+
+__global__ void k_lp_dirty_stuck(const uint8_t* __restrict__ stuck, uint64_t n, uint8_t* __restrict__ dirty) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n && stuck[i]) dirty[i] = 1;
+}
+
 __global__ void k_lp_count_stuck(const uint8_t* __restrict__ stuck, uint64_t n, unsigned long long* __restrict__ out) {
     unsigned long long c = 0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
@@ -427,11 +602,12 @@ struct LpState {
     uint64_t n = 0, ne = 0;
     uint32_t *sa = nullptr, *sb = nullptr, *mem = nullptr, *mem0 = nullptr, *order = nullptr;
     double* ss = nullptr;
-    uint8_t *seen = nullptr, *stuck = nullptr, *eflag = nullptr;
+    uint8_t *seen = nullptr, *stuck = nullptr, *dirty = nullptr, *dirty0 = nullptr, *eflag = nullptr;
     unsigned long long *first = nullptr, *cnt = nullptr;
     uint32_t *ea = nullptr, *eb = nullptr;
     double* lw = nullptr;
     uint64_t m2 = 0, norder = 0;
+    uint64_t m_run = 0;  // traversal-graph edges at the last propagation run
 };
 
 // One propagation call over the traversal graph (m2 edges) and order.
@@ -448,10 +624,13 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     uint32_t* pos_of = (uint32_t*)ctx_scratch(ctx, "lp.pos", n * 4);
     uint32_t* pred = (uint32_t*)ctx_scratch(ctx, "lp.pred", n * 4);
     uint32_t* lvl = (uint32_t*)ctx_scratch(ctx, "lp.lvl", (no + 1) * 4);
-    uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "lp.slot", n * 4);
-    LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", 16);
-    if (!ikey || !ival || !ikey2 || !inc || !deg || !inc_off || !pos_of || !pred || !lvl || !slot_of || !info)
+    uint32_t* lvls = (uint32_t*)ctx_scratch(ctx, "lp.lvls", (no + 1) * 4);
+    uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "lp.slotof", n * 4);
+    LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", sizeof(LevelInfo));
+    if (!ikey || !ival || !ikey2 || !inc || !deg || !inc_off || !pos_of || !pred || !lvl || !lvls || !slot_of ||
+        !info)
         return MDET_ERR_NOMEM;
+    ctx_timer_begin(ctx, "lp_levels");
     MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (n + 1) * 4, s));
     k_lp_inc_keys<<<grid_for(m), 256, 0, s>>>(S.ea, S.eb, m, ikey, ival, deg);
     MDET_LAUNCHED(ctx, "k_lp_inc_keys");
@@ -467,39 +646,53 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         if (!tmp) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, deg, inc_off, (int)(n + 1), s));
     }
-    // dependency levels
+    // dependency levels: per level, the warp contigs (lvls) and the block
+    // contigs (lvl), each list's levels stored one after another
     MDET_CUDA(ctx, cudaMemsetAsync(pos_of, 0xFF, n * 4, s));
     k_lp_pos<<<grid_for(no), 256, 0, s>>>(S.order, (uint32_t)no, pos_of);
     MDET_LAUNCHED(ctx, "k_lp_pos");
-    MDET_CUDA(ctx, cudaMemsetAsync(info, 0, 16, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
     k_lp_pred<<<grid_for(no * 32), 256, 0, s>>>(S.order, (uint32_t)no, pos_of, inc_off, inc, S.ea, S.eb, pred, lvl,
-                                                 info, slot_of);
+                                                 lvls, info, slot_of);
     MDET_LAUNCHED(ctx, "k_lp_pred");
-    std::vector<uint64_t> loff{0};
+    std::vector<uint64_t> loff{0}, soff{0};
     std::vector<LevelInfo> linfo;
     uint64_t done = 0;
-    uint32_t maxdeg = 0, maxbig = 0;
+    uint32_t maxdeg = 0, maxall = 0, maxbig = 0;
     while (true) {
         LevelInfo h;
-        MDET_CUDA(ctx, cudaMemcpyAsync(&h, info, 16, cudaMemcpyDeviceToHost, s));
+        MDET_CUDA(ctx, cudaMemcpyAsync(&h, info, sizeof(LevelInfo), cudaMemcpyDeviceToHost, s));
         MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        if (h.count == 0) break;
+        if (h.count + h.nsmall == 0) break;
         linfo.push_back(h);
         maxdeg = std::max(maxdeg, h.maxdeg);
+        maxall = std::max(maxall, h.maxall);
         maxbig = std::max(maxbig, h.nbig);
-        const uint64_t cur = loff.back();
-        done = cur + h.count;
-        loff.push_back(done);
+        const uint64_t cur = loff.back(), curs = soff.back();
+        loff.push_back(cur + h.count);
+        soff.push_back(curs + h.nsmall);
+        done += h.count + h.nsmall;
         if (done >= no) break;
-        MDET_CUDA(ctx, cudaMemsetAsync(info, 0, 16, s));
-        k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, inc, S.ea,
-                                                                    S.eb, pred, lvl + done, info, slot_of);
-        MDET_LAUNCHED(ctx, "k_lp_kahn");
+        MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
+        if (h.count) {
+            k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, inc, S.ea,
+                                                                        S.eb, pred, lvl + loff.back(),
+                                                                        lvls + soff.back(), info, slot_of);
+            MDET_LAUNCHED(ctx, "k_lp_kahn");
+        }
+        if (h.nsmall) {
+            k_lp_kahn<<<grid_for((uint64_t)h.nsmall * 32), 256, 0, s>>>(lvls + curs, h.nsmall, pos_of, inc_off, inc,
+                                                                         S.ea, S.eb, pred, lvl + loff.back(),
+                                                                         lvls + soff.back(), info, slot_of);
+            MDET_LAUNCHED(ctx, "k_lp_kahn");
+        }
     }
+    ctx_timer_end(ctx, "lp_levels");
     if (done != no) return ctx_fail(ctx, MDET_ERR_INTERNAL, "label propagation: %llu of %llu contigs levelled",
                                     (unsigned long long)done, (unsigned long long)no);
     st->levels_max = std::max<uint64_t>(st->levels_max, linfo.size());
-    st->degree_max = std::max<uint64_t>(st->degree_max, maxdeg);
+    st->degree_max = std::max<uint64_t>(st->degree_max, maxall);
+    maxdeg = std::max(maxdeg, kWarpCap);
     // the CDF's log-factorials up to the largest label count
     double* logfact = (double*)ctx_scratch(ctx, "lp.logfact", ((uint64_t)maxdeg + 2) * 8);
     if (!logfact) return MDET_ERR_NOMEM;
@@ -518,25 +711,43 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     // its starting labels) when a call overfills it
     uint64_t vt_cap = 1u << 20;
     while (vt_cap < 8 * no) vt_cap <<= 1;
+    // which contigs the first sweep evaluates; kept with the labels for a re-run
+    k_lp_dirty_stuck<<<grid_for(n), 256, 0, s>>>(S.stuck, n, S.dirty);
+    MDET_LAUNCHED(ctx, "k_lp_dirty_stuck");
+    if (m > S.m_run) {
+        k_lp_dirty_edges<<<grid_for(m - S.m_run), 256, 0, s>>>(S.ea, S.eb, S.m_run, m, S.dirty);
+        MDET_LAUNCHED(ctx, "k_lp_dirty_edges");
+    }
+    S.m_run = m;
     MDET_CUDA(ctx, cudaMemcpyAsync(S.mem0, S.mem, n * 4, cudaMemcpyDeviceToDevice, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(S.dirty0, S.dirty, n, cudaMemcpyDeviceToDevice, s));
     for (int attempt_table = 0;; ++attempt_table) {
         unsigned long long* vt = (unsigned long long*)ctx_scratch(ctx, "lp.vt", vt_cap * 8);
         if (!vt) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cudaMemsetAsync(vt, 0, vt_cap * 8, s));
         MDET_CUDA(ctx, cudaMemsetAsync(S.stuck, 0, n, s));
         MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 4 * 8, s));
-        LpArgs P{inc_off, inc, S.ea, S.eb, S.lw, S.mem, S.stuck, vt, vt_cap - 1, logfact, S.cnt, big_ws, big_stride,
-                 maxbig, slot_of};
+        LpArgs P{inc_off, inc, S.ea, S.eb, S.lw, S.mem, S.stuck, S.dirty, vt, vt_cap - 1, logfact, S.cnt, big_ws,
+                 big_stride, maxbig, slot_of};
         uint64_t low = INT_MAX, attempt = 0, sweeps = 0;
         unsigned long long hc[4] = {0, 0, 0, 0};
         bool overfull = false;
         while (true) {
             MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 8, s));
+            ctx_timer_begin(ctx, "lp_sweep");
             for (size_t L = 0; L < linfo.size(); ++L) {
-                const uint32_t cap = std::min<uint32_t>(pow2_at_least(linfo[L].maxdeg), kSmallCap);
-                k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), s>>>(P, lvl + loff[L]);
-                MDET_LAUNCHED(ctx, "k_lp_level");
+                if (linfo[L].nsmall) {
+                    k_lp_level_warp<<<(linfo[L].nsmall + kWarpsPerBlock - 1) / kWarpsPerBlock, kThreads, 0, s>>>(
+                        P, lvls + soff[L], linfo[L].nsmall);
+                    MDET_LAUNCHED(ctx, "k_lp_level_warp");
+                }
+                if (linfo[L].count) {
+                    const uint32_t cap = std::min<uint32_t>(pow2_at_least(linfo[L].maxdeg), kSmallCap);
+                    k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), s>>>(P, lvl + loff[L]);
+                    MDET_LAUNCHED(ctx, "k_lp_level");
+                }
             }
+            ctx_timer_end(ctx, "lp_sweep");
             MDET_CUDA(ctx, cudaMemcpyAsync(hc, S.cnt, 32, cudaMemcpyDeviceToHost, s));
             MDET_CUDA(ctx, cudaStreamSynchronize(s));
             ++sweeps;
@@ -563,6 +774,7 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         if (attempt_table >= 6) return ctx_fail(ctx, MDET_ERR_CAPACITY, "label propagation: visited table");
         vt_cap <<= 1;
         MDET_CUDA(ctx, cudaMemcpyAsync(S.mem, S.mem0, n * 4, cudaMemcpyDeviceToDevice, s));
+        MDET_CUDA(ctx, cudaMemcpyAsync(S.dirty, S.dirty0, n, cudaMemcpyDeviceToDevice, s));
     }
     MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
     k_lp_count_stuck<<<std::min<unsigned>(grid_for(n), 1024), 256, 0, s>>>(S.stuck, n, S.cnt + 2);
@@ -592,22 +804,26 @@ int lp_impl(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const d
     S.order = (uint32_t*)ctx_scratch(ctx, "lp.order", n * 4);
     S.seen = (uint8_t*)ctx_scratch(ctx, "lp.seen", n);
     S.stuck = (uint8_t*)ctx_scratch(ctx, "lp.stuck", n);
-    S.eflag = (uint8_t*)ctx_scratch(ctx, "lp.eflag", ne1);
+    S.dirty = (uint8_t*)ctx_scratch(ctx, "lp.dirty", n);
+    S.dirty0 = (uint8_t*)ctx_scratch(ctx, "lp.dirty0", n);
+    S.eflag = (uint8_t*)ctx_scratch(ctx, "lp.eflag", std::min<uint64_t>(ne1, 1ull << 22));
     S.first = (unsigned long long*)ctx_scratch(ctx, "lp.first", n * 8);
     S.cnt = (unsigned long long*)ctx_scratch(ctx, "lp.cnt", 64);
     S.ea = (uint32_t*)ctx_scratch(ctx, "lp.ea", ne1 * 4);
     S.eb = (uint32_t*)ctx_scratch(ctx, "lp.eb", ne1 * 4);
     S.lw = (double*)ctx_scratch(ctx, "lp.lw", ne1 * 8);
-    unsigned long long* fkeys = (unsigned long long*)ctx_scratch(ctx, "lp.fkeys", n * 8);
-    uint32_t* nodes0 = (uint32_t*)ctx_scratch(ctx, "lp.nodes0", n * 4);
-    uint32_t* nodes = (uint32_t*)ctx_scratch(ctx, "lp.nodes", n * 4);
-    uint32_t* sel = (uint32_t*)ctx_scratch(ctx, "lp.sel", ne1 * 4);
-    if (!ord0 || !ord || !key2 || !S.sa || !S.sb || !S.ss || !S.mem || !S.mem0 || !S.order || !S.seen || !S.stuck ||
-        !S.eflag || !S.first || !S.cnt || !S.ea || !S.eb || !S.lw || !fkeys || !nodes0 || !nodes || !sel)
+    const uint64_t kChunk = std::min<uint64_t>(ne1, 1ull << 22);  // edges traversed per pass
+    uint8_t* slot = (uint8_t*)ctx_scratch(ctx, "lp.slot", 2 * kChunk);
+    uint32_t* ssel = (uint32_t*)ctx_scratch(ctx, "lp.ssel", 2 * kChunk * 4);
+    uint32_t* sel = (uint32_t*)ctx_scratch(ctx, "lp.sel", kChunk * 4);
+    if (!ord0 || !ord || !key2 || !S.sa || !S.sb || !S.ss || !S.mem || !S.mem0 || !S.order || !S.seen || !S.stuck || !S.dirty || !S.dirty0 ||
+        !S.eflag || !S.first || !S.cnt || !S.ea || !S.eb || !S.lw || !slot || !ssel || !sel)
         return MDET_ERR_NOMEM;
     k_lp_iota<<<grid_for(n), 256, 0, s>>>(S.mem, n);
     MDET_LAUNCHED(ctx, "k_lp_iota");
     MDET_CUDA(ctx, cudaMemsetAsync(S.seen, 0, n, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(S.stuck, 0, n, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(S.dirty, 0, n, s));
     if (ne) {
         // edges by decreasing score; equal scores keep edge order (stable)
         k_lp_iota<<<grid_for(ne), 256, 0, s>>>(ord0, ne);
@@ -630,93 +846,105 @@ int lp_impl(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to, const d
     for (int i = 1; i <= 10; ++i) sched.push_back(max_p / 10 * i);
     size_t which = 0;
     uint64_t pos = 0;
+    constexpr uint64_t kNone = ~0ull;
+    // select the set flags of [0, cnt) into out; returns how many
+    auto select = [&](const uint8_t* flags, uint64_t cnt, uint32_t* out, const char* tag) -> long long {
+        thrust::counting_iterator<uint32_t> it(0);
+        size_t tb = 0;
+        cub::DeviceSelect::Flagged(nullptr, tb, it, flags, out, S.cnt + 3, (int)cnt, s);
+        void* tmp = ctx_scratch(ctx, tag, tb);
+        if (!tmp) return -MDET_ERR_NOMEM;
+        if (ctx_cuda(ctx, cub::DeviceSelect::Flagged(tmp, tb, it, flags, out, S.cnt + 3, (int)cnt, s), "select"))
+            return -MDET_ERR_CUDA;
+        unsigned long long k = 0;
+        if (ctx_cuda(ctx, cudaMemcpyAsync(&k, S.cnt + 3, 8, cudaMemcpyDeviceToHost, s), "select count") ||
+            ctx_cuda(ctx, cudaStreamSynchronize(s), "select count"))
+            return -MDET_ERR_CUDA;
+        return (long long)k;
+    };
     while (ne && pos < ne) {
-        // the stretch from pos: early stop and first joining edge
-        unsigned long long h2[2] = {~0ull, ~0ull};
-        MDET_CUDA(ctx, cudaMemcpyAsync(S.cnt, h2, 16, cudaMemcpyHostToDevice, s));
-        k_lp_seg<<<std::min<unsigned>(grid_for(ne - pos), 8 * ctx->num_sms), 256, 0, s>>>(S.sa, S.sb, S.ss, pos, ne,
-                                                                                          S.mem, min_s, S.cnt);
-        MDET_LAUNCHED(ctx, "k_lp_seg");
-        MDET_CUDA(ctx, cudaMemcpyAsync(h2, S.cnt, 16, cudaMemcpyDeviceToHost, s));
-        MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        const uint64_t stop = h2[0] < ne ? h2[0] : ne;
-        const uint64_t last = stop < ne ? stop : ne - 1;
-        const uint64_t first_add = h2[1];
-        // first appearances of new contigs over [pos, last], in order
+        ctx_timer_begin(ctx, "lp_traverse");
         MDET_CUDA(ctx, cudaMemsetAsync(S.first, 0xFF, n * 8, s));
-        k_lp_first<<<std::min<unsigned>(grid_for(last - pos + 1), 8 * ctx->num_sms), 256, 0, s>>>(
-            S.sa, S.sb, pos, last, S.mem, S.seen, S.first);
-        MDET_LAUNCHED(ctx, "k_lp_first");
-        k_lp_iota<<<grid_for(n), 256, 0, s>>>(nodes0, n);
-        MDET_LAUNCHED(ctx, "k_lp_iota");
-        {
-            size_t tb = 0;
-            cub::DeviceRadixSort::SortPairs(nullptr, tb, S.first, fkeys, nodes0, nodes, (int)n, 0, 64, s);
-            void* tmp = ctx_scratch(ctx, "lp.nsort", tb);
-            if (!tmp) return MDET_ERR_NOMEM;
-            MDET_CUDA(ctx, cub::DeviceRadixSort::SortPairs(tmp, tb, S.first, fkeys, nodes0, nodes, (int)n, 0, 64, s));
-        }
-        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
-        k_lp_count_le<<<grid_for(n), 256, 0, s>>>(fkeys, n, ~0ull - 1, S.cnt + 2);
-        MDET_LAUNCHED(ctx, "k_lp_count_le");
-        unsigned long long nn = 0;
-        MDET_CUDA(ctx, cudaMemcpyAsync(&nn, S.cnt + 2, 8, cudaMemcpyDeviceToHost, s));
-        MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        // the run position: the first edge where the graph has an edge and
-        // the connected count reaches the schedule, or the last edge
+        // connected contigs the schedule asks for
         const double thr = sched[which];
         uint64_t c_need = (uint64_t)std::ceil(thr * (double)n);
         while (c_need > 0 && (double)(c_need - 1) / (double)n >= thr) --c_need;
         while ((double)c_need / (double)n < thr) ++c_need;
-        const bool have_edge = S.m2 > 0 || first_add <= last;
-        if (!have_edge) break;  // no edge joins: the traversal ends without a run
-        const uint64_t i_e = S.m2 > 0 ? pos : first_add;
-        uint64_t i_run = last;
-        if (c_need <= S.norder) {
-            i_run = std::max(pos, i_e);
-        } else if (c_need <= S.norder + nn) {
-            unsigned long long key = 0;
-            MDET_CUDA(ctx, cudaMemcpyAsync(&key, fkeys + (c_need - S.norder - 1), 8, cudaMemcpyDeviceToHost, s));
+        uint64_t first_add = S.m2 > 0 ? pos : kNone;   // the graph has an edge from here on
+        uint64_t i_c = c_need <= S.norder ? pos : kNone;  // the connected count is reached here
+        uint64_t i_run = kNone;
+        bool at_last = false, ended = false;
+        // the stretch from pos, a chunk at a time, until the run position
+        for (uint64_t p0 = pos;;) {
+            const uint64_t p1 = std::min(ne, p0 + kChunk);
+            unsigned long long h2[2] = {kNone, kNone};
+            MDET_CUDA(ctx, cudaMemcpyAsync(S.cnt, h2, 16, cudaMemcpyHostToDevice, s));
+            k_lp_seg<<<std::min<unsigned>(grid_for(p1 - p0), 8 * ctx->num_sms), 256, 0, s>>>(S.sa, S.sb, S.ss, p0,
+                                                                                             p1, S.mem, min_s, S.cnt);
+            MDET_LAUNCHED(ctx, "k_lp_seg");
+            MDET_CUDA(ctx, cudaMemcpyAsync(h2, S.cnt, 16, cudaMemcpyDeviceToHost, s));
             MDET_CUDA(ctx, cudaStreamSynchronize(s));
-            i_run = std::max<uint64_t>(key >> 1, i_e);
+            const bool stop_here = h2[0] != kNone;
+            const uint64_t end = stop_here ? h2[0] + 1 : p1;   // [p0, end) is traversed
+            const uint64_t last_here = end - 1;
+            const bool is_last = stop_here || p1 == ne;
+            if (first_add == kNone && h2[1] != kNone && h2[1] < end) first_add = h2[1];
+            // the contigs first seen in [p0, end), in first-seen order
+            k_lp_first<<<std::min<unsigned>(grid_for(end - p0), 8 * ctx->num_sms), 256, 0, s>>>(
+                S.sa, S.sb, p0, end, S.mem, S.seen, S.first);
+            MDET_LAUNCHED(ctx, "k_lp_first");
+            k_lp_slots<<<grid_for(end - p0), 256, 0, s>>>(S.sa, S.sb, p0, end - p0, S.mem, S.seen, S.first, slot);
+            MDET_LAUNCHED(ctx, "k_lp_slots");
+            const long long kn = select(slot, 2 * (end - p0), ssel, "lp.seltmp");
+            if (kn < 0) return (int)-kn;
+            if (i_c == kNone && S.norder + (uint64_t)kn >= c_need) {
+                uint32_t sl = 0;
+                MDET_CUDA(ctx, cudaMemcpyAsync(&sl, ssel + (c_need - S.norder - 1), 4, cudaMemcpyDeviceToHost, s));
+                MDET_CUDA(ctx, cudaStreamSynchronize(s));
+                i_c = p0 + (sl >> 1);
+            }
+            if (first_add != kNone && i_c != kNone && std::max(i_c, first_add) <= last_here) {
+                i_run = std::max(i_c, first_add);
+            } else if (is_last) {
+                if (first_add != kNone)
+                    i_run = last_here;
+                else
+                    ended = true;  // no edge joins: the traversal ends without a run
+            }
+            at_last = is_last && i_run == last_here;
+            // commit [p0, cend): the new contigs and the joining edges
+            const uint64_t cend = i_run != kNone ? i_run + 1 : end;
+            uint64_t kc = (uint64_t)kn;
+            if (cend < end && kn > 0) {  // the selected slots below 2 * (cend - p0), by bisection
+                std::vector<uint32_t> hs((size_t)kn);
+                MDET_CUDA(ctx, cudaMemcpyAsync(hs.data(), ssel, (size_t)kn * 4, cudaMemcpyDeviceToHost, s));
+                MDET_CUDA(ctx, cudaStreamSynchronize(s));
+                kc = (uint64_t)(std::lower_bound(hs.begin(), hs.end(), (uint32_t)(2 * (cend - p0))) - hs.begin());
+            }
+            if (kc) {
+                k_lp_take<<<grid_for(kc), 256, 0, s>>>(ssel, kc, p0, S.sa, S.sb, S.order + S.norder, S.seen);
+                MDET_LAUNCHED(ctx, "k_lp_take");
+                S.norder += kc;
+            }
+            k_lp_edge_flags<<<grid_for(cend - p0), 256, 0, s>>>(S.sa, S.sb, S.ss, p0, cend - p0, S.mem, min_s,
+                                                                 S.eflag);
+            MDET_LAUNCHED(ctx, "k_lp_edge_flags");
+            const long long ka = select(S.eflag, cend - p0, sel, "lp.seltmp2");
+            if (ka < 0) return (int)-ka;
+            if (ka) {
+                k_lp_append<<<grid_for((uint64_t)ka), 256, 0, s>>>(sel, (uint64_t)ka, p0, S.sa, S.sb, S.ss,
+                                                                  S.ea + S.m2, S.eb + S.m2, S.lw + S.m2);
+                MDET_LAUNCHED(ctx, "k_lp_append");
+                S.m2 += (uint64_t)ka;
+            }
+            if (i_run != kNone || ended) break;
+            p0 = end;
         }
-        if (i_run > last) i_run = last;
-        // commit [pos, i_run]: new contigs in first-seen order, joining edges
-        MDET_CUDA(ctx, cudaMemsetAsync(S.cnt + 2, 0, 8, s));
-        k_lp_count_le<<<grid_for(nn), 256, 0, s>>>(fkeys, nn, 2ull * i_run + 1, S.cnt + 2);
-        MDET_LAUNCHED(ctx, "k_lp_count_le");
-        unsigned long long kc = 0;
-        MDET_CUDA(ctx, cudaMemcpyAsync(&kc, S.cnt + 2, 8, cudaMemcpyDeviceToHost, s));
-        MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        if (kc) {
-            MDET_CUDA(ctx, cudaMemcpyAsync(S.order + S.norder, nodes, kc * 4, cudaMemcpyDeviceToDevice, s));
-            k_lp_mark<<<grid_for(kc), 256, 0, s>>>(nodes, kc, S.seen);
-            MDET_LAUNCHED(ctx, "k_lp_mark");
-            S.norder += kc;
-        }
-        const uint64_t span = i_run - pos + 1;
-        k_lp_edge_flags<<<grid_for(span), 256, 0, s>>>(S.sa, S.sb, S.ss, pos, span, S.mem, min_s, S.eflag);
-        MDET_LAUNCHED(ctx, "k_lp_edge_flags");
-        {
-            thrust::counting_iterator<uint32_t> it(0);
-            size_t tb = 0;
-            cub::DeviceSelect::Flagged(nullptr, tb, it, S.eflag, sel, S.cnt + 3, (int)span, s);
-            void* tmp = ctx_scratch(ctx, "lp.seltmp", tb);
-            if (!tmp) return MDET_ERR_NOMEM;
-            MDET_CUDA(ctx, cub::DeviceSelect::Flagged(tmp, tb, it, S.eflag, sel, S.cnt + 3, (int)span, s));
-        }
-        unsigned long long ka = 0;
-        MDET_CUDA(ctx, cudaMemcpyAsync(&ka, S.cnt + 3, 8, cudaMemcpyDeviceToHost, s));
-        MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        if (ka) {
-            k_lp_append<<<grid_for(ka), 256, 0, s>>>(sel, ka, pos, S.sa, S.sb, S.ss, S.ea + S.m2, S.eb + S.m2,
-                                                    S.lw + S.m2);
-            MDET_LAUNCHED(ctx, "k_lp_append");
-            S.m2 += ka;
-        }
+        ctx_timer_end(ctx, "lp_traverse");
+        if (ended) break;
         ++st->calls;
         MDET_TRY(lp_call(ctx, S, st));
-        if (++which == sched.size() || i_run == last) break;
+        if (++which == sched.size() || at_last) break;
         pos = i_run + 1;
     }
     st->graph_edges = S.m2;

@@ -31,6 +31,7 @@ CU_UNITS = [
     "graph_exact",
     "graph",
     "learned",
+    "mlp_tc",
     "graph_learned",
     "graph_batch",
     "abundance",

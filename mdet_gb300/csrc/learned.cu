@@ -341,15 +341,7 @@ int mlp_backward(mdet_ctx* ctx, const float* P, const MlpActs& a, uint64_t np, c
 }
 
 int mlp_embed(mdet_ctx* ctx, const float* P, const float* tnf, uint64_t n, float* z) {
-    const uint64_t chunk = 1u << 18;
-    for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
-        const uint64_t k = std::min(chunk, n - r0);
-        MlpActs a;
-        MDET_TRY(mlp_alloc_acts(ctx, "mlpe", k, &a));
-        a.z3 = z + r0 * MLP_OUT;
-        MDET_TRY(mlp_forward(ctx, P, tnf + r0 * MLP_IN, nullptr, k, a));
-    }
-    return MDET_OK;
+    return mlp_embed_tc(ctx, P, tnf, n, z);
 }
 
 int mlp_gram(mdet_ctx* ctx, const float* z, uint64_t n, float* G) {

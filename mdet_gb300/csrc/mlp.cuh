@@ -1,8 +1,9 @@
 // mlp.cuh -- the embedding network of the learned proposal: 136 -> 256 ->
 // 128 -> 64 with GELU, BF16 weights (the FP32 master copy is rounded to
 // BF16 wherever a GEMM reads it), FP32 accumulation.  Kernels are this
-// project's own: tiled SIMT GEMMs for forward and backward, GELU and its
-// derivative, a contrastive pair loss and Adam.
+// project's own: inference on the tensor cores (tcgen05, mlp_tc.cu, BF16
+// activations); training with tiled SIMT GEMMs for forward and backward (FP32
+// activations), GELU and its derivative, a contrastive pair loss and Adam.
 #pragma once
 
 #include "graph.cuh"
@@ -50,8 +51,10 @@ int mlp_forward(mdet_ctx* ctx, const float* params, const float* tnf, const uint
 int mlp_backward(mdet_ctx* ctx, const float* params, const MlpActs& a, uint64_t npairs, const float* labels,
                  float m_pos, float m_neg, float* grad, double* loss_sum);
 int mlp_alloc_acts(mdet_ctx* ctx, const char* tag, uint64_t rows, MlpActs* a);
-// Embeddings of n rows (original order) into z (n x 64).
+// Embeddings of n rows (original order) into z (n x 64): the tensor-core
+// inference kernel of mlp_tc.cu (BF16 activations, FP32 accumulation).
 int mlp_embed(mdet_ctx* ctx, const float* params, const float* tnf, uint64_t n, float* z);
+int mlp_embed_tc(mdet_ctx* ctx, const float* params, const float* tnf, uint64_t n, float* z);
 // G = Z^T Z (64 x 64, accumulated into a zeroed G) and P = Z V (n x k, V 64 x k).
 int mlp_gram(mdet_ctx* ctx, const float* z, uint64_t n, float* G);
 // column sums of Z added into a zeroed s (64)

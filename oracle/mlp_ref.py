@@ -75,6 +75,17 @@ def embed(p: np.ndarray, tnf: np.ndarray) -> np.ndarray:
     return forward(p, tnf)["z3"]
 
 
+def embed_bf16(p: np.ndarray, tnf: np.ndarray) -> np.ndarray:
+    """The inference form: the inputs of every layer (the centred, scaled
+    rows and the two hidden activations) rounded to BF16 as well, float64
+    sums otherwise."""
+    w = unpack(p, True)
+    x = bf16_round((np.asarray(tnf, np.float64) - w["mu"]) * w["scale"])
+    h1 = bf16_round(_gelu(x @ w["W1"].T + w["b1"]))
+    h2 = bf16_round(_gelu(h1 @ w["W2"].T + w["b2"]))
+    return h2 @ w["W3"].T + w["b3"]
+
+
 def loss_and_grad(p: np.ndarray, x: np.ndarray, pairs: np.ndarray, labels: np.ndarray, m_pos: float,
                   m_neg: float, rounded: bool = True):
     """Mean pair loss and its gradient (NTRAIN entries: W1 b1 W2 b2 W3 b3)."""

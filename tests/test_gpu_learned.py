@@ -1,5 +1,5 @@
-"""The learned proposal on the GPU: the network's forward pass and gradient
-against the float64 oracle (oracle/mlp_ref.py), training on one generated
+"""The learned proposal on the GPU: the network's tensor-core inference and
+its training gradient against the float64 oracle (oracle/mlp_ref.py), training on one generated
 assembly and the learned graph on another, with recall against the
 all-pairs graph and the gain over the same method with an untrained network."""
 import os
@@ -61,9 +61,17 @@ def test_embedding_matches_oracle(gpu_ctx):
     torch.cuda.synchronize()
     net.embed_dev(dx.data_ptr(), n, dz.data_ptr())
     z = dz.cpu().numpy()
-    ref = R.embed(p, x)
-    err = np.abs(z - ref).max() / np.abs(ref).max()
-    assert err < 1e-5, err
+    # inference runs on the tensor cores with BF16 layer inputs: against the
+    # oracle that rounds the same inputs, the differences come from FP32
+    # accumulation and from the rare value that lands on the other side of a
+    # BF16 rounding boundary
+    ref = R.embed_bf16(p, x)
+    scale = np.abs(ref).max()
+    err = np.abs(z - ref)
+    assert err.max() / scale < 3e-3, err.max() / scale
+    assert err.mean() / scale < 1e-4, err.mean() / scale
+    # and close to the FP32-activation network the training path computes
+    assert np.abs(z - R.embed(p, x)).max() / scale < 3e-2
     net.close()
 
 

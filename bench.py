@@ -61,18 +61,21 @@ def assembly_seed(rank: int) -> int:
 
 
 def filter_traffic():
-    """DRAM bytes (read + write) per k_filter_tc launch of this step, from the
-    one-pass ncu capture summarised in profiles/k_filter_tc_1M_traffic.md
-    (None when the summary is absent)."""
+    """DRAM bytes (read + write) from the one-pass ncu capture summarised in
+    profiles/k_filter_tc_1M_traffic.md: per k_filter_tc launch of the step
+    (averaged over its 11 launches, like `achieved`), and of the main graph
+    launch with its algorithmic bytes.  None where the summary is absent."""
     path = os.path.join(ROOT, "profiles", "k_filter_tc_1M_traffic.md")
+    out = {}
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":", 1)[1])
+                for key in ("traffic_bytes_per_launch", "main_launch_traffic_bytes", "main_launch_algorithmic_bytes"):
+                    if line.startswith(key + ":"):
+                        out[key] = int(line.split(":", 1)[1])
     except OSError:
         pass
-    return None
+    return out
 
 
 def reduce_max(value: float, device) -> float:
@@ -755,8 +758,11 @@ def run_ours(args):
             flops_step = 2 * 136 * (pairs_graph + pairs_sample)
             achieved = flops_step * args.steps / (dom_ms / 1e3) / 1e12
             peak_v = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+            tr = filter_traffic() if (n == 1_000_000 and args.mode == "bf16" and ws == 1) else {}
             roof = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak_v, "unit": "TFLOP/s",
-                    "frac": achieved / peak_v, "traffic": filter_traffic() if (n == 1_000_000 and args.mode == "bf16") else None,
+                    "frac": achieved / peak_v, "traffic": tr.get("traffic_bytes_per_launch"),
+                    "traffic_main_launch": tr.get("main_launch_traffic_bytes"),
+                    "algorithmic_bytes_main_launch": tr.get("main_launch_algorithmic_bytes"),
                     "algorithmic_per_launch": flops_step * args.steps / dom_launches,
                     "avg_launch_ms": dom_ms / dom_launches, "peak_source": f"bf16 sustained ({pk_kind})"}
         else:

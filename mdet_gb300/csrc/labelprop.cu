@@ -608,6 +608,8 @@ struct LpState {
     double* lw = nullptr;
     uint64_t m2 = 0, norder = 0;
     uint64_t m_run = 0;  // traversal-graph edges at the last propagation run
+    double* logfact = nullptr;  // log(j!) for j < logfact_n
+    uint64_t logfact_n = 0;
 };
 
 // One propagation call over the traversal graph (m2 edges) and order.
@@ -694,10 +696,17 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     st->degree_max = std::max<uint64_t>(st->degree_max, maxall);
     maxdeg = std::max(maxdeg, kWarpCap);
     // the CDF's log-factorials up to the largest label count
-    double* logfact = (double*)ctx_scratch(ctx, "lp.logfact", ((uint64_t)maxdeg + 2) * 8);
-    if (!logfact) return MDET_ERR_NOMEM;
-    k_lp_logfact<<<1, 1, 0, s>>>(logfact, maxdeg + 2);
-    MDET_LAUNCHED(ctx, "k_lp_logfact");
+    // (one thread sums the table in order; it is rebuilt only when a run
+    // needs a longer one)
+    if ((uint64_t)maxdeg + 2 > S.logfact_n) {
+        const uint64_t len = std::max<uint64_t>((uint64_t)maxdeg + 2, 2 * S.logfact_n);
+        S.logfact = (double*)ctx_scratch(ctx, "lp.logfact", len * 8);
+        if (!S.logfact) return MDET_ERR_NOMEM;
+        k_lp_logfact<<<1, 1, 0, s>>>(S.logfact, (uint32_t)len);
+        MDET_LAUNCHED(ctx, "k_lp_logfact");
+        S.logfact_n = len;
+    }
+    const double* logfact = S.logfact;
     // global sort slices for the contigs with more than kSmallCap edges
     const size_t big_stride = maxdeg > kSmallCap ? (ws_bytes(pow2_at_least(maxdeg)) + 255) / 256 * 256 : 0;
     unsigned char* big_ws = nullptr;

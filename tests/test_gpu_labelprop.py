@@ -91,6 +91,30 @@ def test_tnf_graph_scale(gpu_ctx):
     assert st["calls"] == ost["calls"] and st["sweeps"] == ost["sweeps"]
 
 
+def test_config0_scored_graph(gpu_ctx):
+    """The plain config's assembly (20,000 contigs, 50 genomes) through the
+    whole binning front: the GPU's gated graph and its sSCR with 10 samples of
+    depths, then label propagation -- bins equal to the oracle's on the same
+    edges, at the reference's defaults and at a stricter minS."""
+    from gpu_util import synth_set
+
+    from mdet_gb300 import synth
+
+    a, _, tnf = synth_set(seed=7, n=20000, genomes=50)
+    abd, var = synth.abundance(a.genome, 10, 77)
+    gpu_ctx.set_abundance(abd, var)
+    g = gpu_ctx.tnf_graph(tnf, a.log_sizes, 0.95, 200, mode="bf16")
+    sc = gpu_ctx.edges_sscr(g.from_, g.to, g.sTNF)
+    gpu_ctx.set_abundance(None, None)
+    assert np.allclose(sc, oracle.sscr(g.from_, g.to, g.sTNF, abd, var), rtol=1e-12, atol=1e-12)
+    for mp, ms in [(0.95, 0.60), (0.95, 0.80)]:
+        want, ost = oracle.label_prop(g.from_, g.to, sc, 20000, mp, ms)
+        got, st = gpu_ctx.label_propagation(g.from_, g.to, sc, 20000, mp, ms)
+        assert np.array_equal(got, want)
+        assert st["calls"] == ost["calls"] and st["sweeps"] == ost["sweeps"]
+        assert len(np.unique(got)) < 20000
+
+
 def test_degenerate_inputs(gpu_ctx):
     mem, st = gpu_ctx.label_propagation([], [], [], 5)
     assert mem.tolist() == list(range(5)) and st["calls"] == 0

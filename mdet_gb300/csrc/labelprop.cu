@@ -612,6 +612,36 @@ struct LpState {
     uint64_t logfact_n = 0;
 };
 
+// A CUDA graph recorded from a body of stream work (owned; freed on scope exit).
+struct SweepGraph {
+    cudaGraphExec_t exec = nullptr;
+    uint64_t launches = 0;  // kernels in the graph
+    SweepGraph() = default;
+    SweepGraph(const SweepGraph&) = delete;
+    SweepGraph& operator=(const SweepGraph&) = delete;
+    ~SweepGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+    template <class Body>
+    int record(mdet_ctx* ctx, Body body) {
+        if (!ctx->cap_stream)
+            MDET_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        const cudaStream_t cs = ctx->cap_stream;
+        MDET_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        const uint64_t l0 = ctx->launches;
+        body(cs);
+        launches = ctx->launches - l0;
+        ctx->launches = l0;  // counted per replay
+        const cudaError_t le = cudaGetLastError();  // a launch that failed to enqueue
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        int rc = ctx_cuda(ctx, le != cudaSuccess ? le : ce, "sweep capture");
+        if (rc == MDET_OK) rc = ctx_cuda(ctx, cudaGraphInstantiate(&exec, graph, 0), "sweep graph instantiate");
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+};
+
 // One propagation call over the traversal graph (m2 edges) and order.
 int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     cudaStream_t s = ctx->stream;
@@ -739,25 +769,35 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         LpArgs P{inc_off, inc, S.ea, S.eb, S.lw, S.mem, S.stuck, S.dirty, vt, vt_cap - 1, logfact, S.cnt, big_ws,
                  big_stride, maxbig, slot_of};
         uint64_t low = INT_MAX, attempt = 0, sweeps = 0;
-        unsigned long long hc[4] = {0, 0, 0, 0};
+        unsigned long long* hc = (unsigned long long*)ctx_pinned(ctx, 32);
+        if (!hc) return MDET_ERR_NOMEM;
         bool overfull = false;
-        while (true) {
-            MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 8, s));
-            ctx_timer_begin(ctx, "lp_sweep");
+        // one sweep -- the moved counter cleared, a launch or two per level,
+        // the counters copied back -- recorded once as a CUDA graph on the
+        // context's capture stream and replayed on its stream for every sweep
+        SweepGraph sg;
+        MDET_TRY(sg.record(ctx, [&](cudaStream_t cs) {
+            cudaMemsetAsync(S.cnt, 0, 8, cs);
             for (size_t L = 0; L < linfo.size(); ++L) {
                 if (linfo[L].nsmall) {
-                    k_lp_level_warp<<<(linfo[L].nsmall + kWarpsPerBlock - 1) / kWarpsPerBlock, kThreads, 0, s>>>(
+                    k_lp_level_warp<<<(linfo[L].nsmall + kWarpsPerBlock - 1) / kWarpsPerBlock, kThreads, 0, cs>>>(
                         P, lvls + soff[L], linfo[L].nsmall);
-                    MDET_LAUNCHED(ctx, "k_lp_level_warp");
+                    ctx->launches++;
                 }
                 if (linfo[L].count) {
                     const uint32_t cap = std::min<uint32_t>(pow2_at_least(linfo[L].maxdeg), kSmallCap);
-                    k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), s>>>(P, lvl + loff[L]);
-                    MDET_LAUNCHED(ctx, "k_lp_level");
+                    k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), cs>>>(P, lvl + loff[L]);
+                    ctx->launches++;
                 }
             }
+            cudaMemcpyAsync(hc, S.cnt, 32, cudaMemcpyDeviceToHost, cs);
+        }));
+        while (true) {
+            ctx_timer_begin(ctx, "lp_sweep");
+            MDET_CUDA(ctx, cudaGraphLaunch(sg.exec, s));
+            ctx->launches += sg.launches;
+            ctx->total_launches += sg.launches;
             ctx_timer_end(ctx, "lp_sweep");
-            MDET_CUDA(ctx, cudaMemcpyAsync(hc, S.cnt, 32, cudaMemcpyDeviceToHost, s));
             MDET_CUDA(ctx, cudaStreamSynchronize(s));
             ++sweeps;
             if (hc[2] & (kErrSlots | kErrScore))

@@ -115,6 +115,22 @@ def test_config0_scored_graph(gpu_ctx):
         assert len(np.unique(got)) < 20000
 
 
+def test_repeated_edges_and_self_pairs(gpu_ctx):
+    """Edges listed twice (both copies join while their contigs' bins differ)
+    and an edge of a contig with itself (never joins) are taken as the
+    reference takes them."""
+    f, t, s = _planted(12, 500, 5, 5, 0.2)
+    rng = np.random.default_rng(12)
+    dup = rng.choice(s.size, 300, replace=False)
+    f2 = np.concatenate([f, f[dup], [7, 9]])
+    t2 = np.concatenate([t, t[dup], [7, 9]])
+    s2 = np.concatenate([s, s[dup] - 1e-9, [0.99, 0.7]])
+    want, ost = oracle.label_prop(f2, t2, s2, 500)
+    got, st = gpu_ctx.label_propagation(f2, t2, s2, 500)
+    assert np.array_equal(got, want)
+    assert st["graph_edges"] == ost["graph_edges"]
+
+
 def test_degenerate_inputs(gpu_ctx):
     mem, st = gpu_ctx.label_propagation([], [], [], 5)
     assert mem.tolist() == list(range(5)) and st["calls"] == 0

@@ -2,11 +2,14 @@
 // drop-in for the reference program's front half (cuda/Cuda2.cu:1251-1912):
 // same flags, same input validation messages, same "# elapsed time (...)"
 // lines (cuda/metrictime2.hpp), but every GPU stage runs through the C ABI of
-// libmdet_tnf.so.  The reference continues into binning; this host writes
-// the TNF graph instead:
+// libmdet_tnf.so.  The reference continues into binning; this host runs
+// its label propagation over the graph (sSCR = sTNF, the reference's path
+// without a depth file, cuda/Cuda2.cu:1969-2061) and writes:
 //   <out>.tnf_graph.tsv   name_i <TAB> name_j <TAB> sTNF   (i < j)
 //   <out>.TNF.bin         n x 136 float64 rows c/sqrt(sum c^2), the TNF.bin
 //                         layout of openmp/TNF.cpp
+//   <out>.lp_bins.tsv     name <TAB> bin (the index of the contig whose label
+//                         the bin carries), in input order
 #include <charconv>
 #include <chrono>
 #include <cmath>
@@ -32,7 +35,7 @@ struct Opts {
     double maxP = 95, pTNF = 0, minS = 60;
     unsigned long long seed = 0;
     int ct = 32, device = 0;
-    bool verbose = false, help = false, no_tnf_bin = false;
+    bool verbose = false, help = false, no_tnf_bin = false, no_bins = false;
 };
 
 using Clock = std::chrono::high_resolution_clock;
@@ -58,6 +61,7 @@ void usage() {
                  "  --mode arg (=bf16)        plain | bf16 : distance filter of the pairwise stage\n"
                  "  --device arg (=0)         CUDA device\n"
                  "  --noTNFbin                do not write <out>.TNF.bin\n"
+                 "  --noBins                  skip label propagation and <out>.lp_bins.tsv\n"
                  "  -v [ --verbose ]          Verbose output\n";
 }
 
@@ -88,6 +92,8 @@ bool parse(int ac, char** av, Opts& o) {
             o.verbose = true;
         } else if (key == "--noTNFbin") {
             o.no_tnf_bin = true;
+        } else if (key == "--noBins") {
+            o.no_bins = true;
         } else if (key == "-i" || key == "--inFile") {
             if (!val(o.in)) return false;
         } else if (key == "-o" || key == "--outFile") {
@@ -321,6 +327,24 @@ int main(int ac, char** av) {
             for (int c = 0; c < 136; ++c) row[c] = (double)counts[r * 136 + c] / s;
             b.write((const char*)row.data(), 136 * sizeof(double));
         }
+    }
+    if (!o.no_bins) {
+        // binning by label propagation over the graph, sSCR = sTNF
+        std::vector<uint64_t> mem(n);
+        mdet_lp_stats lps{};
+        if (n) check(ctx, mdet_label_propagation(ctx, from.get(), to.get(), stnf.get(), ne, n, o.maxP / 100.,
+                                                 o.minS / 100., mem.data(), &lps),
+                     "label propagation");
+        if (o.verbose)
+            printf("Label propagation: %llu runs, %llu sweeps over %llu edges of %llu contigs\n",
+                   (unsigned long long)lps.calls, (unsigned long long)lps.sweeps,
+                   (unsigned long long)lps.graph_edges, (unsigned long long)lps.connected);
+        std::ofstream b(o.out + ".lp_bins.tsv");
+        if (!b) {
+            std::cerr << "[Error!] can't open the output file: " << o.out << ".lp_bins.tsv" << std::endl;
+            return 1;
+        }
+        for (uint64_t r = 0; r < n; ++r) b << fa.names[r] << '\t' << mem[r] << '\n';
     }
     std::cout << ne << " edges" << std::endl;
     mdet_ctx_destroy(ctx);

@@ -1,6 +1,7 @@
 """The command-line drop-in on the GPU: the record split and counting of a
-FASTA file on the device, the graph at a fixed pTNF, its TSV and TNF.bin
-outputs against the oracle (reader, TNF.cpp normalisation, graph)."""
+FASTA file on the device, the graph at a fixed pTNF, its TSV, TNF.bin and
+label-propagation bins against the oracle (reader, TNF.cpp normalisation,
+graph, binning)."""
 import gzip
 import os
 import subprocess
@@ -47,6 +48,13 @@ def test_cli_graph_and_tnf_bin(tmp_path, mode):
         st.append(float(s))
     assert len(fr) > 0
     compare_graph(np.array(fr), np.array(to), np.array(st), tnf, a.log_sizes, 0.95, 200)
+    # bins: label propagation over the CLI's own graph (sSCR = sTNF, maxP 95, minS 60)
+    want, _ = oracle.label_prop(np.array(fr, np.uint64), np.array(to, np.uint64), np.array(st), n, 0.95, 0.60)
+    got = np.zeros(n, np.uint64)
+    for line in open(str(out) + ".lp_bins.tsv"):
+        name, b = line.rstrip("\n").split("\t")
+        got[idx[name]] = int(b)
+    assert np.array_equal(got, want)
 
 
 def test_cli_rejects_duplicate_names(tmp_path):

@@ -311,50 +311,24 @@ struct PhaseClock {
 // size_major 1 -- size-sorted bands of `seg` contigs, Morton over 8 principal
 // axes within each band.
 int learned_order(mdet_ctx* ctx, const double* d_ls, uint64_t n, const float* z, int size_major, uint32_t seg,
-                  uint32_t* order) {
+                  const float* basis, uint32_t* order) {
     cudaStream_t s = ctx->stream;
-    // principal axes of the embedding: C = Z^T Z / n - mu mu^T
-    float* G = (float*)ctx_scratch(ctx, "lrn.gram", MLP_OUT * MLP_OUT * 4);
-    float* colsum = (float*)ctx_scratch(ctx, "lrn.colsum", MLP_OUT * 4);
-    float* V = (float*)ctx_scratch(ctx, "lrn.v", MLP_OUT * kPcs * 4);
-    float* off = (float*)ctx_scratch(ctx, "lrn.off", 2 * kPcs * 4);
     float* proj = (float*)ctx_scratch(ctx, "lrn.proj", n * kPcs * 4);
     unsigned long long* keys = (unsigned long long*)ctx_scratch(ctx, "lrn.keys", n * 8);
     unsigned long long* keys2 = (unsigned long long*)ctx_scratch(ctx, "lrn.keys2", n * 8);
     unsigned long long* keys3 = (unsigned long long*)ctx_scratch(ctx, "lrn.keys3", n * 8);
     uint32_t* vals = (uint32_t*)ctx_scratch(ctx, "lrn.vals", n * 4);
-    if (!G || !colsum || !V || !off || !proj || !keys || !keys2 || !keys3 || !vals) return MDET_ERR_NOMEM;
-    MDET_CUDA(ctx, cudaMemsetAsync(G, 0, MLP_OUT * MLP_OUT * 4, s));
-    MDET_CUDA(ctx, cudaMemsetAsync(colsum, 0, MLP_OUT * 4, s));
-    MDET_TRY(mlp_gram(ctx, z, n, G));
-    MDET_TRY(mlp_colsum(ctx, z, n, colsum));
-    std::vector<float> hg(MLP_OUT * MLP_OUT), hs(MLP_OUT);
-    MDET_CUDA(ctx, cudaMemcpyAsync(hg.data(), G, hg.size() * 4, cudaMemcpyDeviceToHost, s));
-    MDET_CUDA(ctx, cudaMemcpyAsync(hs.data(), colsum, hs.size() * 4, cudaMemcpyDeviceToHost, s));
-    MDET_CUDA(ctx, cudaStreamSynchronize(s));
-    std::vector<double> C((size_t)MLP_OUT * MLP_OUT), w, E;
-    for (int i = 0; i < MLP_OUT; ++i)
-        for (int j = 0; j < MLP_OUT; ++j)
-            C[(size_t)i * MLP_OUT + j] = (double)hg[(size_t)i * MLP_OUT + j] / (double)n -
-                                         ((double)hs[i] / (double)n) * ((double)hs[j] / (double)n);
-    jacobi_eigen(C, MLP_OUT, w, E);
-    std::vector<int> idx(MLP_OUT);
-    for (int i = 0; i < MLP_OUT; ++i) idx[i] = i;
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return w[a] > w[b]; });
-    std::vector<float> hv((size_t)MLP_OUT * kPcs), hoff(2 * kPcs);
-    for (int p = 0; p < kPcs; ++p) {
-        const int e = idx[p];
-        double mproj = 0;
-        for (int r = 0; r < MLP_OUT; ++r) {
-            hv[(size_t)r * kPcs + p] = (float)E[(size_t)r * MLP_OUT + e];
-            mproj += E[(size_t)r * MLP_OUT + e] * (double)hs[r] / (double)n;
-        }
-        const double sd = std::sqrt(std::max(w[e], 1e-20));
-        hoff[p] = (float)(mproj - 3.0 * sd);            // the key spans mean +- 3 sd
-        hoff[kPcs + p] = (float)(1.0 / (6.0 * sd));
+    if (!proj || !keys || !keys2 || !keys3 || !vals) return MDET_ERR_NOMEM;
+    // the network's principal axes (kept from its training set), else this
+    // assembly's
+    if (!basis) {
+        float* b = (float*)ctx_scratch(ctx, "lrn.basis", MLP_PCA_FLOATS * 4);
+        if (!b) return MDET_ERR_NOMEM;
+        MDET_TRY(mlp_pca_basis(ctx, z, n, b));
+        basis = b;
     }
-    MDET_CUDA(ctx, cudaMemcpyAsync(V, hv.data(), hv.size() * 4, cudaMemcpyHostToDevice, s));
-    MDET_CUDA(ctx, cudaMemcpyAsync(off, hoff.data(), hoff.size() * 4, cudaMemcpyHostToDevice, s));
+    const float* V = basis;
+    const float* off = basis + MLP_OUT * kPcs;
     MDET_TRY(mlp_project(ctx, z, n, V, kPcs, proj));
     // log10 size over 3..7 (1 kb .. 10 Mb)
     const unsigned grid = (unsigned)((n + 255) / 256);
@@ -385,6 +359,51 @@ int learned_order(mdet_ctx* ctx, const double* d_ls, uint64_t n, const float* z,
 }
 
 }  // namespace
+
+// Principal axes of the embeddings z (n x 64) for the Morton key: basis =
+// V (64 x 8, the eigenvectors of the 8 largest eigenvalues of the
+// covariance), then the key's offsets (mean - 3 sd) and inverse spans
+// (1 / 6 sd) along them.
+int mlp_pca_basis(mdet_ctx* ctx, const float* z, uint64_t n, float* basis) {
+    cudaStream_t s = ctx->stream;
+    float* G = (float*)ctx_scratch(ctx, "lrn.gram", MLP_OUT * MLP_OUT * 4);
+    float* colsum = (float*)ctx_scratch(ctx, "lrn.colsum", MLP_OUT * 4);
+    if (!G || !colsum) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(G, 0, MLP_OUT * MLP_OUT * 4, s));
+    MDET_CUDA(ctx, cudaMemsetAsync(colsum, 0, MLP_OUT * 4, s));
+    MDET_TRY(mlp_gram(ctx, z, n, G));
+    MDET_TRY(mlp_colsum(ctx, z, n, colsum));
+    std::vector<float> hg(MLP_OUT * MLP_OUT), hs(MLP_OUT);
+    MDET_CUDA(ctx, cudaMemcpyAsync(hg.data(), G, hg.size() * 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaMemcpyAsync(hs.data(), colsum, hs.size() * 4, cudaMemcpyDeviceToHost, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));
+    std::vector<double> C((size_t)MLP_OUT * MLP_OUT), w, E;
+    for (int i = 0; i < MLP_OUT; ++i)
+        for (int j = 0; j < MLP_OUT; ++j)
+            C[(size_t)i * MLP_OUT + j] = (double)hg[(size_t)i * MLP_OUT + j] / (double)n -
+                                         ((double)hs[i] / (double)n) * ((double)hs[j] / (double)n);
+    jacobi_eigen(C, MLP_OUT, w, E);
+    std::vector<int> idx(MLP_OUT);
+    for (int i = 0; i < MLP_OUT; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return w[a] > w[b]; });
+    std::vector<float> h(MLP_PCA_FLOATS);
+    float* hv = h.data();
+    float* hoff = h.data() + MLP_OUT * kPcs;
+    for (int p = 0; p < kPcs; ++p) {
+        const int e = idx[p];
+        double mproj = 0;
+        for (int r = 0; r < MLP_OUT; ++r) {
+            hv[(size_t)r * kPcs + p] = (float)E[(size_t)r * MLP_OUT + e];
+            mproj += E[(size_t)r * MLP_OUT + e] * (double)hs[r] / (double)n;
+        }
+        const double sd = std::sqrt(std::max(w[e], 1e-20));
+        hoff[p] = (float)(mproj - 3.0 * sd);            // the key spans mean +- 3 sd
+        hoff[kPcs + p] = (float)(1.0 / (6.0 * sd));
+    }
+    MDET_CUDA(ctx, cudaMemcpyAsync(basis, h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
+    MDET_CUDA(ctx, cudaStreamSynchronize(s));  // h is a local
+    return MDET_OK;
+}
 
 int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_t n, double cutoff, uint32_t max_edges,
                   mdet_graph_stats* st, GraphPrep& g, uint64_t* total) {
@@ -429,7 +448,7 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
     if (!z || !order) return MDET_ERR_NOMEM;
     MDET_TRY(mlp_embed(ctx, net->params, d_tnf, n, z));
     tm.mark();
-    MDET_TRY(learned_order(ctx, d_ls, n, z, size_major, seg, order));
+    MDET_TRY(learned_order(ctx, d_ls, n, z, size_major, seg, net->pca_valid ? net->pca : nullptr, order));
     MDET_TRY(prep_sorted(ctx, d_tnf, d_ls, n, true, &g, order));
     MDET_TRY(abd_gate(ctx, g));
     const double L = logit(cutoff);

@@ -1,7 +1,8 @@
-// learned.cu -- the learned proposal's network: training and inference
-// kernels of the 136 -> 256 -> 128 -> 64 GELU MLP (BF16 weights, FP32
-// accumulation), the pair loss, Adam, pair labelling with the exact
-// probability kernel, and the C ABI of the network (mdet_mlp_*).  The
+// learned.cu -- the learned proposal's network: the pair loss, Adam, pair
+// labelling with the exact probability kernel, the training loop and the C
+// ABI of the network (mdet_mlp_*).  The GEMMs of inference and training run
+// on the tensor cores (mlp_tc.cu); the SIMT GEMMs below serve the principal
+// axes of the embedding (Gram matrix, projection).  The
 // reference has no learned component; everything here is this project's.
 #include <cub/cub.cuh>
 
@@ -17,24 +18,14 @@ using namespace mdet_exact;
 
 namespace {
 
-__device__ __forceinline__ float bf16r(float w) { return __bfloat162float(__float2bfloat16_rn(w)); }
-
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
-
-__device__ __forceinline__ float gelu_grad(float z) {
-    const float cdf = 0.5f * (1.f + erff(z * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
-    return cdf + z * pdf;
-}
-
 // C[M x N] = op(A) * op(B) with op(A)(m,k) = TA ? A[k*lda+m] : A[m*lda+k] and
-// op(B)(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n].  RB rounds B to BF16 (weights).
-// MODE 0: C = acc + bias (bias may be null); MODE 1: Zout = acc + bias,
-// C = gelu(Zout); MODE 2: atomicAdd into C over a K slice (blockIdx.z).
-template <bool TA, bool TB, bool RB, int MODE>
+// op(B)(k,n) = TB ? B[n*ldb+k] : B[k*ldb+n] (FP32, SIMT): the principal axes
+// of the embedding.  MODE 0: C = acc; MODE 2: atomicAdd into C over a K
+// slice (blockIdx.z).
+template <bool TA, bool TB, int MODE>
 __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* __restrict__ A, int lda,
                                               const float* __restrict__ B, int ldb, float* __restrict__ C, int ldc,
-                                              const float* __restrict__ bias, float* __restrict__ Zout, int kslice) {
+                                              int kslice) {
     __shared__ float As[16][64 + 4];
     __shared__ float Bs[16][64 + 4];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -64,7 +55,7 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* 
             const int gk2 = k0 + bk, gn = n0 + bn;
             float bv = 0.f;
             if (gn < N && gk2 < kend) bv = TB ? B[(size_t)gn * ldb + gk2] : B[(size_t)gk2 * ldb + gn];
-            Bs[bk][bn] = RB ? bf16r(bv) : bv;
+            Bs[bk][bn] = bv;
         }
         __syncthreads();
 #pragma unroll
@@ -89,24 +80,17 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* 
         for (int j = 0; j < 4; ++j) {
             const int gn = n0 + tx * 4 + j;
             if (gn >= N) continue;
-            float v = acc[i][j];
-            if (MODE == 2) {
+            const float v = acc[i][j];
+            if (MODE == 2)
                 atomicAdd(&C[(size_t)gm * ldc + gn], v);
-            } else {
-                if (bias) v += bias[gn];
-                if (MODE == 1) {
-                    Zout[(size_t)gm * ldc + gn] = v;
-                    v = gelu(v);
-                }
+            else
                 C[(size_t)gm * ldc + gn] = v;
-            }
         }
     }
 }
 
-template <bool TA, bool TB, bool RB, int MODE>
-int gemm(mdet_ctx* ctx, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-         const float* bias, float* Zout) {
+template <bool TA, bool TB, int MODE>
+int gemm(mdet_ctx* ctx, int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc) {
     if (M <= 0 || N <= 0 || K <= 0) return MDET_OK;
     dim3 grid((N + 63) / 64, (M + 63) / 64, 1);
     int kslice = K;
@@ -117,25 +101,9 @@ int gemm(mdet_ctx* ctx, int M, int N, int K, const float* A, int lda, const floa
         kslice = ((K + slices - 1) / slices + 15) / 16 * 16;
         grid.z = (K + kslice - 1) / kslice;
     }
-    k_gemm<TA, TB, RB, MODE><<<grid, 256, 0, ctx->stream>>>(M, N, K, A, lda, B, ldb, C, ldc, bias, Zout, kslice);
+    k_gemm<TA, TB, MODE><<<grid, 256, 0, ctx->stream>>>(M, N, K, A, lda, B, ldb, C, ldc, kslice);
     MDET_LAUNCHED(ctx, "k_gemm");
     return MDET_OK;
-}
-
-__global__ void k_mlp_input(const float* __restrict__ tnf, const uint32_t* __restrict__ idx, uint64_t n,
-                            const float* __restrict__ params, float* __restrict__ x) {
-    const uint64_t r = blockIdx.x;
-    if (r >= n) return;
-    const uint64_t src = idx ? idx[r] : r;
-    const float scale = params[MLP_SCALE];
-    for (int k = threadIdx.x; k < MLP_IN; k += blockDim.x)
-        x[r * MLP_IN + k] = (tnf[src * MLP_IN + k] - params[MLP_MU + k]) * scale;
-}
-
-// dZ = dH * gelu'(Z), in place on dH
-__global__ void k_gelu_back(float* __restrict__ dh, const float* __restrict__ z, uint64_t count) {
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x)
-        dh[i] *= gelu_grad(z[i]);
 }
 
 // column sums of dZ [rows][cols] added into grad (bias gradients)
@@ -277,76 +245,20 @@ void host_init(uint64_t seed, std::vector<float>& p) {
 
 // ------------------------------------------------------------ host side --
 
-int mlp_alloc_acts(mdet_ctx* ctx, const char* tag, uint64_t rows, MlpActs* a) {
-    std::string t(tag);
-    a->x = (float*)ctx_scratch(ctx, (t + ".x").c_str(), rows * MLP_IN * 4);
-    a->z1 = (float*)ctx_scratch(ctx, (t + ".z1").c_str(), rows * MLP_H1 * 4);
-    a->h1 = (float*)ctx_scratch(ctx, (t + ".h1").c_str(), rows * MLP_H1 * 4);
-    a->z2 = (float*)ctx_scratch(ctx, (t + ".z2").c_str(), rows * MLP_H2 * 4);
-    a->h2 = (float*)ctx_scratch(ctx, (t + ".h2").c_str(), rows * MLP_H2 * 4);
-    a->z3 = (float*)ctx_scratch(ctx, (t + ".z3").c_str(), rows * MLP_OUT * 4);
-    return (a->x && a->z1 && a->h1 && a->z2 && a->h2 && a->z3) ? MDET_OK : MDET_ERR_NOMEM;
-}
-
-int mlp_forward(mdet_ctx* ctx, const float* P, const float* tnf, const uint32_t* idx, uint64_t n, const MlpActs& a) {
-    if (n == 0) return MDET_OK;
-    k_mlp_input<<<(unsigned)n, 64, 0, ctx->stream>>>(tnf, idx, n, P, a.x);
-    MDET_LAUNCHED(ctx, "k_mlp_input");
-    const int M = (int)n;
-    MDET_TRY((gemm<false, true, true, 1>(ctx, M, MLP_H1, MLP_IN, a.x, MLP_IN, P + MLP_W1, MLP_IN, a.h1, MLP_H1,
-                                         P + MLP_B1, a.z1)));
-    MDET_TRY((gemm<false, true, true, 1>(ctx, M, MLP_H2, MLP_H1, a.h1, MLP_H1, P + MLP_W2, MLP_H1, a.h2, MLP_H2,
-                                         P + MLP_B2, a.z2)));
-    MDET_TRY((gemm<false, true, true, 0>(ctx, M, MLP_OUT, MLP_H2, a.h2, MLP_H2, P + MLP_W3, MLP_H2, a.z3, MLP_OUT,
-                                         P + MLP_B3, nullptr)));
-    return MDET_OK;
-}
-
-int mlp_backward(mdet_ctx* ctx, const float* P, const MlpActs& a, uint64_t np, const float* labels, float m_pos,
-                 float m_neg, float* grad, double* loss_sum) {
-    cudaStream_t s = ctx->stream;
-    const uint64_t rows = 2 * np;
-    float* d3 = (float*)ctx_scratch(ctx, "mlpg.d3", rows * MLP_OUT * 4);
-    float* d2 = (float*)ctx_scratch(ctx, "mlpg.d2", rows * MLP_H2 * 4);
-    float* d1 = (float*)ctx_scratch(ctx, "mlpg.d1", rows * MLP_H1 * 4);
-    if (!d3 || !d2 || !d1) return MDET_ERR_NOMEM;
-    MDET_CUDA(ctx, cudaMemsetAsync(grad, 0, MLP_NTRAIN * 4, s));
-    k_pair_loss<<<(unsigned)((np + 7) / 8), 256, 0, s>>>(a.z3, np, labels, m_pos, m_neg, d3, loss_sum);
-    MDET_LAUNCHED(ctx, "k_pair_loss");
-    const int M = (int)rows;
-    // layer 3: dW3 = d3^T h2, db3 = colsum d3, dh2 = d3 W3
-    MDET_TRY((gemm<true, false, false, 2>(ctx, MLP_OUT, MLP_H2, M, d3, MLP_OUT, a.h2, MLP_H2, grad + MLP_W3, MLP_H2,
-                                          nullptr, nullptr)));
-    k_colsum_add<<<dim3(1, (unsigned)((rows + 255) / 256)), 64, 0, s>>>(d3, rows, MLP_OUT, grad + MLP_B3);
-    MDET_LAUNCHED(ctx, "k_colsum_add");
-    MDET_TRY((gemm<false, false, true, 0>(ctx, M, MLP_H2, MLP_OUT, d3, MLP_OUT, P + MLP_W3, MLP_H2, d2, MLP_H2,
-                                          nullptr, nullptr)));
-    k_gelu_back<<<std::min<uint64_t>((rows * MLP_H2 + 255) / 256, 4096), 256, 0, s>>>(d2, a.z2, rows * MLP_H2);
-    MDET_LAUNCHED(ctx, "k_gelu_back");
-    // layer 2
-    MDET_TRY((gemm<true, false, false, 2>(ctx, MLP_H2, MLP_H1, M, d2, MLP_H2, a.h1, MLP_H1, grad + MLP_W2, MLP_H1,
-                                          nullptr, nullptr)));
-    k_colsum_add<<<dim3(1, (unsigned)((rows + 255) / 256)), 128, 0, s>>>(d2, rows, MLP_H2, grad + MLP_B2);
-    MDET_LAUNCHED(ctx, "k_colsum_add");
-    MDET_TRY((gemm<false, false, true, 0>(ctx, M, MLP_H1, MLP_H2, d2, MLP_H2, P + MLP_W2, MLP_H1, d1, MLP_H1,
-                                          nullptr, nullptr)));
-    k_gelu_back<<<std::min<uint64_t>((rows * MLP_H1 + 255) / 256, 4096), 256, 0, s>>>(d1, a.z1, rows * MLP_H1);
-    MDET_LAUNCHED(ctx, "k_gelu_back");
-    // layer 1
-    MDET_TRY((gemm<true, false, false, 2>(ctx, MLP_H1, MLP_IN, M, d1, MLP_H1, a.x, MLP_IN, grad + MLP_W1, MLP_IN,
-                                          nullptr, nullptr)));
-    k_colsum_add<<<dim3(1, (unsigned)((rows + 255) / 256)), 256, 0, s>>>(d1, rows, MLP_H1, grad + MLP_B1);
-    MDET_LAUNCHED(ctx, "k_colsum_add");
-    return MDET_OK;
-}
-
 int mlp_embed(mdet_ctx* ctx, const float* P, const float* tnf, uint64_t n, float* z) {
-    return mlp_embed_tc(ctx, P, tnf, n, z);
+    return mlp_embed_tc(ctx, P, tnf, n, z, nullptr);
+}
+
+int mlp_pair_loss(mdet_ctx* ctx, const float* z, uint64_t np, const float* labels, float m_pos, float m_neg,
+                  float* dz, double* loss_sum) {
+    if (np == 0) return MDET_OK;
+    k_pair_loss<<<(unsigned)((np + 7) / 8), 256, 0, ctx->stream>>>(z, np, labels, m_pos, m_neg, dz, loss_sum);
+    MDET_LAUNCHED(ctx, "k_pair_loss");
+    return MDET_OK;
 }
 
 int mlp_gram(mdet_ctx* ctx, const float* z, uint64_t n, float* G) {
-    return gemm<true, false, false, 2>(ctx, MLP_OUT, MLP_OUT, (int)n, z, MLP_OUT, z, MLP_OUT, G, MLP_OUT, nullptr,
-                                       nullptr);
+    return gemm<true, false, 2>(ctx, MLP_OUT, MLP_OUT, (int)n, z, MLP_OUT, z, MLP_OUT, G, MLP_OUT);
 }
 
 int mlp_colsum(mdet_ctx* ctx, const float* z, uint64_t n, float* sum) {
@@ -360,8 +272,7 @@ int mlp_project(mdet_ctx* ctx, const float* z, uint64_t n, const float* V, int k
     const uint64_t chunk = 1u << 20;  // keeps the grid's y extent in range
     for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
         const int rows = (int)std::min(chunk, n - r0);
-        MDET_TRY((gemm<false, false, false, 0>(ctx, rows, k, MLP_OUT, z + r0 * MLP_OUT, MLP_OUT, V, k, P + r0 * k, k,
-                                               nullptr, nullptr)));
+        MDET_TRY((gemm<false, false, 0>(ctx, rows, k, MLP_OUT, z + r0 * MLP_OUT, MLP_OUT, V, k, P + r0 * k, k)));
     }
     return MDET_OK;
 }
@@ -397,6 +308,7 @@ int mdet_mlp_destroy(mdet_mlp* m) {
     cudaFree(m->params);
     cudaFree(m->m);
     cudaFree(m->v);
+    cudaFree(m->pca);
     delete m;
     return MDET_OK;
 }
@@ -412,6 +324,7 @@ int mdet_mlp_get_params(mdet_ctx* ctx, const mdet_mlp* m, float* host, uint64_t 
 int mdet_mlp_set_params(mdet_ctx* ctx, mdet_mlp* m, const float* host, uint64_t count) {
     if (!ctx || !m || !host || count < MLP_NPARAM) return MDET_ERR_INVALID;
     MDET_CUDA(ctx, cudaMemcpy(m->params, host, MLP_NPARAM * 4, cudaMemcpyHostToDevice));
+    m->pca_valid = 0;  // the kept axes belong to the old parameters
     return MDET_OK;
 }
 
@@ -456,10 +369,10 @@ int mdet_mlp_grad(mdet_ctx* ctx, const mdet_mlp* m, const float* x, uint64_t row
     MDET_CUDA(ctx, cudaMemcpyAsync(didx, idx.data(), 2 * np * 4, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(dl, labels, np * 4, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemsetAsync(loss, 0, 8, s));
-    MlpActs a;
-    MDET_TRY(mlp_alloc_acts(ctx, "mlpq", 2 * np, &a));
-    MDET_TRY(mlp_forward(ctx, m->params, dx, didx, 2 * np, a));
-    MDET_TRY(mlp_backward(ctx, m->params, a, np, dl, m_pos, m_neg, g, loss));
+    MlpTcActs a;
+    MDET_TRY(mlp_tc_alloc(ctx, "mlpq", 2 * np, &a));
+    MDET_TRY(mlp_forward_tc(ctx, m->params, dx, didx, 2 * np, a));
+    MDET_TRY(mlp_backward_tc(ctx, m->params, a, np, dl, m_pos, m_neg, g, loss));
     MDET_CUDA(ctx, cudaMemcpyAsync(grad_out, g, MLP_NTRAIN * 4, cudaMemcpyDeviceToHost, s));
     double h = 0;
     MDET_CUDA(ctx, cudaMemcpyAsync(&h, loss, 8, cudaMemcpyDeviceToHost, s));
@@ -507,8 +420,8 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
     const uint64_t hold = std::max<uint64_t>(pool / 100, 1);
     const uint64_t train_pool = pool - hold;
     const uint32_t B = tp->batch_pairs ? tp->batch_pairs : 8192;
-    MlpActs a;
-    MDET_TRY(mlp_alloc_acts(ctx, "mlpt", 2ull * B, &a));
+    MlpTcActs a;
+    MDET_TRY(mlp_tc_alloc(ctx, "mlpt", 2ull * B, &a));
     uint32_t* bidx = (uint32_t*)ctx_scratch(ctx, "mlpt.bidx", 2ull * B * 4);
     float* blab = (float*)ctx_scratch(ctx, "mlpt.blab", (uint64_t)B * 4);
     float* grad = (float*)ctx_scratch(ctx, "mlpt.grad", MLP_NTRAIN * 4);
@@ -530,9 +443,9 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
         k_batch<<<(B + 255) / 256, 256, 0, s>>>(pairs, labels, train_pool, tp->seed * 1315423911ull + st, B, bidx,
                                                 blab);
         MDET_LAUNCHED(ctx, "k_batch");
-        MDET_TRY(mlp_forward(ctx, m->params, g.x32, bidx, 2ull * B, a));
+        MDET_TRY(mlp_forward_tc(ctx, m->params, g.x32, bidx, 2ull * B, a));
         MDET_CUDA(ctx, cudaMemsetAsync(loss, 0, 8, s));
-        MDET_TRY(mlp_backward(ctx, m->params, a, B, blab, tp->m_pos, tp->m_neg, grad, loss));
+        MDET_TRY(mlp_backward_tc(ctx, m->params, a, B, blab, tp->m_pos, tp->m_neg, grad, loss));
         m->step++;
         const float c1 = 1.f - powf(0.9f, (float)m->step), c2 = 1.f - powf(0.999f, (float)m->step);
         const float lr = tp->lr * (st < steps / 10 ? 1.f : 0.5f * (1.f + cosf(3.14159265f * (float)(st - steps / 10) /
@@ -567,10 +480,10 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
             idx[hc + p] = hp[p].y;
         }
         MDET_CUDA(ctx, cudaMemcpyAsync(hidx, idx.data(), 2 * hc * 4, cudaMemcpyHostToDevice, s));
-        MlpActs ha;
-        MDET_TRY(mlp_alloc_acts(ctx, "mlph", 2 * hc, &ha));
-        MDET_TRY(mlp_forward(ctx, m->params, g.x32, hidx, 2 * hc, ha));
-        k_pair_dist<<<(unsigned)((hc + 7) / 8), 256, 0, s>>>(ha.z3, hc, he);
+        float* hz = (float*)ctx_scratch(ctx, "mlph.z", 2 * hc * MLP_OUT * 4);
+        if (!hz) return MDET_ERR_NOMEM;
+        MDET_TRY(mlp_embed_tc(ctx, m->params, g.x32, 2 * hc, hz, hidx));
+        k_pair_dist<<<(unsigned)((hc + 7) / 8), 256, 0, s>>>(hz, hc, he);
         MDET_LAUNCHED(ctx, "k_pair_dist");
         MDET_CUDA(ctx, cudaMemcpyAsync(e.data(), he, hc * 4, cudaMemcpyDeviceToHost, s));
         MDET_CUDA(ctx, cudaStreamSynchronize(s));
@@ -592,6 +505,16 @@ int mdet_mlp_train(mdet_ctx* ctx, mdet_mlp* m, const float* d_tnf, const double*
         size_t below = 0;
         for (float v : neg) below += v <= tau;
         r.neg_below_tau = neg.empty() ? 0 : (double)below / neg.size();
+    }
+    // the principal axes of the training set's embeddings, kept for the
+    // contig order of the learned graph
+    {
+        float* zt = (float*)ctx_scratch(ctx, "mlpt.zall", n * MLP_OUT * 4);
+        if (!zt) return MDET_ERR_NOMEM;
+        if (!m->pca) MDET_CUDA(ctx, cudaMalloc(&m->pca, MLP_PCA_FLOATS * 4));
+        MDET_TRY(mlp_embed(ctx, m->params, d_tnf, n, zt));
+        MDET_TRY(mlp_pca_basis(ctx, zt, n, m->pca));
+        m->pca_valid = 1;
     }
     r.steps = steps;
     r.pairs = pool;

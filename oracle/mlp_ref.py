@@ -3,7 +3,10 @@
 The reference has no learned component, so this is not a restatement of
 reference code: it is the float64 numpy statement of the network that the
 CUDA kernels (mdet_gb300/csrc/learned.cu) train, used by the tests to check
-the forward pass, the contrastive loss and every gradient.
+the forward pass, the contrastive loss and every gradient -- in float64 with
+FP32 activations (the network's definition) and in the form the
+tensor-core kernels compute (BF16 GEMM operands: embed_bf16,
+loss_and_grad_bf16).
 
 Network: x' = (tnf - mu) * scale; h1 = gelu(x' W1^T + b1) (256);
 h2 = gelu(h1 W2^T + b2) (128); z = h2 W3^T + b3 (64).  Weights are read
@@ -112,5 +115,46 @@ def loss_and_grad(p: np.ndarray, x: np.ndarray, pairs: np.ndarray, labels: np.nd
     g[B2:W3] = d2.sum(0)
     d1 = (d2 @ w["W2"]) * _gelu_grad(f["z1"])
     g[W1:B1] = (d1.T @ f["x"]).ravel()
+    g[B1:W2] = d1.sum(0)
+    return loss, g
+
+
+def loss_and_grad_bf16(p: np.ndarray, x: np.ndarray, pairs: np.ndarray, labels: np.ndarray, m_pos: float,
+                       m_neg: float):
+    """The same loss and gradient as the tensor-core training pass computes
+    them: every GEMM operand rounded to BF16 -- the layer inputs in the
+    forward pass (as embed_bf16), and in the backward pass the output
+    gradients that meet a weight matrix or an activation (dz3, dz2, dz1) --
+    with float64 sums otherwise; the bias gradients sum the unrounded
+    output gradients."""
+    pairs = np.asarray(pairs, np.int64).reshape(-1, 2)
+    y = np.asarray(labels, np.float64)
+    npairs = pairs.shape[0]
+    rows = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    w = unpack(p, True)
+    xr = bf16_round((np.asarray(x, np.float64)[rows] - w["mu"]) * w["scale"])
+    z1 = xr @ w["W1"].T + w["b1"]
+    h1 = bf16_round(_gelu(z1))
+    z2 = h1 @ w["W2"].T + w["b2"]
+    h2 = bf16_round(_gelu(z2))
+    z = h2 @ w["W3"].T + w["b3"]
+    d = z[:npairs] - z[npairs:]
+    e = np.sqrt((d * d).sum(1))
+    up = np.maximum(e - m_pos, 0.0)
+    dn = np.maximum(m_neg - e, 0.0)
+    loss = float((y * up * up + (1 - y) * dn * dn).mean())
+    dl = (2 * y * up - 2 * (1 - y) * dn) / npairs
+    fac = np.where(e > 1e-12, dl / np.maximum(e, 1e-300), 0.0)
+    d3 = np.concatenate([fac[:, None] * d, -fac[:, None] * d])
+    d3r = bf16_round(d3)
+    g = np.zeros(NTRAIN)
+    g[W3:B3] = (d3r.T @ h2).ravel()
+    g[B3:MU] = d3.sum(0)
+    d2 = (d3r @ w["W3"]) * _gelu_grad(z2)
+    d2r = bf16_round(d2)
+    g[W2:B2] = (d2r.T @ h1).ravel()
+    g[B2:W3] = d2.sum(0)
+    d1 = (d2r @ w["W2"]) * _gelu_grad(z1)
+    g[W1:B1] = (bf16_round(d1).T @ xr).ravel()
     g[B1:W2] = d1.sum(0)
     return loss, g

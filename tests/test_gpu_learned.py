@@ -32,12 +32,18 @@ def test_gradient_matches_oracle(gpu_ctx):
     y = (rng.random(npairs) < 0.5).astype(np.float32)
     net, p, mp, mn = _net_with_margins(gpu_ctx, 3, x, pairs.astype(np.int64))
     loss, g = net.grad(x, pairs, y, mp, mn)
-    rl, rg = R.loss_and_grad(p, x, pairs, y, mp, mn)
-    assert abs(loss - rl) <= 1e-5 * abs(rl) + 1e-9
+    # the tensor-core pass rounds every GEMM operand to BF16; the oracle's
+    # matching form rounds the same values, so the differences come from FP32
+    # accumulation and from values on the other side of a rounding boundary
+    rl, rg = R.loss_and_grad_bf16(p, x, pairs, y, mp, mn)
+    assert abs(loss - rl) <= 1e-4 * abs(rl) + 1e-9
     gn = np.linalg.norm(rg)
     for lo, hi in [(R.W1, R.B1), (R.B1, R.W2), (R.W2, R.B2), (R.B2, R.W3), (R.W3, R.B3)]:
         err = np.linalg.norm(g[lo:hi] - rg[lo:hi]) / max(np.linalg.norm(rg[lo:hi]), 1e-30)
-        assert err < 1e-4, (lo, hi, err)   # FP32 accumulation against float64
+        assert err < 5e-3, (lo, hi, err)
+    # and close to the network's float64 gradient with FP32 activations
+    _, fg = R.loss_and_grad(p, x, pairs, y, mp, mn)
+    assert np.linalg.norm(g[:R.NTRAIN] - fg) / np.linalg.norm(fg) < 5e-2
     # b3 moves both embeddings of a pair alike: its exact gradient is zero
     assert np.abs(rg[R.B3:R.MU]).max() < 1e-12 * gn
     assert np.linalg.norm(g[R.B3:R.MU]) < 1e-5 * gn

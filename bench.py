@@ -970,12 +970,18 @@ def run_case(args):
         print({"train_s": round(time.time() - t0, 2), **rep})
         cap = args.n * 200
         out = [torch.empty(cap, dtype=t, device=dev) for t in (torch.int64, torch.int64, torch.float64)]
-        # --segs entries "ORDER:SEG" (order 0 embedding-major, 1 size-major)
-        variants = [tuple(int(v) for v in x.split(":")) if ":" in x else (0, int(x)) for x in args.segs.split(",")]
-        runs = [("bf16", 0, 0)] + [("learned", o, sg) for o, sg in variants for _ in range(2)] + [("bf16", 0, 0)]
+        # --segs entries "ORDER:SEG[:Q]" (order 0 embedding-major, 1 size-major;
+        # Q the tau quantile, 0 for the default)
+        def variant(x):
+            f = x.split(":")
+            return int(f[0]), int(f[1]), float(f[2]) if len(f) > 2 else 0.0
+
+        variants = [variant(x) if ":" in x else (0, int(x), 0.0) for x in args.segs.split(",")]
+        runs = [("bf16", 0, 0, 0.0)] + [("learned", o, sg, q) for o, sg, q in variants for _ in range(2)]
+        runs += [("bf16", 0, 0, 0.0)]
         ref = None
-        for mode, order, seg in runs:
-            lr = ctx.set_learned(net, segment=seg, order=order)
+        for mode, order, seg, q in runs:
+            lr = ctx.set_learned(net, segment=seg, order=order, tau_quantile=q)
             ne, st = ctx.tnf_graph_dev(d_tnf.data_ptr(), d_ls.data_ptr(), args.n, args.cutoff, 200, mode,
                                        out[0].data_ptr(), out[1].data_ptr(), out[2].data_ptr(), cap)
             keys = torch.sort(out[0][:ne] * args.n + out[1][:ne])[0]
@@ -1154,8 +1160,8 @@ def main():
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--train-pairs", type=int, default=50_000_000)
     ap.add_argument("--segs", default="0:1024,1:16384",
-                    help="comma-separated ORDER:SEG contig orders to try (learned case): order 0 embedding-major "
-                         "with size-sorted runs of SEG, order 1 size bands of SEG")
+                    help="comma-separated ORDER:SEG[:Q] variants to try (learned case): order 0 embedding-major "
+                         "with size-sorted runs of SEG, order 1 size bands of SEG; Q the tau quantile")
     ap.add_argument("--cutoff", type=float, default=0.95)
     ap.add_argument("--repeat", type=int, default=1)
     args = ap.parse_args()

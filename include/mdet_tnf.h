@@ -353,6 +353,9 @@ typedef struct {
     double tau;                /* out: embedded-distance margin used */
     double ms_embed, ms_order, ms_sample; /* out: network pass; order + row preparation; sampled-row
                                   calibration, tile flags and recall estimate (device time) */
+    double tau_quantile;       /* quantile of the calibration edges' embedded distances that sets tau
+                                  (0: 1 - (1 - recall_target) / 4); lower skips more tiles and may lose
+                                  edges, down to the recall target */
 } mdet_learned_report;
 
 int mdet_mlp_create(mdet_ctx* ctx, uint64_t seed, mdet_mlp** out);

@@ -512,7 +512,8 @@ int graph_learned(mdet_ctx* ctx, const float* d_tnf, const double* d_ls, uint64_
         void* tmp = ctx_scratch(ctx, "lrn.caltmp", tmpb);
         if (!tmp) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cub::DeviceRadixSort::SortKeys(tmp, tmpb, cal, cal2, (int)ncal, 0, 32, s));
-        const double q = 1.0 - (1.0 - target) / 4.0;
+        const double q = rep && rep->tau_quantile > 0 && rep->tau_quantile < 1 ? rep->tau_quantile
+                                                                              : 1.0 - (1.0 - target) / 4.0;
         const uint64_t qi = std::min<uint64_t>(ncal - 1, (uint64_t)std::ceil(q * (double)(ncal - 1)));
         float hq = 0;
         MDET_CUDA(ctx, cudaMemcpyAsync(&hq, cal2 + qi, 4, cudaMemcpyDeviceToHost, s));

@@ -137,6 +137,7 @@ class LearnedReport(ctypes.Structure):
         ("ms_embed", D),
         ("ms_order", D),
         ("ms_sample", D),
+        ("tau_quantile", D),
     ]
 
     def as_dict(self):
@@ -572,7 +573,7 @@ class Context:
 
     # ---- learned proposal -----------------------------------------------
     def set_learned(self, net: "Network | None", recall_target: float = 0.999, recall_rows: int = 2048,
-                    segment: int = 0, order: int = 0):
+                    segment: int = 0, order: int = 0, tau_quantile: float = 0.0):
         """Network used by mode="learned" graph calls; returns the report that
         those calls fill (recall estimate, fallback, tiles skipped, tau, phase
         times).  order 0: embedding-major contig order, order 1: size-major."""
@@ -581,6 +582,7 @@ class Context:
         rep.recall_rows = recall_rows
         rep.segment = segment
         rep.order = order
+        rep.tau_quantile = tau_quantile
         self._learned = (net, rep)  # the context keeps both pointers
         self._check(self.lib.mdet_ctx_set_learned(self.h, net.h if net else None, ctypes.byref(rep)))
         return rep

@@ -77,16 +77,16 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 
 struct LpArgs {
     const uint32_t* inc_off;  // [n + 1]
-    const uint32_t* inc;      // traversal-graph edge ids per contig, increasing
-    const uint32_t* ea;       // the edge's first contig (the reference's to)
-    const uint32_t* eb;       // the edge's second contig (from)
-    const double* lw;         // log(1 - score)
+    const uint32_t* oth;      // per incidence (a contig's traversal edges, increasing): the other contig
+    const double* ilw;        // per incidence: the edge's log(1 - score)
     uint32_t* mem;
     uint8_t* stuck;
     uint8_t* dirty;           // a neighbour's label changed since the contig was last evaluated
     unsigned long long* vt;   // visited (contig, label) table, 0 = empty
     unsigned long long vt_mask;
     const double* logfact;
+    const double* recip;      // 1/j for j < nrecip (the CDF's series steps)
+    uint32_t nrecip;
     unsigned long long* counters;  // [0] moved, [1] table entries, [2] error flags, [3] tied picks
     unsigned char* big_ws;
     size_t big_stride;
@@ -147,10 +147,9 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
     // (neighbour label, edge position) keys and the edges' log(1 - score)
     for (uint32_t j = t; j < N; j += kThreads) {
         if (j < d) {
-            const uint32_t e = P.inc[s + j];
-            const uint32_t o = P.ea[e] == v ? P.eb[e] : P.ea[e];
+            const uint32_t o = P.oth[s + j];
             sk[j] = ((unsigned long long)P.mem[o] << 32) | j;
-            w[j] = P.lw[e];
+            w[j] = P.ilw[s + j];
         } else {
             sk[j] = ~0ull;
         }
@@ -187,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
                 sum = sum + w[(uint32_t)sk[q]];
                 ++q;
             } while (q < d && (uint32_t)(sk[q] >> 32) == lab);
-            vp = lpm::chi2_cdf(2.0 * (double)(q - p), -2.0 * sum, P.logfact);
+            vp = lpm::chi2_cdf(2.0 * (double)(q - p), -2.0 * sum, P.logfact, P.recip, P.nrecip);
             fidx[(uint32_t)sk[p]] = (int32_t)p;
         }
         val[p] = vp;
@@ -254,8 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
     __syncthreads();
     if (s_changed)
         for (uint32_t j = t; j < d; j += kThreads) {
-            const uint32_t e = P.inc[s + j];
-            P.dirty[P.ea[e] == v ? P.eb[e] : P.ea[e]] = 1;
+            P.dirty[P.oth[s + j]] = 1;
         }
 }
 
@@ -286,10 +284,9 @@ __global__ void __launch_bounds__(kThreads) k_lp_level_warp(LpArgs P, const uint
     unsigned long long key = ~0ull;
     uint32_t o = 0;
     if (lane < d) {
-        const uint32_t e = P.inc[s + lane];
-        o = P.ea[e] == v ? P.eb[e] : P.ea[e];
+        o = P.oth[s + lane];
         key = ((unsigned long long)P.mem[o] << 32) | lane;
-        W.w[lane] = P.lw[e];
+        W.w[lane] = P.ilw[s + lane];
     }
     W.fidx[lane] = -1;
     // bitonic sort over the lanes, ascending
@@ -314,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_lp_level_warp(LpArgs P, const uint
             sum = sum + W.w[(uint32_t)W.sk[q]];
             ++q;
         } while (q < d && (uint32_t)(W.sk[q] >> 32) == lab);
-        val = lpm::chi2_cdf(2.0 * (double)(q - lane), -2.0 * sum, P.logfact);
+        val = lpm::chi2_cdf(2.0 * (double)(q - lane), -2.0 * sum, P.logfact, P.recip, P.nrecip);
         W.fidx[(uint32_t)key] = (int32_t)lane;
     }
     W.val[lane] = val;
@@ -384,8 +381,7 @@ __device__ __forceinline__ void lp_enqueue(uint32_t w, uint32_t deg, uint32_t* n
 __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ order, uint32_t norder,
                                                  const uint32_t* __restrict__ pos_of,
                                                  const uint32_t* __restrict__ inc_off,
-                                                 const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
-                                                 const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
+                                                 const uint32_t* __restrict__ oth, uint32_t* __restrict__ pred,
                                                  uint32_t* __restrict__ level0, uint32_t* __restrict__ level0_small,
                                                  LevelInfo* info, uint32_t* __restrict__ slot_of) {
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -393,11 +389,7 @@ __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ or
     const uint32_t u = order[wid], pu = wid;
     const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
     uint32_t c = 0;
-    for (uint32_t j = lane; j < d; j += 32) {
-        const uint32_t e = inc[s + j];
-        const uint32_t o = ea[e] == u ? eb[e] : ea[e];
-        c += pos_of[o] < pu;
-    }
+    for (uint32_t j = lane; j < d; j += 32) c += pos_of[oth[s + j]] < pu;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
     if (lane == 0) {
@@ -411,8 +403,7 @@ __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ or
 __global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cur, uint32_t ncur,
                                                  const uint32_t* __restrict__ pos_of,
                                                  const uint32_t* __restrict__ inc_off,
-                                                 const uint32_t* __restrict__ inc, const uint32_t* __restrict__ ea,
-                                                 const uint32_t* __restrict__ eb, uint32_t* __restrict__ pred,
+                                                 const uint32_t* __restrict__ oth, uint32_t* __restrict__ pred,
                                                  uint32_t* __restrict__ next, uint32_t* __restrict__ next_small,
                                                  LevelInfo* info, uint32_t* __restrict__ slot_of) {
     const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -421,8 +412,7 @@ __global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cu
     const uint32_t pu = pos_of[u];
     const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
     for (uint32_t j = lane; j < d; j += 32) {
-        const uint32_t e = inc[s + j];
-        const uint32_t o = ea[e] == u ? eb[e] : ea[e];
+        const uint32_t o = oth[s + j];
         if (pos_of[o] > pu && atomicSub(pred + o, 1u) == 1u)
             lp_enqueue(o, inc_off[o + 1] - inc_off[o], next, next_small, info, slot_of);
     }
@@ -564,7 +554,24 @@ __global__ void k_lp_inc_keys(const uint32_t* __restrict__ ea, const uint32_t* _
     atomicAdd(deg + eb[e], 1u);
 }
 
+// per incidence (sorted by contig, then edge): the other contig and the
+// edge's log(1 - score), so that the sweeps read them in order
+__global__ void k_lp_inc_fill(const uint32_t* __restrict__ inc, const uint32_t* __restrict__ node, uint64_t cnt,
+                              const uint32_t* __restrict__ ea, const uint32_t* __restrict__ eb,
+                              const double* __restrict__ lw, uint32_t* __restrict__ oth, double* __restrict__ ilw) {
+    const uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (j >= cnt) return;
+    const uint32_t e = inc[j], v = node[j];
+    oth[j] = ea[e] == v ? eb[e] : ea[e];
+    ilw[j] = lw[e];
+}
+
 __global__ void k_lp_logfact(double* out, uint32_t count) { lpm::log_factorials(out, count); }
+
+__global__ void k_lp_recip(double* out, uint32_t count) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < count) out[j] = j ? 1.0 / (double)j : 0.0;  // lpm::reciprocals, one entry per thread
+}
 
 // before a run: contigs with an edge added since the last run, and contigs
 // frozen in the last run (free again now), are evaluated in its first sweep;
@@ -610,6 +617,8 @@ struct LpState {
     uint64_t m_run = 0;  // traversal-graph edges at the last propagation run
     double* logfact = nullptr;  // log(j!) for j < logfact_n
     uint64_t logfact_n = 0;
+    double* recip = nullptr;    // 1/j for j < recip_n
+    uint64_t recip_n = 0;
 };
 
 // A CUDA graph recorded from a body of stream work (owned; freed on scope exit).
@@ -651,6 +660,8 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     uint32_t* ival = (uint32_t*)ctx_scratch(ctx, "lp.ival", 2 * m * 4 + 8);
     uint32_t* ikey2 = (uint32_t*)ctx_scratch(ctx, "lp.ikey2", 2 * m * 4 + 8);
     uint32_t* inc = (uint32_t*)ctx_scratch(ctx, "lp.inc", 2 * m * 4 + 8);
+    uint32_t* oth = (uint32_t*)ctx_scratch(ctx, "lp.oth", 2 * m * 4 + 8);
+    double* ilw = (double*)ctx_scratch(ctx, "lp.ilw", 2 * m * 8 + 8);
     unsigned int* deg = (unsigned int*)ctx_scratch(ctx, "lp.deg", (n + 1) * 4);
     uint32_t* inc_off = (uint32_t*)ctx_scratch(ctx, "lp.incoff", (n + 1) * 4);
     uint32_t* pos_of = (uint32_t*)ctx_scratch(ctx, "lp.pos", n * 4);
@@ -659,8 +670,8 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     uint32_t* lvls = (uint32_t*)ctx_scratch(ctx, "lp.lvls", (no + 1) * 4);
     uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "lp.slotof", n * 4);
     LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", sizeof(LevelInfo));
-    if (!ikey || !ival || !ikey2 || !inc || !deg || !inc_off || !pos_of || !pred || !lvl || !lvls || !slot_of ||
-        !info)
+    if (!ikey || !ival || !ikey2 || !inc || !oth || !ilw || !deg || !inc_off || !pos_of || !pred || !lvl || !lvls ||
+        !slot_of || !info)
         return MDET_ERR_NOMEM;
     ctx_timer_begin(ctx, "lp_levels");
     MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (n + 1) * 4, s));
@@ -678,14 +689,16 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         if (!tmp) return MDET_ERR_NOMEM;
         MDET_CUDA(ctx, cub::DeviceScan::ExclusiveSum(tmp, tb, deg, inc_off, (int)(n + 1), s));
     }
+    k_lp_inc_fill<<<grid_for(2 * m), 256, 0, s>>>(inc, ikey2, 2 * m, S.ea, S.eb, S.lw, oth, ilw);
+    MDET_LAUNCHED(ctx, "k_lp_inc_fill");
     // dependency levels: per level, the warp contigs (lvls) and the block
     // contigs (lvl), each list's levels stored one after another
     MDET_CUDA(ctx, cudaMemsetAsync(pos_of, 0xFF, n * 4, s));
     k_lp_pos<<<grid_for(no), 256, 0, s>>>(S.order, (uint32_t)no, pos_of);
     MDET_LAUNCHED(ctx, "k_lp_pos");
     MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
-    k_lp_pred<<<grid_for(no * 32), 256, 0, s>>>(S.order, (uint32_t)no, pos_of, inc_off, inc, S.ea, S.eb, pred, lvl,
-                                                 lvls, info, slot_of);
+    k_lp_pred<<<grid_for(no * 32), 256, 0, s>>>(S.order, (uint32_t)no, pos_of, inc_off, oth, pred, lvl, lvls, info,
+                                                 slot_of);
     MDET_LAUNCHED(ctx, "k_lp_pred");
     std::vector<uint64_t> loff{0}, soff{0};
     std::vector<LevelInfo> linfo;
@@ -707,15 +720,15 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         if (done >= no) break;
         MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
         if (h.count) {
-            k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, inc, S.ea,
-                                                                        S.eb, pred, lvl + loff.back(),
-                                                                        lvls + soff.back(), info, slot_of);
+            k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, oth, pred,
+                                                                        lvl + loff.back(), lvls + soff.back(), info,
+                                                                        slot_of);
             MDET_LAUNCHED(ctx, "k_lp_kahn");
         }
         if (h.nsmall) {
-            k_lp_kahn<<<grid_for((uint64_t)h.nsmall * 32), 256, 0, s>>>(lvls + curs, h.nsmall, pos_of, inc_off, inc,
-                                                                         S.ea, S.eb, pred, lvl + loff.back(),
-                                                                         lvls + soff.back(), info, slot_of);
+            k_lp_kahn<<<grid_for((uint64_t)h.nsmall * 32), 256, 0, s>>>(lvls + curs, h.nsmall, pos_of, inc_off, oth,
+                                                                         pred, lvl + loff.back(), lvls + soff.back(),
+                                                                         info, slot_of);
             MDET_LAUNCHED(ctx, "k_lp_kahn");
         }
     }
@@ -735,6 +748,13 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         k_lp_logfact<<<1, 1, 0, s>>>(S.logfact, (uint32_t)len);
         MDET_LAUNCHED(ctx, "k_lp_logfact");
         S.logfact_n = len;
+        // the series runs past c by up to a few thousand steps; beyond the
+        // table the CDF divides, with the same result
+        S.recip_n = len + 8192;
+        S.recip = (double*)ctx_scratch(ctx, "lp.recip", S.recip_n * 8);
+        if (!S.recip) return MDET_ERR_NOMEM;
+        k_lp_recip<<<grid_for(S.recip_n), 256, 0, s>>>(S.recip, (uint32_t)S.recip_n);
+        MDET_LAUNCHED(ctx, "k_lp_recip");
     }
     const double* logfact = S.logfact;
     // global sort slices for the contigs with more than kSmallCap edges
@@ -766,8 +786,8 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         MDET_CUDA(ctx, cudaMemsetAsync(vt, 0, vt_cap * 8, s));
         MDET_CUDA(ctx, cudaMemsetAsync(S.stuck, 0, n, s));
         MDET_CUDA(ctx, cudaMemsetAsync(S.cnt, 0, 4 * 8, s));
-        LpArgs P{inc_off, inc, S.ea, S.eb, S.lw, S.mem, S.stuck, S.dirty, vt, vt_cap - 1, logfact, S.cnt, big_ws,
-                 big_stride, maxbig, slot_of};
+        LpArgs P{inc_off,  oth,   ilw,       S.mem,   S.stuck,    S.dirty,          vt,
+                 vt_cap - 1, logfact, S.recip, (uint32_t)S.recip_n, S.cnt, big_ws, big_stride, maxbig, slot_of};
         uint64_t low = INT_MAX, attempt = 0, sweeps = 0;
         unsigned long long* hc = (unsigned long long*)ctx_pinned(ctx, 32);
         if (!hc) return MDET_ERR_NOMEM;

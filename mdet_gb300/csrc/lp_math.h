@@ -16,7 +16,9 @@
 //    lower incomplete gamma P(c, y), y = x/2, for integer c:
 //      y <  c:  P = pois(c; y) * sum_k y^k / ((c+1)...(c+k))
 //      y >= c:  P = 1 - pois(c-1; y) * sum_{i<c} (c-1)!/i! y^(i-c+1)
-//    with pois(j; y) = exp(-y + j log y - log j!) and log j! summed in order.
+//    with pois(j; y) = exp(-y + j log y - log j!) and log j! summed in order;
+//    the series' divisions are multiplications by reciprocals (1/(c+k) and
+//    1/y), which a device table can supply without changing a bit.
 //    This replaces boost::math::cdf(chi_squared(2c), x), which the reference
 //    calls (cuda/Cuda2.cu:611-616); Boost is not part of this build.
 #pragma once
@@ -100,9 +102,22 @@ LP_HD void log_factorials(double* out, uint32_t count) {
     }
 }
 
+// 1/j, from recip[j] when the table holds it (recip[j] = 1.0 / j, so the
+// value is the same either way; the table only spares the division)
+LP_HD double inv(uint32_t j, const double* recip, uint32_t nrecip) {
+    return (recip && j < nrecip) ? recip[j] : 1.0 / (double)j;
+}
+
+// recip[j] = 1.0 / j for 1 <= j < count (recip[0] = 0)
+LP_HD void reciprocals(double* out, uint32_t count) {
+    for (uint32_t j = 0; j < count; ++j) out[j] = j ? 1.0 / (double)j : 0.0;
+}
+
 // chi-squared CDF with dof = 2c degrees of freedom at x (c >= 1 an
-// integer); logfact[j] = log(j!) for j <= c.
-LP_HD double chi2_cdf(double dof, double x, const double* logfact) {
+// integer); logfact[j] = log(j!) for j <= c; recip (optional, nrecip
+// entries) as in inv().  Each series step multiplies by a reciprocal.
+LP_HD double chi2_cdf(double dof, double x, const double* logfact, const double* recip = nullptr,
+                      uint32_t nrecip = 0) {
     const uint32_t c = (uint32_t)(dof * 0.5);
     const double y = x * 0.5;
     if (!(y > 0)) return 0.0;
@@ -112,16 +127,17 @@ LP_HD double chi2_cdf(double dof, double x, const double* logfact) {
         const double lp = (-y + (double)c * ly) - logfact[c];
         double t = 1.0, v = 1.0;
         for (uint32_t k = 1; k < 1000000u; ++k) {
-            t = (t * y) / ((double)c + (double)k);
+            t = (t * y) * inv(c + k, recip, nrecip);
             v = v + t;
             if (t < v * 1e-17) break;
         }
         return lpm::exp(lp) * v;
     }
     const double lq = (-y + (double)(c - 1) * ly) - logfact[c - 1];
+    const double iy = 1.0 / y;
     double u = 1.0, w = 1.0;
     for (uint32_t i = c - 1; i >= 1; --i) {
-        u = (u * (double)i) / y;
+        u = (u * (double)i) * iy;
         w = w + u;
         if (u < w * 1e-17) break;
     }

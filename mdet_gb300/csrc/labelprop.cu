@@ -84,8 +84,8 @@ struct LpArgs {
     uint8_t* dirty;           // a neighbour's label changed since the contig was last evaluated
     unsigned long long* vt;   // visited (contig, label) table, 0 = empty
     unsigned long long vt_mask;
-    const double* logfact;
-    const double* recip;      // 1/j for j < nrecip (the CDF's series steps)
+    const lpf::F2* logfact;
+    const lpf::F2* recip;     // 1/j for j < nrecip (the CDF's series steps)
     uint32_t nrecip;
     unsigned long long* counters;  // [0] moved, [1] table entries, [2] error flags, [3] tied picks
     unsigned char* big_ws;
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_lp_level(LpArgs P, const uint32_t*
                 sum = sum + w[(uint32_t)sk[q]];
                 ++q;
             } while (q < d && (uint32_t)(sk[q] >> 32) == lab);
-            vp = lpm::chi2_cdf(2.0 * (double)(q - p), -2.0 * sum, P.logfact, P.recip, P.nrecip);
+            vp = lpf::chi2_cdf(2.0 * (double)(q - p), -2.0 * sum, P.logfact, P.recip, P.nrecip);
             fidx[(uint32_t)sk[p]] = (int32_t)p;
         }
         val[p] = vp;
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_lp_level_warp(LpArgs P, const uint
             sum = sum + W.w[(uint32_t)W.sk[q]];
             ++q;
         } while (q < d && (uint32_t)(W.sk[q] >> 32) == lab);
-        val = lpm::chi2_cdf(2.0 * (double)(q - lane), -2.0 * sum, P.logfact, P.recip, P.nrecip);
+        val = lpf::chi2_cdf(2.0 * (double)(q - lane), -2.0 * sum, P.logfact, P.recip, P.nrecip);
         W.fidx[(uint32_t)key] = (int32_t)lane;
     }
     W.val[lane] = val;
@@ -566,11 +566,11 @@ __global__ void k_lp_inc_fill(const uint32_t* __restrict__ inc, const uint32_t* 
     ilw[j] = lw[e];
 }
 
-__global__ void k_lp_logfact(double* out, uint32_t count) { lpm::log_factorials(out, count); }
+__global__ void k_lp_logfact(lpf::F2* out, uint32_t count) { lpf::log_factorials(out, count); }
 
-__global__ void k_lp_recip(double* out, uint32_t count) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < count) out[j] = j ? 1.0 / (double)j : 0.0;  // lpm::reciprocals, one entry per thread
+__global__ void k_lp_recip(lpf::F2* out, uint32_t count) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;  // lpf::reciprocals, one entry per thread
+    if (j < count) out[j] = j ? lpf::from_double(1.0 / (double)j) : lpf::make(0.0f, 0.0f);
 }
 
 // before a run: contigs with an edge added since the last run, and contigs
@@ -615,9 +615,9 @@ struct LpState {
     double* lw = nullptr;
     uint64_t m2 = 0, norder = 0;
     uint64_t m_run = 0;  // traversal-graph edges at the last propagation run
-    double* logfact = nullptr;  // log(j!) for j < logfact_n
+    lpf::F2* logfact = nullptr;  // log(j!) for j < logfact_n
     uint64_t logfact_n = 0;
-    double* recip = nullptr;    // 1/j for j < recip_n
+    lpf::F2* recip = nullptr;    // 1/j for j < recip_n
     uint64_t recip_n = 0;
 };
 
@@ -743,7 +743,7 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     // needs a longer one)
     if ((uint64_t)maxdeg + 2 > S.logfact_n) {
         const uint64_t len = std::max<uint64_t>((uint64_t)maxdeg + 2, 2 * S.logfact_n);
-        S.logfact = (double*)ctx_scratch(ctx, "lp.logfact", len * 8);
+        S.logfact = (lpf::F2*)ctx_scratch(ctx, "lp.logfact", len * sizeof(lpf::F2));
         if (!S.logfact) return MDET_ERR_NOMEM;
         k_lp_logfact<<<1, 1, 0, s>>>(S.logfact, (uint32_t)len);
         MDET_LAUNCHED(ctx, "k_lp_logfact");
@@ -751,12 +751,12 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         // the series runs past c by up to a few thousand steps; beyond the
         // table the CDF divides, with the same result
         S.recip_n = len + 8192;
-        S.recip = (double*)ctx_scratch(ctx, "lp.recip", S.recip_n * 8);
+        S.recip = (lpf::F2*)ctx_scratch(ctx, "lp.recip", S.recip_n * sizeof(lpf::F2));
         if (!S.recip) return MDET_ERR_NOMEM;
         k_lp_recip<<<grid_for(S.recip_n), 256, 0, s>>>(S.recip, (uint32_t)S.recip_n);
         MDET_LAUNCHED(ctx, "k_lp_recip");
     }
-    const double* logfact = S.logfact;
+    const lpf::F2* logfact = S.logfact;
     // global sort slices for the contigs with more than kSmallCap edges
     const size_t big_stride = maxdeg > kSmallCap ? (ws_bytes(pow2_at_least(maxdeg)) + 255) / 256 * 256 : 0;
     unsigned char* big_ws = nullptr;

@@ -46,13 +46,13 @@ struct chi_squared {
     explicit chi_squared(double d) : dof(d) {}
 };
 inline double cdf(const chi_squared& d, double x) {
-    static std::vector<double> lf;
+    static std::vector<lpf::F2> lf;
     const size_t c = (size_t)(d.dof * 0.5);
     if (lf.size() <= c) {
         lf.resize(std::max<size_t>(c + 1, 2 * lf.size()));
-        lpm::log_factorials(lf.data(), (uint32_t)lf.size());
+        lpf::log_factorials(lf.data(), (uint32_t)lf.size());
     }
-    return lpm::chi2_cdf(d.dof, x, lf.data());
+    return lpf::chi2_cdf(d.dof, x, lf.data());
 }
 }  // namespace math
 template <class T, class S>

@@ -920,7 +920,8 @@ uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t*
 /* ------------------------------------------------------------------------
  * Label propagation over the scored edge graph (cuda/Cuda2.cu:1980-2061, the
  * traversal of main, and label_propagation, cuda/Cuda2.cu:569-656),
- * restated.  The chi-squared CDF, and the log of 1 - sSCR, are the
+ * restated.  The chi-squared CDF (float-float, lpf::chi2_cdf), and the log
+ * of 1 - sSCR (double, lpm::log), are the
  * project's own host/device functions of mdet_gb300/csrc/lp_math.h (the
  * reference calls Boost's CDF and the C library's log; Boost is not part of
  * this build), so that the device form can be held to the last bit.  The
@@ -943,11 +944,11 @@ struct LpGraph {
 };
 
 struct LpFact {
-    std::vector<double> t;
-    const double* at(uint64_t c) {
+    std::vector<lpf::F2> t;
+    const lpf::F2* at(uint64_t c) {
         if (t.size() <= c) {
             t.resize(std::max<uint64_t>(c + 1, 2 * t.size()));
-            lpm::log_factorials(t.data(), (uint32_t)t.size());
+            lpf::log_factorials(t.data(), (uint32_t)t.size());
         }
         return t.data();
     }
@@ -983,7 +984,7 @@ void lp_call(LpGraph& g, std::vector<uint64_t>& mem, const std::vector<uint64_t>
             if (score.empty()) continue;
             for (auto& kv : score) {
                 const uint64_t c = cnt[kv.first];
-                kv.second = lpm::chi2_cdf(2.0 * (double)c, -2.0 * kv.second, lf.at(c));
+                kv.second = lpf::chi2_cdf(2.0 * (double)c, -2.0 * kv.second, lf.at(c));
             }
             auto best = score.begin();
             for (auto it = score.begin(); it != score.end(); ++it)
@@ -1091,9 +1092,9 @@ void orc_umap_order(const uint64_t* keys, uint64_t k, uint64_t* out) {
 double orc_lp_log(double x) { return lpm::log(x); }
 double orc_lp_exp(double x) { return lpm::exp(x); }
 double orc_lp_chi2_cdf(uint64_t count, double x) {
-    std::vector<double> lf(count + 1);
-    lpm::log_factorials(lf.data(), (uint32_t)lf.size());
-    return lpm::chi2_cdf(2.0 * (double)count, x, lf.data());
+    std::vector<lpf::F2> lf(count + 1);
+    lpf::log_factorials(lf.data(), (uint32_t)lf.size());
+    return lpf::chi2_cdf(2.0 * (double)count, x, lf.data());
 }
 
 }  // extern "C"

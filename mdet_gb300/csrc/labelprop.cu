@@ -359,9 +359,10 @@ __global__ void k_lp_pos(const uint32_t* __restrict__ order, uint32_t norder, ui
 }
 
 // a level's contigs: those with at most kWarpCap edges (a warp each) and the
-// others (a block each; maxdeg and the global slices are theirs)
+// others (a block each; maxdeg and the global slices are theirs); off and
+// soff: where the level starts in the block and warp lists
 struct LevelInfo {
-    unsigned int count, maxdeg, nbig, nsmall, maxall, pad[3];
+    unsigned int count, maxdeg, nbig, nsmall, maxall, off, soff, pad;
 };
 
 __device__ __forceinline__ void lp_enqueue(uint32_t w, uint32_t deg, uint32_t* next, uint32_t* next_small,
@@ -398,23 +399,32 @@ __global__ void __launch_bounds__(256) k_lp_pred(const uint32_t* __restrict__ or
     }
 }
 
-// one Kahn step: contigs whose last earlier neighbour is in this level join
-// the next one
-__global__ void __launch_bounds__(256) k_lp_kahn(const uint32_t* __restrict__ cur, uint32_t ncur,
-                                                 const uint32_t* __restrict__ pos_of,
+// One Kahn step for level L (its size and place read from info[L], so steps
+// can be queued without the host): contigs whose last earlier neighbour is
+// in this level join level L + 1.  A warp per contig, grid-stride.
+__global__ void __launch_bounds__(256) k_lp_kahn(uint32_t L, const uint32_t* __restrict__ pos_of,
                                                  const uint32_t* __restrict__ inc_off,
                                                  const uint32_t* __restrict__ oth, uint32_t* __restrict__ pred,
-                                                 uint32_t* __restrict__ next, uint32_t* __restrict__ next_small,
+                                                 uint32_t* __restrict__ lvl, uint32_t* __restrict__ lvls,
                                                  LevelInfo* info, uint32_t* __restrict__ slot_of) {
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (wid >= ncur) return;
-    const uint32_t u = cur[wid];
-    const uint32_t pu = pos_of[u];
-    const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
-    for (uint32_t j = lane; j < d; j += 32) {
-        const uint32_t o = oth[s + j];
-        if (pos_of[o] > pu && atomicSub(pred + o, 1u) == 1u)
-            lp_enqueue(o, inc_off[o + 1] - inc_off[o], next, next_small, info, slot_of);
+    const LevelInfo cur = info[L];
+    const uint32_t total = cur.count + cur.nsmall;
+    const uint32_t noff = cur.off + cur.count, nsoff = cur.soff + cur.nsmall;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        info[L + 1].off = noff;
+        info[L + 1].soff = nsoff;
+    }
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wid < total; wid += nw) {
+        const uint32_t u = wid < cur.count ? lvl[cur.off + wid] : lvls[cur.soff + wid - cur.count];
+        const uint32_t pu = pos_of[u];
+        const uint32_t s = inc_off[u], d = inc_off[u + 1] - s;
+        for (uint32_t j = lane; j < d; j += 32) {
+            const uint32_t o = oth[s + j];
+            if (pos_of[o] > pu && atomicSub(pred + o, 1u) == 1u)
+                lp_enqueue(o, inc_off[o + 1] - inc_off[o], lvl + noff, lvls + nsoff, info + L + 1, slot_of);
+        }
     }
 }
 
@@ -669,9 +679,8 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     uint32_t* lvl = (uint32_t*)ctx_scratch(ctx, "lp.lvl", (no + 1) * 4);
     uint32_t* lvls = (uint32_t*)ctx_scratch(ctx, "lp.lvls", (no + 1) * 4);
     uint32_t* slot_of = (uint32_t*)ctx_scratch(ctx, "lp.slotof", n * 4);
-    LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", sizeof(LevelInfo));
     if (!ikey || !ival || !ikey2 || !inc || !oth || !ilw || !deg || !inc_off || !pos_of || !pred || !lvl || !lvls ||
-        !slot_of || !info)
+        !slot_of)
         return MDET_ERR_NOMEM;
     ctx_timer_begin(ctx, "lp_levels");
     MDET_CUDA(ctx, cudaMemsetAsync(deg, 0, (n + 1) * 4, s));
@@ -696,7 +705,12 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     MDET_CUDA(ctx, cudaMemsetAsync(pos_of, 0xFF, n * 4, s));
     k_lp_pos<<<grid_for(no), 256, 0, s>>>(S.order, (uint32_t)no, pos_of);
     MDET_LAUNCHED(ctx, "k_lp_pos");
-    MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
+    // levels: Kahn steps queued sixteen at a time, their table read back once
+    // per batch
+    const uint64_t lcap = no + 18;
+    LevelInfo* info = (LevelInfo*)ctx_scratch(ctx, "lp.info", lcap * sizeof(LevelInfo));
+    if (!info) return MDET_ERR_NOMEM;
+    MDET_CUDA(ctx, cudaMemsetAsync(info, 0, lcap * sizeof(LevelInfo), s));
     k_lp_pred<<<grid_for(no * 32), 256, 0, s>>>(S.order, (uint32_t)no, pos_of, inc_off, oth, pred, lvl, lvls, info,
                                                  slot_of);
     MDET_LAUNCHED(ctx, "k_lp_pred");
@@ -704,33 +718,32 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
     std::vector<LevelInfo> linfo;
     uint64_t done = 0;
     uint32_t maxdeg = 0, maxall = 0, maxbig = 0;
-    while (true) {
-        LevelInfo h;
-        MDET_CUDA(ctx, cudaMemcpyAsync(&h, info, sizeof(LevelInfo), cudaMemcpyDeviceToHost, s));
+    const unsigned kgrid = (unsigned)ctx->num_sms * 8;
+    std::vector<LevelInfo> batch(17);
+    for (uint32_t L0 = 0; done < no && L0 + 17 <= lcap;) {
+        for (uint32_t L = L0; L < L0 + 16; ++L) {
+            k_lp_kahn<<<kgrid, 256, 0, s>>>(L, pos_of, inc_off, oth, pred, lvl, lvls, info, slot_of);
+            MDET_LAUNCHED(ctx, "k_lp_kahn");
+        }
+        MDET_CUDA(ctx, cudaMemcpyAsync(batch.data(), info + L0, 17 * sizeof(LevelInfo), cudaMemcpyDeviceToHost, s));
         MDET_CUDA(ctx, cudaStreamSynchronize(s));
-        if (h.count + h.nsmall == 0) break;
-        linfo.push_back(h);
-        maxdeg = std::max(maxdeg, h.maxdeg);
-        maxall = std::max(maxall, h.maxall);
-        maxbig = std::max(maxbig, h.nbig);
-        const uint64_t cur = loff.back(), curs = soff.back();
-        loff.push_back(cur + h.count);
-        soff.push_back(curs + h.nsmall);
-        done += h.count + h.nsmall;
-        if (done >= no) break;
-        MDET_CUDA(ctx, cudaMemsetAsync(info, 0, sizeof(LevelInfo), s));
-        if (h.count) {
-            k_lp_kahn<<<grid_for((uint64_t)h.count * 32), 256, 0, s>>>(lvl + cur, h.count, pos_of, inc_off, oth, pred,
-                                                                        lvl + loff.back(), lvls + soff.back(), info,
-                                                                        slot_of);
-            MDET_LAUNCHED(ctx, "k_lp_kahn");
+        bool ended = false;
+        for (int k = 0; k < 16; ++k) {
+            const LevelInfo& h = batch[k];
+            if (h.count + h.nsmall == 0) {
+                ended = true;
+                break;
+            }
+            linfo.push_back(h);
+            maxdeg = std::max(maxdeg, h.maxdeg);
+            maxall = std::max(maxall, h.maxall);
+            maxbig = std::max(maxbig, h.nbig);
+            loff.push_back(h.off + h.count);
+            soff.push_back(h.soff + h.nsmall);
+            done += h.count + h.nsmall;
         }
-        if (h.nsmall) {
-            k_lp_kahn<<<grid_for((uint64_t)h.nsmall * 32), 256, 0, s>>>(lvls + curs, h.nsmall, pos_of, inc_off, oth,
-                                                                         pred, lvl + loff.back(), lvls + soff.back(),
-                                                                         info, slot_of);
-            MDET_LAUNCHED(ctx, "k_lp_kahn");
-        }
+        if (ended || done >= no) break;
+        L0 += 16;
     }
     ctx_timer_end(ctx, "lp_levels");
     if (done != no) return ctx_fail(ctx, MDET_ERR_INTERNAL, "label propagation: %llu of %llu contigs levelled",

@@ -503,6 +503,46 @@ def batch_leg(ctx, dev, count, nmin, nmax, seed):
     return out
 
 
+def recruit_workload(genome, contig_sizes):
+    """The recruiting inputs for an assembly: labels are the contigs'
+    genomes with 1 % of the contigs split off into singleton bins, 20,000
+    small contigs (1-2.5 kb) drawn from the same genomes, 10 samples of
+    seeded depths (synth.abundance)."""
+    from mdet_gb300 import synth
+
+    rng = np.random.default_rng(99)
+    n = genome.size
+    ns = 20000
+    sg = rng.integers(0, int(genome.max()) + 1, ns).astype(np.uint32)
+    both, _ = synth.abundance(np.concatenate([genome, sg]), 10, 20240611)
+    abd = both[:n].astype(np.float32)
+    sabd = both[n:].astype(np.float32)
+    label = genome.astype(np.int64)
+    tiny = rng.random(n) < 0.01
+    label[tiny] = 1 << 40 | np.arange(int(tiny.sum()))
+    sizes = contig_sizes.astype(np.uint64)
+    ssz = rng.integers(1000, 2500, ns).astype(np.uint64)
+    return abd, sabd, label, sizes, ssz
+
+
+def recruit_case(args, synth, ctx):
+    """--case recruit: the recruit leg's workload on the planned assembly
+    (contig sizes and genomes only, no sequences), --repeat calls through
+    the host-buffer entry point, each one's time and the last one's
+    kernel times."""
+    G = args.genomes or max(10, args.n // 500)
+    L, g, _, _ = synth.plan(3, args.n, G)
+    abd, sabd, label, sizes, ssz = recruit_workload(g, L)
+    for r in range(args.repeat):
+        ctx.set_timing(r == args.repeat - 1)
+        t0 = time.perf_counter()
+        _, _, st = ctx.recruit(abd, sabd, label, sizes, ssz, 200000, int(ssz.sum()))
+        print({"call_s": round(time.perf_counter() - t0, 5), **st}, flush=True)
+    print({k: ctx.kernel_ms(k) for k in ("k_rank_rows", "k_bin_corr", "k_recruit_filter", "k_recruit")})
+    ctx.set_timing(False)
+    ctx.close()
+
+
 def recruit_leg(ctx, a, run_cpu):
     """Dissolving small bins and recruiting leftover and small contigs
     (mdet_recruit) after binning the step's assembly: labels are the contigs'
@@ -512,20 +552,8 @@ def recruit_leg(ctx, a, run_cpu):
     timed calls through the host-buffer entry point.  The CPU oracle (one
     thread, the reference's loops) runs the same workload scaled down to
     every tenth contig and 2,000 small contigs; the GPU is timed on that too."""
-    from mdet_gb300 import synth
-
-    rng = np.random.default_rng(99)
-    n = a.genome.size
-    ns = 20000
-    sg = rng.integers(0, int(a.genome.max()) + 1, ns).astype(np.uint32)
-    both, _ = synth.abundance(np.concatenate([a.genome, sg]), 10, 20240611)
-    abd = both[:n].astype(np.float32)
-    sabd = both[n:].astype(np.float32)
-    label = a.genome.astype(np.int64)
-    tiny = rng.random(n) < 0.01
-    label[tiny] = 1 << 40 | np.arange(int(tiny.sum()))
-    sizes = a.sizes.astype(np.uint64)
-    ssz = rng.integers(1000, 2500, ns).astype(np.uint64)
+    abd, sabd, label, sizes, ssz = recruit_workload(a.genome, a.sizes)
+    n, ns = abd.shape[0], sabd.shape[0]
     tot = int(ssz.sum())
     ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
     ts = []
@@ -534,11 +562,12 @@ def recruit_leg(ctx, a, run_cpu):
         t0 = time.perf_counter()
         out, sout, st = ctx.recruit(abd, sabd, label, sizes, ssz, 200000, tot)
         ts.append(time.perf_counter() - t0)
-    kms = {k: ctx.kernel_ms(k)[0] / 3 for k in ("k_rank_rows", "k_bin_corr", "k_recruit")}
+    kms = {k: ctx.kernel_ms(k)[0] / 3 for k in ("k_rank_rows", "k_bin_corr", "k_recruit_filter", "k_recruit")}
     ctx.set_timing(False)
     leg = {"metric": "dissolve + recruit time (host buffers)", "value": float(np.median(ts)), "unit": "s",
            "contigs": int(n), "small_contigs": ns, "samples": 10, **{k: int(v) for k, v in st.items()},
-           "kernels_ms": kms, "bound": "fp64 (the correlations and their sums in the reference's order)",
+           "kernels_ms": kms, "bound": "fp64 (the bin means and the exact tests: correlations and sums in the reference's order); "
+                    "an fp32 prefilter with a proven error bound settles most (contig, bin) pairs",
            "data": "synthetic depths (synth.abundance, seed 20240611), genome labels, 1 % singleton bins"}
     sub = np.arange(0, n, 10)
     s_abd, s_lab, s_sz = abd[sub], label[sub], sizes[sub]
@@ -908,6 +937,7 @@ def run_ours(args):
 #   --case fasta --n 100000     FASTA record split of ~0.85 GB on the device
 #   --case abd --n 100000       gated graph, then sTNF -> sSCR of its edges with 10 samples
 #   --case lp --n 1000000       graph, then label propagation over its edges (sSCR = sTNF)
+#   --case recruit --n 1000000  dissolving and recruiting on the recruit leg's workload
 # The graph case frees the FASTA before the pairwise call so that only the
 # stage's own buffers (~1-2 GB) are resident when it runs.
 
@@ -919,6 +949,8 @@ def run_case(args):
 
     ctx = m.Context(0)
     dev = torch.device("cuda:0")
+    if args.case == "recruit":
+        return recruit_case(args, synth, ctx)
     if args.case == "batch":
         return batch_case(args, m, synth, ctx, dev, torch)
     G = args.genomes or max(10, args.n // 500)
@@ -1150,7 +1182,8 @@ def main():
     ap.add_argument("--no-lp", action="store_true", help="skip the label propagation leg")
     ap.add_argument("--no-recruit", action="store_true", help="skip the dissolve / recruit leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-assemblies legs")
-    ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd", "lp"], default=None,
+    ap.add_argument("--case", choices=["count", "graph", "learned", "batch", "fasta", "abd", "lp", "recruit"],
+                    default=None,
                     help="run one single-stage case instead of the benchmark (profiler workloads)")
     ap.add_argument("--samples", type=int, default=10)
     ap.add_argument("--count", type=int, default=64)

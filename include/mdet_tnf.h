@@ -391,7 +391,8 @@ int mdet_ctx_set_learned(mdet_ctx* ctx, const mdet_mlp* mlp, mdet_learned_report
  * rejects every small recruit).  abd (n x nabd) and small_abd (n_small x
  * nabd) are the reference's ABD and small_ABD (float, row-major; 1 <= nabd
  * <= 256); they are not modified.  out[i]: the bin label of large contig i
- * afterwards, -1 if it has none; small_out[s] likewise.  The caller applies
+ * afterwards, -1 if it has none; small_out[s] likewise.  n + n_small must
+ * be below 2^32 - 1.  The caller applies
  * the reference's own condition for running this block (!noAdd, nABD >=
  * minSample). */
 typedef struct {
@@ -402,6 +403,10 @@ typedef struct {
     uint64_t n_small_matched;     /* small contigs exactly one bin accepts */
     uint64_t binned_bases, leftover_bases, small_bases;
     int leftovers_accepted, small_accepted; /* the 10 % and 15 % gates */
+    uint64_t pairs_tested;        /* (contig, scored bin) pairs */
+    uint64_t pairs_exact;         /* of those, the ones the FP32 prefilter left to the exact FP64 test */
+    uint64_t pairs_undecided;     /* of those, tests within the error bound of a bin's estimated mean */
+    uint64_t bins_exact;          /* bins whose exact mean was computed (degenerate rows, undecided tests) */
 } mdet_recruit_stats;
 int mdet_recruit(mdet_ctx* ctx, const float* abd, const float* small_abd, uint64_t n, uint64_t n_small,
                  uint32_t nabd, const int64_t* label, const uint64_t* sizes, const uint64_t* small_sizes,

@@ -34,7 +34,8 @@ D = ctypes.c_double
 class RecruitStats(ctypes.Structure):
     _fields_ = [("n_bins", u64), ("n_bins_scored", u64), ("n_leftovers", u64), ("n_leftovers_matched", u64),
                 ("n_small_matched", u64), ("binned_bases", u64), ("leftover_bases", u64), ("small_bases", u64),
-                ("leftovers_accepted", ctypes.c_int), ("small_accepted", ctypes.c_int)]
+                ("leftovers_accepted", ctypes.c_int), ("small_accepted", ctypes.c_int), ("pairs_tested", u64),
+                ("pairs_exact", u64), ("pairs_undecided", u64), ("bins_exact", u64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -6,10 +6,13 @@
 //
 // Layout: the context keeps the reference's ABD (mean depth) and ABD_VAR
 // (variance) as n x nabd row-major FP64 matrices in the original contig order,
-// plus one byte per contig that says whether none of its depths exceeds 1.
+// plus one byte per contig that says whether none of its depths exceeds 1,
+// and, formed once when the depths are set, each contig's per-sample variance
+// and CDF scale and its correlation deviations (k_abd_prep).
 // sSCR runs one thread per edge over its nabd samples -- the crossing points
 // of the two normal densities in FP64 as the reference forms them, the four
-// normal CDFs per sample in float-float from this project's erfc table --
+// normal CDFs per sample in float-float from this project's erfc table, the
+// correlation's cross sum --
 // then three radix sorts (the abundance
 // similarities, sTNF and the depth correlations) turn values into ranks and
 // the ranks into quantiles of the similarity distribution.
@@ -51,14 +54,61 @@ __device__ __forceinline__ ff erfc_ff(ff z) {
     return neg ? ff_add_f(ff_neg(r), 2.f) : r;
 }
 
+// 1 / (sd * sqrt(2)) in float-float: the per-(contig, sample) factor of the
+// normal CDF below.
+__device__ __forceinline__ ff cdf_scale(double sd) {
+    return ff_recip(ff_mul(ff_from_double(sd), ff_make(0x1.6a09e6p+0f, 0x1.9fcef4p-26f)));  // sqrt(2)
+}
+
 // Boost's normal CDF, erfc(-(x - mean) / (sd * sqrt(2))) / 2 (the function
 // the reference calls), with x - mean formed in FP64 as the reference forms
-// it and the rest in float-float; returned in double.
-__device__ __forceinline__ double normal_cdf_ff(double mean, double sd, double x) {
+// it and the rest in float-float (isd = cdf_scale(sd)); returned in double.
+__device__ __forceinline__ double normal_cdf_ff(double mean, ff isd, double x) {
     const ff diff = ff_from_double(x - mean);
-    const ff den = ff_mul(ff_from_double(sd), ff_make(0x1.6a09e6p+0f, 0x1.9fcef4p-26f));  // sqrt(2)
-    const ff z = ff_mul(diff, ff_recip(den));
+    const ff z = ff_mul(diff, isd);
     return ff_to_double(erfc_ff(ff_neg(z))) * 0.5;
+}
+
+// What the scoring needs of one contig's depths, formed once when the depths
+// are set (everything here depends on one contig alone, so per edge it would
+// be formed again for every edge the contig is in):
+//   vv[i]   = s * s, s = sqrt(max(var[i], 1)) (the variance the crossing
+//             points use) and isd[i] = cdf_scale(s), per sample;
+//   dev[i]  = the deviation of depth i + 1 from the running mean of depths
+//             0..i, i < nabd - 1, and dev[nabd - 1] = sqrt of the running
+//             sum of squared deviations times i / (i + 1): the one-row steps
+//             of cal_abd_corr, in its order.  The edge's correlation is then
+//             (sum (dev1[i] * dev2[i]) * ratio[i]) / (sx1 * sx2): the
+//             reference's operations on the reference's values.
+//   ratio[i] = (i + 1) / (i + 2.0), as the reference forms it.
+__global__ void k_abd_prep(const double* __restrict__ abd, const double* __restrict__ var, uint64_t n, uint32_t nabd,
+                           double* __restrict__ vv, float2* __restrict__ isd, double* __restrict__ dev,
+                           double* __restrict__ ratio) {
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t0 + 1 < nabd) ratio[t0] = (t0 + 1) / (t0 + 2.0);
+    for (uint64_t r = t0; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+        const double* a = abd + r * nabd;
+        const double* w = var + r * nabd;
+        double sxx = 0., mx = 0.;
+        for (uint32_t i = 0; i < nabd; ++i) {
+            const double u = w[i];
+            const double sd = sqrt(u < 1 ? 1. : u);
+            vv[r * nabd + i] = sd * sd;
+            const ff f = cdf_scale(sd);
+            isd[r * nabd + i] = make_float2(f.hi, f.lo);
+            const double x = a[i];
+            if (i == 0) {
+                mx = x;
+            } else {
+                const double q = i / (i + 1.0);
+                const double dx = x - mx;
+                sxx += dx * dx * q;
+                mx += dx / (i + 1.0);
+                dev[r * nabd + i - 1] = dx;
+            }
+        }
+        dev[r * nabd + nabd - 1] = sqrt(sxx);
+    }
 }
 
 __global__ void k_abd_low(const double* __restrict__ abd, uint64_t n, uint32_t nabd, uint8_t* __restrict__ low) {
@@ -79,10 +129,9 @@ __global__ void k_low_sorted(const uint32_t* __restrict__ perm, const uint8_t* _
 // Overlap of two normal densities from their crossing points k1 <= k2, the
 // narrower distribution evaluated first (cal_abd_dist2).  The crossing
 // points come from a numerator that cancels when the variances are close, so
-// they are formed in FP64 in the reference's order (bit-identical); the four
-// CDF values, the bulk of the work, run in float-float.
-__device__ double abd_dist2(double m1, double s1, double m2, double s2) {
-    const double v1 = s1 * s1, v2 = s2 * s2;
+// they are formed in FP64 in the reference's order; the four CDF values run
+// in float-float.
+__device__ double abd_dist2(double m1, double v1, ff f1, double m2, double v2, ff f2) {
     double k1, k2;
     if (fabs(v2 - v1) < 1e-4) {
         k1 = k2 = (m1 + m2) / 2;
@@ -96,15 +145,16 @@ __device__ double abd_dist2(double m1, double s1, double m2, double s2) {
         k1 = k2;
         k2 = x;
     }
-    double ma = m1, sa = s1, mb = m2, sb = s2;
+    double ma = m1, mb = m2;
+    ff fa = f1, fb = f2;
     if (v1 > v2) {
         ma = m2;
-        sa = s2;
+        fa = f2;
         mb = m1;
-        sb = s1;
+        fb = f1;
     }
-    if (k1 == k2) return fabs(normal_cdf_ff(ma, sa, k1) - normal_cdf_ff(mb, sb, k1));
-    return fabs(normal_cdf_ff(ma, sa, k2) - normal_cdf_ff(ma, sa, k1) + normal_cdf_ff(mb, sb, k1) - normal_cdf_ff(mb, sb, k2));
+    if (k1 == k2) return fabs(normal_cdf_ff(ma, fa, k1) - normal_cdf_ff(mb, fb, k1));
+    return fabs(normal_cdf_ff(ma, fa, k2) - normal_cdf_ff(ma, fa, k1) + normal_cdf_ff(mb, fb, k1) - normal_cdf_ff(mb, fb, k2));
 }
 
 struct ScoreArgs {
@@ -112,7 +162,10 @@ struct ScoreArgs {
     const uint64_t* to;
     uint64_t ne, n;
     const double* abd;
-    const double* var;
+    const double* vv;     // per contig and sample (k_abd_prep)
+    const float2* isd;
+    const double* dev;
+    const double* ratio;
     uint32_t nabd;
     double min_cv;
     bool corr;
@@ -138,12 +191,17 @@ __global__ void k_abd_score(ScoreArgs p) {
         }
         const double* a1 = p.abd + r1 * p.nabd;
         const double* a2 = p.abd + r2 * p.nabd;
-        const double* w1 = p.var + r1 * p.nabd;
-        const double* w2 = p.var + r2 * p.nabd;
+        const double* q1 = p.vv + r1 * p.nabd;
+        const double* q2 = p.vv + r2 * p.nabd;
+        const float2* f1 = p.isd + r1 * p.nabd;
+        const float2* f2 = p.isd + r2 * p.nabd;
+        const double* d1 = p.dev + r1 * p.nabd;
+        const double* d2 = p.dev + r2 * p.nabd;
         double sum = 0.;
         uint32_t k = 0;
-        // Pearson correlation with running means and co-moments (cal_abd_corr)
-        double sxx = 0., syy = 0., sxy = 0., mx = 0., my = 0.;
+        // the cross sum of the Pearson correlation (cal_abd_corr), from the
+        // rows' own deviations
+        double sxy = 0.;
         for (uint32_t i = 0; i < p.nabd; ++i) {
             const double x = a1[i], y = a2[i];
             // cal_abd_dist for sample i
@@ -151,32 +209,20 @@ __global__ void k_abd_score(ScoreArgs p) {
                 double d = 0.;
                 const double m1 = x < 1e-6 ? 1e-6 : x, m2 = y < 1e-6 ? 1e-6 : y;
                 if (m1 != m2) {
-                    const double u1 = w1[i], u2 = w2[i];
-                    const double v1 = u1 < 1 ? 1. : u1, v2 = u2 < 1 ? 1. : u2;
-                    d = abd_dist2(m1, sqrt(v1), m2, sqrt(v2));
+                    const float2 g1 = f1[i], g2 = f2[i];
+                    d = abd_dist2(m1, q1[i], ff_make(g1.x, g1.y), m2, q2[i], ff_make(g2.x, g2.y));
                 }
                 d = d < 1e-6 ? 1e-6 : d;  // std::min(std::max(d, 1e-6), 1 - 1e-6), NaN kept
                 d = (1. - 1e-6) < d ? 1. - 1e-6 : d;
                 sum += 1. - d;
                 ++k;
             }
-            if (i == 0) {
-                mx = x;
-                my = y;
-            } else {
-                const double ratio = i / (i + 1.0);
-                const double dx = x - mx, dy = y - my;
-                sxx += dx * dx * ratio;
-                syy += dy * dy * ratio;
-                sxy += dx * dy * ratio;
-                mx += dx / (i + 1.0);
-                my += dy / (i + 1.0);
-            }
+            if (i > 0) sxy += d1[i - 1] * d2[i - 1] * __ldg(p.ratio + i - 1);
         }
         if (k == 0) atomicAdd(p.bad, 1ull);
         p.raw[e] = sum / (double)k;
         p.nnz[e] = k;
-        if (p.corr) p.cor[e] = sxy / (sqrt(sxx) * sqrt(syy));
+        if (p.corr) p.cor[e] = sxy / (d1[p.nabd - 1] * d2[p.nabd - 1]);
     }
 }
 
@@ -273,7 +319,10 @@ int sscr_core(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const dou
     p.ne = ne;
     p.n = ctx->abd_n;
     p.abd = (const double*)ctx->bufs["abd.m"].p;
-    p.var = (const double*)ctx->bufs["abd.v"].p;
+    p.vv = (const double*)ctx->bufs["abd.vv"].p;
+    p.isd = (const float2*)ctx->bufs["abd.isd"].p;
+    p.dev = (const double*)ctx->bufs["abd.dev"].p;
+    p.ratio = (const double*)ctx->bufs["abd.ratio"].p;
     p.nabd = ctx->abd_nabd;
     p.min_cv = min_cv;
     p.corr = corr;
@@ -338,11 +387,18 @@ int mdet_ctx_set_abundance(mdet_ctx* ctx, const double* abd, const double* abd_v
     double* dm = (double*)ctx_scratch(ctx, "abd.m", n * nabd * 8);
     double* dv = (double*)ctx_scratch(ctx, "abd.v", n * nabd * 8);
     uint8_t* low = (uint8_t*)ctx_scratch(ctx, "abd.low", n);
-    if (!dm || !dv || !low) return MDET_ERR_NOMEM;
+    double* vv = (double*)ctx_scratch(ctx, "abd.vv", n * nabd * 8);
+    float2* isd = (float2*)ctx_scratch(ctx, "abd.isd", n * nabd * 8);
+    double* dev = (double*)ctx_scratch(ctx, "abd.dev", n * nabd * 8);
+    double* ratio = (double*)ctx_scratch(ctx, "abd.ratio", nabd * 8);
+    if (!dm || !dv || !low || !vv || !isd || !dev || !ratio) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cudaMemcpyAsync(dm, abd, n * nabd * 8, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(dv, abd_var, n * nabd * 8, cudaMemcpyHostToDevice, s));
     k_abd_low<<<grid_for(ctx, n, 256), 256, 0, s>>>(dm, n, nabd, low);
     MDET_LAUNCHED(ctx, "k_abd_low");
+    k_abd_prep<<<std::max<unsigned>(grid_for(ctx, n, 256), (nabd + 255) / 256), 256, 0, s>>>(dm, dv, n, nabd, vv,
+                                                                                            isd, dev, ratio);
+    MDET_LAUNCHED(ctx, "k_abd_prep");
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
     ctx->abd_n = n;
     ctx->abd_nabd = nabd;

@@ -247,7 +247,8 @@ def abundance_leg(ctx, a, d_tnf, d_ls, n, cutoff, d_from, d_to, d_st, cap, mode,
     ctx.set_timing(False)
     leg = {"metric": "sTNF -> sSCR edge scoring throughput", "value": ne / call_s, "unit": "edges/s",
            "edges": int(ne), "samples": ABD_SAMPLES, "ms_per_call": call_s * 1e3,
-           "k_abd_score_ms": score_ms / max(score_n, 1), "bound": "fp64 crossing points (sqrt, log, divisions) + float-float erfc per edge and sample",
+           "k_abd_score_ms": score_ms / max(score_n, 1), "bound": "float-float crossing points and erfc per edge and sample (FP32 pipes), the CDF "
+                    "combination and the branch tests in FP64",
            "gated_graph_ms": st["ms_total"], "data": "synthetic coverage (synth.abundance, seed 20240607)"}
     if run_cpu:
         from oracle import oracle

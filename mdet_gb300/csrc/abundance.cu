@@ -7,11 +7,12 @@
 // Layout: the context keeps the reference's ABD (mean depth) and ABD_VAR
 // (variance) as n x nabd row-major FP64 matrices in the original contig order,
 // plus one byte per contig that says whether none of its depths exceeds 1,
-// and, formed once when the depths are set, each contig's per-sample variance
-// and CDF scale and its correlation deviations (k_abd_prep).
+// and, formed once when the depths are set, each contig's per-sample variance,
+// clamped mean and CDF scale and its correlation deviations (k_abd_prep).
 // sSCR runs one thread per edge over its nabd samples -- the crossing points
-// of the two normal densities in FP64 as the reference forms them, the four
-// normal CDFs per sample in float-float from this project's erfc table, the
+// of the two normal densities in float-float (abd_dist2_ff; in FP64 as the
+// reference forms them where the variances are close), the four normal CDFs
+// per sample in float-float from this project's erfc table, the
 // correlation's cross sum --
 // then three radix sorts (the abundance
 // similarities, sTNF and the depth correlations) turn values into ranks and
@@ -80,10 +81,13 @@ __device__ __forceinline__ double normal_cdf_ff(double mean, ff isd, double x) {
 //             of cal_abd_corr, in its order.  The edge's correlation is then
 //             (sum (dev1[i] * dev2[i]) * ratio[i]) / (sx1 * sx2): the
 //             reference's operations on the reference's values.
-//   ratio[i] = (i + 1) / (i + 2.0), as the reference forms it.
+//   ratio[i] = (i + 1) / (i + 2.0), as the reference forms it;
+//   m3[i]   = the clamped mean max(abd[i], 1e-6) as three floats whose sum is
+//             exactly that double (hi, mid, low), vf[i] = vv[i] in
+//             float-float: the inputs of the float-float crossing points.
 __global__ void k_abd_prep(const double* __restrict__ abd, const double* __restrict__ var, uint64_t n, uint32_t nabd,
                            double* __restrict__ vv, float2* __restrict__ isd, double* __restrict__ dev,
-                           double* __restrict__ ratio) {
+                           double* __restrict__ ratio, float4* __restrict__ m3, float2* __restrict__ vf) {
     const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t0 + 1 < nabd) ratio[t0] = (t0 + 1) / (t0 + 2.0);
     for (uint64_t r = t0; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
@@ -96,7 +100,15 @@ __global__ void k_abd_prep(const double* __restrict__ abd, const double* __restr
             vv[r * nabd + i] = sd * sd;
             const ff f = cdf_scale(sd);
             isd[r * nabd + i] = make_float2(f.hi, f.lo);
+            const ff fv = ff_from_double(sd * sd);
+            vf[r * nabd + i] = make_float2(fv.hi, fv.lo);
             const double x = a[i];
+            // the clamped mean as three floats that sum to it exactly
+            const double mc = x < 1e-6 ? 1e-6 : x;
+            const float mh = __double2float_rn(mc);
+            const double r1 = mc - (double)mh;
+            const float ml = __double2float_rn(r1);
+            m3[r * nabd + i] = make_float4(mh, ml, __double2float_rn(r1 - (double)ml), 0.f);
             if (i == 0) {
                 mx = x;
             } else {
@@ -127,10 +139,10 @@ __global__ void k_low_sorted(const uint32_t* __restrict__ perm, const uint8_t* _
 
 
 // Overlap of two normal densities from their crossing points k1 <= k2, the
-// narrower distribution evaluated first (cal_abd_dist2).  The crossing
-// points come from a numerator that cancels when the variances are close, so
-// they are formed in FP64 in the reference's order; the four CDF values run
-// in float-float.
+// narrower distribution evaluated first (cal_abd_dist2), the FP64 form: the
+// crossing points, whose numerator cancels when the variances are close, in
+// FP64 in the reference's order; the four CDF values in float-float.  Used
+// where abd_dist2_ff declines.
 __device__ double abd_dist2(double m1, double v1, ff f1, double m2, double v2, ff f2) {
     double k1, k2;
     if (fabs(v2 - v1) < 1e-4) {
@@ -157,6 +169,69 @@ __device__ double abd_dist2(double m1, double v1, ff f1, double m2, double v2, f
     return fabs(normal_cdf_ff(ma, fa, k2) - normal_cdf_ff(ma, fa, k1) + normal_cdf_ff(mb, fb, k1) - normal_cdf_ff(mb, fb, k2));
 }
 
+// k - m in float-float, m given exactly as three floats: error ~2^-48 of
+// the result.
+__device__ __forceinline__ ff ff_sub_m3(ff k, float4 m) {
+    ff s = two_sum(k.hi, -m.x);
+    s = ff_add_f(s, k.lo);
+    s = ff_add_f(s, -m.y);
+    return ff_add_f(s, -m.z);
+}
+
+__device__ __forceinline__ double cdf_at(ff k, float4 m, ff isd) {
+    return ff_to_double(erfc_ff(ff_neg(ff_mul(ff_sub_m3(k, m), isd)))) * 0.5;
+}
+
+// cal_abd_dist2 with the crossing points in float-float.  At the crossing
+// points the two densities are equal, so the overlap is stationary in k1
+// and k2: an error e in either moves it by O((e / sd)^2).  Where the
+// variances differ by at least 1e-3 of the larger one, the crossing points'
+// cancellation is bounded by that ratio, and float-float places them within
+// ~1e-9 sd of the true points (the reference's FP64 points are nearer
+// still), so the overlap agrees with the reference's to ~1e-18 -- far inside
+// the CDFs' own error.  The CDF arguments are formed from the three-float
+// means to float-float accuracy, and the four CDF values are combined in
+// FP64 in the reference's order, as in the FP64 path: the combination needs
+// FP64, since for far-apart distributions 1 - d is small and must keep its
+// relative accuracy.  Returns -1 where the FP64 path decides instead: closer
+// variances, values out of the float-float range, crossing points that do
+// not separate.
+__device__ __forceinline__ double abd_dist2_ff(double v1, double v2, float4 mm1, float4 mm2, ff vf1, ff vf2, ff f1,
+                                               ff f2) {
+    if (!(fabs(v1 - v2) >= 1e-3 * fmax(v1, v2))) return -1.;
+    const ff q = ff_mul(vf2, ff_recip(vf1));
+    if (!(q.hi > 1e-30f && q.hi < 1e30f && vf1.hi < 1e15f && vf2.hi < 1e15f && mm1.x < 1e15f && mm2.x < 1e15f))
+        return -1.;
+    const ff m1 = ff_make(mm1.x, mm1.y), m2 = ff_make(mm2.x, mm2.y);
+    const ff L = ff_log(q);  // 2 log(sqrt(v2 / v1))
+    const ff dm = ff_add(m1, ff_neg(m2));
+    const ff dv = ff_add(vf1, ff_neg(vf2));
+    // t = sqrt(v1 v2 ((m1 - m2)^2 - 2 (v1 - v2) log(sqrt(v2 / v1))))
+    const ff A = ff_add(ff_mul(dm, dm), ff_neg(ff_mul(dv, L)));
+    const ff t = ff_sqrt(ff_mul(ff_mul(vf1, vf2), A));
+    const ff c = ff_add(ff_mul(m1, vf2), ff_neg(ff_mul(m2, vf1)));  // m1 v2 - m2 v1
+    const ff idv = ff_recip(dv);
+    ff k1 = ff_mul(ff_add(t, ff_neg(c)), idv);  // (t - m1 v2 + m2 v1) / (v1 - v2)
+    ff k2 = ff_mul(ff_add(t, c), ff_neg(idv));  // (t + m1 v2 - m2 v1) / (v2 - v1)
+    if (!(fabsf(k1.hi) < 1e30f && fabsf(k2.hi) < 1e30f &&
+          fabsf(k1.hi - k2.hi) > 0x1p-30f * (fabsf(k1.hi) + fabsf(k2.hi))))
+        return -1.;
+    if (ff_gt(k1, k2)) {
+        const ff x = k1;
+        k1 = k2;
+        k2 = x;
+    }
+    float4 ma = mm1, mb = mm2;
+    ff fa = f1, fb = f2;
+    if (v1 > v2) {
+        ma = mm2;
+        fa = f2;
+        mb = mm1;
+        fb = f1;
+    }
+    return fabs(cdf_at(k2, ma, fa) - cdf_at(k1, ma, fa) + cdf_at(k1, mb, fb) - cdf_at(k2, mb, fb));
+}
+
 struct ScoreArgs {
     const uint64_t* from;
     const uint64_t* to;
@@ -164,6 +239,8 @@ struct ScoreArgs {
     const double* abd;
     const double* vv;     // per contig and sample (k_abd_prep)
     const float2* isd;
+    const float4* m3;
+    const float2* vf;
     const double* dev;
     const double* ratio;
     uint32_t nabd;
@@ -210,7 +287,10 @@ __global__ void k_abd_score(ScoreArgs p) {
                 const double m1 = x < 1e-6 ? 1e-6 : x, m2 = y < 1e-6 ? 1e-6 : y;
                 if (m1 != m2) {
                     const float2 g1 = f1[i], g2 = f2[i];
-                    d = abd_dist2(m1, q1[i], ff_make(g1.x, g1.y), m2, q2[i], ff_make(g2.x, g2.y));
+                    const float2 w1 = p.vf[r1 * p.nabd + i], w2 = p.vf[r2 * p.nabd + i];
+                    d = abd_dist2_ff(q1[i], q2[i], p.m3[r1 * p.nabd + i], p.m3[r2 * p.nabd + i], ff_make(w1.x, w1.y),
+                                     ff_make(w2.x, w2.y), ff_make(g1.x, g1.y), ff_make(g2.x, g2.y));
+                    if (d < 0.) d = abd_dist2(m1, q1[i], ff_make(g1.x, g1.y), m2, q2[i], ff_make(g2.x, g2.y));
                 }
                 d = d < 1e-6 ? 1e-6 : d;  // std::min(std::max(d, 1e-6), 1 - 1e-6), NaN kept
                 d = (1. - 1e-6) < d ? 1. - 1e-6 : d;
@@ -323,6 +403,8 @@ int sscr_core(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const dou
     p.isd = (const float2*)ctx->bufs["abd.isd"].p;
     p.dev = (const double*)ctx->bufs["abd.dev"].p;
     p.ratio = (const double*)ctx->bufs["abd.ratio"].p;
+    p.m3 = (const float4*)ctx->bufs["abd.m3"].p;
+    p.vf = (const float2*)ctx->bufs["abd.vf"].p;
     p.nabd = ctx->abd_nabd;
     p.min_cv = min_cv;
     p.corr = corr;
@@ -391,13 +473,15 @@ int mdet_ctx_set_abundance(mdet_ctx* ctx, const double* abd, const double* abd_v
     float2* isd = (float2*)ctx_scratch(ctx, "abd.isd", n * nabd * 8);
     double* dev = (double*)ctx_scratch(ctx, "abd.dev", n * nabd * 8);
     double* ratio = (double*)ctx_scratch(ctx, "abd.ratio", nabd * 8);
-    if (!dm || !dv || !low || !vv || !isd || !dev || !ratio) return MDET_ERR_NOMEM;
+    float4* m3 = (float4*)ctx_scratch(ctx, "abd.m3", n * nabd * 16);
+    float2* vf = (float2*)ctx_scratch(ctx, "abd.vf", n * nabd * 8);
+    if (!dm || !dv || !low || !vv || !isd || !dev || !ratio || !m3 || !vf) return MDET_ERR_NOMEM;
     MDET_CUDA(ctx, cudaMemcpyAsync(dm, abd, n * nabd * 8, cudaMemcpyHostToDevice, s));
     MDET_CUDA(ctx, cudaMemcpyAsync(dv, abd_var, n * nabd * 8, cudaMemcpyHostToDevice, s));
     k_abd_low<<<grid_for(ctx, n, 256), 256, 0, s>>>(dm, n, nabd, low);
     MDET_LAUNCHED(ctx, "k_abd_low");
     k_abd_prep<<<std::max<unsigned>(grid_for(ctx, n, 256), (nabd + 255) / 256), 256, 0, s>>>(dm, dv, n, nabd, vv,
-                                                                                            isd, dev, ratio);
+                                                                                            isd, dev, ratio, m3, vf);
     MDET_LAUNCHED(ctx, "k_abd_prep");
     MDET_CUDA(ctx, cudaStreamSynchronize(s));
     ctx->abd_n = n;

@@ -8,7 +8,8 @@
 // operations follow the double-double algorithms of Hida, Li & Bailey (QD
 // library, 2001) at float width.  exp() is this project's own: Cody-Waite
 // reduction by ln 2, a 2^-4 argument scaling, a Taylor polynomial of degree 7
-// evaluated in float-float, and four squarings.
+// evaluated in float-float, and four squarings; log() is one Newton step
+// y + a e^-y - 1 from logf's value.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -135,4 +136,12 @@ __device__ __forceinline__ ff ff_exp(ff a) {
     for (int i = 0; i < 4; ++i) p = ff_mul(p, p);
     const float sc = __int_as_float(((int)k + 127) << 23);  // 2^k, |k| <= 116
     return ff_make(__fmul_rn(p.hi, sc), __fmul_rn(p.lo, sc));
+}
+
+// log a for 1e-30 < a < 1e30: logf's value y (error ~1e-7) and one Newton
+// step y + a e^-y - 1, which squares that error; ~1e-14 absolute.
+__device__ __forceinline__ ff ff_log(ff a) {
+    const ff y = ff_make(logf(a.hi), 0.f);
+    const ff r = ff_add_f(ff_mul(a, ff_exp(ff_neg(y))), -1.f);
+    return ff_add(y, r);
 }

@@ -32,8 +32,10 @@ namespace {
 // generated by gen_erfc_table.py): degree-13 interpolants on 26 pieces of
 // [0, 6.5], absolute error ~5e-16 before the float-float evaluation; 0
 // beyond 6.5 (erfc < 4e-20 there); erfc(-z) = 2 - erfc(z).  The FP32 pipes
-// run this far faster than the FP64 pipe runs the double erfc.
-__device__ __forceinline__ ff erfc_ff(ff z) {
+// run this far faster than the FP64 pipe runs the double erfc.  Kept out of
+// line: the score kernel calls it from eight places, and eight inlined
+// copies stall the kernel on instruction fetch.
+__device__ __noinline__ ff erfc_ff(ff z) {
     const bool neg = z.hi < 0.f;
     if (neg) z = ff_neg(z);
     ff r;
@@ -143,7 +145,7 @@ __global__ void k_low_sorted(const uint32_t* __restrict__ perm, const uint8_t* _
 // crossing points, whose numerator cancels when the variances are close, in
 // FP64 in the reference's order; the four CDF values in float-float.  Used
 // where abd_dist2_ff declines.
-__device__ double abd_dist2(double m1, double v1, ff f1, double m2, double v2, ff f2) {
+__device__ __noinline__ double abd_dist2(double m1, double v1, ff f1, double m2, double v2, ff f2) {
     double k1, k2;
     if (fabs(v2 - v1) < 1e-4) {
         k1 = k2 = (m1 + m2) / 2;
@@ -178,8 +180,9 @@ __device__ __forceinline__ ff ff_sub_m3(ff k, float4 m) {
     return ff_add_f(s, -m.z);
 }
 
-__device__ __forceinline__ double cdf_at(ff k, float4 m, ff isd) {
-    return ff_to_double(erfc_ff(ff_neg(ff_mul(ff_sub_m3(k, m), isd)))) * 0.5;
+// twice the normal CDF at k (erfc of the scaled difference), in double
+__device__ __forceinline__ double cdf2_at(ff k, float4 m, ff isd) {
+    return ff_to_double(erfc_ff(ff_neg(ff_mul(ff_sub_m3(k, m), isd))));
 }
 
 // cal_abd_dist2 with the crossing points in float-float.  At the crossing
@@ -196,9 +199,10 @@ __device__ __forceinline__ double cdf_at(ff k, float4 m, ff isd) {
 // relative accuracy.  Returns -1 where the FP64 path decides instead: closer
 // variances, values out of the float-float range, crossing points that do
 // not separate.
-__device__ __forceinline__ double abd_dist2_ff(double v1, double v2, float4 mm1, float4 mm2, ff vf1, ff vf2, ff f1,
-                                               ff f2) {
-    if (!(fabs(v1 - v2) >= 1e-3 * fmax(v1, v2))) return -1.;
+__device__ __forceinline__ double abd_dist2_ff(float4 mm1, float4 mm2, ff vf1, ff vf2, ff f1, ff f2) {
+    // in FP32: variances (>= 1) this far apart also pass the reference's own
+    // |v2 - v1| >= 1e-4 test, and their order is that of the FP64 values
+    if (!(fabsf(vf1.hi - vf2.hi) >= 1e-3f * fmaxf(vf1.hi, vf2.hi))) return -1.;
     const ff q = ff_mul(vf2, ff_recip(vf1));
     if (!(q.hi > 1e-30f && q.hi < 1e30f && vf1.hi < 1e15f && vf2.hi < 1e15f && mm1.x < 1e15f && mm2.x < 1e15f))
         return -1.;
@@ -223,13 +227,15 @@ __device__ __forceinline__ double abd_dist2_ff(double v1, double v2, float4 mm1,
     }
     float4 ma = mm1, mb = mm2;
     ff fa = f1, fb = f2;
-    if (v1 > v2) {
+    if (vf1.hi > vf2.hi) {
         ma = mm2;
         fa = f2;
         mb = mm1;
         fb = f1;
     }
-    return fabs(cdf_at(k2, ma, fa) - cdf_at(k1, ma, fa) + cdf_at(k1, mb, fb) - cdf_at(k2, mb, fb));
+    // the reference's sum of the four halved values, halved once at the end
+    // (scaling by 1/2 commutes with every rounding here)
+    return fabs(cdf2_at(k2, ma, fa) - cdf2_at(k1, ma, fa) + cdf2_at(k1, mb, fb) - cdf2_at(k2, mb, fb)) * 0.5;
 }
 
 struct ScoreArgs {
@@ -288,7 +294,7 @@ __global__ void k_abd_score(ScoreArgs p) {
                 if (m1 != m2) {
                     const float2 g1 = f1[i], g2 = f2[i];
                     const float2 w1 = p.vf[r1 * p.nabd + i], w2 = p.vf[r2 * p.nabd + i];
-                    d = abd_dist2_ff(q1[i], q2[i], p.m3[r1 * p.nabd + i], p.m3[r2 * p.nabd + i], ff_make(w1.x, w1.y),
+                    d = abd_dist2_ff(p.m3[r1 * p.nabd + i], p.m3[r2 * p.nabd + i], ff_make(w1.x, w1.y),
                                      ff_make(w2.x, w2.y), ff_make(g1.x, g1.y), ff_make(g2.x, g2.y));
                     if (d < 0.) d = abd_dist2(m1, q1[i], ff_make(g1.x, g1.y), m2, q2[i], ff_make(g2.x, g2.y));
                 }

@@ -244,10 +244,12 @@ def abundance_leg(ctx, a, d_tnf, d_ls, n, cutoff, d_from, d_to, d_st, cap, mode,
     torch.cuda.synchronize()
     call_s = (time.perf_counter() - t) / reps
     score_ms, score_n = ctx.kernel_ms("k_abd_score")
+    parts_ms = {k: ctx.kernel_ms(k)[0] / reps for k in ("abd_ranks", "k_sscr")}
     ctx.set_timing(False)
     leg = {"metric": "sTNF -> sSCR edge scoring throughput", "value": ne / call_s, "unit": "edges/s",
            "edges": int(ne), "samples": ABD_SAMPLES, "ms_per_call": call_s * 1e3,
-           "k_abd_score_ms": score_ms / max(score_n, 1), "bound": "float-float crossing points and erfc per edge and sample (FP32 pipes), the CDF "
+           "k_abd_score_ms": score_ms / max(score_n, 1), "ranks_ms": parts_ms["abd_ranks"],
+           "k_sscr_ms": parts_ms["k_sscr"], "bound": "float-float crossing points and erfc per edge and sample (FP32 pipes), the CDF "
                     "combination and the branch tests in FP64",
            "gated_graph_ms": st["ms_total"], "data": "synthetic coverage (synth.abundance, seed 20240607)"}
     if run_cpu:

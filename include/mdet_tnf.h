@@ -306,7 +306,11 @@ int mdet_ctx_set_abundance(mdet_ctx* ctx, const double* abd, const double* abd_v
  * out of range or an edge has no sample above min_cv (the reference would
  * divide 0 by 0).  min_cv, min_sample: the reference's minCV (default 1)
  * and minSample (default 3).  As in the reference, a contig whose depths are
- * the same in every sample makes its correlations undefined. */
+ * the same in every sample makes its correlations undefined.  Accuracy: the
+ * depth correlations, and so their ranks, are the reference's FP64 values
+ * bit for bit; the similarities and the final sSCR are within 1e-12
+ * (absolute or relative) of an FP64 evaluation (float-float normal CDFs,
+ * crossing points and powers). */
 int mdet_edges_sscr(mdet_ctx* ctx, const uint64_t* from, const uint64_t* to, const double* stnf,
                     uint64_t n_edges, double min_cv, uint32_t min_sample, double* sscr);
 int mdet_edges_sscr_dev(mdet_ctx* ctx, const uint64_t* d_from, const uint64_t* d_to,

@@ -89,3 +89,37 @@ def test_sscr_against_reference_code(seed, nabd):
                1.0, 3, ref.ctypes.data)
     got = oracle.sscr(fr, to, st, abd, var)
     assert np.allclose(got, ref, rtol=1e-12, atol=0)
+
+
+def test_overlap_is_stationary_in_the_crossing_points():
+    """The GPU forms cal_abd_dist2's crossing points in float-float where the
+    variances differ by at least 1e-3 of the larger (mdet_gb300/csrc/
+    abundance.cu, abd_dist2_ff).  That rests on the overlap
+    d = |Pa(k2) - Pa(k1) + Pb(k1) - Pb(k2)| being stationary in k1 and k2
+    (the densities are equal there): moving both by 1e-9 sd, far more than
+    float-float's error, moves d by less than 1e-16 -- checked here in
+    50-digit arithmetic on seeded normal pairs in that regime."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 50
+    rng = np.random.default_rng(17)
+    for _ in range(200):
+        m1, m2 = rng.lognormal(2, 1.2, 2)
+        v1 = max(1.0, m1 * rng.uniform(0.3, 3))
+        v2 = max(1.0, m2 * rng.uniform(0.3, 3))
+        if abs(v1 - v2) < 1e-3 * max(v1, v2):
+            continue
+        m1, m2, v1, v2 = (mp.mpf(float(x)) for x in (m1, m2, v1, v2))
+        t = mp.sqrt(v1 * v2 * ((m1 - m2) ** 2 - 2 * (v1 - v2) * mp.log(mp.sqrt(v2 / v1))))
+        k1, k2 = sorted([(t - m1 * v2 + m2 * v1) / (v1 - v2), (t + m1 * v2 - m2 * v1) / (v2 - v1)])
+        (ma, va), (mb, vb) = sorted([(m1, v1), (m2, v2)], key=lambda p: p[1])
+
+        def cdf(m, v, x):
+            return mp.erfc(-(x - m) / mp.sqrt(2 * v)) / 2
+
+        def d(a, b):
+            return abs(cdf(ma, va, b) - cdf(ma, va, a) + cdf(mb, vb, a) - cdf(mb, vb, b))
+
+        sd = mp.sqrt(min(va, vb))
+        for e1, e2 in [(1, 1), (1, -1), (-1, 1)]:
+            moved = d(k1 + e1 * mp.mpf("1e-9") * sd, k2 + e2 * mp.mpf("1e-9") * sd)
+            assert abs(moved - d(k1, k2)) < 1e-16

@@ -124,8 +124,8 @@ int mdet_tnf_count_dev(mdet_ctx* ctx, const char* d_bytes, uint64_t nbytes, cons
  * of sequence (about 4 GB); larger inputs return MDET_ERR_CAPACITY, and a
  * contig view outside [0, nbytes) returns MDET_ERR_INVALID, both checked
  * on the device before any sequence byte is read.  The first call on a
- * device resolves the array's device address there; make that first call
- * before any stream capture begins.  All calls share the one array, so calls
+ * device resolves the array's device address there.  All calls share the
+ * one array, so calls
  * whose work overlaps on the GPU race; serialise them.  Every call,
  * successful or not, synchronises `stream` before it returns.  Errors are
  * status codes only (there is no context for mdet_last_error). */

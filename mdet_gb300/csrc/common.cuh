@@ -92,6 +92,10 @@ struct mdet_ctx {
     // stream CUDA-graph recordings are captured on (the caller's stream may be
     // the legacy default stream, which cannot be captured)
     cudaStream_t cap_stream = nullptr;
+    // a second capture stream and the events that fork work onto it and join
+    // it back, for recordings with independent branches
+    cudaStream_t cap_stream2 = nullptr;
+    cudaEvent_t cap_fork = nullptr, cap_join = nullptr;
     // abundance set by mdet_ctx_set_abundance: contigs and samples (the
     // matrices and per-contig low flags live in scratch "abd.m", "abd.v",
     // "abd.low"); nabd == 0: none

@@ -299,6 +299,9 @@ int mdet_ctx_destroy(mdet_ctx* ctx) {
     if (ctx->io_in) cudaStreamDestroy(ctx->io_in);
     if (ctx->io_out) cudaStreamDestroy(ctx->io_out);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+    if (ctx->cap_stream2) cudaStreamDestroy(ctx->cap_stream2);
+    if (ctx->cap_fork) cudaEventDestroy(ctx->cap_fork);
+    if (ctx->cap_join) cudaEventDestroy(ctx->cap_join);
     delete ctx;
     return MDET_OK;
 }

@@ -645,6 +645,10 @@ struct SweepGraph {
     int record(mdet_ctx* ctx, Body body) {
         if (!ctx->cap_stream)
             MDET_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+        if (!ctx->cap_stream2)
+            MDET_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->cap_stream2, cudaStreamNonBlocking));
+        if (!ctx->cap_fork) MDET_CUDA(ctx, cudaEventCreateWithFlags(&ctx->cap_fork, cudaEventDisableTiming));
+        if (!ctx->cap_join) MDET_CUDA(ctx, cudaEventCreateWithFlags(&ctx->cap_join, cudaEventDisableTiming));
         const cudaStream_t cs = ctx->cap_stream;
         MDET_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         const uint64_t l0 = ctx->launches;
@@ -807,11 +811,21 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
         bool overfull = false;
         // one sweep -- the moved counter cleared, a launch or two per level,
         // the counters copied back -- recorded once as a CUDA graph on the
-        // context's capture stream and replayed on its stream for every sweep
+        // context's capture stream and replayed on its stream for every sweep.
+        // A level's contigs are never neighbours of one another (a contig's
+        // level exceeds its earlier neighbours'), so its warp-per-contig and
+        // block-per-contig launches are independent branches of the graph,
+        // joined before the next level.
         SweepGraph sg;
         MDET_TRY(sg.record(ctx, [&](cudaStream_t cs) {
+            const cudaStream_t cs2 = ctx->cap_stream2;
             cudaMemsetAsync(S.cnt, 0, 8, cs);
             for (size_t L = 0; L < linfo.size(); ++L) {
+                const bool both = linfo[L].nsmall && linfo[L].count;
+                if (both) {
+                    cudaEventRecord(ctx->cap_fork, cs);
+                    cudaStreamWaitEvent(cs2, ctx->cap_fork, 0);
+                }
                 if (linfo[L].nsmall) {
                     k_lp_level_warp<<<(linfo[L].nsmall + kWarpsPerBlock - 1) / kWarpsPerBlock, kThreads, 0, cs>>>(
                         P, lvls + soff[L], linfo[L].nsmall);
@@ -819,8 +833,12 @@ int lp_call(mdet_ctx* ctx, LpState& S, mdet_lp_stats* st) {
                 }
                 if (linfo[L].count) {
                     const uint32_t cap = std::min<uint32_t>(pow2_at_least(linfo[L].maxdeg), kSmallCap);
-                    k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), cs>>>(P, lvl + loff[L]);
+                    k_lp_level<<<linfo[L].count, kThreads, ws_bytes(cap), both ? cs2 : cs>>>(P, lvl + loff[L]);
                     ctx->launches++;
+                }
+                if (both) {
+                    cudaEventRecord(ctx->cap_join, cs2);
+                    cudaStreamWaitEvent(cs, ctx->cap_join, 0);
                 }
             }
             cudaMemcpyAsync(hc, S.cnt, 32, cudaMemcpyDeviceToHost, cs);

@@ -893,9 +893,9 @@ def run_ours(args):
         if not args.no_recruit:
             result["recruit"] = recruit_leg(ctx, a, not args.no_cpu and ws == 1)
         if not args.no_batch:
-            # SURVEY config 4 (64 assemblies of 5k-300k contigs) and the case the
-            # batch is for: many small assemblies, where per-call overhead rules
-            result["batched"] = {"config4": batch_leg(ctx, dev, 64, 5000, 300000, 41),
+            # 64 assemblies of 5k-300k contigs, and the case the batch is for:
+            # many small assemblies, where per-call overhead rules
+            result["batched"] = {"mixed_sizes": batch_leg(ctx, dev, 64, 5000, 300000, 41),
                                  "small_assemblies": batch_leg(ctx, dev, 256, 1000, 20000, 42)}
         if not args.no_tf32 and args.mode == "bf16":
             result["tf32"] = tf32_leg(ctx, d_tnf, d_ls, n, cut, o_from, o_to, o_st, cap, ne, d_from, d_to, d_st, st,

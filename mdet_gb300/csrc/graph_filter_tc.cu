@@ -201,11 +201,11 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
 //
 // It takes two dependent rounds of loads (block metadata, then the two d*
 // table cells), split here so that a caller can run them ahead of use.
-struct R2Meta {  // round 1: the blocks' metadata and the table selector
+struct R2Meta {  // first loads: the blocks' metadata and the table selector
     BlockMeta ma, mb0, mb1;
     uint32_t tsel;
 };
-struct R2Cells {  // round 2: the table cells (loads in flight) and the other terms
+struct R2Cells {  // second loads: the table cells (in flight) and the other terms
     float t0, t1, E, N;
 };
 template <int BN>

@@ -22,7 +22,7 @@
 //    the series' divisions are multiplications by reciprocals (1/(c+k) and
 //    1/y), which a device table can supply without changing a bit.
 //    This replaces boost::math::cdf(chi_squared(2c), x), which the reference
-//    calls (cuda/Cuda2.cu:611-616); Boost is not part of this build.
+//    calls (cuda/Cuda2.cu:611-616); Boost is not used here.
 #pragma once
 
 #include <cmath>

@@ -7,7 +7,7 @@
  * reference's own cuda/ranker.h.  What those spans expect from the rest of
  * Cuda2.cu is defined here: the Graph class's members, the option globals,
  * logging and memory-report helpers (no-ops), and in place of Boost --
- * which is not part of this build -- boost::math::chi_squared and its cdf,
+ * which is not used here -- boost::math::chi_squared and its cdf,
  * computed by lp_math.h, whose functions are the ones the device form uses.
  * LOG, which the reference defines as the C library's log, is lp_math.h's
  * log for the same reason.

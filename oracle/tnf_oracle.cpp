@@ -923,8 +923,8 @@ uint64_t orc_fasta_index(const char* b, uint64_t nbytes, uint64_t cap, uint64_t*
  * restated.  The chi-squared CDF (float-float, lpf::chi2_cdf), and the log
  * of 1 - sSCR (double, lpm::log), are the
  * project's own host/device functions of mdet_gb300/csrc/lp_math.h (the
- * reference calls Boost's CDF and the C library's log; Boost is not part of
- * this build), so that the device form can be held to the last bit.  The
+ * reference calls Boost's CDF and the C library's log; Boost is not used
+ * here), so that the device form can be held to the last bit.  The
  * per-contig label tallies are std::unordered_map / unordered_set, as in the
  * reference: the label picked among exact ties is the first in that map's
  * iteration order.

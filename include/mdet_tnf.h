@@ -396,9 +396,10 @@ int mdet_ctx_set_learned(mdet_ctx* ctx, const mdet_mlp* mlp, mdet_learned_report
  * nabd) are the reference's ABD and small_ABD (float, row-major; 1 <= nabd
  * <= 256); they are not modified.  out[i]: the bin label of large contig i
  * afterwards, -1 if it has none; small_out[s] likewise.  n + n_small must
- * be below 2^32 - 1.  The caller applies
- * the reference's own condition for running this block (!noAdd, nABD >=
- * minSample). */
+ * be below 2^32 - 1.  The reference dissolves small bins in every run but
+ * recruits only when !noAdd and nABD >= minSample; this call does both, so
+ * in the other runs a caller keeps the reference's dissolving loop
+ * (cuda/Cuda2.cu:2081-2101) and does not call it. */
 typedef struct {
     uint64_t n_bins;              /* bins kept (sizes sum to >= min_cls_size) */
     uint64_t n_bins_scored;       /* kept bins with >= 10 members: the ones that recruit */
